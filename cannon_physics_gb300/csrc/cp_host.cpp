@@ -1,0 +1,1146 @@
+// cp_host.cpp -- host runtime behind include/cannon_gpu.h.
+//
+//  * setup: the Body / Shape constructor arithmetic (inertia from the body
+//    AABB, bounding radii, convex hull tables) restated on the host, because
+//    a caller that has no Dart objects still needs the state they would hold;
+//  * worlds: one device allocation for the persistent state of a world and
+//    one for its step scratch (regrown when a step reports an overflow);
+//  * stepping: cp_world_step launches the persistent step kernel on one world;
+//    cp_batch_step launches it on many, with the nsteps sequence captured in
+//    a CUDA graph that is replayed while the world set and dt stay the same.
+//
+// Built with -ffp-contract=off: the host arithmetic must round like Dart's.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cannon_gpu.h"
+#include "cp_kernels.h"
+#include "cp_types.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(x)                                                                         \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess) return fail(CP_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// host arithmetic (binary64 compute, binary32 store), vector_math semantics
+
+struct h3 { float x = 0.f, y = 0.f, z = 0.f; };
+struct hq { float x = 0.f, y = 0.f, z = 0.f, w = 1.f; };
+
+h3 mk3(double x, double y, double z) { h3 v; v.x = (float)x; v.y = (float)y; v.z = (float)z; return v; }
+double dot3(const h3& a, const h3& b) {
+  double s = (double)a.x * (double)b.x;
+  s += (double)a.y * (double)b.y;
+  s += (double)a.z * (double)b.z;
+  return s;
+}
+double len3(const h3& a) { return std::sqrt(dot3(a, a)); }
+h3 norm3(h3 v) {
+  double l = len3(v);
+  if (l == 0.0) return v;
+  double d = 1.0 / l;
+  return mk3(v.x * d, v.y * d, v.z * d);
+}
+h3 sub3(const h3& a, const h3& b) { return mk3((double)a.x - (double)b.x, (double)a.y - (double)b.y, (double)a.z - (double)b.z); }
+h3 add3(const h3& a, const h3& b) { return mk3((double)a.x + (double)b.x, (double)a.y + (double)b.y, (double)a.z + (double)b.z); }
+h3 cross3(const h3& a, const h3& v) {
+  double vx = v.x, vy = v.y, vz = v.z;
+  return mk3((double)a.y * vz - (double)a.z * vy, (double)a.z * vx - (double)a.x * vz, (double)a.x * vy - (double)a.y * vx);
+}
+bool near3(const h3& a, const h3& v) {
+  return !(std::fabs((double)a.x - v.x) > 1e-6 || std::fabs((double)a.y - v.y) > 1e-6 || std::fabs((double)a.z - v.z) > 1e-6);
+}
+h3 qrot(const hq& q, const h3& v) {
+  double x = v.x, y = v.y, z = v.z, qx = q.x, qy = q.y, qz = q.z, qw = q.w;
+  double ix = qw * x + qy * z - qz * y;
+  double iy = qw * y + qz * x - qx * z;
+  double iz = qw * z + qx * y - qy * x;
+  double iw = -qx * x - qy * y - qz * z;
+  return mk3(ix * qw + iw * -qx + iy * -qz - iz * -qy, iy * qw + iw * -qy + iz * -qx - ix * -qz,
+             iz * qw + iw * -qz + ix * -qy - iy * -qx);
+}
+hq qmul(const hq& a, const hq& b) {
+  double ax = a.x, ay = a.y, az = a.z, aw = a.w, bx = b.x, by = b.y, bz = b.z, bw = b.w;
+  hq t;
+  t.x = (float)(ax * bw + aw * bx + ay * bz - az * by);
+  t.y = (float)(ay * bw + aw * by + az * bx - ax * bz);
+  t.z = (float)(az * bw + aw * bz + ax * by - ay * bx);
+  t.w = (float)(aw * bw - ax * bx - ay * by - az * bz);
+  return t;
+}
+// Body.updateInertiaWorld(force = true) (rigid_body.dart:459-464)
+void inertia_world(const hq& q, const h3& I, float* out) {
+  double x = q.x, y = q.y, z = q.z, w = q.w;
+  double x2 = x + x, y2 = y + y, z2 = z + z;
+  double xx = x * x2, xy = x * y2, xz = x * z2, yy = y * y2, yz = y * z2, zz = z * z2;
+  double wx = w * x2, wy = w * y2, wz = w * z2;
+  float m[9];
+  m[0] = (float)(1 - (yy + zz)); m[1] = (float)(xy - wz); m[2] = (float)(xz + wy);
+  m[3] = (float)(xy + wz); m[4] = (float)(1 - (xx + zz)); m[5] = (float)(yz - wx);
+  m[6] = (float)(xz - wy); m[7] = (float)(yz + wx); m[8] = (float)(1 - (xx + yy));
+  float t[9] = {m[0], m[3], m[6], m[1], m[4], m[7], m[2], m[5], m[8]};
+  float a[9];
+  for (int i = 0; i < 3; i++) {
+    a[3 * i + 0] = (float)((double)I.x * m[3 * i + 0]);
+    a[3 * i + 1] = (float)((double)I.y * m[3 * i + 1]);
+    a[3 * i + 2] = (float)((double)I.z * m[3 * i + 2]);
+  }
+  for (int r = 0; r < 3; r++) {
+    double a1 = a[3 * r], a2 = a[3 * r + 1], a3 = a[3 * r + 2];
+    for (int c = 0; c < 3; c++) out[3 * r + c] = (float)(a1 * t[c] + a2 * t[3 + c] + a3 * t[6 + c]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// convex hulls (convex_polyhedron.dart:80-185, box.dart:41-78, cylinder.dart:222-294)
+
+struct Hull {
+  std::vector<h3> verts;
+  std::vector<std::vector<int>> faces;
+  std::vector<h3> normals;
+  std::vector<h3> edges;
+  bool has_axes = false;
+};
+
+void hull_finish(Hull& h) {
+  h.normals.clear();
+  for (auto& f : h.faces) {
+    const h3 &va = h.verts[f[0]], &vb = h.verts[f[1]], &vc = h.verts[f[2]];
+    h3 ab = sub3(vb, va), cb = sub3(vc, vb);
+    h3 n = cross3(cb, ab);
+    if (!(n.x == 0 && n.y == 0 && n.z == 0)) n = norm3(n);
+    n.x = -n.x; n.y = -n.y; n.z = -n.z;
+    h.normals.push_back(n);
+  }
+  h.edges.clear();
+  for (auto& f : h.faces) {
+    int nv = (int)f.size();
+    for (int j = 0; j < nv; j++) {
+      h3 e = norm3(sub3(h.verts[f[j]], h.verts[f[(j + 1) % nv]]));
+      bool found = false;
+      for (auto& u : h.edges)
+        if (near3(u, e)) { found = true; break; }
+      if (!found) h.edges.push_back(e);
+    }
+  }
+}
+
+int build_hull(const cp_shape_desc& d, Hull& h) {
+  if (d.type == CP_SHAPE_BOX) {
+    double sx = d.half_extents[0], sy = d.half_extents[1], sz = d.half_extents[2];
+    h.verts = {mk3(-sx, -sy, -sz), mk3(sx, -sy, -sz), mk3(sx, sy, -sz), mk3(-sx, sy, -sz),
+               mk3(-sx, -sy, sz), mk3(sx, -sy, sz), mk3(sx, sy, sz), mk3(-sx, sy, sz)};
+    h.faces = {{3, 2, 1, 0}, {4, 5, 6, 7}, {5, 4, 0, 1}, {2, 3, 7, 6}, {0, 4, 7, 3}, {1, 2, 6, 5}};
+    h.has_axes = true;
+  } else if (d.type == CP_SHAPE_CYLINDER) {
+    const int N = d.num_segments;
+    if (d.radius_top < 0 || d.radius_bottom < 0 || N < 3) return fail(CP_ERR_ARG, "invalid cylinder");
+    double rt = d.radius_top, rb = d.radius_bottom, ht = d.height;
+    std::vector<int> bottom, top;
+    h.verts.push_back(mk3(-rb * std::sin(0.0), -ht * 0.5, rb * std::cos(0.0)));
+    bottom.push_back(0);
+    h.verts.push_back(mk3(-rt * std::sin(0.0), ht * 0.5, rt * std::cos(0.0)));
+    top.push_back(1);
+    for (int i = 0; i < N; i++) {
+      double theta = ((2 * M_PI) / N) * (i + 1);
+      if (i < N - 1) {
+        h.verts.push_back(mk3(-rb * std::sin(theta), -ht * 0.5, rb * std::cos(theta)));
+        bottom.push_back(2 * i + 2);
+        h.verts.push_back(mk3(-rt * std::sin(theta), ht * 0.5, rt * std::cos(theta)));
+        top.push_back(2 * i + 3);
+        h.faces.push_back({2 * i, 2 * i + 1, 2 * i + 3, 2 * i + 2});
+      } else {
+        h.faces.push_back({2 * i, 2 * i + 1, 1, 0});
+      }
+    }
+    h.faces.push_back(bottom);
+    std::vector<int> rev(top.rbegin(), top.rend());
+    h.faces.push_back(rev);
+    h.has_axes = true;
+  } else if (d.type == CP_SHAPE_CONVEX) {
+    if (d.num_vertices < 4 || d.num_faces < 4 || !d.vertices || !d.face_sizes || !d.face_indices)
+      return fail(CP_ERR_ARG, "convex shape needs >= 4 vertices and faces");
+    for (int i = 0; i < d.num_vertices; i++) h.verts.push_back(mk3(d.vertices[3 * i], d.vertices[3 * i + 1], d.vertices[3 * i + 2]));
+    int off = 0;
+    for (int f = 0; f < d.num_faces; f++) {
+      std::vector<int> face;
+      if (d.face_sizes[f] < 3) return fail(CP_ERR_ARG, "convex face %d has < 3 vertices", f);
+      for (int k = 0; k < d.face_sizes[f]; k++) {
+        int vi = d.face_indices[off + k];
+        if (vi < 0 || vi >= d.num_vertices) return fail(CP_ERR_ARG, "convex face index out of range");
+        face.push_back(vi);
+      }
+      off += d.face_sizes[f];
+      h.faces.push_back(face);
+    }
+    h.has_axes = d.has_axes != 0;
+  } else {
+    return fail(CP_ERR_ARG, "shape type %d has no hull", d.type);
+  }
+  hull_finish(h);
+  if ((int)h.verts.size() > CP_MAX_HULL_VERTS || (int)h.faces.size() > CP_MAX_HULL_VERTS || (int)h.edges.size() > CP_MAX_HULL_VERTS)
+    return fail(CP_ERR_UNSUPPORTED, "hull larger than %d vertices / faces / edges", CP_MAX_HULL_VERTS);
+  for (auto& f : h.faces)
+    if ((int)f.size() > CP_MAX_FACE_VERTS) return fail(CP_ERR_UNSUPPORTED, "hull face larger than %d vertices", CP_MAX_FACE_VERTS);
+  return CP_OK;
+}
+
+double shape_bsr(const cp_shape_desc& d, const Hull* h) {
+  switch (d.type) {
+    case CP_SHAPE_SPHERE: return d.radius;
+    case CP_SHAPE_PLANE: return INFINITY;
+    case CP_SHAPE_BOX: return len3(mk3(d.half_extents[0], d.half_extents[1], d.half_extents[2]));
+    default: {
+      double m2 = 0;
+      for (auto& v : h->verts) { double n2 = dot3(v, v); if (n2 > m2) m2 = n2; }
+      return std::sqrt(m2);
+    }
+  }
+}
+
+// Shape.calculateWorldAABB
+void shape_aabb(const cp_shape_desc& d, const Hull* h, const h3& pos, const hq& q, h3& mn, h3& mx) {
+  if (d.type == CP_SHAPE_SPHERE) {
+    double r = d.radius;
+    mn = mk3(pos.x - r, pos.y - r, pos.z - r);
+    mx = mk3(pos.x + r, pos.y + r, pos.z + r);
+  } else if (d.type == CP_SHAPE_PLANE) {
+    h3 n = qrot(q, mk3(0, 0, 1));
+    mn = mk3(-INFINITY, -INFINITY, -INFINITY);
+    mx = mk3(INFINITY, INFINITY, INFINITY);
+    if (n.x == 1) mx.x = pos.x; else if (n.x == -1) mn.x = pos.x;
+    if (n.y == 1) mx.y = pos.y; else if (n.y == -1) mn.y = pos.y;
+    if (n.z == 1) mx.z = pos.z; else if (n.z == -1) mn.z = pos.z;
+  } else if (d.type == CP_SHAPE_BOX) {
+    float ex = d.half_extents[0], ey = d.half_extents[1], ez = d.half_extents[2];
+    const float c[8][3] = {{ex, ey, ez}, {-ex, ey, ez}, {-ex, -ey, ez}, {-ex, -ey, -ez},
+                           {ex, -ey, -ez}, {ex, ey, -ez}, {-ex, ey, -ez}, {ex, -ey, ez}};
+    for (int i = 0; i < 8; i++) {
+      h3 w = add3(qrot(q, mk3(c[i][0], c[i][1], c[i][2])), pos);
+      if (i == 0) { mn = w; mx = w; continue; }
+      if (w.x > mx.x) mx.x = w.x;
+      if (w.y > mx.y) mx.y = w.y;
+      if (w.z > mx.z) mx.z = w.z;
+      if (w.x < mn.x) mn.x = w.x;
+      if (w.y < mn.y) mn.y = w.y;
+      if (w.z < mn.z) mn.z = w.z;
+    }
+  } else {
+    for (size_t i = 0; i < h->verts.size(); i++) {
+      h3 w = add3(qrot(q, h->verts[i]), pos);
+      if (i == 0) { mn = w; mx = w; continue; }
+      if (w.x < mn.x) mn.x = w.x;
+      if (w.x > mx.x) mx.x = w.x;
+      if (w.y < mn.y) mn.y = w.y;
+      if (w.y > mx.y) mx.y = w.y;
+      if (w.z < mn.z) mn.z = w.z;
+      if (w.z > mx.z) mx.z = w.z;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// device allocation layout
+
+struct Layout {
+  size_t off = 0;
+  size_t take(size_t bytes) {
+    size_t o = (off + 255) & ~(size_t)255;
+    off = o + bytes;
+    return o;
+  }
+};
+
+struct WorldRec {
+  bool live = false;
+  char* state = nullptr;   // device: params, bodies, shapes, hulls, materials, constraints, sap order, damping
+  char* scratch = nullptr; // device: per-step lists
+  DWorld dw{};
+  int nb = 0, nshapes = 0, nmat = 0, ncm = 0, ncons = 0, ncon_rows = 0;
+  int broadphase = 0, nbins = 0;
+  int pairs_cap = 0, contacts_cap = 0, rows_cap = 0, bins_cap = 0;
+  double dt_cached = -1.0;
+  std::vector<double> lin_damp, ang_damp;
+  std::vector<DContactMaterial> cms;  // host copy for SPOOK updates
+};
+
+}  // namespace
+
+struct cp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<WorldRec> worlds;
+  DWorld* d_worlds = nullptr;
+  int d_worlds_cap = 0;
+  int* d_ids = nullptr;
+  int d_ids_cap = 0;
+  int* d_queue = nullptr;
+  int* d_one = nullptr;  // world id of the plain path
+  long long* d_status = nullptr;
+  int d_status_cap = 0;
+  int sms = 0, blocks_per_sm = 1;
+  long long launches = 0;
+  std::mutex mu;
+  // batched-step graph cache
+  cudaGraphExec_t graph = nullptr;
+  std::vector<int> graph_ids;
+  double graph_dt = 0;
+  int graph_steps = 0;
+};
+
+namespace {
+
+int upload_world_entry(cp_ctx* c, int id) {
+  if (id >= c->d_worlds_cap) {
+    int nc = std::max(64, 2 * (id + 1));
+    DWorld* nw = nullptr;
+    CUDA_TRY(cudaMalloc(&nw, sizeof(DWorld) * nc));
+    if (c->d_worlds) {
+      CUDA_TRY(cudaMemcpy(nw, c->d_worlds, sizeof(DWorld) * c->d_worlds_cap, cudaMemcpyDeviceToDevice));
+      cudaFree(c->d_worlds);
+    }
+    c->d_worlds = nw;
+    c->d_worlds_cap = nc;
+    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  }
+  CUDA_TRY(cudaMemcpy(c->d_worlds + id, &c->worlds[id].dw, sizeof(DWorld), cudaMemcpyHostToDevice));
+  return CP_OK;
+}
+
+int pow2_at_least(int v) {
+  int p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+// (re)allocate the scratch of a world for its current capacities
+int alloc_scratch(WorldRec& w) {
+  if (w.scratch) { cudaFree(w.scratch); w.scratch = nullptr; }
+  const int nb = w.nb, cc = w.contacts_cap, rc = w.rows_cap;
+  const int pc = std::max(w.pairs_cap, nb);  // SAP also keeps one count per list position in the pair arrays
+  const int cand_cap = 3 * cc + w.ncon_rows + 1;
+  const int hash_cap = w.broadphase == CP_BROAD_GRID ? pow2_at_least(2 * pc + 2) : 2;
+  Layout L;
+  size_t o_bscr = L.take(sizeof(DBodyScr) * (nb + 1));
+  size_t o_tmp = L.take(sizeof(int) * (nb + 1));
+  size_t o_pa = L.take(sizeof(int) * (pc + 1));
+  size_t o_pb = L.take(sizeof(int) * (pc + 1));
+  size_t o_pc = L.take(sizeof(int) * (pc + 1));
+  size_t o_pt = L.take(sizeof(int) * (pc + 1));
+  size_t o_hv = L.take(sizeof(int) * (pc + 1));
+  size_t o_ct = L.take(sizeof(DContact) * (cc + 1));
+  size_t o_co = L.take(sizeof(DContact) * (cc + 1));
+  size_t o_cs = L.take(sizeof(int) * (cc + 1));
+  size_t o_cd = L.take(sizeof(int) * (cand_cap + 1));
+  size_t o_rw = L.take(sizeof(DRow) * (rc + 1));
+  size_t o_ab = L.take(sizeof(double) * (rc + 1));
+  size_t o_lo = L.take(sizeof(int) * (rc + 1));
+  size_t o_lr = L.take(sizeof(int) * (rc + 1));
+  size_t o_ls = L.take(sizeof(int) * (rc + 2));
+  size_t o_lc = L.take(sizeof(int) * (rc + 2));
+  size_t o_sk = L.take(sizeof(float) * (nb + 1));
+  const int nbins = w.broadphase == CP_BROAD_GRID ? w.nbins : 0;
+  size_t o_bc = L.take(sizeof(int) * (nbins + 2));
+  size_t o_bs = L.take(sizeof(int) * (nbins + 2));
+  size_t o_bb = L.take(sizeof(int) * (w.bins_cap + 1));
+  size_t o_ba = L.take(sizeof(float) * (w.broadphase == CP_BROAD_GRID ? 3 * 4096 : 1));
+  size_t o_hk = L.take(sizeof(long long) * hash_cap);
+  size_t o_hw = L.take(sizeof(int) * hash_cap);
+  char* base = nullptr;
+  cudaError_t e = cudaMalloc(&base, L.off);
+  if (e != cudaSuccess) return fail(CP_ERR_OOM, "scratch allocation of %zu bytes failed: %s", L.off, cudaGetErrorString(e));
+  w.scratch = base;
+  DWorld& d = w.dw;
+  d.bscr = (DBodyScr*)(base + o_bscr);
+  d.sap_tmp = (int*)(base + o_tmp);
+  d.pair_a = (int*)(base + o_pa);
+  d.pair_b = (int*)(base + o_pb);
+  d.pair_cnt = (int*)(base + o_pc);
+  d.pair_tstart = (int*)(base + o_pt);
+  d.heavy = (int*)(base + o_hv);
+  d.ctmp = (DContact*)(base + o_ct);
+  d.contacts = (DContact*)(base + o_co);
+  d.cscr = (int*)(base + o_cs);
+  d.cand = (int*)(base + o_cd);
+  d.rows = (DRow*)(base + o_rw);
+  d.absdl = (double*)(base + o_ab);
+  d.level_of = (int*)(base + o_lo);
+  d.level_rows = (int*)(base + o_lr);
+  d.level_start = (int*)(base + o_ls);
+  d.level_cursor = (int*)(base + o_lc);
+  d.sap_key = (float*)(base + o_sk);
+  d.bin_cnt = (int*)(base + o_bc);
+  d.bin_start = (int*)(base + o_bs);
+  d.bin_body = (int*)(base + o_bb);
+  d.bin_acc = (float*)(base + o_ba);
+  d.hkeys = (long long*)(base + o_hk);
+  d.hvals = (int*)(base + o_hw);
+  d.hash_cap = hash_cap;
+  return CP_OK;
+}
+
+void body_to_device(const cp_body_desc& s, DBody& b) {
+  std::memset(&b, 0, sizeof(b));
+  std::memcpy(b.pos, s.position, 12);
+  std::memcpy(b.quat, s.quaternion, 16);
+  std::memcpy(b.vel, s.velocity, 12);
+  std::memcpy(b.avel, s.angular_velocity, 12);
+  std::memcpy(b.force, s.force, 12);
+  std::memcpy(b.torque, s.torque, 12);
+  std::memcpy(b.iw, s.inv_inertia_world, 36);
+  std::memcpy(b.inv_inertia, s.inv_inertia, 12);
+  std::memcpy(b.lin_factor, s.linear_factor, 12);
+  std::memcpy(b.ang_factor, s.angular_factor, 12);
+  std::memcpy(b.aabb_lo, s.aabb_lower, 12);
+  std::memcpy(b.aabb_hi, s.aabb_upper, 12);
+  std::memcpy(b.shape_off, s.shape_offset, 12);
+  std::memcpy(b.shape_quat, s.shape_orientation, 16);
+  std::memcpy(b.prev_pos, s.previous_position, 12);
+  std::memcpy(b.prev_quat, s.previous_quaternion, 16);
+  b.mass = s.mass; b.inv_mass = s.inv_mass;
+  b.lin_damp = s.linear_damping; b.ang_damp = s.angular_damping;
+  b.sleep_speed_limit = s.sleep_speed_limit; b.sleep_time_limit = s.sleep_time_limit;
+  b.time_last_sleepy = s.time_last_sleepy; b.bounding_radius = s.bounding_radius;
+  b.type = s.type; b.sleep_state = s.sleep_state;
+  b.flags = (s.allow_sleep ? BF_ALLOW_SLEEP : 0) | (s.wake_up_after_narrowphase ? BF_WAKE : 0) |
+            (s.collision_response ? BF_RESPONSE : 0) | (s.is_trigger ? BF_TRIGGER : 0) |
+            (s.fixed_rotation ? BF_FIXED_ROT : 0) | (s.aabb_needs_update ? BF_AABB_DIRTY : 0);
+  b.group = s.collision_filter_group; b.mask = s.collision_filter_mask;
+  b.material = s.material; b.shape = s.shape;
+  b.brad32 = (float)s.bounding_radius;
+}
+
+void body_from_device(const DBody& b, cp_body_desc& s) {
+  std::memset(&s, 0, sizeof(s));
+  std::memcpy(s.position, b.pos, 12);
+  std::memcpy(s.quaternion, b.quat, 16);
+  std::memcpy(s.velocity, b.vel, 12);
+  std::memcpy(s.angular_velocity, b.avel, 12);
+  std::memcpy(s.force, b.force, 12);
+  std::memcpy(s.torque, b.torque, 12);
+  std::memcpy(s.inv_inertia_world, b.iw, 36);
+  std::memcpy(s.inv_inertia, b.inv_inertia, 12);
+  std::memcpy(s.linear_factor, b.lin_factor, 12);
+  std::memcpy(s.angular_factor, b.ang_factor, 12);
+  std::memcpy(s.aabb_lower, b.aabb_lo, 12);
+  std::memcpy(s.aabb_upper, b.aabb_hi, 12);
+  std::memcpy(s.shape_offset, b.shape_off, 12);
+  std::memcpy(s.shape_orientation, b.shape_quat, 16);
+  std::memcpy(s.previous_position, b.prev_pos, 12);
+  std::memcpy(s.previous_quaternion, b.prev_quat, 16);
+  s.mass = b.mass; s.inv_mass = b.inv_mass;
+  s.linear_damping = b.lin_damp; s.angular_damping = b.ang_damp;
+  s.sleep_speed_limit = b.sleep_speed_limit; s.sleep_time_limit = b.sleep_time_limit;
+  s.time_last_sleepy = b.time_last_sleepy; s.bounding_radius = b.bounding_radius;
+  s.type = b.type; s.sleep_state = b.sleep_state;
+  s.allow_sleep = (b.flags & BF_ALLOW_SLEEP) != 0;
+  s.wake_up_after_narrowphase = (b.flags & BF_WAKE) != 0;
+  s.collision_response = (b.flags & BF_RESPONSE) != 0;
+  s.is_trigger = (b.flags & BF_TRIGGER) != 0;
+  s.fixed_rotation = (b.flags & BF_FIXED_ROT) != 0;
+  s.aabb_needs_update = (b.flags & BF_AABB_DIRTY) != 0;
+  s.collision_filter_group = b.group; s.collision_filter_mask = b.mask;
+  s.material = b.material; s.shape = b.shape;
+}
+
+// Equation.setSpookParams (equation_class.dart:53-60)
+void spook(double stiffness, double relaxation, double h, double& a, double& b, double& eps) {
+  double d = relaxation, k = stiffness;
+  a = 4.0 / (h * (1 + 4 * d));
+  b = 4.0 * d / (1 + 4 * d);
+  eps = 4.0 / (h * h * k * (1 + 4 * d));
+}
+
+// dt-dependent tables: damping powers (libm pow, as Dart's math.pow) and the
+// contact materials' SPOOK parameters (createContactEquation uses world.dt)
+int ensure_dt(cp_ctx* c, WorldRec& w, double dt) {
+  if (w.dt_cached == dt) return CP_OK;
+  std::vector<double> p(2 * (size_t)w.nb);
+  for (int i = 0; i < w.nb; i++) {
+    p[2 * i] = std::pow(1.0 - w.lin_damp[i], dt);
+    p[2 * i + 1] = std::pow(1.0 - w.ang_damp[i], dt);
+  }
+  for (auto& m : w.cms) {
+    spook(m.cs, m.cr, dt, m.ca, m.cb, m.ceps);
+    spook(m.fs, m.fr, dt, m.fa, m.fb, m.feps);
+  }
+  CUDA_TRY(cudaMemcpyAsync(w.dw.dpow, p.data(), sizeof(double) * p.size(), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(w.dw.cms, w.cms.data(), sizeof(DContactMaterial) * w.cms.size(), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  w.dt_cached = dt;
+  return CP_OK;
+}
+
+int check_world(cp_ctx* c, int id) {
+  if (!c) return fail(CP_ERR_ARG, "null context");
+  if (id < 0 || id >= (int)c->worlds.size() || !c->worlds[id].live) return fail(CP_ERR_ARG, "no world %d", id);
+  return CP_OK;
+}
+
+int read_params(cp_ctx* c, WorldRec& w, DWorldParams& p) {
+  CUDA_TRY(cudaMemcpyAsync(&p, w.dw.P, sizeof(p), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return CP_OK;
+}
+
+// grow the capacities a failed step reported and clear the status
+int grow(cp_ctx* c, int id, int status) {
+  WorldRec& w = c->worlds[id];
+  if (status & ST_HULL_OVERFLOW) return fail(CP_ERR_CAPACITY, "a clipped polygon exceeded %d vertices", CP_MAX_CLIP);
+  if (status & ST_PAIRS_OVERFLOW) w.pairs_cap *= 2;
+  if (status & ST_CONTACTS_OVERFLOW) w.contacts_cap *= 2;
+  if (status & ST_ROWS_OVERFLOW) w.rows_cap *= 2;
+  if (status & ST_BINS_OVERFLOW) w.bins_cap *= 2;
+  if (w.pairs_cap > (1 << 28) || w.contacts_cap > (1 << 28) || w.rows_cap > (1 << 28)) return fail(CP_ERR_CAPACITY, "capacity limit");
+  int st = alloc_scratch(w);
+  if (st) return st;
+  DWorldParams p;
+  st = read_params(c, w, p);
+  if (st) return st;
+  p.status = 0;
+  p.pairs_cap = w.pairs_cap;
+  p.contacts_cap = w.contacts_cap;
+  p.rows_cap = w.rows_cap;
+  p.bins_cap = w.bins_cap;
+  CUDA_TRY(cudaMemcpy(w.dw.P, &p, sizeof(p), cudaMemcpyHostToDevice));
+  return upload_world_entry(c, id);
+}
+
+int ensure_ids(cp_ctx* c, int n) {
+  if (n > c->d_ids_cap) {
+    if (c->d_ids) cudaFree(c->d_ids);
+    if (c->d_status) cudaFree(c->d_status);
+    int cap = std::max(256, 2 * n);
+    CUDA_TRY(cudaMalloc(&c->d_ids, sizeof(int) * cap));
+    CUDA_TRY(cudaMalloc(&c->d_status, sizeof(long long) * 4 * cap));
+    c->d_ids_cap = cap;
+    c->d_status_cap = cap;
+    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  }
+  return CP_OK;
+}
+
+int plain_steps(cp_ctx* c, int id, double dt, int nsteps) {
+  WorldRec& w = c->worlds[id];
+  int st = ensure_dt(c, w, dt);
+  if (st) return st;
+  CUDA_TRY(cudaMemcpyAsync(c->d_one, &id, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  DWorldParams p;
+  st = read_params(c, w, p);
+  if (st) return st;
+  long long target = p.stepnumber + nsteps;
+  for (int guard = 0; guard < 64; guard++) {
+    long long done = p.stepnumber;
+    for (long long s = done; s < target; s++) {
+      CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_one, 1, dt, c->d_queue, 1, c->stream));
+      c->launches += 2;
+    }
+    st = read_params(c, w, p);
+    if (st) return st;
+    if (p.status == 0) break;
+    st = grow(c, id, p.status);
+    if (st) return st;
+    st = read_params(c, w, p);
+    if (st) return st;
+  }
+  if (p.status != 0 || p.stepnumber != target) return fail(CP_ERR_CAPACITY, "world %d could not complete its steps", id);
+  return CP_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char* cp_last_error(void) { return g_err.c_str(); }
+int cp_abi_version(void) { return CP_ABI_VERSION; }
+
+int cp_shape_setup(cp_shape_desc* s) {
+  if (!s) return fail(CP_ERR_ARG, "null shape");
+  Hull h;
+  if (s->type == CP_SHAPE_SPHERE) {
+    if (s->radius < 0) return fail(CP_ERR_ARG, "The sphere radius cannot be negative.");
+  } else if (s->type != CP_SHAPE_PLANE) {
+    int st = build_hull(*s, h);
+    if (st) return st;
+  }
+  s->bounding_sphere_radius = shape_bsr(*s, &h);
+  return CP_OK;
+}
+
+int cp_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc* bodies, int32_t num_bodies) {
+  if (!bodies || num_bodies < 0 || num_shapes < 0 || (num_shapes > 0 && !shapes)) return fail(CP_ERR_ARG, "bad arguments");
+  std::vector<Hull> hulls(num_shapes);
+  std::vector<char> has_hull(num_shapes, 0);
+  for (int k = 0; k < num_bodies; k++) {
+    cp_body_desc& b = bodies[k];
+    if (b.shape >= num_shapes) return fail(CP_ERR_ARG, "body %d: shape %d out of range", k, b.shape);
+    std::memcpy(b.previous_position, b.position, 12);
+    std::memcpy(b.previous_quaternion, b.quaternion, 16);
+    b.inv_mass = b.mass > 0 ? 1.0 / b.mass : 0;
+    if (b.type < 0) b.type = b.mass <= 0.0 ? CP_BODY_STATIC : CP_BODY_DYNAMIC;
+    h3 he = mk3(0, 0, 0);
+    hq q; q.x = b.quaternion[0]; q.y = b.quaternion[1]; q.z = b.quaternion[2]; q.w = b.quaternion[3];
+    h3 mn = mk3(0, 0, 0), mx = mk3(0, 0, 0);
+    b.bounding_radius = 0;
+    if (b.shape >= 0) {
+      const cp_shape_desc& sd = shapes[b.shape];
+      if (sd.type != CP_SHAPE_SPHERE && sd.type != CP_SHAPE_PLANE && !has_hull[b.shape]) {
+        int st = build_hull(sd, hulls[b.shape]);
+        if (st) return st;
+        has_hull[b.shape] = 1;
+      }
+      h3 off = mk3(b.shape_offset[0], b.shape_offset[1], b.shape_offset[2]);
+      h3 pos = mk3(b.position[0], b.position[1], b.position[2]);
+      hq so; so.x = b.shape_orientation[0]; so.y = b.shape_orientation[1]; so.z = b.shape_orientation[2]; so.w = b.shape_orientation[3];
+      h3 wpos = add3(qrot(q, off), pos);
+      hq wq = qmul(q, so);
+      shape_aabb(sd, &hulls[b.shape], wpos, wq, mn, mx);
+      he = mk3(((double)mx.x - mn.x) / 2, ((double)mx.y - mn.y) / 2, ((double)mx.z - mn.z) / 2);
+      double r = shape_bsr(sd, &hulls[b.shape]);
+      double o = len3(off);
+      if (o + r > 0) b.bounding_radius = o + r;
+    }
+    b.aabb_lower[0] = mn.x; b.aabb_lower[1] = mn.y; b.aabb_lower[2] = mn.z;
+    b.aabb_upper[0] = mx.x; b.aabb_upper[1] = mx.y; b.aabb_upper[2] = mx.z;
+    // Box.calculateInertia (box.dart:88-94)
+    double m = b.mass;
+    float Ix = (float)(1.0 / 12.0 * m * (2 * (double)he.y * 2 * he.y + 2 * (double)he.z * 2 * he.z));
+    float Iy = (float)(1.0 / 12.0 * m * (2 * (double)he.x * 2 * he.x + 2 * (double)he.z * 2 * he.z));
+    float Iz = (float)(1.0 / 12.0 * m * (2 * (double)he.y * 2 * he.y + 2 * (double)he.x * 2 * he.x));
+    bool fixed = b.fixed_rotation != 0;
+    h3 inv = mk3(Ix > 0 && !fixed ? 1.0 / Ix : 0, Iy > 0 && !fixed ? 1.0 / Iy : 0, Iz > 0 && !fixed ? 1.0 / Iz : 0);
+    b.inv_inertia[0] = inv.x; b.inv_inertia[1] = inv.y; b.inv_inertia[2] = inv.z;
+    inertia_world(q, inv, b.inv_inertia_world);
+    b.aabb_needs_update = 1;
+  }
+  return CP_OK;
+}
+
+int cp_create(const cp_config* cfg, cp_ctx** out) {
+  if (!out) return fail(CP_ERR_ARG, "null out");
+  *out = nullptr;
+  int dev = cfg ? cfg->device : 0;
+  int ndev = 0;
+  CUDA_TRY(cudaGetDeviceCount(&ndev));
+  if (dev < 0 || dev >= ndev) return fail(CP_ERR_ARG, "no CUDA device %d (%d present)", dev, ndev);
+  CUDA_TRY(cudaSetDevice(dev));
+  cp_ctx* c = new cp_ctx();
+  c->device = dev;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_queue, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_one, sizeof(int));
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(CP_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
+  }
+  c->blocks_per_sm = std::max(1, cpk_max_resident_blocks());
+  *out = c;
+  return CP_OK;
+}
+
+int cp_destroy(cp_ctx* c) {
+  if (!c) return CP_OK;
+  cudaSetDevice(c->device);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  for (auto& w : c->worlds) {
+    if (w.state) cudaFree(w.state);
+    if (w.scratch) cudaFree(w.scratch);
+  }
+  if (c->d_worlds) cudaFree(c->d_worlds);
+  if (c->d_ids) cudaFree(c->d_ids);
+  if (c->d_status) cudaFree(c->d_status);
+  if (c->d_queue) cudaFree(c->d_queue);
+  if (c->d_one) cudaFree(c->d_one);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return CP_OK;
+}
+
+int cp_world_create(cp_ctx* c, const cp_world_desc* d, int32_t* world_id) {
+  if (!c || !d || !world_id) return fail(CP_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  if (d->num_bodies < 0 || d->num_shapes < 0 || d->num_materials < 0 || d->num_contact_materials < 0 || d->num_constraints < 0)
+    return fail(CP_ERR_ARG, "negative count");
+  if ((d->num_bodies && !d->bodies) || (d->num_shapes && !d->shapes) || (d->num_materials && !d->materials) ||
+      (d->num_contact_materials && !d->contact_materials) || (d->num_constraints && !d->constraints))
+    return fail(CP_ERR_ARG, "null array");
+  if (d->enable_friction_reduction) return fail(CP_ERR_UNSUPPORTED, "Narrowphase.enableFrictionReduction is not supported");
+  if (d->broadphase < CP_BROAD_NAIVE || d->broadphase > CP_BROAD_GRID) return fail(CP_ERR_ARG, "unknown broadphase %d", d->broadphase);
+  if (d->solver_iterations < 0) return fail(CP_ERR_ARG, "negative solver iterations");
+  const int nb = d->num_bodies, ns = d->num_shapes, nm = d->num_materials;
+  for (int i = 0; i < nb; i++) {
+    const cp_body_desc& b = d->bodies[i];
+    if (b.shape < -1 || b.shape >= ns) return fail(CP_ERR_ARG, "body %d: shape %d out of range", i, b.shape);
+    if (b.material < -1 || b.material >= nm) return fail(CP_ERR_ARG, "body %d: material out of range", i);
+    if (b.type < 0 || b.type > 2) return fail(CP_ERR_ARG, "body %d: type %d (run cp_body_setup first)", i, b.type);
+  }
+  // shapes and hulls
+  std::vector<DShape> shapes(ns);
+  std::vector<DHull> hulls;
+  std::vector<DFace> faces;
+  std::vector<float> hverts, hedges;
+  std::vector<int> hfi, hconn;
+  for (int s = 0; s < ns; s++) {
+    const cp_shape_desc& sd = d->shapes[s];
+    if (sd.material < -1 || sd.material >= nm) return fail(CP_ERR_ARG, "shape %d: material out of range", s);
+    DShape& o = shapes[s];
+    std::memset(&o, 0, sizeof(o));
+    o.type = sd.type; o.group = sd.collision_filter_group; o.mask = sd.collision_filter_mask;
+    o.response = sd.collision_response != 0; o.material = sd.material; o.hull = -1;
+    o.radius = sd.radius;
+    o.he[0] = sd.half_extents[0]; o.he[1] = sd.half_extents[1]; o.he[2] = sd.half_extents[2];
+    Hull h;
+    if (sd.type == CP_SHAPE_SPHERE || sd.type == CP_SHAPE_PLANE) {
+      if (sd.type == CP_SHAPE_SPHERE && sd.radius < 0) return fail(CP_ERR_ARG, "The sphere radius cannot be negative.");
+      o.bsr = shape_bsr(sd, nullptr);
+      continue;
+    }
+    if (sd.type != CP_SHAPE_BOX && sd.type != CP_SHAPE_CONVEX && sd.type != CP_SHAPE_CYLINDER)
+      return fail(CP_ERR_UNSUPPORTED, "shape type %d", sd.type);
+    int st = build_hull(sd, h);
+    if (st) return st;
+    o.bsr = shape_bsr(sd, &h);
+    DHull dh;
+    dh.v0 = (int)hverts.size() / 4; dh.nv = (int)h.verts.size();
+    dh.f0 = (int)faces.size(); dh.nf = (int)h.faces.size();
+    dh.e0 = (int)hedges.size() / 4; dh.ne = (int)h.edges.size();
+    dh.has_axes = h.has_axes; dh.pad = 0;
+    for (auto& v : h.verts) { hverts.push_back(v.x); hverts.push_back(v.y); hverts.push_back(v.z); hverts.push_back(0.f); }
+    for (auto& e : h.edges) { hedges.push_back(e.x); hedges.push_back(e.y); hedges.push_back(e.z); hedges.push_back(0.f); }
+    for (size_t f = 0; f < h.faces.size(); f++) {
+      DFace F;
+      std::memset(&F, 0, sizeof(F));
+      F.i0 = (int)hfi.size(); F.n = (int)h.faces[f].size();
+      for (int vi : h.faces[f]) hfi.push_back(vi);
+      // connected faces of face f in the order clipFaceAgainstHull builds them (convex_polyhedron.dart:457-473)
+      F.c0 = (int)hconn.size();
+      std::vector<int> conn;
+      for (size_t i = 0; i < h.faces.size(); i++)
+        for (int vj : h.faces[i])
+          if (std::find(h.faces[f].begin(), h.faces[f].end(), vj) != h.faces[f].end() && i != f &&
+              std::find(conn.begin(), conn.end(), (int)i) == conn.end())
+            conn.push_back((int)i);
+      for (int x : conn) hconn.push_back(x);
+      F.nc = (int)conn.size();
+      F.normal[0] = h.normals[f].x; F.normal[1] = h.normals[f].y; F.normal[2] = h.normals[f].z;
+      F.plane_const = -dot3(h.normals[f], h.verts[h.faces[f][0]]);  // getPlaneConstantOfFace
+      faces.push_back(F);
+    }
+    o.hull = (int)hulls.size();
+    hulls.push_back(dh);
+  }
+  // materials and contact material table ([0] = world default)
+  std::vector<DMaterial> mats(nm);
+  for (int i = 0; i < nm; i++) { mats[i].friction = d->materials[i].friction; mats[i].restitution = d->materials[i].restitution; }
+  std::vector<DContactMaterial> cms(1 + d->num_contact_materials);
+  auto cmOf = [](const cp_contact_material& m) {
+    DContactMaterial o;
+    std::memset(&o, 0, sizeof(o));
+    o.friction = m.friction; o.restitution = m.restitution;
+    o.cs = m.contact_stiffness; o.cr = m.contact_relaxation; o.fs = m.friction_stiffness; o.fr = m.friction_relaxation;
+    return o;
+  };
+  cms[0] = cmOf(d->default_contact_material);
+  std::vector<int> cmt((size_t)std::max(1, nm * nm), -1);
+  for (int i = 0; i < d->num_contact_materials; i++) {
+    const cp_contact_material& m = d->contact_materials[i];
+    if (m.material_a < 0 || m.material_a >= nm || m.material_b < 0 || m.material_b >= nm) return fail(CP_ERR_ARG, "contact material %d: bad materials", i);
+    cms[1 + i] = cmOf(m);
+    cmt[m.material_a * nm + m.material_b] = 1 + i;  // TupleDictionary: last set wins
+    cmt[m.material_b * nm + m.material_a] = 1 + i;
+  }
+  // constraints
+  std::vector<DConstraint> cons(d->num_constraints);
+  std::vector<int> nocollide;
+  int con_rows = 0;
+  const double cos_max = std::cos(M_PI / 2);  // RotationalEquation default maxAngle (rotational_equation.dart:203)
+  for (int k = 0; k < d->num_constraints; k++) {
+    const cp_constraint_desc& cd = d->constraints[k];
+    if (cd.body_a < 0 || cd.body_a >= nb || cd.body_b < 0 || cd.body_b >= nb) return fail(CP_ERR_ARG, "constraint %d: bad bodies", k);
+    if (cd.type < CP_CON_POINT_TO_POINT || cd.type > CP_CON_DISTANCE) return fail(CP_ERR_ARG, "constraint %d: type", k);
+    DConstraint& o = cons[k];
+    std::memset(&o, 0, sizeof(o));
+    o.type = cd.type; o.a = cd.body_a; o.b = cd.body_b; o.collide = cd.collide_connected != 0;
+    o.row0 = con_rows;
+    o.nrows = cd.type == CP_CON_DISTANCE ? 1 : (cd.type == CP_CON_HINGE ? 6 : 3);
+    o.motor = cd.motor_enabled != 0;
+    con_rows += o.nrows;
+    h3 pa = mk3(cd.pivot_a[0], cd.pivot_a[1], cd.pivot_a[2]), pb = mk3(cd.pivot_b[0], cd.pivot_b[1], cd.pivot_b[2]);
+    o.piv_a[0] = pa.x; o.piv_a[1] = pa.y; o.piv_a[2] = pa.z;
+    o.piv_b[0] = pb.x; o.piv_b[1] = pb.y; o.piv_b[2] = pb.z;
+    if (cd.type == CP_CON_HINGE) {  // HingeConstraint normalizes its axes (hinge_constraint.dart:172-176)
+      h3 aa = norm3(mk3(cd.axis_a[0], cd.axis_a[1], cd.axis_a[2])), ab = norm3(mk3(cd.axis_b[0], cd.axis_b[1], cd.axis_b[2]));
+      o.axis_a[0] = aa.x; o.axis_a[1] = aa.y; o.axis_a[2] = aa.z;
+      o.axis_b[0] = ab.x; o.axis_b[1] = ab.y; o.axis_b[2] = ab.z;
+    }
+    if (cd.type == CP_CON_DISTANCE) {
+      const float* A = d->bodies[cd.body_a].position;
+      const float* B = d->bodies[cd.body_b].position;
+      double px = B[0], py = B[1], pz = B[2];
+      o.distance = cd.distance >= 0 ? cd.distance
+                                     : std::sqrt((px - A[0]) * (px - A[0]) + (py - A[1]) * (py - A[1]) + (pz - A[2]) * (pz - A[2]));
+    }
+    o.max_force = cd.max_force;
+    o.motor_target = cd.motor_target_velocity;
+    o.motor_max_force = cd.motor_max_force > 0 ? cd.motor_max_force : cd.max_force;
+    spook(cd.spook_stiffness, cd.spook_relaxation, cd.spook_time_step, o.sa, o.sb, o.seps);
+    o.cos_max = cos_max;
+    if (!o.collide) { nocollide.push_back(cd.body_a); nocollide.push_back(cd.body_b); }
+  }
+  // bodies
+  std::vector<DBody> bodies(nb);
+  WorldRec w;
+  w.nb = nb; w.nshapes = ns; w.nmat = nm; w.ncm = (int)cms.size(); w.ncons = d->num_constraints; w.ncon_rows = con_rows;
+  w.broadphase = d->broadphase;
+  w.lin_damp.resize(nb); w.ang_damp.resize(nb);
+  for (int i = 0; i < nb; i++) {
+    body_to_device(d->bodies[i], bodies[i]);
+    w.lin_damp[i] = d->bodies[i].linear_damping;
+    w.ang_damp[i] = d->bodies[i].angular_damping;
+  }
+  w.cms = cms;
+  // params
+  DWorldParams P;
+  std::memset(&P, 0, sizeof(P));
+  P.time = d->time; P.tolerance = d->solver_tolerance; P.dt_cached = -1; P.stepnumber = d->stepnumber;
+  for (int k = 0; k < 3; k++) {
+    P.gravity[k] = d->gravity[k]; P.fgrav[k] = d->friction_gravity[k];
+    P.grid_min[k] = d->grid_aabb_min[k]; P.grid_max[k] = d->grid_aabb_max[k];
+  }
+  P.nb = nb; P.nshapes = ns; P.nmat = nm; P.ncm = (int)cms.size();
+  P.ncons = d->num_constraints; P.ncon_rows = con_rows; P.iterations = d->solver_iterations; P.broadphase = d->broadphase;
+  P.sap_axis = d->sap_axis; P.use_bb = d->use_bounding_boxes != 0; P.allow_sleep = d->allow_sleep != 0; P.qn_skip = d->quat_normalize_skip;
+  P.qn_fast = d->quat_normalize_fast != 0; P.has_fgrav = d->has_friction_gravity != 0;
+  P.grid_nx = d->grid_n[0]; P.grid_ny = d->grid_n[1]; P.grid_nz = d->grid_n[2];
+  P.n_nocollide = (int)nocollide.size() / 2;
+  if (d->sap_axis < 0 || d->sap_axis > 2) return fail(CP_ERR_ARG, "sap_axis %d", d->sap_axis);
+  if (d->broadphase == CP_BROAD_GRID) {
+    if (P.grid_nx <= 0 || P.grid_ny <= 0 || P.grid_nz <= 0) return fail(CP_ERR_ARG, "GridBroadphase: Each dimension's n must be >0");
+    if (P.grid_nx + P.grid_ny + P.grid_nz > 3 * 4096 || (long long)P.grid_nx * P.grid_ny * P.grid_nz > (1 << 26))
+      return fail(CP_ERR_UNSUPPORTED, "grid too large");
+    w.nbins = P.grid_nx * P.grid_ny * P.grid_nz;
+  }
+  P.nbins = w.nbins;
+  // capacities (grown on overflow)
+  long long allpairs = (long long)nb * (nb - 1) / 2;
+  w.pairs_cap = (int)std::max<long long>(16, std::min<long long>(allpairs, 4LL * nb + 64));
+  w.contacts_cap = 2 * w.pairs_cap + 64;
+  w.rows_cap = 3 * w.contacts_cap + con_rows + 64;
+  w.bins_cap = 4 * nb + (d->broadphase == CP_BROAD_GRID ? w.nbins : 0) + 64;
+  P.pairs_cap = w.pairs_cap; P.contacts_cap = w.contacts_cap; P.rows_cap = w.rows_cap; P.bins_cap = w.bins_cap;
+  // state allocation
+  Layout L;
+  size_t o_P = L.take(sizeof(DWorldParams));
+  size_t o_b = L.take(sizeof(DBody) * (nb + 1));
+  size_t o_s = L.take(sizeof(DShape) * (ns + 1));
+  size_t o_h = L.take(sizeof(DHull) * (hulls.size() + 1));
+  size_t o_f = L.take(sizeof(DFace) * (faces.size() + 1));
+  size_t o_hv = L.take(sizeof(float) * (hverts.size() + 4));
+  size_t o_he = L.take(sizeof(float) * (hedges.size() + 4));
+  size_t o_hfi = L.take(sizeof(int) * (hfi.size() + 1));
+  size_t o_hc = L.take(sizeof(int) * (hconn.size() + 1));
+  size_t o_m = L.take(sizeof(DMaterial) * (nm + 1));
+  size_t o_ct = L.take(sizeof(int) * cmt.size());
+  size_t o_cm = L.take(sizeof(DContactMaterial) * cms.size());
+  size_t o_cn = L.take(sizeof(DConstraint) * (cons.size() + 1));
+  size_t o_nc = L.take(sizeof(int) * (nocollide.size() + 2));
+  size_t o_dp = L.take(sizeof(double) * (2 * nb + 2));
+  size_t o_so = L.take(sizeof(int) * (nb + 1));
+  std::vector<char> host(L.off, 0);
+  std::memcpy(&host[o_P], &P, sizeof(P));
+  if (nb) std::memcpy(&host[o_b], bodies.data(), sizeof(DBody) * nb);
+  if (ns) std::memcpy(&host[o_s], shapes.data(), sizeof(DShape) * ns);
+  if (!hulls.empty()) std::memcpy(&host[o_h], hulls.data(), sizeof(DHull) * hulls.size());
+  if (!faces.empty()) std::memcpy(&host[o_f], faces.data(), sizeof(DFace) * faces.size());
+  if (!hverts.empty()) std::memcpy(&host[o_hv], hverts.data(), sizeof(float) * hverts.size());
+  if (!hedges.empty()) std::memcpy(&host[o_he], hedges.data(), sizeof(float) * hedges.size());
+  if (!hfi.empty()) std::memcpy(&host[o_hfi], hfi.data(), sizeof(int) * hfi.size());
+  if (!hconn.empty()) std::memcpy(&host[o_hc], hconn.data(), sizeof(int) * hconn.size());
+  if (nm) std::memcpy(&host[o_m], mats.data(), sizeof(DMaterial) * nm);
+  std::memcpy(&host[o_ct], cmt.data(), sizeof(int) * cmt.size());
+  std::memcpy(&host[o_cm], cms.data(), sizeof(DContactMaterial) * cms.size());
+  if (!cons.empty()) std::memcpy(&host[o_cn], cons.data(), sizeof(DConstraint) * cons.size());
+  if (!nocollide.empty()) std::memcpy(&host[o_nc], nocollide.data(), sizeof(int) * nocollide.size());
+  std::vector<int> order(nb);
+  for (int i = 0; i < nb; i++) {
+    order[i] = d->sap_axis_list ? d->sap_axis_list[i] : i;
+    if (order[i] < 0 || order[i] >= nb) return fail(CP_ERR_ARG, "sap_axis_list[%d] out of range", i);
+  }
+  if (nb) std::memcpy(&host[o_so], order.data(), sizeof(int) * nb);
+  cudaError_t e = cudaMalloc(&w.state, L.off);
+  if (e != cudaSuccess) return fail(CP_ERR_OOM, "world allocation of %zu bytes failed: %s", L.off, cudaGetErrorString(e));
+  e = cudaMemcpy(w.state, host.data(), L.off, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(w.state); return fail(CP_ERR_CUDA, "world upload: %s", cudaGetErrorString(e)); }
+  char* base = w.state;
+  DWorld& dw = w.dw;
+  std::memset(&dw, 0, sizeof(dw));
+  dw.P = (DWorldParams*)(base + o_P);
+  dw.bodies = (DBody*)(base + o_b);
+  dw.shapes = (DShape*)(base + o_s);
+  dw.hulls = (DHull*)(base + o_h);
+  dw.faces = (DFace*)(base + o_f);
+  dw.hverts = (float*)(base + o_hv);
+  dw.hedges = (float*)(base + o_he);
+  dw.haxes = nullptr;
+  dw.hfi = (int*)(base + o_hfi);
+  dw.hconn = (int*)(base + o_hc);
+  dw.mats = (DMaterial*)(base + o_m);
+  dw.cm_table = (int*)(base + o_ct);
+  dw.cms = (DContactMaterial*)(base + o_cm);
+  dw.cons = (DConstraint*)(base + o_cn);
+  dw.nocollide = (int*)(base + o_nc);
+  dw.dpow = (double*)(base + o_dp);
+  dw.sap_order = (int*)(base + o_so);
+  int st = alloc_scratch(w);
+  if (st) { cudaFree(w.state); return st; }
+  w.live = true;
+  int id = -1;
+  for (size_t i = 0; i < c->worlds.size(); i++)
+    if (!c->worlds[i].live) { id = (int)i; break; }
+  if (id < 0) { id = (int)c->worlds.size(); c->worlds.emplace_back(); }
+  c->worlds[id] = std::move(w);
+  st = upload_world_entry(c, id);
+  if (st) return st;
+  *world_id = id;
+  return CP_OK;
+}
+
+int cp_world_destroy(cp_ctx* c, int32_t id) {
+  int st = check_world(c, id);
+  if (st) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  WorldRec& w = c->worlds[id];
+  if (w.state) cudaFree(w.state);
+  if (w.scratch) cudaFree(w.scratch);
+  w = WorldRec();
+  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  return CP_OK;
+}
+
+int cp_world_step(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
+  int st = check_world(c, id);
+  if (st) return st;
+  if (nsteps < 0 || !(dt > 0)) return fail(CP_ERR_ARG, "need dt > 0 and nsteps >= 0");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  return plain_steps(c, id, dt, nsteps);
+}
+
+int cp_world_get_bodies(cp_ctx* c, int32_t id, cp_body_desc* out, int32_t n) {
+  int st = check_world(c, id);
+  if (st) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  WorldRec& w = c->worlds[id];
+  if (!out || n != w.nb) return fail(CP_ERR_ARG, "expected %d bodies", w.nb);
+  std::vector<DBody> b(w.nb);
+  CUDA_TRY(cudaMemcpyAsync(b.data(), w.dw.bodies, sizeof(DBody) * w.nb, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < w.nb; i++) body_from_device(b[i], out[i]);
+  return CP_OK;
+}
+
+int cp_world_set_bodies(cp_ctx* c, int32_t id, const cp_body_desc* in, int32_t n) {
+  int st = check_world(c, id);
+  if (st) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  WorldRec& w = c->worlds[id];
+  if (!in || n != w.nb) return fail(CP_ERR_ARG, "expected %d bodies", w.nb);
+  std::vector<DBody> b(w.nb);
+  for (int i = 0; i < w.nb; i++) {
+    if (in[i].shape < -1 || in[i].shape >= w.nshapes) return fail(CP_ERR_ARG, "body %d: shape out of range", i);
+    body_to_device(in[i], b[i]);
+    w.lin_damp[i] = in[i].linear_damping;
+    w.ang_damp[i] = in[i].angular_damping;
+  }
+  CUDA_TRY(cudaMemcpyAsync(w.dw.bodies, b.data(), sizeof(DBody) * w.nb, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  w.dt_cached = -1.0;
+  return CP_OK;
+}
+
+int cp_world_get_info(cp_ctx* c, int32_t id, cp_step_info* out) {
+  int st = check_world(c, id);
+  if (st) return st;
+  if (!out) return fail(CP_ERR_ARG, "null out");
+  std::lock_guard<std::mutex> lock(c->mu);
+  DWorldParams p;
+  st = read_params(c, c->worlds[id], p);
+  if (st) return st;
+  std::memset(out, 0, sizeof(*out));
+  out->stepnumber = p.stepnumber;
+  out->time = p.time;
+  out->num_pairs = p.num_pairs;
+  out->num_contacts = p.num_contacts;
+  out->num_rows = p.num_rows;
+  out->iterations = p.last_iterations;
+  out->status = p.status;
+  out->num_bodies = p.nb;
+  return CP_OK;
+}
+
+int cp_world_get_pairs(cp_ctx* c, int32_t id, int32_t* p1, int32_t* p2, int32_t cap, int32_t* count) {
+  int st = check_world(c, id);
+  if (st) return st;
+  if (!count) return fail(CP_ERR_ARG, "null count");
+  std::lock_guard<std::mutex> lock(c->mu);
+  WorldRec& w = c->worlds[id];
+  DWorldParams p;
+  st = read_params(c, w, p);
+  if (st) return st;
+  *count = p.num_pairs;
+  if (p.num_pairs > cap || (p.num_pairs && (!p1 || !p2))) return fail(CP_ERR_CAPACITY, "need room for %d pairs", p.num_pairs);
+  if (p.num_pairs) {
+    CUDA_TRY(cudaMemcpy(p1, w.dw.pair_a, sizeof(int) * p.num_pairs, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(p2, w.dw.pair_b, sizeof(int) * p.num_pairs, cudaMemcpyDeviceToHost));
+  }
+  return CP_OK;
+}
+
+int cp_world_get_contacts(cp_ctx* c, int32_t id, cp_contact* out, int32_t cap, int32_t* count) {
+  int st = check_world(c, id);
+  if (st) return st;
+  if (!count) return fail(CP_ERR_ARG, "null count");
+  std::lock_guard<std::mutex> lock(c->mu);
+  WorldRec& w = c->worlds[id];
+  DWorldParams p;
+  st = read_params(c, w, p);
+  if (st) return st;
+  *count = p.num_contacts;
+  if (p.num_contacts > cap || (p.num_contacts && !out)) return fail(CP_ERR_CAPACITY, "need room for %d contacts", p.num_contacts);
+  std::vector<DContact> v(p.num_contacts);
+  if (p.num_contacts) CUDA_TRY(cudaMemcpy(v.data(), w.dw.contacts, sizeof(DContact) * v.size(), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < p.num_contacts; i++) {
+    cp_contact& o = out[i];
+    o.bi = v[i].bi; o.bj = v[i].bj; o.si = v[i].si; o.sj = v[i].sj;
+    std::memcpy(o.ni, v[i].ni, 12); std::memcpy(o.ri, v[i].ri, 12); std::memcpy(o.rj, v[i].rj, 12);
+    o.enabled = v[i].enabled; o.pair = v[i].pair; o.restitution = v[i].restitution;
+  }
+  return CP_OK;
+}
+
+int cp_world_get_rows(cp_ctx* c, int32_t id, cp_row* out, int32_t cap, int32_t* count) {
+  int st = check_world(c, id);
+  if (st) return st;
+  if (!count) return fail(CP_ERR_ARG, "null count");
+  std::lock_guard<std::mutex> lock(c->mu);
+  WorldRec& w = c->worlds[id];
+  DWorldParams p;
+  st = read_params(c, w, p);
+  if (st) return st;
+  *count = p.num_rows;
+  if (p.num_rows > cap || (p.num_rows && !out)) return fail(CP_ERR_CAPACITY, "need room for %d rows", p.num_rows);
+  std::vector<DRow> v(p.num_rows);
+  if (p.num_rows) CUDA_TRY(cudaMemcpy(v.data(), w.dw.rows, sizeof(DRow) * v.size(), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < p.num_rows; i++) {
+    cp_row& o = out[i];
+    o.kind = v[i].kind; o.bi = v[i].bi; o.bj = v[i].bj; o.pad = 0;
+    o.B = v[i].B; o.inv_c = v[i].invC; o.lambda = v[i].lambda; o.multiplier = v[i].mult;
+    o.min_force = v[i].minF; o.max_force = v[i].maxF; o.eps = v[i].eps;
+  }
+  return CP_OK;
+}
+
+int cp_world_get_sap_order(cp_ctx* c, int32_t id, int32_t* out, int32_t n) {
+  int st = check_world(c, id);
+  if (st) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  WorldRec& w = c->worlds[id];
+  if (!out || n != w.nb) return fail(CP_ERR_ARG, "expected %d entries", w.nb);
+  CUDA_TRY(cudaMemcpy(out, w.dw.sap_order, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  return CP_OK;
+}
+
+int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t nsteps) {
+  if (!c || (n > 0 && !ids) || n < 0 || nsteps < 0 || !(dt > 0)) return fail(CP_ERR_ARG, "bad arguments");
+  if (n == 0 || nsteps == 0) return CP_OK;
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  for (int i = 0; i < n; i++) {
+    if (ids[i] < 0 || ids[i] >= (int)c->worlds.size() || !c->worlds[ids[i]].live) return fail(CP_ERR_ARG, "no world %d", ids[i]);
+    int st = ensure_dt(c, c->worlds[ids[i]], dt);
+    if (st) return st;
+  }
+  // largest worlds first: the persistent blocks take them from the queue in this order
+  std::vector<int> order(ids, ids + n);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return c->worlds[a].nb > c->worlds[b].nb; });
+  int st = ensure_ids(c, n);
+  if (st) return st;
+  const int grid = std::max(1, std::min(n, c->sms * c->blocks_per_sm));
+  bool reuse = c->graph && c->graph_ids == order && c->graph_dt == dt && c->graph_steps == nsteps;
+  CUDA_TRY(cudaMemcpyAsync(c->d_ids, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+  if (!reuse) {
+    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    cudaGraph_t g;
+    CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < nsteps; s++) {
+      cudaError_t e = cpk_launch_step(c->d_worlds, c->d_ids, n, dt, c->d_queue, grid, c->stream);
+      if (e != cudaSuccess) {
+        cudaStreamEndCapture(c->stream, &g);
+        return fail(CP_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
+      }
+    }
+    CUDA_TRY(cudaStreamEndCapture(c->stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(CP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    c->graph_ids = order;
+    c->graph_dt = dt;
+    c->graph_steps = nsteps;
+  }
+  // step numbers before the launch, to finish worlds whose step overflowed
+  CUDA_TRY(cpk_gather_status(c->d_worlds, c->d_ids, n, c->d_status, c->stream));
+  std::vector<long long> before(4 * (size_t)n), after(4 * (size_t)n);
+  CUDA_TRY(cudaMemcpyAsync(before.data(), c->d_status, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaGraphLaunch(c->graph, c->stream));
+  c->launches += 2LL * nsteps + 1;
+  CUDA_TRY(cpk_gather_status(c->d_worlds, c->d_ids, n, c->d_status, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(after.data(), c->d_status, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->launches += 1;
+  for (int i = 0; i < n; i++) {
+    if (after[4 * i] != 0) {  // overflowed part way: grow and finish on the plain path
+      int id = order[i];
+      long long left = before[4 * i + 1] + nsteps - after[4 * i + 1];
+      st = grow(c, id, (int)after[4 * i]);
+      if (st) return st;
+      st = plain_steps(c, id, dt, (int)left);
+      if (st) return st;
+    }
+  }
+  return CP_OK;
+}
+
+int64_t cp_kernel_launches(cp_ctx* c) { return c ? c->launches : 0; }
+
+}  // extern "C"

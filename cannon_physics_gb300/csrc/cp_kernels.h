@@ -1,0 +1,17 @@
+// cp_kernels.h -- launch entry points of the step kernels (cp_step.cu),
+// called by the host runtime (cp_host.cpp).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "cp_types.h"
+
+int cpk_block_threads();
+int cpk_max_resident_blocks();
+// One World.step for each of the n worlds ids[0..n) of the world table, by a
+// persistent grid of `grid` blocks pulling worlds from *d_queue.
+cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, int n, double dt, int* d_queue, int grid,
+                            cudaStream_t stream);
+// status, stepnumber and counts of the listed worlds, gathered into out[4*i..]
+cudaError_t cpk_gather_status(const DWorld* d_worlds, const int* d_ids, int n, long long* d_out, cudaStream_t stream);
+// clear the status of the listed worlds
+cudaError_t cpk_clear_status(const DWorld* d_worlds, const int* d_ids, int n, cudaStream_t stream);

@@ -1,0 +1,527 @@
+// cp_narrow.cuh -- narrowphase resolvers (lib/world/narrow_phase.dart and
+// lib/rigid_body_shapes/convex_polyhedron.dart), one thread per body pair.
+//
+// A resolver computes the contacts of one pair into registers / local memory,
+// counts them, reserves that many slots in the world's contact staging area
+// with one shared-memory atomic, and writes them.  The caller records
+// (count, first slot) per pair; a block scan over the counts then puts every
+// contact at the place the reference appends it (pair order, then resolver
+// order).
+#pragma once
+#include "cp_math.cuh"
+#include "cp_types.h"
+
+struct NarrowCtx {
+  const DWorld* W;
+  int* cursor;     // shared-memory slot cursor of the staging area
+  int cap;
+  int* overflow;   // shared flag
+  int cm;          // contact material index (currentContactMaterial)
+  int pair;
+};
+
+struct ContactOut {
+  f3 ni, ri, rj;
+};
+
+// narrow_phase.dart:492-528 createContactEquation: everything except the
+// geometry.  shA/shB are the shapes handed to the resolver (type order),
+// rsi/rsj the shapes ContactEquation.si/.sj end up holding.
+DI void fill_contact(const NarrowCtx& C, DContact& c, int bA, int bB, int shA, int shB, int rsi, int rsj, const ContactOut& g) {
+  const DWorld& W = *C.W;
+  const DBody& A = W.bodies[bA];
+  const DBody& B = W.bodies[bB];
+  const DShape& SA = W.shapes[shA];
+  const DShape& SB = W.shapes[shB];
+  c.bi = bA; c.bj = bB; c.si = rsi; c.sj = rsj;
+  st3(c.ni, g.ni); st3(c.ri, g.ri); st3(c.rj, g.rj);
+  c.enabled = (A.flags & BF_RESPONSE) && (B.flags & BF_RESPONSE) && SA.response && SB.response;
+  c.pair = C.pair;
+  c.cm = C.cm;
+  c.frow = -1;
+  c.slip = 0.0;
+  double rest = W.cms[C.cm].restitution;
+  int ma = SA.material >= 0 ? SA.material : A.material;
+  int mb = SB.material >= 0 ? SB.material : B.material;
+  if (ma >= 0 && mb >= 0 && W.mats[ma].restitution >= 0 && W.mats[mb].restitution >= 0)
+    rest = W.mats[ma].restitution * W.mats[mb].restitution;
+  c.restitution = rest;
+}
+
+DI int reserve(const NarrowCtx& C, int n) {
+  if (n == 0) return 0;
+  int s = atomicAdd(C.cursor, n);
+  if (s + n > C.cap) { atomicOr(C.overflow, ST_CONTACTS_OVERFLOW); return -1; }
+  return s;
+}
+
+// "Make it relative to the body": r += x - body.position
+DI f3 rel(f3 r, f3 x, const DBody& b) { return sub(add(r, x), ld3(b.pos)); }
+
+// narrow_phase.dart:723-765
+DI int sphere_sphere(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, int& start) {
+  const DWorld& W = *C.W;
+  ContactOut g;
+  g.ni = normalized(sub(xB, xA));
+  g.ri = scale(g.ni, W.shapes[shA].radius);
+  g.rj = scale(g.ni, -W.shapes[shB].radius);
+  g.ri = rel(g.ri, xA, W.bodies[bA]);
+  g.rj = rel(g.rj, xB, W.bodies[bB]);
+  start = reserve(C, 1);
+  if (start >= 0) fill_contact(C, W.ctmp[start], bA, bB, shA, shB, rsi, rsj, g);
+  return 1;
+}
+
+// narrow_phase.dart:766-815
+DI int sphere_plane(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
+  const DWorld& W = *C.W;
+  double R = W.shapes[shA].radius;
+  ContactOut g;
+  g.ni = normalized(neg(vmult(qB, f3{0.f, 0.f, 1.f})));
+  g.ri = scale(g.ni, R);
+  f3 pops = sub(xA, xB);
+  f3 ortho = scale(g.ni, dot(g.ni, pops));
+  g.rj = sub(pops, ortho);
+  if (!(-dot(pops, g.ni) <= R)) return 0;
+  g.ri = rel(g.ri, xA, W.bodies[bA]);
+  g.rj = rel(g.rj, xB, W.bodies[bB]);
+  start = reserve(C, 1);
+  if (start >= 0) fill_contact(C, W.ctmp[start], bA, bB, shA, shB, rsi, rsj, g);
+  return 1;
+}
+
+// narrow_phase.dart:816-1038 (box.dart:99-115 for the side vectors)
+DI int sphere_box(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
+  const DWorld& W = *C.W;
+  const DShape& sb = W.shapes[shB];
+  double R = W.shapes[shA].radius;
+  f3 sides[6];
+  sides[0] = vmult(qB, f3{sb.he[0], 0.f, 0.f});
+  sides[1] = vmult(qB, f3{0.f, sb.he[1], 0.f});
+  sides[2] = vmult(qB, f3{0.f, 0.f, sb.he[2]});
+  sides[3] = vmult(qB, f3{-sb.he[0], 0.f, 0.f});
+  sides[4] = vmult(qB, f3{0.f, -sb.he[1], 0.f});
+  sides[5] = vmult(qB, f3{0.f, 0.f, -sb.he[2]});
+  f3 b2s = sub(xA, xB);
+  f3 sideNs{0, 0, 0}, sideNs1{0, 0, 0}, sideNs2{0, 0, 0};
+  double sideH = 0, sideDot1 = 0, sideDot2 = 0, sideDist = 0;
+  bool haveDist = false;
+  int sidePen = 0;
+  for (int idx = 0; idx < 6; idx++) {
+    f3 ns = sides[idx];
+    double h = length(ns);
+    ns = normalized(ns);
+    double d = dot(b2s, ns);
+    if (d < h + R && d > 0) {
+      f3 ns1 = sides[(idx + 1) % 3], ns2 = sides[(idx + 2) % 3];
+      double h1 = length(ns1), h2 = length(ns2);
+      ns1 = normalized(ns1);
+      ns2 = normalized(ns2);
+      double d1 = dot(b2s, ns1), d2 = dot(b2s, ns2);
+      if (d1 < h1 && d1 > -h1 && d2 < h2 && d2 > -h2) {
+        double dist = fabs(d - h - R);
+        if (!haveDist || dist < sideDist) {
+          haveDist = true;
+          sideDist = dist; sideDot1 = d1; sideDot2 = d2; sideH = h;
+          sideNs = ns; sideNs1 = ns1; sideNs2 = ns2;
+          sidePen++;
+        }
+      }
+    }
+  }
+  ContactOut g;
+  bool found = false;
+  if (sidePen != 0) {
+    found = true;
+    g.ri = scale(sideNs, -R);
+    g.ni = neg(sideNs);
+    f3 t = scale(sideNs, sideH);
+    f3 t1 = scale(sideNs1, sideDot1);
+    t = add(t, t1);
+    f3 t2 = scale(sideNs2, sideDot2);
+    g.rj = add(t, t2);
+  }
+  for (int j = 0; j != 2 && !found; j++)
+    for (int k = 0; k != 2 && !found; k++)
+      for (int l = 0; l != 2 && !found; l++) {
+        f3 rj{0.f, 0.f, 0.f};
+        rj = j != 0 ? add(rj, sides[0]) : sub(rj, sides[0]);
+        rj = k != 0 ? add(rj, sides[1]) : sub(rj, sides[1]);
+        rj = l != 0 ? add(rj, sides[2]) : sub(rj, sides[2]);
+        f3 s2c = sub(add(xB, rj), xA);
+        if (length2(s2c) < R * R) {
+          found = true;
+          g.ri = normalized(s2c);
+          g.ni = g.ri;
+          g.ri = scale(g.ri, R);
+          g.rj = rj;
+        }
+      }
+  for (int j = 0; j != 6 && !found; j++)
+    for (int k = 0; k != 6 && !found; k++) {
+      if (j % 3 != k % 3) {
+        f3 edgeTangent = normalized(cross(sides[k], sides[j]));
+        f3 edgeCenter = add(sides[j], sides[k]);
+        f3 r = sub(sub(xA, edgeCenter), xB);
+        double orthonorm = dot(r, edgeTangent);
+        f3 orthogonal = scale(edgeTangent, orthonorm);
+        int l = 0;
+        while (l == j % 3 || l == k % 3) l++;
+        f3 dist = sub(sub(sub(xA, orthogonal), edgeCenter), xB);
+        double tdist = fabs(orthonorm);
+        double ndist = length(dist);
+        if (tdist < length(sides[l]) && ndist < R) {
+          found = true;
+          g.rj = add(edgeCenter, orthogonal);
+          g.ni = normalized(neg(dist));
+          f3 ri = sub(add(g.rj, xB), xA);
+          g.ri = scale(normalized(ri), R);
+        }
+      }
+    }
+  if (!found) return 0;
+  g.ri = rel(g.ri, xA, W.bodies[bA]);
+  g.rj = rel(g.rj, xB, W.bodies[bB]);
+  start = reserve(C, 1);
+  if (start >= 0) fill_contact(C, W.ctmp[start], bA, bB, shA, shB, rsi, rsj, g);
+  return 1;
+}
+
+// narrow_phase.dart:2584-2617
+DI bool point_in_polygon(const f3* verts, int N, f3 normal, f3 p) {
+  int state = -1;
+  for (int i = 0; i != N; i++) {
+    f3 v = verts[i];
+    f3 edge = sub(verts[(i + 1) % N], v);
+    f3 exn = cross(edge, normal);
+    f3 vtp = sub(p, v);
+    double r = dot(exn, vtp);
+    if (state == -1 || (r > 0 && state == 1) || (r <= 0 && state == 0)) {
+      if (state == -1) state = r > 0 ? 1 : 0;
+      continue;
+    }
+    return false;
+  }
+  return true;
+}
+
+DI f3 hv(const DWorld& W, int i) { return ld3(W.hverts + 4 * i); }
+
+// narrow_phase.dart:1039-1257
+DI int sphere_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
+  const DWorld& W = *C.W;
+  const DHull H = W.hulls[W.shapes[shB].hull];
+  double R = W.shapes[shA].radius;
+  ContactOut g;
+  bool got = false;
+  for (int i = 0; i < H.nv && !got; i++) {
+    f3 wc = add(vmult(qB, hv(W, H.v0 + i)), xB);
+    f3 s2c = sub(wc, xA);
+    if (length2(s2c) < R * R) {
+      g.ri = normalized(s2c);
+      g.ni = g.ri;
+      g.ri = scale(g.ri, R);
+      g.rj = sub(wc, xB);
+      got = true;
+    }
+  }
+  for (int i = 0; i < H.nf && !got; i++) {
+    const DFace F = W.faces[H.f0 + i];
+    f3 wn = vmult(qB, ld3(F.normal));
+    f3 wp = add(vmult(qB, hv(W, H.v0 + W.hfi[F.i0])), xB);
+    f3 wsp = add(xA, scale(wn, -R));
+    f3 pv = sub(wsp, wp);
+    double pen = dot(pv, wn);
+    f3 wp2s = sub(xA, wp);
+    if (pen < 0 && dot(wp2s, wn) > 0) {
+      f3 fv[CP_MAX_FACE_VERTS];
+      if (F.n > CP_MAX_FACE_VERTS) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
+      int nfv = F.n;
+      for (int j = 0; j < nfv; j++) fv[j] = add(vmult(qB, hv(W, H.v0 + W.hfi[F.i0 + j])), xB);
+      if (point_in_polygon(fv, nfv, wn, xA)) {
+        g.ri = scale(wn, -R);
+        g.ni = neg(wn);
+        f3 pv2 = scale(wn, -pen);
+        f3 psp = scale(wn, -R);
+        f3 rj = sub(xA, xB);
+        rj = add(rj, psp);
+        rj = add(rj, pv2);
+        g.rj = rj;
+        got = true;
+      } else {
+        for (int j = 0; j < nfv && !got; j++) {
+          f3 v1 = add(vmult(qB, hv(W, H.v0 + W.hfi[F.i0 + (j + 1) % nfv])), xB);
+          f3 v2 = add(vmult(qB, hv(W, H.v0 + W.hfi[F.i0 + (j + 2) % nfv])), xB);
+          f3 edge = sub(v2, v1);
+          f3 eu = unit(edge);
+          f3 v1x = sub(xA, v1);
+          double d = dot(v1x, eu);
+          f3 p = add(scale(eu, d), v1);
+          f3 x2p = sub(p, xA);
+          if (d > 0 && d * d < length2(edge) && length2(x2p) < R * R) {
+            g.rj = sub(p, xB);
+            g.ni = normalized(sub(p, xA));
+            g.ri = scale(g.ni, R);
+            got = true;
+          }
+        }
+      }
+    }
+  }
+  if (!got) return 0;
+  g.ri = rel(g.ri, xA, W.bodies[bA]);
+  g.rj = rel(g.rj, xB, W.bodies[bB]);
+  start = reserve(C, 1);
+  if (start >= 0) fill_contact(C, W.ctmp[start], bA, bB, shA, shB, rsi, rsj, g);
+  return 1;
+}
+
+// narrow_phase.dart:1847-1915 (planeBox forwards here with its own shapes)
+DI int plane_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qA, q4 qB, int& start) {
+  const DWorld& W = *C.W;
+  const DHull H = W.hulls[W.shapes[shB].hull];
+  f3 wn = vmult(qA, f3{0.f, 0.f, 1.f});
+  f3 wv[CP_MAX_HULL_VERTS];
+  double dv[CP_MAX_HULL_VERTS];
+  int n = 0;
+  if (H.nv > CP_MAX_HULL_VERTS) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
+  int nv = H.nv;
+  for (int i = 0; i < nv; i++) {
+    wv[i] = add(vmult(qB, hv(W, H.v0 + i)), xB);
+    f3 relpos = sub(wv[i], xA);
+    dv[i] = dot(wn, relpos);
+    if (dv[i] <= 0.0) n++;
+  }
+  if (n == 0) return 0;
+  start = reserve(C, n);
+  if (start < 0) return n;
+  const DBody& BA = W.bodies[bA];
+  const DBody& BB = W.bodies[bB];
+  int k = 0;
+  for (int i = 0; i < nv; i++) {
+    if (dv[i] <= 0.0) {
+      ContactOut g;
+      f3 proj = sub(wv[i], scale(wn, dv[i]));
+      g.ri = sub(proj, xA);
+      g.ni = wn;
+      g.rj = sub(wv[i], xB);
+      g.ri = rel(g.ri, xA, BA);
+      g.rj = rel(g.rj, xB, BB);
+      fill_contact(C, W.ctmp[start + k], bA, bB, shA, shB, rsi, rsj, g);
+      k++;
+    }
+  }
+  return n;
+}
+
+// ---- convex-convex (convex_polyhedron.dart:189-587,843-883) ----
+
+struct HullPose {
+  DHull H;
+  f3 x;
+  q4 q;
+  f3 origin;  // Transform.pointToLocalFrame(pos, quat, 0): the same for every axis
+};
+
+// ConvexPolyhedron.project
+DI void project(const DWorld& W, const HullPose& h, f3 axis, double& mx, double& mn) {
+  f3 la = vector_to_local(h.q, axis);
+  double addv = dot(h.origin, la);
+  double max = dot(hv(W, h.H.v0), la), min = max;
+  for (int i = 1; i < h.H.nv; i++) {
+    double v = dot(hv(W, h.H.v0 + i), la);
+    if (v > max) max = v;
+    if (v < min) min = v;
+  }
+  min -= addv;
+  max -= addv;
+  if (min > max) { double t = min; min = max; max = t; }
+  mx = max;
+  mn = min;
+}
+
+// testSepAxis; false when the hulls are separated along `axis`
+DI bool test_sep_axis(const DWorld& W, const HullPose& A, const HullPose& B, f3 axis, double& depth) {
+  double maxA, minA, maxB, minB;
+  project(W, A, axis, maxA, minA);
+  project(W, B, axis, maxB, minB);
+  if (maxA < minB || maxB < minA) return false;
+  double d0 = maxA - minB, d1 = maxB - minA;
+  depth = d0 < d1 ? d0 : d1;
+  return true;
+}
+
+// findSeparatingAxis: face normals of A (when A has uniqueAxes), face normals
+// of B (when B has uniqueAxes), then every edge-pair cross product; the first
+// smallest depth wins; the axis is flipped to point from B towards A.
+DI bool find_separating_axis(const DWorld& W, const HullPose& A, const HullPose& B, const f3* wnA, const f3* wnB, f3& target) {
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  double d;
+  if (A.H.has_axes)
+    for (int i = 0; i < A.H.nf; i++) {
+      if (!test_sep_axis(W, A, B, wnA[i], d)) return false;
+      if (d < dmin) { dmin = d; target = wnA[i]; }
+    }
+  if (B.H.has_axes)
+    for (int i = 0; i < B.H.nf; i++) {
+      if (!test_sep_axis(W, A, B, wnB[i], d)) return false;
+      if (d < dmin) { dmin = d; target = wnB[i]; }
+    }
+  f3 weB[CP_MAX_HULL_VERTS];
+  int neB = B.H.ne;
+  for (int e1 = 0; e1 < neB; e1++) weB[e1] = vmult(B.q, ld3(W.hedges + 4 * (B.H.e0 + e1)));
+  for (int e0 = 0; e0 < A.H.ne; e0++) {
+    f3 we0 = vmult(A.q, ld3(W.hedges + 4 * (A.H.e0 + e0)));
+    for (int e1 = 0; e1 < neB; e1++) {
+      f3 cr = cross(we0, weB[e1]);
+      if (!almost_zero(cr)) {
+        cr = normalized(cr);
+        if (!test_sep_axis(W, A, B, cr, d)) return false;
+        if (d < dmin) { dmin = d; target = cr; }
+      }
+    }
+  }
+  f3 deltaC = sub(B.x, A.x);
+  if (dot(deltaC, target) > 0.0) target = neg(target);
+  return true;
+}
+
+// clipFaceAgainstPlane
+DI int clip_face_against_plane(const f3* in, int nin, f3* out, f3 n, double c) {
+  if (nin < 2) return 0;
+  int nout = 0;
+  f3 first = in[nin - 1];
+  double nDotFirst = dot(n, first) + c;
+  for (int vi = 0; vi < nin; vi++) {
+    f3 last = in[vi];
+    double nDotLast = dot(n, last) + c;
+    if (nDotFirst < 0) {
+      if (nDotLast < 0) {
+        if (nout < CP_MAX_CLIP) out[nout] = last;
+        nout++;
+      } else {
+        if (nout < CP_MAX_CLIP) out[nout] = lerp(first, last, nDotFirst / (nDotFirst - nDotLast));
+        nout++;
+      }
+    } else if (nDotLast < 0) {
+      if (nout < CP_MAX_CLIP) out[nout] = lerp(first, last, nDotFirst / (nDotFirst - nDotLast));
+      nout++;
+      if (nout < CP_MAX_CLIP) out[nout] = last;
+      nout++;
+    }
+    first = last;
+    nDotFirst = nDotLast;
+  }
+  return nout;
+}
+
+// narrow_phase.dart:1981-2043 convexConvex, with clipAgainstHull /
+// clipFaceAgainstHull (convex_polyhedron.dart:189-227,417-541)
+DI int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qA, q4 qB, int& start) {
+  const DWorld& W = *C.W;
+  const DShape& SA = W.shapes[shA];
+  const DShape& SB = W.shapes[shB];
+  if (distance_to(xA, xB) > SA.bsr + SB.bsr) return 0;
+  HullPose A, B;
+  A.H = W.hulls[SA.hull]; A.x = xA; A.q = qA; A.origin = point_to_local(xA, qA, f3{0.f, 0.f, 0.f});
+  B.H = W.hulls[SB.hull]; B.x = xB; B.q = qB; B.origin = point_to_local(xB, qB, f3{0.f, 0.f, 0.f});
+  if (A.H.nf > CP_MAX_HULL_VERTS || B.H.nf > CP_MAX_HULL_VERTS || B.H.ne > CP_MAX_HULL_VERTS) {
+    atomicOr(C.overflow, ST_HULL_OVERFLOW);
+    return 0;
+  }
+  f3 wnA[CP_MAX_HULL_VERTS], wnB[CP_MAX_HULL_VERTS];
+  for (int i = 0; i < A.H.nf; i++) wnA[i] = vmult(qA, ld3(W.faces[A.H.f0 + i].normal));
+  for (int i = 0; i < B.H.nf; i++) wnB[i] = vmult(qB, ld3(W.faces[B.H.f0 + i].normal));
+  f3 sep{0.f, 0.f, 0.f};
+  if (!find_separating_axis(W, A, B, wnA, wnB, sep)) return 0;
+  // clipAgainstHull: face of B most aligned with the axis
+  int cfb = -1;
+  double dmax = __longlong_as_double(0xfff0000000000000LL);
+  for (int f = 0; f < B.H.nf; f++) {
+    double d = dot(wnB[f], sep);
+    if (d > dmax) { dmax = d; cfb = f; }
+  }
+  if (cfb < 0) return 0;
+  f3 bufA[CP_MAX_CLIP], bufB[CP_MAX_CLIP];
+  const DFace FB = W.faces[B.H.f0 + cfb];
+  if (FB.n > CP_MAX_CLIP) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
+  int nin = FB.n;
+  for (int i = 0; i < nin; i++) bufA[i] = add(vmult(qB, hv(W, B.H.v0 + W.hfi[FB.i0 + i])), xB);
+  // clipFaceAgainstHull: face of A most anti-aligned with the axis
+  int cfa = -1;
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  for (int f = 0; f < A.H.nf; f++) {
+    double d = dot(wnA[f], sep);
+    if (d < dmin) { dmin = d; cfa = f; }
+  }
+  if (cfa < 0) return 0;
+  const DFace FA = W.faces[A.H.f0 + cfa];
+  f3* pin = bufA;
+  f3* pout = bufB;
+  for (int i = 0; i < FA.n; i++) {
+    int other = FA.nc > i ? W.hconn[FA.c0 + i] : 0;
+    const DFace FO = W.faces[A.H.f0 + other];
+    f3 pn = wnA[other];
+    double planeEqWS = FO.plane_const - dot(pn, xA);
+    int nout = clip_face_against_plane(pin, nin, pout, pn, planeEqWS);
+    if (nout > CP_MAX_CLIP) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
+    f3* t = pin; pin = pout; pout = t;
+    nin = nout;
+  }
+  f3 pn = wnA[cfa];
+  double planeEqWS = FA.plane_const - dot(pn, xA);
+  double depth[CP_MAX_CLIP];
+  int n = 0;
+  for (int i = 0; i < nin; i++) {
+    double dd = dot(pn, pin[i]) + planeEqWS;
+    if (dd <= -100.0) dd = -100.0;
+    depth[i] = dd;
+    if (dd <= 100.0 && dd <= 1e-6) n++;
+  }
+  if (n == 0) return 0;
+  start = reserve(C, n);
+  if (start < 0) return n;
+  const DBody& BA = W.bodies[bA];
+  const DBody& BB = W.bodies[bB];
+  f3 ni = neg(sep);
+  int k = 0;
+  for (int i = 0; i < nin; i++) {
+    double dd = depth[i];
+    if (dd <= 100.0 && dd <= 1e-6) {
+      ContactOut g;
+      g.ni = ni;
+      f3 q = scale(neg(pn), dd);
+      g.ri = add(pin[i], q);
+      g.rj = pin[i];
+      g.ri = sub(g.ri, xA);
+      g.rj = sub(g.rj, xB);
+      g.ri = rel(g.ri, xA, BA);
+      g.rj = rel(g.rj, xB, BB);
+      fill_contact(C, W.ctmp[start + k], bA, bB, shA, shB, rsi, rsj, g);
+      k++;
+    }
+  }
+  return n;
+}
+
+// Resolver choice of narrow_phase.dart:116-238,476-489,706-710.  The shape
+// with the lower ShapeType index goes first (for equal types the call is the
+// swapped one); (rsi, rsj) stay in getContacts order.
+enum ResolverKind { RK_NONE = 0, RK_SS, RK_SP, RK_SB, RK_SC, RK_PB, RK_PC, RK_BB, RK_BC, RK_CC };
+
+DI int resolver_kind(int ta, int tb) {  // ta <= tb
+  if (ta == 0) {
+    if (tb == 0) return RK_SS;
+    if (tb == 1) return RK_SP;
+    if (tb == 2) return RK_SB;
+    return RK_SC;
+  }
+  if (ta == 1) {
+    if (tb == 1) return RK_NONE;
+    if (tb == 2) return RK_PB;
+    return RK_PC;
+  }
+  if (ta == 2) return tb == 2 ? RK_BB : RK_BC;
+  return RK_CC;
+}
+DI bool is_heavy(int rk) { return rk >= RK_BB; }

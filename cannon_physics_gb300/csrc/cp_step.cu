@@ -1,0 +1,1327 @@
+// cp_step.cu -- one World.step (lib/world/world_class.dart:433-701) per
+// thread block, as a persistent kernel that pulls worlds from a queue.
+//
+// Phases, each a block-wide loop followed by __syncthreads():
+//   prepare      shape world transforms, AABBs the broadphase reads
+//   broadphase   Naive / SAP / Grid pair list, in the reference's order
+//   narrowphase  contacts per pair (cheap shapes first, then convex-convex),
+//                ordered by a scan over per-pair counts
+//   rows         friction rows, contact rows, constraint rows (solver.dart
+//                addEquation order and filter), wake-ups
+//   solve        GSSolver: rows grouped into dependency levels so that rows of
+//                one level touch disjoint dynamic bodies; each level runs in
+//                parallel and the per-body update sequence is the reference's
+//   integrate    damping, Body.integrate, clearForces, sleepTick
+// A capacity overflow is detected before the first write to body state; the
+// step then returns with a status bit set and the state untouched.
+#include <cuda_runtime.h>
+
+#include "cp_kernels.h"
+#include "cp_narrow.cuh"
+#include "cp_types.h"
+
+#define BT 256
+#define NWARP (BT / 32)
+
+struct __align__(16) Smem {
+  DWorld W;
+  DWorldParams P;
+  int warp[32];
+  double dwarp[32];
+  int n_pairs, n_contacts, n_heavy, n_rows;
+  int n_fric, n_cand, n_levels, cursor;
+  int overflow, converged, wi, pad;
+};
+
+// ---------------------------------------------------------------------------
+// block utilities
+
+DI int block_excl_scan(Smem& S, int v, int& total) {
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) S.warp[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < NWARP ? S.warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < NWARP) S.warp[lane] = w;
+  }
+  __syncthreads();
+  int pre = (wid > 0 ? S.warp[wid - 1] : 0) + x - v;
+  total = S.warp[NWARP - 1];
+  __syncthreads();
+  return pre;
+}
+
+// in-place exclusive scan of a[0..n); returns the total
+DI int block_scan_array(Smem& S, int* a, int n) {
+  int carry = 0;
+  for (int base = 0; base < n; base += BT * 4) {
+    int i0 = base + threadIdx.x * 4;
+    int v[4], s = 0;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      v[m] = i0 + m < n ? a[i0 + m] : 0;
+      s += v[m];
+    }
+    int tot;
+    int pre = block_excl_scan(S, s, tot);
+    int run = carry + pre;
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+      if (i0 + m < n) {
+        a[i0 + m] = run;
+        run += v[m];
+      }
+    carry += tot;
+  }
+  return carry;
+}
+
+DI double block_sum(Smem& S, double v) {
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) S.dwarp[wid] = v;
+  __syncthreads();
+  double t = 0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < NWARP; w++) t += S.dwarp[w];
+    S.dwarp[0] = t;
+  }
+  __syncthreads();
+  t = S.dwarp[0];
+  __syncthreads();
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// prepare
+
+// Shape.calculateWorldAABB (sphere.dart:146-156, plane.dart:201-226,
+// box.dart:149-192, convex_polyhedron.dart:663-703)
+DI void shape_world_aabb(const DWorld& W, const DShape& s, f3 pos, q4 q, f3& mn, f3& mx) {
+  const float INF = __int_as_float(0x7f800000);
+  if (s.type == CP_SHAPE_SPHERE) {
+    double r = s.radius;
+    mn = mkf3(pos.x - r, pos.y - r, pos.z - r);
+    mx = mkf3(pos.x + r, pos.y + r, pos.z + r);
+  } else if (s.type == CP_SHAPE_PLANE) {
+    f3 n = vmult(q, f3{0.f, 0.f, 1.f});
+    mn = f3{-INF, -INF, -INF};
+    mx = f3{INF, INF, INF};
+    if (n.x == 1) mx.x = pos.x; else if (n.x == -1) mn.x = pos.x;
+    if (n.y == 1) mx.y = pos.y; else if (n.y == -1) mn.y = pos.y;
+    if (n.z == 1) mx.z = pos.z; else if (n.z == -1) mn.z = pos.z;
+  } else if (s.type == CP_SHAPE_BOX) {
+    float ex = s.he[0], ey = s.he[1], ez = s.he[2];
+    const f3 c[8] = {{ex, ey, ez}, {-ex, ey, ez}, {-ex, -ey, ez}, {-ex, -ey, -ez},
+                     {ex, -ey, -ez}, {ex, ey, -ez}, {-ex, ey, -ez}, {ex, -ey, ez}};
+    f3 w = add(vmult(q, c[0]), pos);
+    mx = w; mn = w;
+    for (int i = 1; i < 8; i++) {
+      w = add(vmult(q, c[i]), pos);
+      if (w.x > mx.x) mx.x = w.x;
+      if (w.y > mx.y) mx.y = w.y;
+      if (w.z > mx.z) mx.z = w.z;
+      if (w.x < mn.x) mn.x = w.x;
+      if (w.y < mn.y) mn.y = w.y;
+      if (w.z < mn.z) mn.z = w.z;
+    }
+  } else {
+    const DHull H = W.hulls[s.hull];
+    f3 w = add(vmult(q, hv(W, H.v0)), pos);
+    mn = w; mx = w;
+    for (int i = 1; i < H.nv; i++) {
+      w = add(vmult(q, hv(W, H.v0 + i)), pos);
+      if (w.x < mn.x) mn.x = w.x;
+      if (w.x > mx.x) mx.x = w.x;
+      if (w.y < mn.y) mn.y = w.y;
+      if (w.y > mx.y) mx.y = w.y;
+      if (w.z < mn.z) mn.z = w.z;
+      if (w.z > mx.z) mx.z = w.z;
+    }
+  }
+}
+
+DI void ph_prepare(Smem& S) {
+  const DWorld& W = S.W;
+  const int nb = S.P.nb;
+  const int bp = S.P.broadphase;
+  const bool aabb_all = bp == CP_BROAD_SAP || (bp == CP_BROAD_NAIVE && S.P.use_bb);
+  const bool aabb_grid = bp == CP_BROAD_GRID;
+  for (int i = threadIdx.x; i < nb; i += BT) {
+    DBody& B = W.bodies[i];
+    q4 q = ld4q(B.quat);
+    f3 p = ld3(B.pos);
+    f3 xs = add(vmult(q, ld3(B.shape_off)), p);  // getContacts :671-680, updateAABB :430-434
+    q4 qs = qmul(q, ld4q(B.shape_quat));
+    st3(W.bscr[i].xs, xs);
+    st4q(W.bscr[i].qs, qs);
+    if ((B.flags & BF_AABB_DIRTY) && B.shape >= 0) {
+      const DShape s = W.shapes[B.shape];
+      if (aabb_all || (aabb_grid && s.type != CP_SHAPE_SPHERE && s.type != CP_SHAPE_PLANE)) {
+        f3 mn, mx;
+        shape_world_aabb(W, s, xs, qs, mn, mx);
+        st3(B.aabb_lo, mn);
+        st3(B.aabb_hi, mx);
+        B.flags &= ~BF_AABB_DIRTY;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// broadphase
+
+// Broadphase.needBroadphaseCollision (broadphase.dart:44-63)
+DI bool need_pair(const DBody& A, const DBody& B) {
+  if ((A.group & B.mask) == 0 || (B.group & A.mask) == 0) return false;
+  bool sa = A.type == CP_BODY_STATIC || A.sleep_state == CP_SLEEPING;
+  bool sb = B.type == CP_BODY_STATIC || B.sleep_state == CP_SLEEPING;
+  return !(sa && sb);
+}
+
+// doBoundingSphereBroadphase (broadphase.dart:77-86): |xB - xA|^2 < (rA+rB)^2
+// in binary64.  A binary32 evaluation with a relative margin settles almost
+// every pair; only pairs within the margin are evaluated in binary64.
+DI bool sphere_overlap(const DBody& A, const DBody& B) {
+  f3 r = sub(ld3(B.pos), ld3(A.pos));
+  float sf = A.brad32 + B.brad32;
+  float bf = sf * sf;
+  if (bf < 1e30f) {
+    float n2f = r.x * r.x + r.y * r.y + r.z * r.z;
+    if (n2f < bf * 0.999996f) return true;
+    if (n2f > bf * 1.000004f) return false;
+  }
+  double s = A.bounding_radius + B.bounding_radius;
+  return length2(r) < s * s;
+}
+
+// AABB.overlaps (aabb.dart:131-147)
+DI bool aabb_overlap(const DBody& A, const DBody& B) {
+  const float *l1 = A.aabb_lo, *u1 = A.aabb_hi, *l2 = B.aabb_lo, *u2 = B.aabb_hi;
+  bool ox = (l2[0] <= u1[0] && u1[0] <= u2[0]) || (l1[0] <= u2[0] && u2[0] <= u1[0]);
+  bool oy = (l2[1] <= u1[1] && u1[1] <= u2[1]) || (l1[1] <= u2[1] && u2[1] <= u1[1]);
+  bool oz = (l2[2] <= u1[2] && u1[2] <= u2[2]) || (l1[2] <= u2[2] && u2[2] <= u1[2]);
+  return ox && oy && oz;
+}
+
+DI bool intersection_test(const Smem& S, const DBody& A, const DBody& B) {
+  return S.P.use_bb ? aabb_overlap(A, B) : sphere_overlap(A, B);
+}
+
+// NaiveBroadphase.collisionPairs (naive_broadphase.dart:14-33): i ascending,
+// j < i ascending, pair (bodies[i], bodies[j]).
+DI void ph_broad_naive(Smem& S) {
+  const DWorld& W = S.W;
+  const int nb = S.P.nb;
+  const long long T = (long long)nb * (nb - 1) / 2;
+  const int cap = S.P.pairs_cap;
+  int out = 0;
+  for (long long tile = 0; tile < T; tile += BT * 4) {
+    long long k0 = tile + (long long)threadIdx.x * 4;
+    int bits = 0, cnt = 0;
+    int i = 0, j = 0;
+    if (k0 < T) {
+      i = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)k0)) * 0.5f);
+      while ((long long)i * (i - 1) / 2 > k0) i--;
+      while ((long long)(i + 1) * i / 2 <= k0) i++;
+      j = (int)(k0 - (long long)i * (i - 1) / 2);
+      int ii = i, jj = j;
+      for (int m = 0; m < 4 && k0 + m < T; m++) {
+        const DBody& A = W.bodies[ii];
+        const DBody& B = W.bodies[jj];
+        if (need_pair(A, B) && intersection_test(S, A, B)) {
+          bits |= 1 << m;
+          cnt++;
+        }
+        if (++jj == ii) { ii++; jj = 0; }
+      }
+    }
+    int tot;
+    int pre = block_excl_scan(S, cnt, tot);
+    if (cnt) {
+      int o = out + pre;
+      int ii = i, jj = j;
+      for (int m = 0; m < 4; m++) {
+        if (bits & (1 << m)) {
+          if (o < cap) { W.pair_a[o] = ii; W.pair_b[o] = jj; }
+          o++;
+        }
+        if (++jj == ii) { ii++; jj = 0; }
+      }
+    }
+    out += tot;
+  }
+  if (threadIdx.x == 0) {
+    S.n_pairs = out;
+    if (out > cap) S.overflow |= ST_PAIRS_OVERFLOW;
+  }
+  __syncthreads();
+}
+
+DI float axis_f(const float* v, int a) { return v[a]; }
+
+// SAPBroadphase.checkBounds (sap_broadphase.dart:41-62) in binary64, with a
+// binary32 pre-test whose error bound decides almost every call.
+DI bool check_bounds(const DBody& bi, const DBody& bj, int axis) {
+  float pi = bi.pos[axis], pj = bj.pos[axis];
+  float ri = bi.brad32, rj = bj.brad32;
+  if (fabsf(ri) < 1e30f && fabsf(rj) < 1e30f) {
+    float a2 = pi + ri, b1 = pj - rj;
+    float tol = 3.0e-7f * (fabsf(pi) + fabsf(ri) + fabsf(pj) + fabsf(rj)) + 1e-30f;
+    if (b1 < a2 - tol) return true;
+    if (b1 > a2 + tol) return false;
+  }
+  double boundA2 = (double)pi + bi.bounding_radius;
+  double boundB1 = (double)pj - bj.bounding_radius;
+  return boundB1 < boundA2;
+}
+
+// SAPBroadphase.sortList + collisionPairs (sap_broadphase.dart:66-79,138-189).
+// The persistent axisList is re-sorted stably by aabb.lowerBound[axis]: the
+// new rank of the entry at position p is #{keys < key_p} + #{q < p, key_q ==
+// key_p}, which is exactly where insertion sort leaves it.
+DI void ph_broad_sap(Smem& S) {
+  const DWorld& W = S.W;
+  const int nb = S.P.nb;
+  const int axis = S.P.sap_axis;
+  float* key = W.sap_key;
+  for (int p = threadIdx.x; p < nb; p += BT) key[p] = W.bodies[W.sap_order[p]].aabb_lo[axis];
+  __syncthreads();
+  for (int p = threadIdx.x; p < nb; p += BT) {
+    float kp = key[p];
+    int r = 0;
+    for (int q = 0; q < nb; q++) {
+      float kq = key[q];
+      r += (kq < kp) || (kq == kp && q < p);
+    }
+    W.sap_tmp[r] = W.sap_order[p];
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < nb; p += BT) W.sap_order[p] = W.sap_tmp[p];
+  __syncthreads();
+  // pass 1: pair count per list position
+  for (int i = threadIdx.x; i < nb; i += BT) {
+    const DBody& bi = W.bodies[W.sap_order[i]];
+    int c = 0;
+    for (int j = i + 1; j < nb; j++) {
+      const DBody& bj = W.bodies[W.sap_order[j]];
+      if (!need_pair(bi, bj)) continue;
+      if (!check_bounds(bi, bj, axis)) break;
+      if (intersection_test(S, bi, bj)) c++;
+    }
+    W.pair_cnt[i] = c;
+  }
+  __syncthreads();
+  int total = block_scan_array(S, W.pair_cnt, nb);
+  const int cap = S.P.pairs_cap;
+  if (total <= cap) {
+    for (int i = threadIdx.x; i < nb; i += BT) {
+      int ai = W.sap_order[i];
+      const DBody& bi = W.bodies[ai];
+      int o = W.pair_cnt[i];
+      for (int j = i + 1; j < nb; j++) {
+        int aj = W.sap_order[j];
+        const DBody& bj = W.bodies[aj];
+        if (!need_pair(bi, bj)) continue;
+        if (!check_bounds(bi, bj, axis)) break;
+        if (intersection_test(S, bi, bj)) {
+          W.pair_a[o] = ai;
+          W.pair_b[o] = aj;
+          o++;
+        }
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    S.n_pairs = total;
+    if (total > cap) S.overflow |= ST_PAIRS_OVERFLOW;
+  }
+  __syncthreads();
+}
+
+DI void grid_consts(const DWorldParams& P, double* c) {
+  // c: xmin ymin zmin xmult ymult zmult bsx bsy bsz binRadius
+  double xmax = P.grid_max[0], ymax = P.grid_max[1], zmax = P.grid_max[2];
+  double xmin = P.grid_min[0], ymin = P.grid_min[1], zmin = P.grid_min[2];
+  c[0] = xmin; c[1] = ymin; c[2] = zmin;
+  c[3] = P.grid_nx / (xmax - xmin); c[4] = P.grid_ny / (ymax - ymin); c[5] = P.grid_nz / (zmax - zmin);
+  c[6] = (xmax - xmin) / P.grid_nx; c[7] = (ymax - ymin) / P.grid_ny; c[8] = (zmax - zmin) / P.grid_nz;
+  c[9] = sqrt(c[6] * c[6] + c[7] * c[7] + c[8] * c[8]) * 0.5;
+}
+
+// bin box of a non-plane body (addBoxToBins arguments); false for planes
+DI bool grid_box(const DWorld& W, const DWorldParams& P, const double* c, int i, int* lo, int* hi) {
+  const DBody& b = W.bodies[i];
+  if (b.shape < 0) return false;
+  const DShape& s = W.shapes[b.shape];
+  if (s.type == CP_SHAPE_PLANE) return false;
+  double a0[3], a1[3];
+  if (s.type == CP_SHAPE_SPHERE) {
+    double r = s.radius;
+    for (int d = 0; d < 3; d++) { a0[d] = (double)b.pos[d] - r; a1[d] = (double)b.pos[d] + r; }
+  } else {
+    for (int d = 0; d < 3; d++) { a0[d] = b.aabb_lo[d]; a1[d] = b.aabb_hi[d]; }
+  }
+  const int n[3] = {P.grid_nx, P.grid_ny, P.grid_nz};
+  for (int d = 0; d < 3; d++) {
+    double f0 = floor((a0[d] - c[d]) * c[3 + d]);
+    double f1 = ceil((a1[d] - c[d]) * c[3 + d]);
+    lo[d] = f0 < 0 ? 0 : (f0 >= n[d] ? n[d] - 1 : (int)f0);
+    hi[d] = f1 < 0 ? 0 : (f1 >= n[d] ? n[d] - 1 : (int)f1);
+  }
+  return true;
+}
+
+DI bool is_plane_body(const DWorld& W, int i) {
+  int sh = W.bodies[i].shape;
+  return sh >= 0 && W.shapes[sh].type == CP_SHAPE_PLANE;
+}
+
+// Bin-centre offsets d = centre - plane position for a plane body, with d
+// accumulated in binary32 along the reference's loop order
+// (grid_broadphase.dart:169-198): one sequence per axis.
+DI void grid_plane_acc(Smem& S, const double* c, int i) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  const DBody& b = W.bodies[i];
+  DShape& sh = W.shapes[b.shape];
+  if (threadIdx.x == 0) {
+    if (!sh.plane_done) {  // Plane.computeWorldNormal runs once (plane.dart:182-187)
+      st3(sh.plane_n, vmult(ld4q(b.quat), f3{0.f, 0.f, 1.f}));
+      sh.plane_done = 1;
+    }
+    const int n[3] = {P.grid_nx, P.grid_ny, P.grid_nz};
+    int off = 0;
+    for (int d = 0; d < 3; d++) {
+      double reset = c[d] + c[6 + d] * 0.5 - b.pos[d];
+      float v = (float)reset;
+      for (int k = 0; k < n[d]; k++) {
+        W.bin_acc[off + k] = v;
+        v = (float)(v + c[6 + d]);
+      }
+      off += n[d];
+    }
+  }
+  __syncthreads();
+}
+
+DI bool grid_plane_hit(const DWorld& W, const DWorldParams& P, const double* c, int shape, int bin) {
+  int xi = bin / (P.grid_ny * P.grid_nz), yi = (bin / P.grid_nz) % P.grid_ny, zi = bin % P.grid_nz;
+  f3 d{W.bin_acc[xi], W.bin_acc[P.grid_nx + yi], W.bin_acc[P.grid_nx + P.grid_ny + zi]};
+  return dot(d, ld3(W.shapes[shape].plane_n)) < c[9];
+}
+
+DI unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+// GridBroadphase.collisionPairs (grid_broadphase.dart:59-239) with per-bin
+// lists, then the de-duplication broadphase.dart:105-134 intends: unique
+// unordered pairs in order of first appearance.  Bins list their bodies in
+// body order, so every appearance of a pair has the same orientation.
+DI void ph_broad_grid(Smem& S) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  const int nb = P.nb;
+  const int nBins = P.grid_nx * P.grid_ny * P.grid_nz;
+  const int yz = P.grid_ny * P.grid_nz;
+  double c[10];
+  grid_consts(P, c);
+  for (int pass = 0; pass < 2; pass++) {
+    // pass 0 counts bin memberships, pass 1 places them
+    if (pass == 0)
+      for (int b = threadIdx.x; b < nBins; b += BT) W.bin_cnt[b] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += BT) {
+      int lo[3], hi[3];
+      if (!grid_box(W, P, c, i, lo, hi)) continue;
+      for (int x = lo[0]; x <= hi[0]; x++)
+        for (int y = lo[1]; y <= hi[1]; y++)
+          for (int z = lo[2]; z <= hi[2]; z++) {
+            int bin = x * yz + y * P.grid_nz + z;
+            int pos = atomicAdd(&W.bin_cnt[bin], 1);
+            if (pass == 1 && pos < P.bins_cap) W.bin_body[pos] = i;
+          }
+    }
+    for (int i = 0; i < nb; i++) {
+      if (!is_plane_body(W, i)) continue;
+      grid_plane_acc(S, c, i);
+      for (int b = threadIdx.x; b < nBins; b += BT)
+        if (grid_plane_hit(W, P, c, W.bodies[i].shape, b)) {
+          int pos = atomicAdd(&W.bin_cnt[b], 1);
+          if (pass == 1 && pos < P.bins_cap) W.bin_body[pos] = i;
+        }
+      __syncthreads();
+    }
+    __syncthreads();
+    if (pass == 0) {
+      int total = block_scan_array(S, W.bin_cnt, nBins);
+      for (int b = threadIdx.x; b < nBins; b += BT) W.bin_start[b] = W.bin_cnt[b];
+      if (threadIdx.x == 0) {
+        W.bin_start[nBins] = total;
+        if (total > P.bins_cap) S.overflow |= ST_BINS_OVERFLOW;
+      }
+      __syncthreads();
+      if (S.overflow) return;
+    }
+  }
+  // per-bin lists in body order
+  for (int b = threadIdx.x; b < nBins; b += BT) {
+    int s0 = W.bin_start[b], s1 = W.bin_start[b + 1];
+    for (int x = s0 + 1; x < s1; x++) {
+      int v = W.bin_body[x];
+      int y = x - 1;
+      while (y >= s0 && W.bin_body[y] > v) { W.bin_body[y + 1] = W.bin_body[y]; y--; }
+      W.bin_body[y + 1] = v;
+    }
+  }
+  __syncthreads();
+  // candidate pairs, bin by bin: (bin[xi], bin[yi]) for yi < xi
+  for (int pass = 0; pass < 2; pass++) {
+    for (int b = threadIdx.x; b < nBins; b += BT) {
+      int s0 = W.bin_start[b], len = W.bin_start[b + 1] - s0;
+      int o = pass == 1 ? W.bin_cnt[b] : 0;
+      int cnt = 0;
+      if (len > 1)
+        for (int xi = 0; xi < len; xi++) {
+          int ia = W.bin_body[s0 + xi];
+          for (int yi = 0; yi < xi; yi++) {
+            int ib = W.bin_body[s0 + yi];
+            const DBody& A = W.bodies[ia];
+            const DBody& B = W.bodies[ib];
+            if (need_pair(A, B) && intersection_test(S, A, B)) {
+              if (pass == 1) { W.pair_a[o + cnt] = ia; W.pair_b[o + cnt] = ib; }
+              cnt++;
+            }
+          }
+        }
+      if (pass == 0) W.bin_cnt[b] = cnt;
+    }
+    __syncthreads();
+    if (pass == 0) {
+      int total = block_scan_array(S, W.bin_cnt, nBins);
+      if (threadIdx.x == 0) {
+        S.n_pairs = total;
+        if (total > P.pairs_cap || 2 * total > W.hash_cap) S.overflow |= ST_PAIRS_OVERFLOW;
+      }
+      __syncthreads();
+      if (S.overflow) return;
+    }
+  }
+  const int ncand = S.n_pairs;
+  // first appearance of each unordered pair: hash slot -> smallest candidate index
+  const int hmask = W.hash_cap - 1;
+  for (int h = threadIdx.x; h < W.hash_cap; h += BT) { W.hkeys[h] = -1; W.hvals[h] = 0x7fffffff; }
+  __syncthreads();
+  for (int k = threadIdx.x; k < ncand; k += BT) {
+    int a = W.pair_a[k], b = W.pair_b[k];
+    long long key = ((long long)min(a, b) << 32) | (unsigned)max(a, b);
+    int h = (int)(mix64((unsigned long long)key) & hmask);
+    for (int probe = 0; probe < W.hash_cap; probe++) {
+      unsigned long long prev = atomicCAS((unsigned long long*)&W.hkeys[h], 0xffffffffffffffffULL, (unsigned long long)key);
+      if (prev == 0xffffffffffffffffULL || prev == (unsigned long long)key) { atomicMin(&W.hvals[h], k); break; }
+      h = (h + 1) & hmask;
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < ncand; k += BT) {
+    int a = W.pair_a[k], b = W.pair_b[k];
+    long long key = ((long long)min(a, b) << 32) | (unsigned)max(a, b);
+    int h = (int)(mix64((unsigned long long)key) & hmask);
+    int keep = 0;
+    for (int probe = 0; probe < W.hash_cap; probe++) {
+      if (W.hkeys[h] == key) { keep = W.hvals[h] == k; break; }
+      h = (h + 1) & hmask;
+    }
+    W.pair_cnt[k] = keep;
+    W.pair_tstart[k] = a;
+    W.heavy[k] = b;
+  }
+  __syncthreads();
+  int kept = block_scan_array(S, W.pair_cnt, ncand);
+  for (int k = threadIdx.x; k < ncand; k += BT) {
+    int nxt = k + 1 < ncand ? W.pair_cnt[k + 1] : kept;
+    if (nxt > W.pair_cnt[k]) {
+      W.pair_a[W.pair_cnt[k]] = W.pair_tstart[k];
+      W.pair_b[W.pair_cnt[k]] = W.heavy[k];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) S.n_pairs = kept;
+  __syncthreads();
+}
+
+// World.internalStep removes the pairs of constraints with
+// collideConnected == false (world_class.dart:487-499); a stable filter.
+DI void ph_nocollide(Smem& S) {
+  const DWorld& W = S.W;
+  const int nn = S.P.n_nocollide;
+  const int np = S.n_pairs;
+  for (int k = threadIdx.x; k < np; k += BT) {
+    int a = W.pair_a[k], b = W.pair_b[k];
+    int keep = 1;
+    for (int c = 0; c < nn; c++) {
+      int ca = W.nocollide[2 * c], cb = W.nocollide[2 * c + 1];
+      if ((ca == a && cb == b) || (cb == a && ca == b)) keep = 0;
+    }
+    W.pair_cnt[k] = keep;
+    W.pair_tstart[k] = a;
+    W.heavy[k] = b;
+  }
+  __syncthreads();
+  int kept = block_scan_array(S, W.pair_cnt, np);
+  for (int k = threadIdx.x; k < np; k += BT) {
+    int nxt = k + 1 < np ? W.pair_cnt[k + 1] : kept;
+    if (nxt > W.pair_cnt[k]) {
+      W.pair_a[W.pair_cnt[k]] = W.pair_tstart[k];
+      W.pair_b[W.pair_cnt[k]] = W.heavy[k];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) S.n_pairs = kept;
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// narrowphase (narrow_phase.dart:634-721)
+
+DI int contact_material(const DWorld& W, const DWorldParams& P, int ma, int mb) {
+  if (ma < 0 || mb < 0) return -1;
+  return W.cm_table[ma * P.nmat + mb];
+}
+
+DI void narrow_pair(Smem& S, int k, bool heavy_pass) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  int i = W.pair_a[k], j = W.pair_b[k];
+  const DBody& bi = W.bodies[i];
+  const DBody& bj = W.bodies[j];
+  int cnt = 0, start = 0;
+  bool just_test = (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_STATIC) ||
+                   (bi.type == CP_BODY_STATIC && bj.type == CP_BODY_KINEMATIC) ||
+                   (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_KINEMATIC);
+  do {
+    if (bi.shape < 0 || bj.shape < 0 || just_test) break;
+    const DShape& si = W.shapes[bi.shape];
+    const DShape& sj = W.shapes[bj.shape];
+    bool swap = !(si.type < sj.type);
+    int rk = swap ? resolver_kind(sj.type, si.type) : resolver_kind(si.type, sj.type);
+    if (rk == RK_NONE) break;
+    if (is_heavy(rk) != heavy_pass) {
+      if (!heavy_pass) W.heavy[atomicAdd(&S.n_heavy, 1)] = k;
+      return;
+    }
+    if (!((si.mask & sj.group) != 0 && (sj.mask & si.group) != 0)) break;
+    f3 xi = ld3(W.bscr[i].xs), xj = ld3(W.bscr[j].xs);
+    q4 qi = ld4q(W.bscr[i].qs), qj = ld4q(W.bscr[j].qs);
+    if (distance_to(xi, xj) > si.bsr + sj.bsr) break;
+    int cm = contact_material(W, P, si.material, sj.material);
+    if (cm < 0) cm = contact_material(W, P, bi.material, bj.material);
+    if (cm < 0) cm = 0;
+    NarrowCtx C;
+    C.W = &W; C.cursor = &S.cursor; C.cap = P.contacts_cap; C.overflow = &S.overflow; C.cm = cm; C.pair = k;
+    int rsi = bi.shape, rsj = bj.shape;
+    int bA = swap ? j : i, bB = swap ? i : j;
+    int shA = swap ? bj.shape : bi.shape, shB = swap ? bi.shape : bj.shape;
+    f3 xA = swap ? xj : xi, xB = swap ? xi : xj;
+    q4 qA = swap ? qj : qi, qB = swap ? qi : qj;
+    switch (rk) {
+      case RK_SS: cnt = sphere_sphere(C, bA, bB, shA, shB, rsi, rsj, xA, xB, start); break;
+      case RK_SP: cnt = sphere_plane(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qB, start); break;
+      case RK_SB: cnt = sphere_box(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qB, start); break;
+      case RK_SC: cnt = sphere_convex(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qB, start); break;
+      case RK_PB: cnt = plane_convex(C, bA, bB, shA, shB, shA, shB, xA, xB, qA, qB, start); break;
+      case RK_PC: cnt = plane_convex(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qA, qB, start); break;
+      case RK_BB: cnt = convex_convex(C, bA, bB, shA, shB, shA, shB, xA, xB, qA, qB, start); break;
+      case RK_BC: cnt = convex_convex(C, bA, bB, shA, shB, shA, shB, xA, xB, qA, qB, start); break;
+      default: cnt = convex_convex(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qA, qB, start); break;
+    }
+  } while (0);
+  W.pair_cnt[k] = cnt;
+  W.pair_tstart[k] = start;
+}
+
+DI void ph_narrow(Smem& S) {
+  const DWorld& W = S.W;
+  const int np = S.n_pairs;
+  if (threadIdx.x == 0) { S.n_heavy = 0; S.cursor = 0; }
+  __syncthreads();
+  for (int k = threadIdx.x; k < np; k += BT) narrow_pair(S, k, false);
+  __syncthreads();
+  const int nh = S.n_heavy;
+  for (int h = threadIdx.x; h < nh; h += BT) narrow_pair(S, W.heavy[h], true);
+  __syncthreads();
+  // order: contacts of pair k follow those of pairs < k
+  for (int k = threadIdx.x; k < np; k += BT) W.heavy[k] = W.pair_cnt[k];
+  __syncthreads();
+  int total = block_scan_array(S, W.heavy, np);
+  if (threadIdx.x == 0) {
+    S.n_contacts = total;
+    if (total > S.P.contacts_cap) S.overflow |= ST_CONTACTS_OVERFLOW;
+  }
+  __syncthreads();
+  if (S.overflow) return;
+  for (int k = threadIdx.x; k < np; k += BT) {
+    int c = W.pair_cnt[k], t = W.pair_tstart[k], o = W.heavy[k];
+    for (int m = 0; m < c; m++) W.contacts[o + m] = W.ctmp[t + m];
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// rows
+
+// friction of a contact: createFrictionEquationsFromContact (narrow_phase.dart:530-586)
+DI double contact_friction(const DWorld& W, const DContact& c) {
+  double friction = W.cms[c.cm].friction;
+  int ma = W.shapes[c.si].material >= 0 ? W.shapes[c.si].material : W.bodies[c.bi].material;
+  int mb = W.shapes[c.sj].material >= 0 ? W.shapes[c.sj].material : W.bodies[c.bj].material;
+  if (ma >= 0 && mb >= 0 && W.mats[ma].friction >= 0 && W.mats[mb].friction >= 0)
+    friction = W.mats[ma].friction * W.mats[mb].friction;
+  return friction;
+}
+
+DI bool row_kept(const DWorld& W, int bi, int bj, bool enabled) {  // Solver.addEquation (solver.dart:30-34)
+  return enabled && !(W.bodies[bi].flags & BF_TRIGGER) && !(W.bodies[bj].flags & BF_TRIGGER);
+}
+
+// Candidates, in World.internalStep order (world_class.dart:539-635):
+//   [0, nF)          friction rows, two per contact with friction > 0
+//   [nF, nF+nC)      contact rows
+//   [nF+nC, ...)     constraint rows (constraint order, equation order)
+DI void ph_rows_list(Smem& S) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  const int nc = S.n_contacts;
+  // friction rows per contact
+  for (int c = threadIdx.x; c < nc; c += BT) {
+    DContact& ct = W.contacts[c];
+    double fr = contact_friction(W, ct);
+    W.cscr[c] = fr > 0 ? 2 : 0;  // friction rows of contact c
+    if (fr > 0) {
+      double mug = fr * length(P.has_fgrav ? ld3(P.fgrav) : ld3(P.gravity));
+      double red = W.bodies[ct.bi].inv_mass + W.bodies[ct.bj].inv_mass;
+      if (red > 0) red = 1 / red;
+      ct.slip = mug * red;
+    }
+  }
+  __syncthreads();
+  int nF = block_scan_array(S, W.cscr, nc);
+  for (int c = threadIdx.x; c < nc; c += BT) {
+    DContact& ct = W.contacts[c];
+    int f0 = W.cscr[c];
+    int has = (c + 1 < nc ? W.cscr[c + 1] : nF) - f0;
+    ct.frow = has ? f0 : -1;
+    bool keep = row_kept(W, ct.bi, ct.bj, ct.enabled);
+    if (has) { W.cand[f0] = keep; W.cand[f0 + 1] = keep; }
+    W.cand[nF + c] = keep;
+  }
+  for (int k = threadIdx.x; k < P.ncons; k += BT) {
+    const DConstraint& cn = W.cons[k];
+    int base = nF + nc + cn.row0;
+    for (int r = 0; r < cn.nrows; r++) {
+      bool enabled = !(cn.type == CP_CON_HINGE && r == 5 && !cn.motor);
+      W.cand[base + r] = row_kept(W, cn.a, cn.b, enabled);
+    }
+  }
+  __syncthreads();
+  const int ncand = nF + nc + P.ncon_rows;
+  int nrows = block_scan_array(S, W.cand, ncand);
+  if (threadIdx.x == 0) {
+    S.n_fric = nF;
+    S.n_cand = ncand;
+    S.n_rows = nrows;
+    if (nrows > P.rows_cap) S.overflow |= ST_ROWS_OVERFLOW;
+  }
+  __syncthreads();
+}
+
+DI bool cand_kept(const DWorld& W, int c, int ncand, int nrows) {
+  int nxt = c + 1 < ncand ? W.cand[c + 1] : nrows;
+  return nxt > W.cand[c];
+}
+
+// restitution override, wake-up tests (world_class.dart:544-624) and
+// constraint geometry (Constraint.update)
+DI void ph_contacts_post(Smem& S) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  const int nc = S.n_contacts;
+  for (int c = threadIdx.x; c < nc; c += BT) {
+    DContact& ct = W.contacts[c];
+    const DBody& bi = W.bodies[ct.bi];
+    const DBody& bj = W.bodies[ct.bj];
+    if (bi.material >= 0 && bj.material >= 0) {
+      double ra = W.mats[bi.material].restitution, rb = W.mats[bj.material].restitution;
+      if (ra >= 0 && rb >= 0) ct.restitution = ra * rb;
+    }
+    if ((bi.flags & BF_ALLOW_SLEEP) && bi.type == CP_BODY_DYNAMIC && bi.sleep_state == CP_SLEEPING &&
+        bj.sleep_state == CP_AWAKE && bj.type != CP_BODY_STATIC) {
+      double s2 = length2(ld3(bj.vel)) + length2(ld3(bj.avel));
+      double l2 = bj.sleep_speed_limit * bj.sleep_speed_limit;
+      if (s2 >= l2 * 2) atomicOr(&W.bodies[ct.bi].flags, BF_WAKE);
+    }
+    if ((bj.flags & BF_ALLOW_SLEEP) && bj.type == CP_BODY_DYNAMIC && bj.sleep_state == CP_SLEEPING &&
+        bi.sleep_state == CP_AWAKE && bi.type != CP_BODY_STATIC) {
+      double s2 = length2(ld3(bi.vel)) + length2(ld3(bi.avel));
+      double l2 = bi.sleep_speed_limit * bi.sleep_speed_limit;
+      if (s2 >= l2 * 2) atomicOr(&W.bodies[ct.bj].flags, BF_WAKE);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < P.nb; i += BT) {
+    DBody& b = W.bodies[i];
+    if (b.flags & BF_WAKE) {
+      b.sleep_state = CP_AWAKE;
+      b.flags &= ~BF_WAKE;
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < P.ncons; k += BT) {
+    DConstraint& cn = W.cons[k];
+    const DBody& A = W.bodies[cn.a];
+    const DBody& B = W.bodies[cn.b];
+    if (cn.type == CP_CON_DISTANCE) {  // distance_constraint.dart:269-280
+      double half = cn.distance * 0.5;
+      f3 n = normalized(sub(ld3(B.pos), ld3(A.pos)));
+      st3(cn.n, n);
+      st3(cn.ri, scale(n, half));
+      st3(cn.rj, scale(n, -half));
+    } else {  // point_to_point_constraint.dart:122-137, hinge_constraint.dart:217-242
+      q4 qa = ld4q(A.quat), qb = ld4q(B.quat);
+      st3(cn.ri, vmult(qa, ld3(cn.piv_a)));
+      st3(cn.rj, vmult(qb, ld3(cn.piv_b)));
+      if (cn.type == CP_CON_HINGE) {
+        f3 wa = vmult(qa, ld3(cn.axis_a));
+        f3 wb = vmult(qb, ld3(cn.axis_b));
+        f3 t1, t2;
+        tangents(wa, t1, t2);
+        st3(cn.r1a, t1);
+        st3(cn.r2a, t2);
+        st3(cn.wb, wb);
+        if (cn.motor) {
+          st3(cn.ma, vmult(qa, ld3(cn.axis_a)));
+          st3(cn.mb, vmult(qb, ld3(cn.axis_b)));
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Body solve state: gravity (world_class.dart:460-471, applied here because
+// nothing between it and the solver reads Body.force), updateSolveMassProperties
+// (rigid_body.dart:303-314), vlambda/wlambda reset and the per-body parts of
+// computeGiMf.
+DI void ph_solve_prep(Smem& S) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  double gx = P.gravity[0], gy = P.gravity[1], gz = P.gravity[2];
+  for (int i = threadIdx.x; i < P.nb; i += BT) {
+    DBody& b = W.bodies[i];
+    DBodyScr& s = W.bscr[i];
+    if (b.type == CP_BODY_DYNAMIC) {
+      double m = b.mass;
+      b.force[0] = (float)(b.force[0] + m * gx);
+      b.force[1] = (float)(b.force[1] + m * gy);
+      b.force[2] = (float)(b.force[2] + m * gz);
+    }
+    bool zero = b.sleep_state == CP_SLEEPING || b.type == CP_BODY_KINEMATIC;
+    double im = zero ? 0.0 : b.inv_mass;
+    bool any_iw = false;
+    float iw[9];
+#pragma unroll
+    for (int e = 0; e < 9; e++) {
+      iw[e] = zero ? 0.f : b.iw[e];
+      any_iw |= iw[e] != 0.f;
+    }
+    s.im_solve = im;
+    s.active = (im != 0.0) || any_iw;
+    st3(s.vl, f3{0.f, 0.f, 0.f});
+    st3(s.wl, f3{0.f, 0.f, 0.f});
+    st3(s.imf, scale(ld3(b.force), im));
+    st3(s.iit, mvmult(iw, ld3(b.torque)));
+  }
+  __syncthreads();
+}
+
+// Row assembly: Jacobians and computeB (contact_equation.dart:34-77,
+// friction_equation.dart:19-47, rotational_equation.dart:34-58,
+// rotational_motor_equation.dart:17-33), computeC (equation_class.dart:129-174)
+struct RowGeom {
+  int kind, bi, bj;
+  f3 ri, rj, n;       // contact: ni; friction: t
+  f3 axA, axB;        // rotational / motor axes
+  double restitution, a, b, eps, minF, maxF, cos_max, target;
+};
+
+DI void assemble_row(const Smem& S, const RowGeom& G, DRow& R, double h) {
+  const DWorld& W = S.W;
+  const DBody& bi = W.bodies[G.bi];
+  const DBody& bj = W.bodies[G.bj];
+  const DBodyScr& si = W.bscr[G.bi];
+  const DBodyScr& sj = W.bscr[G.bj];
+  f3 gaS{0, 0, 0}, gaR{0, 0, 0}, gbS{0, 0, 0}, gbR{0, 0, 0};
+  double B;
+  if (G.kind == CP_ROW_CONTACT) {
+    f3 rixn = cross(G.ri, G.n), rjxn = cross(G.rj, G.n);
+    gaS = neg(G.n); gaR = neg(rixn); gbS = G.n; gbR = rjxn;
+    f3 pen = ld3(bj.pos);
+    pen = add(pen, G.rj);
+    pen = sub(pen, ld3(bi.pos));
+    pen = sub(pen, G.ri);
+    double g = dot(G.n, pen);
+    double e1 = G.restitution + 1;
+    double gw = e1 * dot(ld3(bj.vel), G.n) - e1 * dot(ld3(bi.vel), G.n) + dot(ld3(bj.avel), rjxn) - dot(ld3(bi.avel), rixn);
+    double giMf = (dot(ld3(si.imf), gaS) + dot(ld3(si.iit), gaR)) + (dot(ld3(sj.imf), gbS) + dot(ld3(sj.iit), gbR));
+    B = -g * G.a - gw * G.b - h * giMf;
+  } else if (G.kind == CP_ROW_FRICTION) {
+    f3 rixt = cross(G.ri, G.n), rjxt = cross(G.rj, G.n);
+    gaS = neg(G.n); gaR = neg(rixt); gbS = G.n; gbR = rjxt;
+    double gw = (dot(ld3(bi.vel), gaS) + dot(ld3(bi.avel), gaR)) + (dot(ld3(bj.vel), gbS) + dot(ld3(bj.avel), gbR));
+    double giMf = (dot(ld3(si.imf), gaS) + dot(ld3(si.iit), gaR)) + (dot(ld3(sj.imf), gbS) + dot(ld3(sj.iit), gbR));
+    B = -gw * G.b - h * giMf;
+  } else if (G.kind == CP_ROW_ROTATIONAL) {
+    f3 nixnj = cross(G.axA, G.axB), njxni = cross(G.axB, G.axA);
+    gaR = njxni; gbR = nixnj;
+    double g = G.cos_max - dot(G.axA, G.axB);
+    double gW = (dot(ld3(bi.vel), gaS) + dot(ld3(bi.avel), gaR)) + (dot(ld3(bj.vel), gbS) + dot(ld3(bj.avel), gbR));
+    double giMf = (dot(ld3(si.imf), gaS) + dot(ld3(si.iit), gaR)) + (dot(ld3(sj.imf), gbS) + dot(ld3(sj.iit), gbR));
+    B = -g * G.a - gW * G.b - h * giMf;
+  } else {
+    gaR = G.axA; gbR = neg(G.axB);
+    double gw = (dot(ld3(bi.vel), gaS) + dot(ld3(bi.avel), gaR)) + (dot(ld3(bj.vel), gbS) + dot(ld3(bj.avel), gbR)) - G.target;
+    double giMf = (dot(ld3(si.imf), gaS) + dot(ld3(si.iit), gaR)) + (dot(ld3(sj.imf), gbS) + dot(ld3(sj.iit), gbR));
+    B = -gw * G.b - h * giMf;
+  }
+  float iwa[9], iwb[9];
+  bool za = bi.sleep_state == CP_SLEEPING || bi.type == CP_BODY_KINEMATIC;
+  bool zb = bj.sleep_state == CP_SLEEPING || bj.type == CP_BODY_KINEMATIC;
+#pragma unroll
+  for (int e = 0; e < 9; e++) {
+    iwa[e] = za ? 0.f : bi.iw[e];
+    iwb[e] = zb ? 0.f : bj.iw[e];
+  }
+  f3 iMaR = mvmult(iwa, gaR), iMbR = mvmult(iwb, gbR);
+  double C = si.im_solve + sj.im_solve;
+  C += dot(iMaR, gaR);
+  C += dot(iMbR, gbR);
+  C = C + G.eps;
+  st3(R.gaS, gaS); st3(R.gaR, gaR); st3(R.gbS, gbS); st3(R.gbR, gbR);
+  st3(R.iMaR, iMaR); st3(R.iMbR, iMbR);
+  R.B = B;
+  R.invC = 1.0 / C;
+  R.eps = G.eps;
+  R.minF = G.minF;
+  R.maxF = G.maxF;
+  R.lambda = 0.0;
+  R.imA = si.im_solve;
+  R.imB = sj.im_solve;
+  R.bi = G.bi;
+  R.bj = G.bj;
+  R.kind = G.kind;
+}
+
+DI void ph_rows_assemble(Smem& S, double h) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  const int nc = S.n_contacts, nF = S.n_fric, ncand = S.n_cand, nrows = S.n_rows;
+  for (int c = threadIdx.x; c < nc; c += BT) {
+    const DContact& ct = W.contacts[c];
+    const DContactMaterial& cm = W.cms[ct.cm];
+    RowGeom G;
+    G.bi = ct.bi; G.bj = ct.bj;
+    G.ri = ld3(ct.ri); G.rj = ld3(ct.rj);
+    f3 ni = ld3(ct.ni);
+    if (ct.frow >= 0) {
+      f3 t1, t2;
+      tangents(ni, t1, t2);
+      G.kind = CP_ROW_FRICTION;
+      G.a = cm.fa; G.b = cm.fb; G.eps = cm.feps;
+      G.minF = -ct.slip; G.maxF = ct.slip;
+      for (int m = 0; m < 2; m++) {
+        int cd = ct.frow + m;
+        if (cand_kept(W, cd, ncand, nrows)) {
+          G.n = m == 0 ? t1 : t2;
+          DRow& R = W.rows[W.cand[cd]];
+          assemble_row(S, G, R, h);
+          R.src = cd;
+        }
+      }
+    }
+    int cd = nF + c;
+    if (cand_kept(W, cd, ncand, nrows)) {
+      G.kind = CP_ROW_CONTACT;
+      G.n = ni;
+      G.restitution = ct.restitution;
+      G.a = cm.ca; G.b = cm.cb; G.eps = cm.ceps;
+      G.minF = 0.0; G.maxF = 1e6;
+      DRow& R = W.rows[W.cand[cd]];
+      assemble_row(S, G, R, h);
+      R.src = cd;
+    }
+  }
+  for (int k = threadIdx.x; k < P.ncons; k += BT) {
+    const DConstraint& cn = W.cons[k];
+    int base = nF + nc + cn.row0;
+    RowGeom G;
+    G.bi = cn.a; G.bj = cn.b;
+    G.a = cn.sa; G.b = cn.sb; G.eps = cn.seps;
+    G.minF = -cn.max_force; G.maxF = cn.max_force;
+    G.restitution = 0.0;
+    G.cos_max = cn.cos_max;
+    G.target = cn.motor_target;
+    for (int r = 0; r < cn.nrows; r++) {
+      int cd = base + r;
+      if (!cand_kept(W, cd, ncand, nrows)) continue;
+      if (cn.type == CP_CON_DISTANCE) {
+        G.kind = CP_ROW_CONTACT;
+        G.ri = ld3(cn.ri); G.rj = ld3(cn.rj); G.n = ld3(cn.n);
+      } else if (r < 3) {
+        G.kind = CP_ROW_CONTACT;
+        G.ri = ld3(cn.ri); G.rj = ld3(cn.rj);
+        G.n = r == 0 ? f3{1.f, 0.f, 0.f} : (r == 1 ? f3{0.f, 1.f, 0.f} : f3{0.f, 0.f, 1.f});
+      } else if (r < 5) {
+        G.kind = CP_ROW_ROTATIONAL;
+        G.axA = ld3(r == 3 ? cn.r1a : cn.r2a);
+        G.axB = ld3(cn.wb);
+      } else {
+        G.kind = CP_ROW_MOTOR;
+        G.axA = ld3(cn.ma);
+        G.axB = ld3(cn.mb);
+        G.minF = -cn.motor_max_force; G.maxF = cn.motor_max_force;
+      }
+      DRow& R = W.rows[W.cand[cd]];
+      assemble_row(S, G, R, h);
+      R.src = cd;
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// GSSolver.solve (gs_solver.dart:74-180)
+
+// Dependency levels: a row waits for the latest earlier row that shares a
+// dynamic body with it.  Bodies with zero solve mass and inertia
+// (static, sleeping, kinematic) keep vlambda = wlambda = +0 exactly, so they
+// order nothing.
+DI void ph_levels(Smem& S) {
+  const DWorld& W = S.W;
+  const int nrows = S.n_rows;
+  const int nb = S.P.nb;
+  for (int i = threadIdx.x; i < nb; i += BT) W.bscr[i].last_level = -1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nl = 0;
+    for (int r = 0; r < nrows; r++) {
+      int a = W.rows[r].bi, b = W.rows[r].bj;
+      int aa = W.bscr[a].active, ba = W.bscr[b].active;
+      int la = aa ? W.bscr[a].last_level : -1;
+      int lb = ba ? W.bscr[b].last_level : -1;
+      int l = (la > lb ? la : lb) + 1;
+      if (aa) W.bscr[a].last_level = l;
+      if (ba) W.bscr[b].last_level = l;
+      W.level_of[r] = l;
+      if (l + 1 > nl) nl = l + 1;
+    }
+    S.n_levels = nl;
+  }
+  __syncthreads();
+  const int nl = S.n_levels;
+  for (int l = threadIdx.x; l <= nl; l += BT) W.level_start[l] = 0;
+  __syncthreads();
+  for (int r = threadIdx.x; r < nrows; r += BT) atomicAdd(&W.level_start[W.level_of[r]], 1);
+  __syncthreads();
+  block_scan_array(S, W.level_start, nl + 1);
+  for (int l = threadIdx.x; l < nl; l += BT) W.level_cursor[l] = W.level_start[l];
+  __syncthreads();
+  for (int r = threadIdx.x; r < nrows; r += BT) W.level_rows[atomicAdd(&W.level_cursor[W.level_of[r]], 1)] = r;
+  __syncthreads();
+}
+
+// One row of one sweep (gs_solver.dart:127-148 with Equation.computeGWlambda
+// and addToWlambda, equation_class.dart:95-169)
+DI double gs_row(const DWorld& W, DRow& R) {
+  DBodyScr& A = W.bscr[R.bi];
+  DBodyScr& B = W.bscr[R.bj];
+  f3 vla = ld3(A.vl), wla = ld3(A.wl), vlb = ld3(B.vl), wlb = ld3(B.wl);
+  double gwl = (dot(vla, ld3(R.gaS)) + dot(wla, ld3(R.gaR))) + (dot(vlb, ld3(R.gbS)) + dot(wlb, ld3(R.gbR)));
+  double lj = R.lambda;
+  double dl = R.invC * (R.B - gwl - R.eps * lj);
+  if (lj + dl < R.minF) dl = R.minF - lj;
+  else if (lj + dl > R.maxF) dl = R.maxF - lj;
+  R.lambda = lj + dl;
+  if (A.active) {
+    st3(A.vl, add_scaled(vla, R.imA * dl, ld3(R.gaS)));
+  }
+  if (B.active) {
+    // re-read: bi == bj is possible for a constraint between a body and itself
+    f3 v = R.bi == R.bj ? ld3(B.vl) : vlb;
+    st3(B.vl, add_scaled(v, R.imB * dl, ld3(R.gbS)));
+  }
+  if (A.active) st3(A.wl, add_scaled(wla, dl, ld3(R.iMaR)));
+  if (B.active) {
+    f3 w = R.bi == R.bj ? ld3(B.wl) : wlb;
+    st3(B.wl, add_scaled(w, dl, ld3(R.iMbR)));
+  }
+  return dl > 0.0 ? dl : -dl;
+}
+
+DI void ph_solve(Smem& S, double h) {
+  const DWorld& W = S.W;
+  const int nrows = S.n_rows;
+  const int nl = S.n_levels;
+  const int maxIter = S.P.iterations;
+  const double tol2 = S.P.tolerance * S.P.tolerance;
+  int iter = 0;
+  for (iter = 0; iter != maxIter; iter++) {
+    double part = 0.0;
+    for (int l = 0; l < nl; l++) {
+      int e = W.level_start[l + 1];
+      for (int x = W.level_start[l] + threadIdx.x; x < e; x += BT) {
+        int r = W.level_rows[x];
+        double a = gs_row(W, W.rows[r]);
+        W.absdl[r] = a;
+        part += a;
+      }
+      __syncthreads();
+    }
+    // deltalambdaTot is the sum in row order.  The block sum has the same
+    // terms in another order; both are within 2(n-1)u of the exact sum
+    // (non-negative terms), so unless tol^2 falls inside that band the
+    // comparison is decided by the block sum; otherwise thread 0 adds the
+    // terms in row order.
+    double sp = block_sum(S, part);
+    if (threadIdx.x == 0) {
+      double band = 2.2 * (double)nrows * 1.1102230246251565e-16;
+      double hi = sp * (1.0 + band), lo = sp * (1.0 - band);
+      int conv;
+      if (hi * hi * (1.0 + 4.5e-16) < tol2) conv = 1;
+      else if (lo * lo * (1.0 - 4.5e-16) >= tol2 && lo >= 0.0) conv = 0;
+      else {
+        double t = 0.0;
+        for (int r = 0; r < nrows; r++) t += W.absdl[r];
+        conv = t * t < tol2;
+      }
+      S.converged = conv;
+    }
+    __syncthreads();
+    if (S.converged) break;
+  }
+  if (threadIdx.x == 0) S.P.last_iterations = iter;
+  __syncthreads();
+}
+
+// Add result to velocity; multipliers (gs_solver.dart:157-176)
+DI void ph_solve_apply(Smem& S, double h) {
+  const DWorld& W = S.W;
+  for (int i = threadIdx.x; i < S.P.nb; i += BT) {
+    DBody& b = W.bodies[i];
+    DBodyScr& s = W.bscr[i];
+    f3 vl = mul(ld3(s.vl), ld3(b.lin_factor));
+    st3(b.vel, add(ld3(b.vel), vl));
+    f3 wl = mul(ld3(s.wl), ld3(b.ang_factor));
+    st3(b.avel, add(ld3(b.avel), wl));
+    st3(s.vl, vl);
+    st3(s.wl, wl);
+  }
+  double invDt = 1 / h;
+  for (int r = threadIdx.x; r < S.n_rows; r += BT) W.rows[r].mult = W.rows[r].lambda * invDt;
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// damping, integrate, clearForces, sleepTick (world_class.dart:647-700,
+// rigid_body.dart:263-300,627-680)
+DI void ph_integrate(Smem& S, double dt) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  const bool qn = (P.stepnumber % (long long)(P.qn_skip + 1)) == 0;
+  const double time = P.time;
+  for (int i = threadIdx.x; i < P.nb; i += BT) {
+    DBody& b = W.bodies[i];
+    f3 v = ld3(b.vel), w = ld3(b.avel);
+    if (b.type == CP_BODY_DYNAMIC) {
+      v = scale(v, W.dpow[2 * i]);
+      w = scale(w, W.dpow[2 * i + 1]);
+    }
+    f3 p = ld3(b.pos);
+    q4 q = ld4q(b.quat);
+    st3(b.prev_pos, p);
+    st4q(b.prev_quat, q);
+    if ((b.type == CP_BODY_DYNAMIC || b.type == CP_BODY_KINEMATIC) && b.sleep_state != CP_SLEEPING) {
+      double iMdt = b.inv_mass * dt;
+      f3 lf = ld3(b.lin_factor), af = ld3(b.ang_factor);
+      f3 f = ld3(b.force), t = ld3(b.torque);
+      v.x = (float)(v.x + f.x * iMdt * lf.x);
+      v.y = (float)(v.y + f.y * iMdt * lf.y);
+      v.z = (float)(v.z + f.z * iMdt * lf.z);
+      const float* e = b.iw;
+      double tx = (double)t.x * af.x, ty = (double)t.y * af.y, tz = (double)t.z * af.z;
+      w.x = (float)(w.x + dt * (e[0] * tx + e[1] * ty + e[2] * tz));
+      w.y = (float)(w.y + dt * (e[3] * tx + e[4] * ty + e[5] * tz));
+      w.z = (float)(w.z + dt * (e[6] * tx + e[7] * ty + e[8] * tz));
+      p.x = (float)(p.x + v.x * dt);
+      p.y = (float)(p.y + v.y * dt);
+      p.z = (float)(p.z + v.z * dt);
+      q = qintegrate(q, w, dt, af);
+      if (qn) q = P.qn_fast ? qnormalize_fast(q) : qnormalize(q);
+      st3(b.pos, p);
+      st4q(b.quat, q);
+      b.flags |= BF_AABB_DIRTY;
+      f3 I = ld3(b.inv_inertia);
+      if (!(I.x == I.y && I.y == I.z)) inertia_world(q, I, b.iw);
+    }
+    st3(b.force, f3{0.f, 0.f, 0.f});
+    st3(b.torque, f3{0.f, 0.f, 0.f});
+    if (P.allow_sleep && (b.flags & BF_ALLOW_SLEEP)) {
+      int st = b.sleep_state;
+      double s2 = length2(v) + length2(w);
+      double lim2 = b.sleep_speed_limit * b.sleep_speed_limit;
+      if (st == CP_AWAKE && s2 < lim2) {
+        b.sleep_state = CP_SLEEPY;
+        b.time_last_sleepy = time;
+      } else if (st == CP_SLEEPY && s2 > lim2) {
+        b.sleep_state = CP_AWAKE;
+        b.flags &= ~BF_WAKE;
+      } else if (st == CP_SLEEPY && time - b.time_last_sleepy > b.sleep_time_limit) {
+        b.sleep_state = CP_SLEEPING;
+        v = f3{0.f, 0.f, 0.f};
+        w = f3{0.f, 0.f, 0.f};
+        b.flags &= ~BF_WAKE;
+      }
+    }
+    st3(b.vel, v);
+    st3(b.avel, w);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+
+DI void step_world(Smem& S, double dt) {
+  if (threadIdx.x == 0) {
+    S.overflow = 0;
+    S.n_pairs = S.n_contacts = S.n_rows = S.n_levels = 0;
+    S.n_fric = S.n_cand = 0;
+  }
+  __syncthreads();
+  ph_prepare(S);
+  if (S.P.broadphase == CP_BROAD_SAP) ph_broad_sap(S);
+  else if (S.P.broadphase == CP_BROAD_GRID) ph_broad_grid(S);
+  else ph_broad_naive(S);
+  if (S.overflow) return;
+  if (S.P.n_nocollide > 0) ph_nocollide(S);
+  ph_narrow(S);
+  if (S.overflow) return;
+  ph_rows_list(S);
+  if (S.overflow) return;
+  // ---- body state changes from here on ----
+  ph_contacts_post(S);
+  ph_solve_prep(S);
+  ph_rows_assemble(S, dt);
+  if (S.n_rows > 0) {
+    ph_levels(S);
+    ph_solve(S, dt);
+    ph_solve_apply(S, dt);
+  } else if (threadIdx.x == 0) {
+    S.P.last_iterations = 0;
+  }
+  __syncthreads();
+  ph_integrate(S, dt);
+}
+
+__global__ void __launch_bounds__(BT, 1) k_step_worlds(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n,
+                                                       double dt, int* __restrict__ queue) {
+  __shared__ Smem S;
+  for (;;) {
+    if (threadIdx.x == 0) S.wi = atomicAdd(queue, 1);
+    __syncthreads();
+    const int wi = S.wi;
+    if (wi >= n) break;
+    if (threadIdx.x == 0) {
+      S.W = worlds[ids[wi]];
+      S.P = *S.W.P;
+    }
+    __syncthreads();
+    if (S.P.status == 0) {
+      step_world(S, dt);
+      if (threadIdx.x == 0) {
+        DWorldParams* gp = S.W.P;
+        gp->num_pairs = S.n_pairs;
+        gp->num_contacts = S.n_contacts;
+        gp->num_rows = S.n_rows;
+        gp->num_levels = S.n_levels;
+        if (S.overflow) {
+          gp->status = S.overflow;
+        } else {
+          gp->last_iterations = S.P.last_iterations;
+          gp->stepnumber = S.P.stepnumber + 1;
+          gp->time = S.P.time + dt;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_gather_status(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n, long long* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const DWorldParams* p = worlds[ids[i]].P;
+  out[4 * i + 0] = p->status;
+  out[4 * i + 1] = p->stepnumber;
+  out[4 * i + 2] = p->num_pairs;
+  out[4 * i + 3] = ((long long)p->num_contacts << 32) | (unsigned)p->num_rows;
+}
+
+__global__ void k_clear_status(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) worlds[ids[i]].P->status = 0;
+}
+
+// ---------------------------------------------------------------------------
+
+cudaError_t cpk_gather_status(const DWorld* d_worlds, const int* d_ids, int n, long long* d_out, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  k_gather_status<<<(n + 255) / 256, 256, 0, stream>>>(d_worlds, d_ids, n, d_out);
+  return cudaGetLastError();
+}
+
+cudaError_t cpk_clear_status(const DWorld* d_worlds, const int* d_ids, int n, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  k_clear_status<<<(n + 255) / 256, 256, 0, stream>>>(d_worlds, d_ids, n);
+  return cudaGetLastError();
+}
+
+int cpk_block_threads() { return BT; }
+
+cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, int n, double dt, int* d_queue, int grid,
+                            cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
+  if (e != cudaSuccess) return e;
+  k_step_worlds<<<grid, BT, 0, stream>>>(d_worlds, d_ids, n, dt, d_queue);
+  return cudaGetLastError();
+}
+
+int cpk_max_resident_blocks() {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_worlds, BT, 0);
+  return nb;
+}

@@ -1,0 +1,191 @@
+// cp_types.h -- device-resident world layout shared by the host runtime
+// (cp_host.cpp) and the step kernels (cp_step.cu).
+//
+// One World is a set of arrays in device memory.  Bodies are 512-byte
+// records: every phase of a step touches a handful of fields of a body, and
+// pairs and solver rows gather bodies by index, so a record per body keeps
+// those gathers to a few cache lines.  Scratch (pairs, contacts, rows,
+// solver levels) belongs to the world and keeps the last step's lists for
+// cp_world_get_pairs / get_contacts / get_rows.
+#pragma once
+#include <cstdint>
+
+#include "../../include/cannon_gpu.h"
+
+#define CP_MAX_HULL_VERTS 32
+#define CP_MAX_FACE_VERTS 16
+#define CP_MAX_CLIP 48
+#define CP_MAX_PAIR_CONTACTS 32
+
+// body flags
+#define BF_ALLOW_SLEEP 1
+#define BF_WAKE 2
+#define BF_RESPONSE 4
+#define BF_TRIGGER 8
+#define BF_FIXED_ROT 16
+#define BF_AABB_DIRTY 32
+
+// step status bits (DWorldParams.status)
+#define ST_PAIRS_OVERFLOW 1
+#define ST_CONTACTS_OVERFLOW 2
+#define ST_ROWS_OVERFLOW 4
+#define ST_LEVELS_OVERFLOW 8
+#define ST_HULL_OVERFLOW 16
+#define ST_BINS_OVERFLOW 32
+#define ST_NONFINITE 64
+#define ST_TIMEOUT 128
+
+struct __align__(16) DBody {
+  float pos[4];     // Body.position
+  float quat[4];    // Body.quaternion (x, y, z, w)
+  float vel[4];     // Body.velocity
+  float avel[4];    // Body.angularVelocity
+  float force[4];   // Body.force
+  float torque[4];  // Body.torque
+  float iw[12];     // Body.invInertiaWorld, e[3*row+col]
+  float inv_inertia[4];
+  float lin_factor[4];
+  float ang_factor[4];
+  float aabb_lo[4];
+  float aabb_hi[4];
+  float shape_off[4];
+  float shape_quat[4];
+  float prev_pos[4];
+  float prev_quat[4];
+  double mass, inv_mass, lin_damp, ang_damp;
+  double sleep_speed_limit, sleep_time_limit, time_last_sleepy, bounding_radius;
+  int type, sleep_state, flags, group;
+  int mask, material, shape, pad0;
+  float brad32;  // bounding_radius rounded to float (broadphase filter only)
+  float pad1[3];
+};
+
+struct __align__(16) DShape {
+  int type, group, mask, response;
+  int material, hull, plane_done, pad1;
+  double radius, bsr;
+  float he[4];
+  float plane_n[4];  // Plane.worldNormal, computed once by the grid broadphase (plane.dart:182-187)
+};
+
+// Convex hull tables (ConvexPolyhedron: vertices, faces, faceNormals,
+// uniqueEdges), plus the per-face data the clipping code derives every time
+// in the reference: the connected faces of each face and -n.v0.
+struct __align__(16) DHull {
+  int v0, nv, f0, nf;        // vertices [v0, v0+nv), faces [f0, f0+nf)
+  int e0, ne, has_axes, pad; // unique edges [e0, e0+ne)
+};
+struct __align__(16) DFace {
+  int i0, n;     // vertex indices hfi[i0 .. i0+n)
+  int c0, nc;    // connected faces hconn[c0 .. c0+nc)
+  float normal[4];
+  double plane_const;
+};
+
+struct DMaterial { double friction, restitution; };
+
+struct DContactMaterial {
+  double friction, restitution, cs, cr, fs, fr;
+  double ca, cb, ceps, fa, fb, feps;  // SPOOK a, b, eps for contact / friction rows at the current dt
+};
+
+struct __align__(16) DConstraint {
+  int type, a, b, collide;
+  int row0, nrows, motor, pad;
+  float piv_a[4], piv_b[4], axis_a[4], axis_b[4];
+  double distance, max_force, motor_target, motor_max_force;
+  double sa, sb, seps, cos_max;  // SPOOK params of the constraint rows; cos(maxAngle) from libm
+  // per-step geometry
+  float ri[4], rj[4], n[4];
+  float r1a[4], r2a[4], wb[4], ma[4], mb[4];
+};
+
+struct __align__(16) DContact {
+  int bi, bj, si, sj;
+  float ni[4], ri[4], rj[4];
+  int enabled, pair, cm, frow;  // frow: index of the first friction candidate, -1 if none
+  double restitution;
+  double slip;  // mug * reducedMass
+};
+
+struct __align__(16) DRow {
+  float gaS[4], gaR[4], gbS[4], gbR[4];
+  float iMaR[4], iMbR[4];  // invInertiaWorldSolve * rotational Jacobians (the addToWlambda temp)
+  double B, invC, eps, minF, maxF, lambda;
+  double imA, imB;          // invMassSolve of bi, bj
+  double mult;              // Equation.multiplier = lambda / h
+  int bi, bj, kind, src;
+};
+
+struct __align__(16) DBodyScr {
+  float xs[4];   // shape world position
+  float qs[4];   // shape world orientation
+  float vl[4];   // vlambda
+  float wl[4];   // wlambda
+  float imf[4];  // force * invMassSolve (computeGiMf)
+  float iit[4];  // invInertiaWorldSolve * torque
+  double im_solve;
+  int active, last_level;
+};
+
+struct __align__(16) DWorldParams {
+  double time, tolerance, dt_cached;
+  long long stepnumber;
+  float gravity[4], fgrav[4];
+  float grid_min[4], grid_max[4];
+  int nb, nshapes, nmat, ncm;
+  int ncons, ncon_rows, iterations, broadphase;
+  int sap_axis, use_bb, allow_sleep, qn_skip;
+  int qn_fast, has_fgrav, grid_nx, grid_ny;
+  int grid_nz, nbins, status, last_iterations;
+  int num_pairs, num_contacts, num_rows, num_levels;
+  int pairs_cap, contacts_cap, rows_cap, bins_cap;
+  int grid_plane_done, n_nocollide, pad[2];
+  float grid_plane_n[4];
+};
+
+struct DWorld {
+  DWorldParams* P;
+  DBody* bodies;
+  DShape* shapes;
+  DHull* hulls;
+  DFace* faces;
+  float* hverts;   // float4 per vertex
+  float* hedges;   // float4 per unique edge
+  float* haxes;    // unused by the step (uniqueAxes only gate face tests)
+  int* hfi;        // face vertex indices
+  int* hconn;      // connected faces
+  DMaterial* mats;
+  int* cm_table;   // nmat*nmat -> contact material index or -1
+  DContactMaterial* cms;  // [0] = world default
+  DConstraint* cons;
+  int* nocollide;  // body pairs (a, b) of constraints with collideConnected == false
+  double* dpow;    // per body: pow(1 - linearDamping, dt), pow(1 - angularDamping, dt) for the cached dt
+  // scratch
+  DBodyScr* bscr;
+  int* sap_order;
+  int* sap_tmp;
+  int* pair_a;
+  int* pair_b;
+  int* pair_cnt;
+  int* pair_tstart;
+  int* heavy;
+  DContact* ctmp;
+  DContact* contacts;
+  int* cscr;       // per-contact scratch (contacts_cap + 1)
+  int* cand;       // row candidate -> kept row index, or -1
+  DRow* rows;
+  double* absdl;
+  int* level_of;
+  int* level_rows;
+  int* level_start;
+  int* level_cursor;
+  float* sap_key;
+  int* bin_cnt;    // grid: per-bin counts / cursors (nbins + 1)
+  int* bin_start;  // nbins + 1
+  int* bin_body;   // bins_cap entries, bodies of each bin in body order
+  float* bin_acc;  // nx + ny + nz accumulated bin-centre offsets
+  long long* hkeys;  // pair de-duplication hash (hash_cap)
+  int* hvals;
+  int hash_cap;
+};

@@ -1,0 +1,153 @@
+"""ctypes binding of libcannon_gpu.so (include/cannon_gpu.h).
+
+`Context` owns a CUDA stream and the device worlds; `GpuWorld` is one World
+resident in HBM.  There is no CPU fallback: if the library is missing the
+import of the engine fails with instructions to build it.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi as A
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libcannon_gpu.so")
+_lib = None
+
+
+class CannonError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"status {status}: {msg}")
+        self.status = status
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        vp, i32, f64 = C.c_void_p, C.c_int32, C.c_double
+        L.cp_last_error.restype = C.c_char_p
+        L.cp_abi_version.restype = C.c_int
+        L.cp_shape_setup.argtypes = [vp]
+        L.cp_body_setup.argtypes = [vp, i32, vp, i32]
+        L.cp_create.argtypes = [vp, vp]
+        L.cp_destroy.argtypes = [vp]
+        L.cp_world_create.argtypes = [vp, vp, vp]
+        L.cp_world_destroy.argtypes = [vp, i32]
+        L.cp_world_step.argtypes = [vp, i32, f64, i32]
+        L.cp_world_get_bodies.argtypes = [vp, i32, vp, i32]
+        L.cp_world_set_bodies.argtypes = [vp, i32, vp, i32]
+        L.cp_world_get_pairs.argtypes = [vp, i32, vp, vp, i32, vp]
+        L.cp_world_get_contacts.argtypes = [vp, i32, vp, i32, vp]
+        L.cp_world_get_rows.argtypes = [vp, i32, vp, i32, vp]
+        L.cp_world_get_info.argtypes = [vp, i32, vp]
+        L.cp_world_get_sap_order.argtypes = [vp, i32, vp, i32]
+        L.cp_batch_step.argtypes = [vp, vp, i32, f64, i32]
+        L.cp_kernel_launches.argtypes = [vp]
+        L.cp_kernel_launches.restype = C.c_int64
+        _lib = L
+    return _lib
+
+
+def check(status, what=""):
+    if status != A.CP_OK:
+        raise CannonError(status, f"{what}: {lib().cp_last_error().decode()}")
+
+
+def setup_scene(scene):
+    """Run the Shape / Body constructor arithmetic (cp_shape_setup, cp_body_setup)
+    over a scene in place; host-only, no GPU needed."""
+    L = lib()
+    for i in range(len(scene.shapes)):
+        check(L.cp_shape_setup(scene.shapes[i:i + 1].ctypes.data), "cp_shape_setup")
+    check(L.cp_body_setup(A.ptr(scene.shapes), len(scene.shapes), A.ptr(scene.bodies), len(scene.bodies)), "cp_body_setup")
+    return scene
+
+
+class Context:
+    def __init__(self, device=0):
+        cfg = A.Config(device, 0, 0)
+        h = C.c_void_p()
+        check(lib().cp_create(C.byref(cfg), C.byref(h)), "cp_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().cp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def launches(self):
+        return int(lib().cp_kernel_launches(self.h))
+
+    def world(self, scene):
+        return GpuWorld(self, scene)
+
+    def batch_step(self, worlds, dt, nsteps):
+        ids = np.array([w.id for w in worlds], dtype=np.int32)
+        check(lib().cp_batch_step(self.h, ids.ctypes.data, len(ids), dt, nsteps), "cp_batch_step")
+
+
+class GpuWorld:
+    def __init__(self, ctx, scene):
+        self.ctx = ctx
+        self.scene = scene
+        self.n = scene.num_bodies
+        desc = scene.world_desc()
+        wid = C.c_int32()
+        check(lib().cp_world_create(ctx.h, C.byref(desc), C.byref(wid)), "cp_world_create")
+        self.id = wid.value
+
+    def destroy(self):
+        if self.id is not None and self.ctx.h:
+            check(lib().cp_world_destroy(self.ctx.h, self.id), "cp_world_destroy")
+            self.id = None
+
+    def step(self, dt=None, nsteps=1):
+        check(lib().cp_world_step(self.ctx.h, self.id, self.scene.dt if dt is None else dt, nsteps), "cp_world_step")
+
+    def bodies(self):
+        out = np.zeros(self.n, dtype=A.BODY_DTYPE)
+        check(lib().cp_world_get_bodies(self.ctx.h, self.id, out.ctypes.data, self.n), "get_bodies")
+        return out
+
+    def set_bodies(self, bodies):
+        bodies = np.ascontiguousarray(bodies, dtype=A.BODY_DTYPE)
+        check(lib().cp_world_set_bodies(self.ctx.h, self.id, bodies.ctypes.data, self.n), "set_bodies")
+
+    def info(self):
+        inf = A.StepInfo()
+        check(lib().cp_world_get_info(self.ctx.h, self.id, C.byref(inf)), "get_info")
+        return inf
+
+    def pairs(self):
+        n = self.info().num_pairs
+        p1 = np.zeros(max(n, 1), np.int32)
+        p2 = np.zeros(max(n, 1), np.int32)
+        cnt = C.c_int32()
+        check(lib().cp_world_get_pairs(self.ctx.h, self.id, p1.ctypes.data, p2.ctypes.data, len(p1), C.byref(cnt)), "pairs")
+        return p1[:cnt.value], p2[:cnt.value]
+
+    def contacts(self):
+        n = self.info().num_contacts
+        out = np.zeros(max(n, 1), dtype=A.CONTACT_DTYPE)
+        cnt = C.c_int32()
+        check(lib().cp_world_get_contacts(self.ctx.h, self.id, out.ctypes.data, len(out), C.byref(cnt)), "contacts")
+        return out[:cnt.value]
+
+    def rows(self):
+        n = self.info().num_rows
+        out = np.zeros(max(n, 1), dtype=A.ROW_DTYPE)
+        cnt = C.c_int32()
+        check(lib().cp_world_get_rows(self.ctx.h, self.id, out.ctypes.data, len(out), C.byref(cnt)), "rows")
+        return out[:cnt.value]
+
+    def sap_order(self):
+        out = np.zeros(self.n, np.int32)
+        check(lib().cp_world_get_sap_order(self.ctx.h, self.id, out.ctypes.data, self.n), "sap order")
+        return out

@@ -1,0 +1,369 @@
+"""Seeded synthetic scenes for the World.step workloads.
+
+The reference publishes no benchmark scenes, so these stand in for them with
+the shapes, sizes and value distributions of the five workloads:
+
+  spheres_on_plane   64 Sphere(0.5) dropped on a Plane, NaiveBroadphase, 10 iterations
+  box_pile           4096 random boxes piled on a Plane, SAPBroadphase(x), 20 iterations
+  mixed_chains       8192 spheres/boxes/cylinders, 128 chains of 16 joined by
+                     PointToPoint/Hinge/Distance, GridBroadphase(cell 1.0), sleeping
+  batch_worlds       4096 worlds of log-uniform 8..512 spheres/boxes, Naive, 10 iterations
+  serve_requests     Poisson arrivals of worlds with 16..4096 bodies and horizons 1..240
+
+Random numbers come from SplitMix64 (53-bit uniform doubles) and random unit
+quaternions from Shoemake's method, so every scene is reproducible from its
+seed.  Bodies are built the way the reference builds them:
+Body(mass, position, quaternion) then addShape, so inertia comes from the
+rotated AABB (lib/objects/rigid_body.dart:587-609).
+"""
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi as A
+
+_GAMMA = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+class SplitMix64:
+    """SplitMix64 stream; `uniform(n)` returns n doubles in [0, 1)."""
+
+    def __init__(self, seed):
+        self.state = np.uint64(seed & 0xFFFFFFFFFFFFFFFF)
+
+    def next_u64(self, n):
+        with np.errstate(over="ignore"):
+            k = np.arange(1, n + 1, dtype=np.uint64)
+            z = self.state + k * _GAMMA
+            self.state = self.state + np.uint64(n) * _GAMMA
+            z = (z ^ (z >> np.uint64(30))) * _M1
+            z = (z ^ (z >> np.uint64(27))) * _M2
+            z = z ^ (z >> np.uint64(31))
+        return z
+
+    def uniform(self, n):
+        return (self.next_u64(n) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def shoemake(u1, u2, u3):
+    """Uniform random unit quaternions (x, y, z, w) from three uniforms."""
+    a = np.sqrt(1.0 - u1)
+    b = np.sqrt(u1)
+    t2 = 2.0 * math.pi * u2
+    t3 = 2.0 * math.pi * u3
+    return np.stack([a * np.sin(t2), a * np.cos(t2), b * np.sin(t3), b * np.cos(t3)], axis=-1)
+
+
+def euler_xyz(x, y, z):
+    """Quaternion.setFromEuler(x, y, z, Order.xyz) (lib/math/quaternion.dart:358-370)."""
+    c1, c2, c3 = math.cos(x / 2), math.cos(y / 2), math.cos(z / 2)
+    s1, s2, s3 = math.sin(x / 2), math.sin(y / 2), math.sin(z / 2)
+    return (s1 * c2 * c3 + c1 * s2 * s3, c1 * s2 * c3 - s1 * c2 * s3, c1 * c2 * s3 + s1 * s2 * c3, c1 * c2 * c3 - s1 * s2 * s3)
+
+
+@dataclass
+class Scene:
+    """A World descriptor held as numpy arrays (layouts of include/cannon_gpu.h)."""
+
+    name: str
+    shapes: np.ndarray
+    bodies: np.ndarray
+    gravity: tuple = (0.0, -9.82, 0.0)
+    materials: np.ndarray = field(default_factory=lambda: np.zeros(0, dtype=A.MATERIAL_DTYPE))
+    contact_materials: np.ndarray = field(default_factory=lambda: np.zeros(0, dtype=A.CONTACT_MATERIAL_DTYPE))
+    constraints: np.ndarray = field(default_factory=lambda: np.zeros(0, dtype=A.CONSTRAINT_DTYPE))
+    friction: float = 0.3
+    restitution: float = 0.0
+    iterations: int = 10
+    tolerance: float = 1e-7
+    broadphase: int = A.BROAD_NAIVE
+    sap_axis: int = 0
+    grid_n: tuple = (10, 10, 10)
+    grid_min: tuple = (0.0, 0.0, 0.0)
+    grid_max: tuple = (1.0, 1.0, 1.0)
+    allow_sleep: bool = False
+    dt: float = 1.0 / 60.0
+    steps: int = 1
+    quat_normalize_skip: int = 0
+    quat_normalize_fast: bool = False
+    use_bounding_boxes: bool = False
+    enable_friction_reduction: bool = False
+    time: float = 0.0
+    stepnumber: int = 0
+    _keep: list = field(default_factory=list)
+
+    @property
+    def num_bodies(self):
+        return len(self.bodies)
+
+    def world_desc(self):
+        """cp_world_desc pointing at this scene's arrays (kept alive by the scene)."""
+        d = A.WorldDesc()
+        d.num_bodies = len(self.bodies)
+        d.num_shapes = len(self.shapes)
+        d.num_materials = len(self.materials)
+        d.num_contact_materials = len(self.contact_materials)
+        d.num_constraints = len(self.constraints)
+        d.allow_sleep = int(self.allow_sleep)
+        d.quat_normalize_skip = self.quat_normalize_skip
+        d.quat_normalize_fast = int(self.quat_normalize_fast)
+        d.solver_iterations = self.iterations
+        d.broadphase = self.broadphase
+        d.use_bounding_boxes = int(self.use_bounding_boxes)
+        d.sap_axis = self.sap_axis
+        d.grid_n[:] = list(self.grid_n)
+        d.enable_friction_reduction = int(self.enable_friction_reduction)
+        d.has_friction_gravity = 0
+        d.stepnumber = self.stepnumber
+        d.solver_tolerance = self.tolerance
+        d.time = self.time
+        d.gravity[:] = list(self.gravity)
+        d.grid_aabb_min[:] = list(self.grid_min)
+        d.grid_aabb_max[:] = list(self.grid_max)
+        for arr in (self.bodies, self.shapes, self.materials, self.contact_materials, self.constraints):
+            assert arr.flags["C_CONTIGUOUS"]
+        d.bodies = A.ptr(self.bodies)
+        d.shapes = A.ptr(self.shapes)
+        d.materials = A.ptr(self.materials)
+        d.contact_materials = A.ptr(self.contact_materials)
+        d.constraints = A.ptr(self.constraints)
+        d.sap_axis_list = 0
+        d.default_contact_material = A.default_contact_material(self.friction, self.restitution)
+        return d
+
+
+def _plane_body(bodies, shapes, i, shape_index, y=0.0):
+    q = euler_xyz(-math.pi / 2, 0.0, 0.0)  # groundBody.quaternion.setFromEuler(-pi/2, 0, 0)
+    shapes[shape_index]["type"] = A.SHAPE_PLANE
+    bodies[i]["mass"] = 0.0
+    bodies[i]["position"] = (0.0, y, 0.0)
+    bodies[i]["quaternion"] = q
+    bodies[i]["shape"] = shape_index
+
+
+def spheres_on_plane(n=64, seed=1, radius=0.5):
+    """64 Sphere(0.5), mass 1, positions U[-5,5]xU[1,20]xU[-5,5], on a Plane at y=0."""
+    rng = SplitMix64(seed)
+    shapes = A.default_shapes(2)
+    bodies = A.default_bodies(n + 1)
+    _plane_body(bodies, shapes, 0, 0)
+    shapes[1]["type"] = A.SHAPE_SPHERE
+    shapes[1]["radius"] = radius
+    u = rng.uniform(3 * n).reshape(n, 3)
+    pos = np.stack([-5 + 10 * u[:, 0], 1 + 19 * u[:, 1], -5 + 10 * u[:, 2]], axis=1)
+    bodies["mass"][1:] = 1.0
+    bodies["position"][1:] = pos
+    bodies["shape"][1:] = 1
+    return Scene("spheres_on_plane", shapes, bodies, friction=0.3, restitution=0.0, iterations=10,
+                 broadphase=A.BROAD_NAIVE, dt=1 / 60, steps=600)
+
+
+def _box_shapes(shapes, first, he):
+    k = len(he)
+    shapes["type"][first:first + k] = A.SHAPE_BOX
+    shapes["half_extents"][first:first + k] = he
+
+
+def box_pile(nx=16, nz=16, layers=16, seed=2, pitch=1.1):
+    """4096 boxes (half-extents U[0.2,0.5], density 1, random orientation) in a
+    16x16 footprint of 16 layers above a Plane; SAP on x, 20 iterations."""
+    rng = SplitMix64(seed)
+    n = nx * nz * layers
+    shapes = A.default_shapes(n + 1)
+    bodies = A.default_bodies(n + 1)
+    _plane_body(bodies, shapes, 0, 0)
+    u = rng.uniform(6 * n).reshape(n, 6)
+    he = (0.2 + 0.3 * u[:, :3]).astype(np.float32)
+    _box_shapes(shapes, 1, he)
+    q = shoemake(u[:, 3], u[:, 4], u[:, 5])
+    idx = np.arange(n)
+    ix, iz, k = idx % nx, (idx // nx) % nz, idx // (nx * nz)
+    pos = np.stack([(ix - (nx - 1) / 2) * pitch, 0.6 + pitch * k, (iz - (nz - 1) / 2) * pitch], axis=1)
+    hed = he.astype(np.float64)
+    bodies["mass"][1:] = 8.0 * hed[:, 0] * hed[:, 1] * hed[:, 2] * 1.0
+    bodies["position"][1:] = pos
+    bodies["quaternion"][1:] = q
+    bodies["shape"][1:] = np.arange(1, n + 1)
+    return Scene("box_pile", shapes, bodies, friction=0.4, restitution=0.0, iterations=20,
+                 broadphase=A.BROAD_SAP, sap_axis=0, dt=1 / 60, steps=300)
+
+
+def mixed_chains(nx=32, nz=16, layers=16, seed=3, pitch=1.3, chains=128, chain_len=16, segments=10):
+    """8192 bodies (40% Sphere r U[0.2,0.6], 40% Box as box_pile, 20% Cylinder
+    with 10 segments r U[0.2,0.5] h U[0.4,1.0]) on a lattice; the first 2048
+    form 128 chains of 16 along x joined by PointToPoint / Hinge(axis z) /
+    Distance by link index mod 3.  GridBroadphase with unit cells over the
+    scene bounds +-1, sleeping on, 15 iterations, dt 1/120."""
+    rng = SplitMix64(seed)
+    n = nx * nz * layers
+    shapes = A.default_shapes(n + 1)
+    bodies = A.default_bodies(n + 1)
+    _plane_body(bodies, shapes, 0, 0)
+    u = rng.uniform(8 * n).reshape(n, 8)
+    kind = np.arange(n) % 5  # 0,1 sphere; 2,3 box; 4 cylinder
+    idx = np.arange(n)
+    ix, iz, k = idx % nx, (idx // nx) % nz, idx // (nx * nz)
+    pos = np.stack([(ix - (nx - 1) / 2) * pitch, 1.0 + pitch * k, (iz - (nz - 1) / 2) * pitch], axis=1)
+    mass = np.zeros(n)
+    sph = kind <= 1
+    box = (kind == 2) | (kind == 3)
+    cyl = kind == 4
+    s = shapes[1:]
+    s["type"][sph] = A.SHAPE_SPHERE
+    r = 0.2 + 0.4 * u[sph, 0]
+    s["radius"][sph] = r
+    mass[sph] = 4.0 / 3.0 * math.pi * r ** 3
+    he = (0.2 + 0.3 * u[box, :3]).astype(np.float32)
+    s["type"][box] = A.SHAPE_BOX
+    s["half_extents"][box] = he
+    hed = he.astype(np.float64)
+    mass[box] = 8.0 * hed[:, 0] * hed[:, 1] * hed[:, 2]
+    s["type"][cyl] = A.SHAPE_CYLINDER
+    rc = 0.2 + 0.3 * u[cyl, 0]
+    hc = 0.4 + 0.6 * u[cyl, 1]
+    s["radius_top"][cyl] = rc
+    s["radius_bottom"][cyl] = rc
+    s["height"][cyl] = hc
+    s["num_segments"][cyl] = segments
+    mass[cyl] = math.pi * rc ** 2 * hc
+    q = shoemake(u[:, 3], u[:, 4], u[:, 5])
+    q[sph] = (0.0, 0.0, 0.0, 1.0)
+    bodies["mass"][1:] = mass
+    bodies["position"][1:] = pos
+    bodies["quaternion"][1:] = q
+    bodies["shape"][1:] = np.arange(1, n + 1)
+    cons = np.zeros(chains * (chain_len - 1), dtype=A.CONSTRAINT_DTYPE)
+    c = 0
+    for ch in range(chains):
+        first = 1 + ch * chain_len
+        for j in range(chain_len - 1):
+            rec = cons[c]
+            rec["type"] = (A.CON_P2P, A.CON_HINGE, A.CON_DISTANCE)[j % 3]
+            rec["body_a"] = first + j
+            rec["body_b"] = first + j + 1
+            rec["collide_connected"] = 1
+            rec["pivot_a"] = (pitch / 2, 0.0, 0.0)
+            rec["pivot_b"] = (-pitch / 2, 0.0, 0.0)
+            rec["axis_a"] = (0.0, 0.0, 1.0)
+            rec["axis_b"] = (0.0, 0.0, 1.0)
+            rec["distance"] = -1.0
+            rec["max_force"] = 1e6
+            rec["spook_stiffness"] = 1e7
+            rec["spook_relaxation"] = 4.0
+            rec["spook_time_step"] = 1.0 / 60.0
+            c += 1
+    lo = np.minimum(pos.min(axis=0), 0.0) - 1.0
+    hi = pos.max(axis=0) + 1.0
+    lo32 = lo.astype(np.float32).astype(np.float64)
+    hi32 = hi.astype(np.float32).astype(np.float64)
+    gn = tuple(int(max(1, math.ceil(e))) for e in (hi32 - lo32))
+    return Scene("mixed_chains", shapes, bodies, constraints=cons, friction=0.3, restitution=0.0, iterations=15,
+                 broadphase=A.BROAD_GRID, grid_n=gn, grid_min=tuple(lo), grid_max=tuple(hi), allow_sleep=True,
+                 dt=1 / 120, steps=240)
+
+
+def column_world(n, seed, mix="sphere_box", footprint=None, pitch=1.2, name="world"):
+    """One world of `n` bodies dropped in a column above a Plane (the plane is
+    body 0, so the world holds n+1 bodies).  mix="sphere_box": 50/50 Sphere(0.5)
+    mass 1 / Box as box_pile; mix="mixed": the 40/40/20 sphere/box/cylinder mix."""
+    rng = SplitMix64(seed)
+    side = footprint or max(2, int(math.ceil(math.sqrt(n / 8.0))))
+    shapes = A.default_shapes(n + 1)
+    bodies = A.default_bodies(n + 1)
+    _plane_body(bodies, shapes, 0, 0)
+    u = rng.uniform(8 * n).reshape(n, 8)
+    idx = np.arange(n)
+    cell, layer = idx % (side * side), idx // (side * side)
+    jitter = (u[:, 6:8] - 0.5) * 0.1
+    pos = np.stack([(cell % side - (side - 1) / 2) * pitch + jitter[:, 0], 1.0 + pitch * layer,
+                    (cell // side - (side - 1) / 2) * pitch + jitter[:, 1]], axis=1)
+    s = shapes[1:]
+    mass = np.zeros(n)
+    if mix == "sphere_box":
+        sph = u[:, 7] < 0.5
+        box = ~sph
+        cyl = np.zeros(n, dtype=bool)
+        r = np.full(int(sph.sum()), 0.5)
+    else:
+        kind = (u[:, 7] * 5).astype(np.int64)
+        sph = kind <= 1
+        box = (kind == 2) | (kind == 3)
+        cyl = kind == 4
+        r = 0.2 + 0.4 * u[sph, 0]
+    s["type"][sph] = A.SHAPE_SPHERE
+    s["radius"][sph] = r
+    mass[sph] = 1.0 if mix == "sphere_box" else 4.0 / 3.0 * math.pi * r ** 3
+    he = (0.2 + 0.3 * u[box, :3]).astype(np.float32)
+    s["type"][box] = A.SHAPE_BOX
+    s["half_extents"][box] = he
+    hed = he.astype(np.float64)
+    mass[box] = 8.0 * hed[:, 0] * hed[:, 1] * hed[:, 2]
+    if cyl.any():
+        rc = 0.2 + 0.3 * u[cyl, 0]
+        hc = 0.4 + 0.6 * u[cyl, 1]
+        s["type"][cyl] = A.SHAPE_CYLINDER
+        s["radius_top"][cyl] = rc
+        s["radius_bottom"][cyl] = rc
+        s["height"][cyl] = hc
+        s["num_segments"][cyl] = 10
+        mass[cyl] = math.pi * rc ** 2 * hc
+    q = shoemake(u[:, 3], u[:, 4], u[:, 5])
+    q[sph] = (0.0, 0.0, 0.0, 1.0)
+    bodies["mass"][1:] = mass
+    bodies["position"][1:] = pos
+    bodies["quaternion"][1:] = q
+    bodies["shape"][1:] = np.arange(1, n + 1)
+    return Scene(name, shapes, bodies, friction=0.3, restitution=0.0, iterations=10, broadphase=A.BROAD_NAIVE,
+                 dt=1 / 60, steps=120)
+
+
+def batch_sizes(n_worlds=4096, seed=1000, lo=8, hi=512):
+    """Body counts floor(exp(U[ln lo, ln hi])) of the batched workload, one
+    SplitMix64 stream per world (seed+w)."""
+    out = np.empty(n_worlds, dtype=np.int64)
+    for w in range(n_worlds):
+        u = SplitMix64(seed + w).uniform(1)[0]
+        out[w] = int(math.floor(math.exp(math.log(lo) + u * (math.log(hi) - math.log(lo)))))
+    return np.minimum(out, hi)
+
+
+def batch_worlds(n_worlds=4096, seed=1000, lo=8, hi=512):
+    """The batched workload: world w has batch_sizes()[w] bodies plus its plane,
+    built from seed (seed+w)*7919+1."""
+    sizes = batch_sizes(n_worlds, seed, lo, hi)
+    return [column_world(int(sizes[w]), (seed + w) * 7919 + 1, "sphere_box", name=f"batch{w}") for w in range(n_worlds)]
+
+
+@dataclass
+class Request:
+    arrival: float
+    n_bodies: int
+    horizon: int
+    seed: int
+
+
+def serve_requests(rate=2000.0, window=60.0, seed=77, lo=16, hi=4096, max_horizon=240):
+    """Poisson arrivals at `rate` req/s over `window` seconds; each request is a
+    world of floor(exp(U[ln lo, ln hi])) bodies in the 40/40/20 mix and a
+    horizon uniform in 1..max_horizon steps."""
+    rng = SplitMix64(seed)
+    reqs = []
+    t = 0.0
+    i = 0
+    while True:
+        u = rng.uniform(3)
+        t += -math.log(1.0 - u[0]) / rate
+        if t >= window:
+            break
+        n = int(math.floor(math.exp(math.log(lo) + u[1] * (math.log(hi) - math.log(lo)))))
+        h = 1 + min(max_horizon - 1, int(u[2] * max_horizon))
+        reqs.append(Request(t, min(n, hi), h, seed * 1000003 + i))
+        i += 1
+    return reqs
+
+
+def request_world(req):
+    return column_world(req.n_bodies, req.seed, "mixed", name=f"req{req.seed}")

@@ -1,0 +1,273 @@
+/*
+ * cannon_gpu.h -- C ABI of the GB300 World.step engine for cannon_physics.
+ *
+ * The reference (Dart package cannon_physics 0.0.2) has no FFI.  Its pluggable
+ * seams are Dart objects hung on World: `World.internalStep(double dt)`
+ * (lib/world/world_class.dart:433-701), `Broadphase.collisionPairs`
+ * (lib/collision/broadphase.dart:39), `Narrowphase.getContacts`
+ * (lib/world/narrow_phase.dart:634) and `Solver.solve`
+ * (lib/solver/gs_solver.dart:74).  A Dart `GpuWorld extends World` overrides
+ * `internalStep` and reaches the entry points below through dart:ffi; every
+ * entry point names the reference code it stands in for.
+ *
+ * Conventions
+ *  - Every call returns a status (CP_OK or a CP_ERR_* code); `cp_last_error`
+ *    gives a thread-local message for the last failing call.
+ *  - No pointer passed in is retained after the call returns; host buffers are
+ *    read or written only during the call.
+ *  - Vector fields are binary32 because the reference stores Vector3,
+ *    Quaternion and Matrix3 components in Float32List (package:vector_math);
+ *    scalars (mass, damping, radii, time) are binary64 like Dart doubles.
+ *  - Matrix3 storage is the 9-float array the reference indexes as
+ *    e[3*row+col] (lib/math/mat3.dart:9-108).
+ *  - Calls on one context are serialized by the context.
+ */
+#ifndef CANNON_GPU_H
+#define CANNON_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CP_ABI_VERSION 1
+
+/* status codes */
+#define CP_OK               0
+#define CP_ERR_ARG          1   /* invalid argument or descriptor */
+#define CP_ERR_CAPACITY     2   /* a scratch capacity was exceeded (state left as before the step) */
+#define CP_ERR_NONFINITE    3   /* NaN/Inf found in body state after a step */
+#define CP_ERR_TIMEOUT      4   /* a bounded device-side wait gave up */
+#define CP_ERR_OOM          5   /* device or host allocation failed */
+#define CP_ERR_CUDA         6   /* CUDA runtime error */
+#define CP_ERR_UNSUPPORTED  7   /* feature outside the supported subset */
+
+/* ShapeType order of lib/rigid_body_shapes/shape.dart:6-18 (the order decides
+ * which shape is passed first to a narrowphase resolver). */
+enum cp_shape_type {
+  CP_SHAPE_SPHERE = 0,
+  CP_SHAPE_PLANE = 1,
+  CP_SHAPE_BOX = 2,
+  CP_SHAPE_CONVEX = 3,
+  CP_SHAPE_CYLINDER = 4
+};
+
+/* BodyTypes / BodySleepStates, lib/objects/rigid_body.dart:15-16 */
+enum cp_body_type { CP_BODY_DYNAMIC = 0, CP_BODY_STATIC = 1, CP_BODY_KINEMATIC = 2 };
+enum cp_sleep_state { CP_AWAKE = 0, CP_SLEEPY = 1, CP_SLEEPING = 2 };
+
+/* Broadphase plugins: NaiveBroadphase (lib/collision/naive_broadphase.dart),
+ * SAPBroadphase (lib/collision/sap_broadphase.dart), GridBroadphase
+ * (lib/collision/grid_broadphase.dart, with per-bin lists and a working pair
+ * de-duplication; the reference version throws on its first step). */
+enum cp_broadphase_kind { CP_BROAD_NAIVE = 0, CP_BROAD_SAP = 1, CP_BROAD_GRID = 2 };
+
+/* Constraint classes, lib/constraints/*.dart */
+enum cp_constraint_type { CP_CON_POINT_TO_POINT = 0, CP_CON_HINGE = 1, CP_CON_DISTANCE = 2 };
+
+/* Equation classes appearing as solver rows, lib/equations/*.dart */
+enum cp_row_kind { CP_ROW_CONTACT = 0, CP_ROW_FRICTION = 1, CP_ROW_ROTATIONAL = 2, CP_ROW_MOTOR = 3 };
+
+/* Shape (lib/rigid_body_shapes/{sphere,plane,box,convex_polyhedron,cylinder}.dart).
+ * A CONVEX shape lists its hull: `vertices` (3 floats each), `face_sizes`
+ * (vertex count per face) and `face_indices` (concatenated faces); `axes`
+ * (3 floats each) is the optional `uniqueAxes` list (has_axes=0 means null). */
+typedef struct cp_shape_desc {
+  int32_t type;
+  int32_t collision_filter_group;   /* Shape default -1 */
+  int32_t collision_filter_mask;    /* Shape default -1 */
+  int32_t collision_response;       /* default 1 */
+  int32_t material;                 /* index into cp_world_desc.materials, -1 = null */
+  int32_t num_segments;             /* cylinder */
+  double radius;                    /* sphere */
+  double radius_top, radius_bottom, height;  /* cylinder */
+  float half_extents[3];            /* box */
+  int32_t num_vertices, num_faces, num_axes, has_axes;  /* convex */
+  const float* vertices;
+  const int32_t* face_sizes;
+  const int32_t* face_indices;
+  const float* axes;
+  double bounding_sphere_radius;    /* output of cp_shape_setup */
+} cp_shape_desc;
+
+/* Body state (lib/objects/rigid_body.dart:27-260).  One shape per body, at
+ * `shape_offset` / `shape_orientation` in the body frame. */
+typedef struct cp_body_desc {
+  float position[3];
+  float quaternion[4];              /* x, y, z, w */
+  float velocity[3];
+  float angular_velocity[3];
+  float force[3];
+  float torque[3];
+  float linear_factor[3];
+  float angular_factor[3];
+  float inv_inertia[3];
+  float inv_inertia_world[9];
+  float aabb_lower[3];
+  float aabb_upper[3];
+  float shape_offset[3];
+  float shape_orientation[4];
+  float previous_position[3];
+  float previous_quaternion[4];
+  double mass, inv_mass;
+  double linear_damping, angular_damping;
+  double sleep_speed_limit, sleep_time_limit, time_last_sleepy;
+  double bounding_radius;
+  int32_t type, sleep_state, allow_sleep, wake_up_after_narrowphase;
+  int32_t collision_filter_group, collision_filter_mask, collision_response, is_trigger;
+  int32_t material;                 /* -1 = null */
+  int32_t shape;                    /* index into cp_world_desc.shapes */
+  int32_t fixed_rotation, aabb_needs_update;
+} cp_body_desc;
+
+/* Material (lib/material/material.dart): -1 means "not set". */
+typedef struct cp_material {
+  double friction, restitution;
+} cp_material;
+
+/* ContactMaterial (lib/material/contact_material.dart:63-101). */
+typedef struct cp_contact_material {
+  int32_t material_a, material_b;   /* ignored for the world default */
+  double friction, restitution;
+  double contact_stiffness, contact_relaxation;
+  double friction_stiffness, friction_relaxation;
+} cp_contact_material;
+
+/* PointToPoint / Hinge / Distance constraint (lib/constraints/*.dart).
+ * spook_* are the Equation SPOOK parameters of the constraint rows; the
+ * reference constructor uses (1e7, 4, 1/60) whatever the step size
+ * (lib/equations/equation_class.dart:38). */
+typedef struct cp_constraint_desc {
+  int32_t type, body_a, body_b, collide_connected;
+  int32_t motor_enabled, pad0;
+  float pivot_a[3], pivot_b[3];
+  float axis_a[3], axis_b[3];
+  double distance;                  /* DistanceConstraint; <0 = use the current distance */
+  double max_force;
+  double motor_target_velocity, motor_max_force;
+  double spook_stiffness, spook_relaxation, spook_time_step;
+} cp_constraint_desc;
+
+/* World (lib/world/world_class.dart:135-162) plus solver/broadphase settings. */
+typedef struct cp_world_desc {
+  int32_t num_bodies, num_shapes, num_materials, num_contact_materials, num_constraints;
+  int32_t allow_sleep, quat_normalize_skip, quat_normalize_fast;
+  int32_t solver_iterations;        /* Solver.iterations, default 10 */
+  int32_t broadphase;               /* cp_broadphase_kind */
+  int32_t use_bounding_boxes;       /* Broadphase.useBoundingBoxes */
+  int32_t sap_axis;                 /* 0 = x, 1 = y, 2 = z */
+  int32_t grid_n[3];
+  int32_t enable_friction_reduction;
+  int32_t has_friction_gravity;
+  int32_t stepnumber;
+  double solver_tolerance;          /* default 1e-7 */
+  double time;
+  float gravity[3];
+  float friction_gravity[3];
+  float grid_aabb_min[3], grid_aabb_max[3];
+  const cp_body_desc* bodies;
+  const cp_shape_desc* shapes;
+  const cp_material* materials;
+  const cp_contact_material* contact_materials;
+  const cp_constraint_desc* constraints;
+  const int32_t* sap_axis_list;     /* optional persisted SAP order, NULL = body order */
+  cp_contact_material default_contact_material;
+} cp_world_desc;
+
+/* One narrowphase contact, in the order the reference appends them. */
+typedef struct cp_contact {
+  int32_t bi, bj;                   /* ContactEquation.bi / .bj body indices */
+  int32_t si, sj;                   /* ContactEquation.si / .sj shape indices */
+  float ni[3], ri[3], rj[3];
+  int32_t enabled, pair;            /* pair = index in the broadphase pair list */
+  double restitution;
+} cp_contact;
+
+/* One solver row, in GSSolver equation order. */
+typedef struct cp_row {
+  int32_t kind, bi, bj, pad;
+  double B, inv_c, lambda, multiplier, min_force, max_force, eps;
+} cp_row;
+
+typedef struct cp_step_info {
+  int64_t stepnumber;
+  double time;
+  int32_t num_pairs, num_contacts, num_rows, iterations;
+  int32_t status, num_bodies;
+  double profile_ms[4];             /* broadphase+narrowphase, rows, solve, integrate (plain path only) */
+} cp_step_info;
+
+typedef struct cp_config {
+  int32_t device;                   /* CUDA device ordinal */
+  int32_t block_threads;            /* 0 = autotuned */
+  int64_t arena_bytes;              /* 0 = grow on demand */
+} cp_config;
+
+typedef struct cp_ctx cp_ctx;
+
+/* ---- host-side setup (Body / Shape constructors) ------------------------ */
+
+/* Shape constructor work: Sphere/Box/Cylinder/ConvexPolyhedron init and
+ * updateBoundingSphereRadius (sphere.dart:119-144, box.dart:21-126,
+ * cylinder.dart:222-294, convex_polyhedron.dart:80-185,648-660).  Fills
+ * shape->bounding_sphere_radius. */
+int cp_shape_setup(cp_shape_desc* shape);
+
+/* Body(mass, position, quaternion) followed by addShape(shape, offset,
+ * orientation), for each of `num_bodies` bodies: updateMassProperties
+ * (rigid_body.dart:587-609, inertia from the body AABB) and
+ * updateBoundingRadius (:395-412).  Reads mass, position, quaternion, shape,
+ * shape_offset, shape_orientation, fixed_rotation and type (-1 = derive from
+ * mass); writes inv_mass, type, inertia-derived fields, aabb,
+ * bounding_radius, previous_* and aabb_needs_update.  Other fields are left
+ * as given (callers start from the Body constructor defaults). */
+int cp_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc* bodies, int32_t num_bodies);
+
+/* ---- context and worlds ------------------------------------------------- */
+
+int cp_create(const cp_config* cfg, cp_ctx** out);
+int cp_destroy(cp_ctx* ctx);
+
+/* Pack a World (bodies, shapes, materials, constraints, settings) into
+ * device memory.  Replaces World.addBody/addConstraint/addContactMaterial as
+ * the way state reaches the step (world_class.dart:224,282-299,343-348). */
+int cp_world_create(cp_ctx* ctx, const cp_world_desc* desc, int32_t* world_id);
+int cp_world_destroy(cp_ctx* ctx, int32_t world_id);
+
+/* World.step(dt) in fixed mode, nsteps times: internalStep then time += dt
+ * (world_class.dart:392-399,433-701). */
+int cp_world_step(cp_ctx* ctx, int32_t world_id, double dt, int32_t nsteps);
+
+/* Read back / overwrite body state (Body fields). */
+int cp_world_get_bodies(cp_ctx* ctx, int32_t world_id, cp_body_desc* out, int32_t n);
+int cp_world_set_bodies(cp_ctx* ctx, int32_t world_id, const cp_body_desc* in, int32_t n);
+
+/* Last step's broadphase pairs (worldStepP1/P2, world_class.dart:481-499),
+ * contacts (World.contacts) and solver rows (Solver.equations with B, 1/C,
+ * lambda and multiplier, gs_solver.dart:105-176). */
+int cp_world_get_pairs(cp_ctx* ctx, int32_t world_id, int32_t* p1, int32_t* p2, int32_t cap, int32_t* count);
+int cp_world_get_contacts(cp_ctx* ctx, int32_t world_id, cp_contact* out, int32_t cap, int32_t* count);
+int cp_world_get_rows(cp_ctx* ctx, int32_t world_id, cp_row* out, int32_t cap, int32_t* count);
+int cp_world_get_info(cp_ctx* ctx, int32_t world_id, cp_step_info* out);
+
+/* SAP axisList order (sap_broadphase.dart:11), kept across steps. */
+int cp_world_get_sap_order(cp_ctx* ctx, int32_t world_id, int32_t* out, int32_t n);
+
+/* ---- batched form ------------------------------------------------------- */
+
+/* Step many independent worlds together: one persistent fused launch per
+ * step, the nsteps sequence captured in a CUDA graph and replayed.  Each
+ * world's result equals cp_world_step on that world alone. */
+int cp_batch_step(cp_ctx* ctx, const int32_t* world_ids, int32_t n, double dt, int32_t nsteps);
+
+/* Number of GPU kernel launches issued by this context so far. */
+int64_t cp_kernel_launches(cp_ctx* ctx);
+
+const char* cp_last_error(void);
+int cp_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CANNON_GPU_H */

@@ -1,0 +1,124 @@
+"""ctypes front end of the CPU oracle -- test infrastructure only.
+
+Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, as
+the checker.  The cannon_physics_gb300 package never imports this module.
+"""
+import ctypes as C
+
+import numpy as np
+
+from cannon_physics_gb300 import _abi as A
+
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        vp, i32, f64 = C.c_void_p, C.c_int32, C.c_double
+        L.orc_shape_setup.argtypes = [vp]
+        L.orc_body_setup.argtypes = [vp, i32, vp, i32]
+        L.orc_world_create.argtypes = [vp]
+        L.orc_world_create.restype = vp
+        L.orc_world_destroy.argtypes = [vp]
+        L.orc_world_step.argtypes = [vp, f64, i32]
+        L.orc_world_get_bodies.argtypes = [vp, vp, i32]
+        L.orc_world_get_pairs.argtypes = [vp, vp, vp, i32, vp]
+        L.orc_world_get_contacts.argtypes = [vp, vp, i32, vp]
+        L.orc_world_get_rows.argtypes = [vp, vp, i32, vp]
+        L.orc_world_get_info.argtypes = [vp, vp]
+        L.orc_world_get_sap_order.argtypes = [vp, vp, i32]
+        L.orc_worlds_step_parallel.argtypes = [vp, i32, f64, i32, i32]
+        L.orc_shape_hull.argtypes = [vp, vp, i32, vp, vp, i32, vp, vp, i32, vp]
+        _lib = L
+    return _lib
+
+
+def _check(st, what):
+    if st != A.CP_OK:
+        raise RuntimeError(f"oracle {what} failed with status {st}")
+
+
+def setup_scene(scene):
+    """Run the oracle's Shape/Body constructor restatement over a scene in place."""
+    L = lib()
+    for i in range(len(scene.shapes)):
+        _check(L.orc_shape_setup(scene.shapes[i:i + 1].ctypes.data), "shape setup")
+    _check(L.orc_body_setup(A.ptr(scene.shapes), len(scene.shapes), A.ptr(scene.bodies), len(scene.bodies)), "body setup")
+    return scene
+
+
+class OracleWorld:
+    def __init__(self, scene):
+        self.scene = scene
+        self.n = scene.num_bodies
+        desc = scene.world_desc()
+        self.h = lib().orc_world_create(C.byref(desc))
+        if not self.h:
+            raise RuntimeError("oracle world create failed")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_world_destroy(self.h)
+            self.h = None
+
+    def step(self, dt=None, nsteps=1):
+        _check(lib().orc_world_step(self.h, self.scene.dt if dt is None else dt, nsteps), "step")
+
+    def bodies(self):
+        out = np.zeros(self.n, dtype=A.BODY_DTYPE)
+        _check(lib().orc_world_get_bodies(self.h, out.ctypes.data, self.n), "get bodies")
+        return out
+
+    def info(self):
+        inf = A.StepInfo()
+        _check(lib().orc_world_get_info(self.h, C.byref(inf)), "info")
+        return inf
+
+    def pairs(self):
+        inf = self.info()
+        n = inf.num_pairs
+        p1 = np.zeros(max(n, 1), np.int32)
+        p2 = np.zeros(max(n, 1), np.int32)
+        cnt = C.c_int32()
+        _check(lib().orc_world_get_pairs(self.h, p1.ctypes.data, p2.ctypes.data, len(p1), C.byref(cnt)), "pairs")
+        return p1[:cnt.value], p2[:cnt.value]
+
+    def contacts(self):
+        inf = self.info()
+        out = np.zeros(max(inf.num_contacts, 1), dtype=A.CONTACT_DTYPE)
+        cnt = C.c_int32()
+        _check(lib().orc_world_get_contacts(self.h, out.ctypes.data, len(out), C.byref(cnt)), "contacts")
+        return out[:cnt.value]
+
+    def rows(self):
+        inf = self.info()
+        out = np.zeros(max(inf.num_rows, 1), dtype=A.ROW_DTYPE)
+        cnt = C.c_int32()
+        _check(lib().orc_world_get_rows(self.h, out.ctypes.data, len(out), C.byref(cnt)), "rows")
+        return out[:cnt.value]
+
+    def sap_order(self):
+        out = np.zeros(self.n, np.int32)
+        _check(lib().orc_world_get_sap_order(self.h, out.ctypes.data, self.n), "sap order")
+        return out
+
+
+def step_parallel(worlds, dt, nsteps, threads):
+    arr = (C.c_void_p * len(worlds))(*[w.h for w in worlds])
+    _check(lib().orc_worlds_step_parallel(arr, len(worlds), dt, nsteps, threads), "parallel step")
+
+
+def shape_hull(shape_rec):
+    L = lib()
+    v = np.zeros(3 * 256, np.float32)
+    n = np.zeros(3 * 256, np.float32)
+    e = np.zeros(3 * 256, np.float32)
+    nv, nf, ne = C.c_int32(), C.c_int32(), C.c_int32()
+    _check(L.orc_shape_hull(shape_rec.ctypes.data, v.ctypes.data, 256, C.byref(nv), n.ctypes.data, 256, C.byref(nf),
+                            e.ctypes.data, 256, C.byref(ne)), "hull")
+    return v[:3 * nv.value].reshape(-1, 3), n[:3 * nf.value].reshape(-1, 3), e[:3 * ne.value].reshape(-1, 3)
