@@ -1,0 +1,319 @@
+#!/usr/bin/env python3
+"""Batched World.step throughput on GB300: body-steps/s.
+
+Workload (the batched form of cannon_physics' World.step): 4096 independent
+worlds, body counts floor(exp(U[ln 8, ln 512])) plus a ground Plane each,
+50/50 Sphere(0.5) / random Box, NaiveBroadphase, GSSolver 10 iterations,
+dt 1/60, stepped together by one persistent launch per step (CUDA graph).
+A step is one World.step of every world.  Body-steps count every body,
+planes included.
+
+Reported on one JSON line:
+  value       device-timed body-steps/s (CUDA events on the library stream),
+              state resident in HBM
+  e2e         the same metric through the public C ABI with host buffers:
+              per step cp_batch_set_forces (force/torque, pinned host -> device),
+              cp_batch_step, cp_batch_get_poses (pose + velocities, device ->
+              pinned host), timed by the host clock
+  plain       the single-world drop-in path (cp_world_step) on a sample of the
+              same worlds, and the batched/plain ratio
+  roofline    HBM roofline of the step kernel (algorithmic bytes per body-step
+              x body-steps / kernel time), peak from MEASURED_PEAKS.json
+  cpu_baseline  the C++ oracle (a port of the reference) on the host cores,
+              one world per thread, on a sample of the worlds
+
+`--impl reference` times the reference algorithm on the CPU (the oracle port,
+all host threads, one world per thread) on the same workload: the reference
+is Dart + Flutter, neither of which exists on the box.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "body-steps/s batched vs plain on 1 GB300 at <=1e-9 rel; p50/p99 request latency"
+UNIT = "body-steps/s"
+ALG_BYTES_PER_BODY_STEP = 208  # binary32 state x,q,v,w and invInertiaWorld read+written, static per-body data read
+DT = 1.0 / 60.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=120)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--worlds", type=int, default=4096)
+    ap.add_argument("--plain-worlds", type=int, default=48)
+    ap.add_argument("--plain-steps", type=int, default=10)
+    ap.add_argument("--cpu-sample", type=int, default=16, help="every k-th world goes into the CPU baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [ln.strip().split(",") for ln in self.f.read().splitlines() if ln.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per body-step of the step kernel from the committed ncu summary
+    (profiles/k_step_worlds_batch.txt: 'dram_bytes_per_body_step: X')."""
+    path = os.path.join(ROOT, "profiles", "k_step_worlds_batch.txt")
+    try:
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_body_step:"):
+                return float(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def build_worlds(n, seed):
+    from cannon_physics_gb300 import scenes
+    return scenes.batch_worlds(n, seed)
+
+
+def workload_config(n_worlds, total_bodies):
+    return {"workload": f"batch_worlds: {n_worlds} independent worlds, bodies floor(exp(U[ln 8, ln 512])) + 1 Plane each "
+                        f"({total_bodies} bodies), 50/50 Sphere(0.5)/Box(U[0.2,0.5]), NaiveBroadphase, GSSolver 10 iterations, "
+                        "dt 1/60, one persistent launch per step (CUDA graph)",
+            "worlds": n_worlds, "bodies": total_bodies, "arithmetic": "binary64 compute, binary32 vector storage (as Dart + vector_math)",
+            "l2": "inputs larger than L2 (body state alone is ~240 MB)", "parity": "bit-exact vs oracle"}
+
+
+def cpu_baseline(scenes_list, every, steps, threads=None):
+    """The oracle port on the host cores, one world per thread."""
+    from oracle import oracle_py as O
+    sample = scenes_list[::every]
+    worlds = [O.OracleWorld(s) for s in sample]
+    threads = threads or os.cpu_count() or 1
+    bodies = sum(s.num_bodies for s in sample)
+    O.step_parallel(worlds, DT, 1, threads)  # warm-up
+    t0 = time.perf_counter()
+    O.step_parallel(worlds, DT, steps, threads)
+    sec = time.perf_counter() - t0
+    return {"value": bodies * steps / sec, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(sample)} of the worlds (every {every}th, {bodies} bodies) x {steps} steps, one world per thread"}
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from cannon_physics_gb300 import build as B
+    from cannon_physics_gb300 import engine
+
+    B.build()
+    scs = build_worlds(args.worlds, 1000 + rank * args.worlds)  # weak scaling: each rank its own worlds
+    for s in scs:
+        engine.setup_scene(s)
+    ctx = engine.Context(device=local)
+    worlds = [ctx.world(s) for s in scs]
+    batch = engine.Batch(ctx, worlds)
+    total = batch.total
+    ext = torch.cuda.ExternalStream(ctx.stream_handle())
+
+    for _ in range(args.warmup):
+        batch.step(DT)
+    ctx.batch_profile()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # device-timed throughput, state resident
+    clocks = Clocks(local)
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launches()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(args.steps):
+        batch.step(DT)
+    e1.record(ext)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier()
+    launches = ctx.launches() - launches0
+    ms = e0.elapsed_time(e1)
+    graph_ms, graph_steps = ctx.batch_profile()
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = total * ws * args.steps / (ms / 1e3)
+
+    # end to end through the C ABI with pinned host buffers
+    ft = torch.zeros(total * 6, dtype=torch.float32, pin_memory=True)
+    poses = torch.empty(total * 13, dtype=torch.float32, pin_memory=True)
+    e2e_steps = max(3, args.steps // 4)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        batch.set_forces(ft.data_ptr())
+        batch.step(DT)
+        batch.get_poses(poses.data_ptr())
+    e2e_sec = time.perf_counter() - t0
+    barrier()
+    if ws > 1:
+        t = torch.tensor([e2e_sec], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_sec = float(t.item())
+    e2e = {"value": total * ws * e2e_steps / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": total * 6 * 4,
+           "d2h_bytes_per_step": total * 13 * 4, "steps": e2e_steps}
+    assert np.isfinite(poses.numpy()).all()
+
+    # plain single-world path on a sample of the same worlds (fresh copies)
+    idx = np.linspace(0, len(scs) - 1, args.plain_worlds).astype(int)
+    plain_worlds = [ctx.world(scs[i]) for i in idx]
+    for w in plain_worlds:
+        w.step(DT, 1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for w in plain_worlds:
+        w.step(DT, args.plain_steps)
+    plain_sec = time.perf_counter() - t0
+    plain_bodies = sum(w.n for w in plain_worlds)
+    plain = {"value": plain_bodies * args.plain_steps / plain_sec, "unit": UNIT,
+             "sample": f"{len(plain_worlds)} worlds ({plain_bodies} bodies) x {args.plain_steps} steps, one cp_world_step per world"}
+
+    if rank != 0:
+        ctx.close()
+        return
+    peak, peak_kind = peaks()
+    kernel_ms = graph_ms / max(graph_steps, 1)
+    achieved = ALG_BYTES_PER_BODY_STEP * total / (kernel_ms / 1e3) / 1e9
+    traffic_per_bs = profiled_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded SplitMix64 scenes; the reference publishes no benchmark scenes)",
+        "config": workload_config(args.worlds, total),
+        "e2e": e2e,
+        "plain": plain,
+        "batched_over_plain": value / ws / plain["value"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "kernel": "k_step_worlds",
+                     "alg_bytes_per_body_step": ALG_BYTES_PER_BODY_STEP, "kernel_ms": kernel_ms,
+                     "traffic": None if traffic_per_bs is None else traffic_per_bs * total,
+                     "note": "the step is bound by binary64 issue on GB300, not HBM; see DESIGN.md"},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(scs, args.cpu_sample, args.cpu_steps)
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_reference(args):
+    ws, rank, local = dist_info()
+    if rank != 0:
+        return
+    from oracle import oracle_py as O
+    scs = build_worlds(args.worlds, 1000)
+    for s in scs:
+        O.setup_scene(s)
+    worlds = [O.OracleWorld(s) for s in scs]
+    threads = os.cpu_count() or 1
+    total = sum(s.num_bodies for s in scs)
+    O.step_parallel(worlds, DT, args.warmup, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.step_parallel(worlds, DT, 1, threads)
+    sec = time.perf_counter() - t0
+    value = total * args.steps / sec
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args.worlds, total),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"all {args.worlds} worlds, every step; the Dart reference needs a Flutter SDK, "
+                                       "absent here and on the GPU box, so its C++ port (oracle/) runs it"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

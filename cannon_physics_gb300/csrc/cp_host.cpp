@@ -306,6 +306,16 @@ struct cp_ctx {
   int sms = 0, blocks_per_sm = 1;
   long long launches = 0;
   std::mutex mu;
+  // batched host I/O
+  int* d_io_ids = nullptr;
+  long long* d_io_first = nullptr;
+  int io_cap = 0;
+  float* d_io = nullptr;
+  long long io_floats = 0;
+  std::vector<int> io_ids;  // ids whose offsets are on the device
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double graph_ms = 0.0;
+  long long graph_step_launches = 0;
   // batched-step graph cache
   cudaGraphExec_t graph = nullptr;
   std::vector<int> graph_ids;
@@ -594,7 +604,7 @@ int cp_shape_setup(cp_shape_desc* s) {
 }
 
 int cp_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc* bodies, int32_t num_bodies) {
-  if (!bodies || num_bodies < 0 || num_shapes < 0 || (num_shapes > 0 && !shapes)) return fail(CP_ERR_ARG, "bad arguments");
+  if ((!bodies && num_bodies > 0) || num_bodies < 0 || num_shapes < 0 || (num_shapes > 0 && !shapes)) return fail(CP_ERR_ARG, "bad arguments");
   std::vector<Hull> hulls(num_shapes);
   std::vector<char> has_hull(num_shapes, 0);
   for (int k = 0; k < num_bodies; k++) {
@@ -655,6 +665,8 @@ int cp_create(const cp_config* cfg, cp_ctx** out) {
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_queue, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_one, sizeof(int));
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) {
     delete c;
@@ -678,6 +690,11 @@ int cp_destroy(cp_ctx* c) {
   if (c->d_status) cudaFree(c->d_status);
   if (c->d_queue) cudaFree(c->d_queue);
   if (c->d_one) cudaFree(c->d_one);
+  if (c->d_io_ids) cudaFree(c->d_io_ids);
+  if (c->d_io_first) cudaFree(c->d_io_first);
+  if (c->d_io) cudaFree(c->d_io);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return CP_OK;
@@ -961,7 +978,8 @@ int cp_world_get_bodies(cp_ctx* c, int32_t id, cp_body_desc* out, int32_t n) {
   if (st) return st;
   std::lock_guard<std::mutex> lock(c->mu);
   WorldRec& w = c->worlds[id];
-  if (!out || n != w.nb) return fail(CP_ERR_ARG, "expected %d bodies", w.nb);
+  if ((!out && n > 0) || n != w.nb) return fail(CP_ERR_ARG, "expected %d bodies", w.nb);
+  if (w.nb == 0) return CP_OK;
   std::vector<DBody> b(w.nb);
   CUDA_TRY(cudaMemcpyAsync(b.data(), w.dw.bodies, sizeof(DBody) * w.nb, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -974,7 +992,8 @@ int cp_world_set_bodies(cp_ctx* c, int32_t id, const cp_body_desc* in, int32_t n
   if (st) return st;
   std::lock_guard<std::mutex> lock(c->mu);
   WorldRec& w = c->worlds[id];
-  if (!in || n != w.nb) return fail(CP_ERR_ARG, "expected %d bodies", w.nb);
+  if ((!in && n > 0) || n != w.nb) return fail(CP_ERR_ARG, "expected %d bodies", w.nb);
+  if (w.nb == 0) return CP_OK;
   std::vector<DBody> b(w.nb);
   for (int i = 0; i < w.nb; i++) {
     if (in[i].shape < -1 || in[i].shape >= w.nshapes) return fail(CP_ERR_ARG, "body %d: shape out of range", i);
@@ -1075,8 +1094,8 @@ int cp_world_get_sap_order(cp_ctx* c, int32_t id, int32_t* out, int32_t n) {
   if (st) return st;
   std::lock_guard<std::mutex> lock(c->mu);
   WorldRec& w = c->worlds[id];
-  if (!out || n != w.nb) return fail(CP_ERR_ARG, "expected %d entries", w.nb);
-  CUDA_TRY(cudaMemcpy(out, w.dw.sap_order, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  if ((!out && n > 0) || n != w.nb) return fail(CP_ERR_ARG, "expected %d entries", w.nb);
+  if (n) CUDA_TRY(cudaMemcpy(out, w.dw.sap_order, sizeof(int) * n, cudaMemcpyDeviceToHost));
   return CP_OK;
 }
 
@@ -1122,11 +1141,17 @@ int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t n
   CUDA_TRY(cpk_gather_status(c->d_worlds, c->d_ids, n, c->d_status, c->stream));
   std::vector<long long> before(4 * (size_t)n), after(4 * (size_t)n);
   CUDA_TRY(cudaMemcpyAsync(before.data(), c->d_status, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
   CUDA_TRY(cudaGraphLaunch(c->graph, c->stream));
+  CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
   c->launches += 2LL * nsteps + 1;
   CUDA_TRY(cpk_gather_status(c->d_worlds, c->d_ids, n, c->d_status, c->stream));
   CUDA_TRY(cudaMemcpyAsync(after.data(), c->d_status, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
+  float gms = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&gms, c->ev0, c->ev1));
+  c->graph_ms += gms;
+  c->graph_step_launches += nsteps;
   c->launches += 1;
   for (int i = 0; i < n; i++) {
     if (after[4 * i] != 0) {  // overflowed part way: grow and finish on the plain path
@@ -1141,6 +1166,93 @@ int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t n
   return CP_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// world list + packed offsets on the device for the batched I/O calls
+int prepare_io(cp_ctx* c, const int32_t* ids, int n, int64_t total, int floats_per_body) {
+  if (!c || (n > 0 && !ids) || n < 0) return fail(CP_ERR_ARG, "bad arguments");
+  std::vector<long long> first(n);
+  long long acc = 0;
+  for (int i = 0; i < n; i++) {
+    if (ids[i] < 0 || ids[i] >= (int)c->worlds.size() || !c->worlds[ids[i]].live) return fail(CP_ERR_ARG, "no world %d", ids[i]);
+    first[i] = acc;
+    acc += c->worlds[ids[i]].nb;
+  }
+  if (acc != total) return fail(CP_ERR_ARG, "total_bodies %lld != %lld", (long long)total, acc);
+  if (n > c->io_cap) {
+    if (c->d_io_ids) cudaFree(c->d_io_ids);
+    if (c->d_io_first) cudaFree(c->d_io_first);
+    int cap = std::max(256, 2 * n);
+    CUDA_TRY(cudaMalloc(&c->d_io_ids, sizeof(int) * cap));
+    CUDA_TRY(cudaMalloc(&c->d_io_first, sizeof(long long) * cap));
+    c->io_cap = cap;
+    c->io_ids.clear();
+  }
+  long long need = acc * floats_per_body;
+  if (need > c->io_floats) {
+    if (c->d_io) cudaFree(c->d_io);
+    long long cap = std::max<long long>(1 << 16, need + need / 4);
+    CUDA_TRY(cudaMalloc(&c->d_io, sizeof(float) * cap));
+    c->io_floats = cap;
+  }
+  if (c->io_ids.size() != (size_t)n || !std::equal(c->io_ids.begin(), c->io_ids.end(), ids)) {
+    CUDA_TRY(cudaMemcpyAsync(c->d_io_ids, ids, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->d_io_first, first.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->io_ids.assign(ids, ids + n);
+  }
+  return CP_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int cp_batch_set_forces(cp_ctx* c, const int32_t* ids, int32_t n, const float* ft, int64_t total) {
+  if (!c) return fail(CP_ERR_ARG, "null context");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  int st = prepare_io(c, ids, n, total, 6);
+  if (st) return st;
+  if (total == 0) return CP_OK;
+  if (!ft) return fail(CP_ERR_ARG, "null buffer");
+  CUDA_TRY(cudaMemcpyAsync(c->d_io, ft, sizeof(float) * 6 * total, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cpk_scatter_forces(c->d_worlds, c->d_io_ids, c->d_io_first, n, c->d_io, c->stream));
+  c->launches += 1;
+  return CP_OK;  // ordered before the next step on the context's stream
+}
+
+int cp_batch_get_poses(cp_ctx* c, const int32_t* ids, int32_t n, float* out, int64_t total) {
+  if (!c) return fail(CP_ERR_ARG, "null context");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  int st = prepare_io(c, ids, n, total, 13);
+  if (st) return st;
+  if (total == 0) return CP_OK;
+  if (!out) return fail(CP_ERR_ARG, "null buffer");
+  CUDA_TRY(cpk_gather_poses(c->d_worlds, c->d_io_ids, c->d_io_first, n, c->d_io, c->stream));
+  c->launches += 1;
+  CUDA_TRY(cudaMemcpyAsync(out, c->d_io, sizeof(float) * 13 * total, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return CP_OK;
+}
+
 int64_t cp_kernel_launches(cp_ctx* c) { return c ? c->launches : 0; }
+
+int cp_get_stream(cp_ctx* c, void** stream) {
+  if (!c || !stream) return fail(CP_ERR_ARG, "null argument");
+  *stream = (void*)c->stream;
+  return CP_OK;
+}
+
+int cp_batch_profile(cp_ctx* c, double* graph_ms, int64_t* step_launches) {
+  if (!c || !graph_ms || !step_launches) return fail(CP_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lock(c->mu);
+  *graph_ms = c->graph_ms;
+  *step_launches = c->graph_step_launches;
+  c->graph_ms = 0.0;
+  c->graph_step_launches = 0;
+  return CP_OK;
+}
 
 }  // extern "C"

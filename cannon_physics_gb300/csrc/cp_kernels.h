@@ -15,3 +15,9 @@ cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, int n, dou
 cudaError_t cpk_gather_status(const DWorld* d_worlds, const int* d_ids, int n, long long* d_out, cudaStream_t stream);
 // clear the status of the listed worlds
 cudaError_t cpk_clear_status(const DWorld* d_worlds, const int* d_ids, int n, cudaStream_t stream);
+// scatter 6 floats per body into Body.force/torque, gather 13 pose floats per body;
+// d_first[i] = index of world ids[i]'s first body in the packed buffer
+cudaError_t cpk_scatter_forces(const DWorld* d_worlds, const int* d_ids, const long long* d_first, int n, const float* d_in,
+                               cudaStream_t stream);
+cudaError_t cpk_gather_poses(const DWorld* d_worlds, const int* d_ids, const long long* d_first, int n, float* d_out,
+                             cudaStream_t stream);

@@ -1310,6 +1310,47 @@ cudaError_t cpk_clear_status(const DWorld* d_worlds, const int* d_ids, int n, cu
   return cudaGetLastError();
 }
 
+__global__ void k_scatter_forces(const DWorld* __restrict__ worlds, const int* __restrict__ ids, const long long* __restrict__ first,
+                                 const float* __restrict__ in) {
+  const DWorld& W = worlds[ids[blockIdx.x]];
+  const int nb = W.P->nb;
+  const float* src = in + 6 * first[blockIdx.x];
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    DBody& b = W.bodies[i];
+    b.force[0] = src[6 * i]; b.force[1] = src[6 * i + 1]; b.force[2] = src[6 * i + 2];
+    b.torque[0] = src[6 * i + 3]; b.torque[1] = src[6 * i + 4]; b.torque[2] = src[6 * i + 5];
+  }
+}
+
+__global__ void k_gather_poses(const DWorld* __restrict__ worlds, const int* __restrict__ ids, const long long* __restrict__ first,
+                               float* __restrict__ out) {
+  const DWorld& W = worlds[ids[blockIdx.x]];
+  const int nb = W.P->nb;
+  float* dst = out + 13 * first[blockIdx.x];
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    const DBody& b = W.bodies[i];
+    float* o = dst + 13 * i;
+    o[0] = b.pos[0]; o[1] = b.pos[1]; o[2] = b.pos[2];
+    o[3] = b.quat[0]; o[4] = b.quat[1]; o[5] = b.quat[2]; o[6] = b.quat[3];
+    o[7] = b.vel[0]; o[8] = b.vel[1]; o[9] = b.vel[2];
+    o[10] = b.avel[0]; o[11] = b.avel[1]; o[12] = b.avel[2];
+  }
+}
+
+cudaError_t cpk_scatter_forces(const DWorld* d_worlds, const int* d_ids, const long long* d_first, int n, const float* d_in,
+                               cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  k_scatter_forces<<<n, 128, 0, stream>>>(d_worlds, d_ids, d_first, d_in);
+  return cudaGetLastError();
+}
+
+cudaError_t cpk_gather_poses(const DWorld* d_worlds, const int* d_ids, const long long* d_first, int n, float* d_out,
+                             cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  k_gather_poses<<<n, 128, 0, stream>>>(d_worlds, d_ids, d_first, d_out);
+  return cudaGetLastError();
+}
+
 int cpk_block_threads() { return BT; }
 
 cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, int n, double dt, int* d_queue, int grid,

@@ -46,8 +46,12 @@ def lib():
         L.cp_world_get_info.argtypes = [vp, i32, vp]
         L.cp_world_get_sap_order.argtypes = [vp, i32, vp, i32]
         L.cp_batch_step.argtypes = [vp, vp, i32, f64, i32]
+        L.cp_batch_set_forces.argtypes = [vp, vp, i32, vp, C.c_int64]
+        L.cp_batch_get_poses.argtypes = [vp, vp, i32, vp, C.c_int64]
         L.cp_kernel_launches.argtypes = [vp]
         L.cp_kernel_launches.restype = C.c_int64
+        L.cp_get_stream.argtypes = [vp, vp]
+        L.cp_batch_profile.argtypes = [vp, vp, vp]
         _lib = L
     return _lib
 
@@ -85,12 +89,45 @@ class Context:
     def launches(self):
         return int(lib().cp_kernel_launches(self.h))
 
+    def stream_handle(self):
+        s = C.c_void_p()
+        check(lib().cp_get_stream(self.h, C.byref(s)), "cp_get_stream")
+        return s.value
+
+    def batch_profile(self):
+        """(device ms, step launches) of batched graphs since the last call."""
+        ms = C.c_double()
+        n = C.c_int64()
+        check(lib().cp_batch_profile(self.h, C.byref(ms), C.byref(n)), "cp_batch_profile")
+        return ms.value, n.value
+
     def world(self, scene):
         return GpuWorld(self, scene)
 
     def batch_step(self, worlds, dt, nsteps):
         ids = np.array([w.id for w in worlds], dtype=np.int32)
         check(lib().cp_batch_step(self.h, ids.ctypes.data, len(ids), dt, nsteps), "cp_batch_step")
+
+
+class Batch:
+    """A fixed list of worlds stepped together, with packed host I/O."""
+
+    def __init__(self, ctx, worlds):
+        self.ctx = ctx
+        self.worlds = list(worlds)
+        self.ids = np.array([w.id for w in self.worlds], dtype=np.int32)
+        self.total = int(sum(w.n for w in self.worlds))
+
+    def step(self, dt, nsteps=1):
+        check(lib().cp_batch_step(self.ctx.h, self.ids.ctypes.data, len(self.ids), dt, nsteps), "cp_batch_step")
+
+    def set_forces(self, ft_ptr):
+        """ft_ptr: address of total*6 float32 (force xyz, torque xyz per body)."""
+        check(lib().cp_batch_set_forces(self.ctx.h, self.ids.ctypes.data, len(self.ids), ft_ptr, self.total), "set_forces")
+
+    def get_poses(self, out_ptr):
+        """out_ptr: address of total*13 float32 (pos, quat, vel, angular vel per body)."""
+        check(lib().cp_batch_get_poses(self.ctx.h, self.ids.ctypes.data, len(self.ids), out_ptr, self.total), "get_poses")
 
 
 class GpuWorld:

@@ -93,6 +93,7 @@ class Scene:
     enable_friction_reduction: bool = False
     time: float = 0.0
     stepnumber: int = 0
+    friction_gravity: tuple = None
     _keep: list = field(default_factory=list)
 
     @property
@@ -116,7 +117,9 @@ class Scene:
         d.sap_axis = self.sap_axis
         d.grid_n[:] = list(self.grid_n)
         d.enable_friction_reduction = int(self.enable_friction_reduction)
-        d.has_friction_gravity = 0
+        d.has_friction_gravity = 0 if self.friction_gravity is None else 1
+        if self.friction_gravity is not None:
+            d.friction_gravity[:] = list(self.friction_gravity)
         d.stepnumber = self.stepnumber
         d.solver_tolerance = self.tolerance
         d.time = self.time

@@ -261,8 +261,29 @@ int cp_world_get_sap_order(cp_ctx* ctx, int32_t world_id, int32_t* out, int32_t 
  * world's result equals cp_world_step on that world alone. */
 int cp_batch_step(cp_ctx* ctx, const int32_t* world_ids, int32_t n, double dt, int32_t nsteps);
 
+/* Per-step host I/O of a batch, the way a game or RL loop drives it.
+ * The bodies of the listed worlds are concatenated in list order
+ * (`total_bodies` = the sum of their body counts).
+ * set_forces overwrites Body.force / Body.torque (6 floats per body: force
+ * xyz, torque xyz), i.e. what applyForce / applyTorque accumulated on the host
+ * before World.step (rigid_body.dart:472-525);
+ * get_poses reads position xyz, quaternion xyzw, velocity xyz and angular
+ * velocity xyz (13 floats per body), what a Dart GpuWorld writes back into
+ * its Body objects after each step.  Host buffers may be pinned or pageable;
+ * each call is one host-device copy plus one scatter / gather launch. */
+int cp_batch_set_forces(cp_ctx* ctx, const int32_t* world_ids, int32_t n, const float* ft, int64_t total_bodies);
+int cp_batch_get_poses(cp_ctx* ctx, const int32_t* world_ids, int32_t n, float* out, int64_t total_bodies);
+
 /* Number of GPU kernel launches issued by this context so far. */
 int64_t cp_kernel_launches(cp_ctx* ctx);
+
+/* The CUDA stream (cudaStream_t) all work of the context runs on, so callers
+ * can order their own work or time with events on it. */
+int cp_get_stream(cp_ctx* ctx, void** stream);
+
+/* Device time (CUDA events on the context stream) of the batched-step graph
+ * launches since the previous call, and how many step launches they held. */
+int cp_batch_profile(cp_ctx* ctx, double* graph_ms, int64_t* step_launches);
 
 const char* cp_last_error(void);
 int cp_abi_version(void);

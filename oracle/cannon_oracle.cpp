@@ -1819,7 +1819,7 @@ int orc_shape_setup(cp_shape_desc* shape) {
 
 // rigid_body.dart:27-86 (constructor) then addShape :348-369
 int orc_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc* bodies, int32_t num_bodies) {
-  if (!bodies || num_bodies < 0 || num_shapes < 0) return CP_ERR_ARG;
+  if ((!bodies && num_bodies > 0) || num_bodies < 0 || num_shapes < 0) return CP_ERR_ARG;
   std::vector<Shape> sh(num_shapes);
   for (int i = 0; i < num_shapes; i++) { int st = buildShape(shapes[i], sh[i]); if (st) return st; }
   for (int k = 0; k < num_bodies; k++) {
@@ -1867,7 +1867,7 @@ int orc_world_step(orc_world* o, double dt, int32_t nsteps) {
 }
 
 int orc_world_get_bodies(orc_world* o, cp_body_desc* out, int32_t n) {
-  if (!o || !out || n != (int32_t)o->w.bodies.size()) return CP_ERR_ARG;
+  if (!o || (!out && n > 0) || n != (int32_t)o->w.bodies.size()) return CP_ERR_ARG;
   for (int i = 0; i < n; i++) bodyToDesc(o->w.bodies[i], out[i]);
   return CP_OK;
 }
@@ -1927,7 +1927,7 @@ int orc_world_get_info(orc_world* o, cp_step_info* out) {
 }
 
 int orc_world_get_sap_order(orc_world* o, int32_t* out, int32_t n) {
-  if (!o || !out || n != (int32_t)o->w.axisList.size()) return CP_ERR_ARG;
+  if (!o || (!out && n > 0) || n != (int32_t)o->w.axisList.size()) return CP_ERR_ARG;
   for (int i = 0; i < n; i++) out[i] = o->w.axisList[i];
   return CP_OK;
 }
