@@ -55,7 +55,6 @@ def parse():
     ap.add_argument("--plain-worlds", type=int, default=48)
     ap.add_argument("--plain-steps", type=int, default=10)
     ap.add_argument("--cpu-sample", type=int, default=16, help="every k-th world goes into the CPU baseline sample")
-    ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -150,19 +149,21 @@ def workload_config(n_worlds, total_bodies):
             "l2": "inputs larger than L2 (body state alone is ~240 MB)", "parity": "bit-exact vs oracle"}
 
 
-def cpu_baseline(scenes_list, every, steps, threads=None):
-    """The oracle port on the host cores, one world per thread."""
+def cpu_baseline(scenes_list, every, warmup, steps, threads=None):
+    """The oracle port on the host cores, one world per thread, over the same
+    step range as the timed GPU region."""
     from oracle import oracle_py as O
     sample = scenes_list[::every]
     worlds = [O.OracleWorld(s) for s in sample]
     threads = threads or os.cpu_count() or 1
     bodies = sum(s.num_bodies for s in sample)
-    O.step_parallel(worlds, DT, 1, threads)  # warm-up
+    O.step_parallel(worlds, DT, warmup, threads)
     t0 = time.perf_counter()
     O.step_parallel(worlds, DT, steps, threads)
     sec = time.perf_counter() - t0
     return {"value": bodies * steps / sec, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{len(sample)} of the worlds (every {every}th, {bodies} bodies) x {steps} steps, one world per thread"}
+            "sample": f"{len(sample)} of the worlds (every {every}th, {bodies} bodies), steps {warmup}..{warmup + steps - 1}, "
+                      "one world per thread"}
 
 
 def run_ours(args):
@@ -188,7 +189,13 @@ def run_ours(args):
 
     for _ in range(args.warmup):
         batch.step(DT)
+    # the autotuner times one kernel variant per batched call until all are timed
+    tune_calls = 0
+    while ctx.autotune_info()["variant"] < 0 and tune_calls < 16:
+        batch.step(DT)
+        tune_calls += 1
     ctx.batch_profile()
+    ctx.phase_profile()
 
     def barrier():
         if ws > 1:
@@ -211,6 +218,7 @@ def run_ours(args):
     launches = ctx.launches() - launches0
     ms = e0.elapsed_time(e1)
     graph_ms, graph_steps = ctx.batch_profile()
+    phases = ctx.phase_profile()
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -273,9 +281,11 @@ def run_ours(args):
                      "note": "the step is bound by binary64 issue on GB300, not HBM; see DESIGN.md"},
         "gpu_launches": launches,
         "clocks": clk,
+        "autotune": dict(ctx.autotune_info(), warmup_calls=args.warmup + tune_calls),
+        "phase_share": {k: round(v / max(sum(phases.values()), 1.0), 4) for k, v in phases.items()},
     }
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(scs, args.cpu_sample, args.cpu_steps)
+        line["cpu_baseline"] = cpu_baseline(scs, args.cpu_sample, args.warmup, args.steps)
     print(json.dumps(line), flush=True)
     ctx.close()
 

@@ -1,0 +1,259 @@
+// cp_cc.cuh -- convex-convex contacts (narrow_phase.dart:1981-2043 with
+// ConvexPolyhedron.findSeparatingAxis / clipAgainstHull,
+// convex_polyhedron.dart:189-587,843-883) in binary64 registers holding the
+// reference's binary32 values, rounded by r32 where the reference stores.
+//
+// Three exact shortcuts, each giving the reference's result bit for bit:
+//  * Canonical axes.  A face normal or unique edge whose exact negation
+//    appears earlier in its hull's list yields the same depth as that earlier
+//    entry (every operation of project/testSepAxis is odd in the axis and
+//    round-to-nearest is symmetric), and it comes later in the loop order, so
+//    under "first strict minimum wins" it can never be chosen, and if it
+//    separates the hulls the earlier entry already did.  The same holds for
+//    edge pairs built from such edges.  Only canonical entries are tested.
+//  * Negated faces in clipping.  The world normal of a non-canonical face is
+//    the exact negation of its canonical twin's, and so is its dot product.
+//  * Box projection.  A box hull's vertices are all sign combinations of
+//    (sx, sy, sz), each v.x*a.x is exact in binary64, and rounding is
+//    monotonic, so the largest vertex projection is fl(fl(|sx ax| +
+//    |sy ay|) + |sz az|) and the smallest is its negation.
+#pragma once
+#include "cp_math.cuh"
+#include "cp_types.h"
+
+struct d4 { double x, y, z, w; };
+
+DI d4 d4of(q4 q) { return d4{(double)q.x, (double)q.y, (double)q.z, (double)q.w}; }
+
+DI d3 dvmult(d4 q, d3 v) {  // Quat.vmult with the Vector3 store
+  double x = v.x, y = v.y, z = v.z;
+  double qx = q.x, qy = q.y, qz = q.z, qw = q.w;
+  double ix = qw * x + qy * z - qz * y;
+  double iy = qw * y + qz * x - qx * z;
+  double iz = qw * z + qx * y - qy * x;
+  double iw = -qx * x - qy * y - qz * z;
+  return d3{r32(ix * qw + iw * -qx + iy * -qz - iz * -qy), r32(iy * qw + iw * -qy + iz * -qx - ix * -qz),
+            r32(iz * qw + iw * -qz + ix * -qy - iy * -qx)};
+}
+DI d3 dneg(d3 v) { return d3{-v.x, -v.y, -v.z}; }
+DI d3 dadd(d3 a, d3 b) { return d3{r32(a.x + b.x), r32(a.y + b.y), r32(a.z + b.z)}; }
+DI d3 dsub(d3 a, d3 b) { return d3{r32(a.x - b.x), r32(a.y - b.y), r32(a.z - b.z)}; }
+DI d3 dscale(d3 a, double s) { return d3{r32(s * a.x), r32(s * a.y), r32(s * a.z)}; }
+DI d3 dcross(d3 a, d3 v) {
+  return d3{r32(a.y * v.z - a.z * v.y), r32(a.z * v.x - a.x * v.z), r32(a.x * v.y - a.y * v.x)};
+}
+DI d3 dnormalized(d3 v) {
+  double l = sqrt(ddot(v, v));
+  if (l == 0.0) return v;
+  double d = 1.0 / l;
+  return d3{r32(v.x * d), r32(v.y * d), r32(v.z * d)};
+}
+DI bool dalmost_zero(d3 a) { return !(fabs(a.x) > 1e-6 || fabs(a.y) > 1e-6 || fabs(a.z) > 1e-6); }
+DI d3 dlerp(d3 a, d3 v, double t) { return d3{r32(a.x + (v.x - a.x) * t), r32(a.y + (v.y - a.y) * t), r32(a.z + (v.z - a.z) * t)}; }
+DI d3 hvd(const DWorld& W, int i) { return ldd3(W.hvd + 4 * i); }
+
+struct DHullPose {
+  DHull H;
+  d3 x;
+  d4 q;
+  d3 origin;  // Transform.pointToLocalFrame(pos, quat, 0)
+};
+
+// ConvexPolyhedron.project
+DI void dproject(const DWorld& W, const DHullPose& h, d3 axis, double& mx, double& mn) {
+  d3 la = dvmult(d4{h.q.x, h.q.y, h.q.z, -h.q.w}, axis);
+  double addv = ddot(h.origin, la);
+  double max, min;
+  if (h.H.is_box) {
+    double a = fabs(h.H.he[0] * la.x), b = fabs(h.H.he[1] * la.y), c = fabs(h.H.he[2] * la.z);
+    max = (a + b) + c;
+    min = -max;
+  } else {
+    max = ddot(hvd(W, h.H.v0), la);
+    min = max;
+    for (int i = 1; i < h.H.nv; i++) {
+      double v = ddot(hvd(W, h.H.v0 + i), la);
+      if (v > max) max = v;
+      if (v < min) min = v;
+    }
+  }
+  min -= addv;
+  max -= addv;
+  if (min > max) { double t = min; min = max; max = t; }
+  mx = max;
+  mn = min;
+}
+
+DI bool dtest_sep_axis(const DWorld& W, const DHullPose& A, const DHullPose& B, d3 axis, double& depth) {
+  double maxA, minA, maxB, minB;
+  dproject(W, A, axis, maxA, minA);
+  dproject(W, B, axis, maxB, minB);
+  if (maxA < minB || maxB < minA) return false;
+  double d0 = maxA - minB, d1 = maxB - minA;
+  depth = d0 < d1 ? d0 : d1;
+  return true;
+}
+
+// world normal of face f given the canonical world normals wn[] (indexed by face)
+DI d3 face_wn(const DWorld& W, const DHull& H, const d3* wn, int f) {
+  int c = W.faces[H.f0 + f].canon;
+  return c == f ? wn[f] : dneg(wn[c]);
+}
+
+DI bool dfind_separating_axis(const DWorld& W, const DHullPose& A, const DHullPose& B, const d3* wnA, const d3* wnB, d3& target) {
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  double d;
+  if (A.H.has_axes)
+    for (int k = 0; k < A.H.ncf; k++) {
+      int f = W.hcanon[A.H.cf0 + k];
+      if (!dtest_sep_axis(W, A, B, wnA[f], d)) return false;
+      if (d < dmin) { dmin = d; target = wnA[f]; }
+    }
+  if (B.H.has_axes)
+    for (int k = 0; k < B.H.ncf; k++) {
+      int f = W.hcanon[B.H.cf0 + k];
+      if (!dtest_sep_axis(W, A, B, wnB[f], d)) return false;
+      if (d < dmin) { dmin = d; target = wnB[f]; }
+    }
+  d3 weB[CP_MAX_HULL_VERTS];
+  for (int k = 0; k < B.H.nce; k++) weB[k] = dvmult(B.q, ldd3(W.hed + 4 * (B.H.e0 + W.hcanon[B.H.ce0 + k])));
+  for (int k0 = 0; k0 < A.H.nce; k0++) {
+    d3 we0 = dvmult(A.q, ldd3(W.hed + 4 * (A.H.e0 + W.hcanon[A.H.ce0 + k0])));
+    for (int k1 = 0; k1 < B.H.nce; k1++) {
+      d3 cr = dcross(we0, weB[k1]);
+      if (!dalmost_zero(cr)) {
+        cr = dnormalized(cr);
+        if (!dtest_sep_axis(W, A, B, cr, d)) return false;
+        if (d < dmin) { dmin = d; target = cr; }
+      }
+    }
+  }
+  d3 deltaC = dsub(B.x, A.x);
+  if (ddot(deltaC, target) > 0.0) target = dneg(target);
+  return true;
+}
+
+DI int dclip_face_against_plane(const d3* in, int nin, d3* out, d3 n, double c) {
+  if (nin < 2) return 0;
+  int nout = 0;
+  d3 first = in[nin - 1];
+  double nDotFirst = ddot(n, first) + c;
+  for (int vi = 0; vi < nin; vi++) {
+    d3 last = in[vi];
+    double nDotLast = ddot(n, last) + c;
+    if (nDotFirst < 0) {
+      if (nDotLast < 0) {
+        if (nout < CP_MAX_CLIP) out[nout] = last;
+        nout++;
+      } else {
+        if (nout < CP_MAX_CLIP) out[nout] = dlerp(first, last, nDotFirst / (nDotFirst - nDotLast));
+        nout++;
+      }
+    } else if (nDotLast < 0) {
+      if (nout < CP_MAX_CLIP) out[nout] = dlerp(first, last, nDotFirst / (nDotFirst - nDotLast));
+      nout++;
+      if (nout < CP_MAX_CLIP) out[nout] = last;
+      nout++;
+    }
+    first = last;
+    nDotFirst = nDotLast;
+  }
+  return nout;
+}
+
+DI int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xAf, f3 xBf, q4 qAf, q4 qBf, int& start) {
+  const DWorld& W = *C.W;
+  const DShape& SA = W.shapes[shA];
+  const DShape& SB = W.shapes[shB];
+  if (distance_to(xAf, xBf) > SA.bsr + SB.bsr) return 0;
+  DHullPose A, B;
+  A.H = W.hulls[SA.hull]; A.x = d3of(xAf); A.q = d4of(qAf);
+  B.H = W.hulls[SB.hull]; B.x = d3of(xBf); B.q = d4of(qBf);
+  A.origin = dvmult(d4{-A.q.x, -A.q.y, -A.q.z, A.q.w}, dsub(d3{0.0, 0.0, 0.0}, A.x));
+  B.origin = dvmult(d4{-B.q.x, -B.q.y, -B.q.z, B.q.w}, dsub(d3{0.0, 0.0, 0.0}, B.x));
+  if (A.H.nf > CP_MAX_HULL_VERTS || B.H.nf > CP_MAX_HULL_VERTS || B.H.nce > CP_MAX_HULL_VERTS) {
+    atomicOr(C.overflow, ST_HULL_OVERFLOW);
+    return 0;
+  }
+  d3 wnA[CP_MAX_HULL_VERTS], wnB[CP_MAX_HULL_VERTS];
+  for (int k = 0; k < A.H.ncf; k++) {
+    int f = W.hcanon[A.H.cf0 + k];
+    wnA[f] = dvmult(A.q, ldd3(W.faces[A.H.f0 + f].dnormal));
+  }
+  for (int k = 0; k < B.H.ncf; k++) {
+    int f = W.hcanon[B.H.cf0 + k];
+    wnB[f] = dvmult(B.q, ldd3(W.faces[B.H.f0 + f].dnormal));
+  }
+  d3 sep = d3{0.0, 0.0, 0.0};
+  if (!dfind_separating_axis(W, A, B, wnA, wnB, sep)) return 0;
+  // clipAgainstHull: face of B most aligned with the axis
+  int cfb = -1;
+  double dmax = __longlong_as_double(0xfff0000000000000LL);
+  for (int f = 0; f < B.H.nf; f++) {
+    double d = ddot(face_wn(W, B.H, wnB, f), sep);
+    if (d > dmax) { dmax = d; cfb = f; }
+  }
+  if (cfb < 0) return 0;
+  d3 bufA[CP_MAX_CLIP], bufB[CP_MAX_CLIP];
+  const DFace FB = W.faces[B.H.f0 + cfb];
+  if (FB.n > CP_MAX_CLIP) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
+  int nin = FB.n;
+  for (int i = 0; i < nin; i++) bufA[i] = dadd(dvmult(B.q, hvd(W, B.H.v0 + W.hfi[FB.i0 + i])), B.x);
+  // clipFaceAgainstHull: face of A most anti-aligned with the axis
+  int cfa = -1;
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  for (int f = 0; f < A.H.nf; f++) {
+    double d = ddot(face_wn(W, A.H, wnA, f), sep);
+    if (d < dmin) { dmin = d; cfa = f; }
+  }
+  if (cfa < 0) return 0;
+  const DFace FA = W.faces[A.H.f0 + cfa];
+  d3* pin = bufA;
+  d3* pout = bufB;
+  for (int i = 0; i < FA.n; i++) {
+    int other = FA.nc > i ? W.hconn[FA.c0 + i] : 0;
+    d3 pn = face_wn(W, A.H, wnA, other);
+    double planeEqWS = W.faces[A.H.f0 + other].plane_const - ddot(pn, A.x);
+    int nout = dclip_face_against_plane(pin, nin, pout, pn, planeEqWS);
+    if (nout > CP_MAX_CLIP) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
+    d3* t = pin; pin = pout; pout = t;
+    nin = nout;
+  }
+  d3 pn = face_wn(W, A.H, wnA, cfa);
+  double planeEqWS = FA.plane_const - ddot(pn, A.x);
+  double depth[CP_MAX_CLIP];
+  int n = 0;
+  for (int i = 0; i < nin; i++) {
+    double dd = ddot(pn, pin[i]) + planeEqWS;
+    if (dd <= -100.0) dd = -100.0;
+    depth[i] = dd;
+    if (dd <= 100.0 && dd <= 1e-6) n++;
+  }
+  if (n == 0) return 0;
+  start = reserve(C, n);
+  if (start < 0) return n;
+  const DBody& BA = W.bodies[bA];
+  const DBody& BB = W.bodies[bB];
+  d3 ni = dneg(sep);
+  d3 pa = d3of(ld3(BA.pos)), pb = d3of(ld3(BB.pos));
+  int k = 0;
+  for (int i = 0; i < nin; i++) {
+    double dd = depth[i];
+    if (dd <= 100.0 && dd <= 1e-6) {
+      d3 q = dscale(dneg(pn), dd);
+      d3 ri = dadd(pin[i], q);
+      d3 rj = pin[i];
+      ri = dsub(ri, A.x);
+      rj = dsub(rj, B.x);
+      ri = dsub(dadd(ri, A.x), pa);
+      rj = dsub(dadd(rj, B.x), pb);
+      ContactOut g;
+      g.ni = f3{(float)ni.x, (float)ni.y, (float)ni.z};
+      g.ri = f3{(float)ri.x, (float)ri.y, (float)ri.z};
+      g.rj = f3{(float)rj.x, (float)rj.y, (float)rj.z};
+      fill_contact(C, W.ctmp[start + k], bA, bB, shA, shB, rsi, rsj, g);
+      k++;
+    }
+  }
+  return n;
+}

@@ -303,7 +303,13 @@ struct cp_ctx {
   int* d_one = nullptr;  // world id of the plain path
   long long* d_status = nullptr;
   int d_status_cap = 0;
-  int sms = 0, blocks_per_sm = 1;
+  int sms = 0;
+  std::vector<int> blocks_per_sm;  // per kernel variant
+  // autotuner: one timed step per kernel variant, then the fastest
+  std::vector<double> tune_ms;
+  int tune_next = 0;
+  int best = -1;
+  std::vector<int> tune_ids;
   long long launches = 0;
   std::mutex mu;
   // batched host I/O
@@ -567,7 +573,7 @@ int plain_steps(cp_ctx* c, int id, double dt, int nsteps) {
   for (int guard = 0; guard < 64; guard++) {
     long long done = p.stepnumber;
     for (long long s = done; s < target; s++) {
-      CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_one, 1, dt, c->d_queue, 1, c->stream));
+      CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_one, 1, dt, c->d_queue, 1, c->stream, w.nb > 512 ? 0 : 2));
       c->launches += 2;
     }
     st = read_params(c, w, p);
@@ -672,7 +678,7 @@ int cp_create(const cp_config* cfg, cp_ctx** out) {
     delete c;
     return fail(CP_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
   }
-  c->blocks_per_sm = std::max(1, cpk_max_resident_blocks());
+  for (int v = 0; v < cpk_num_variants(); v++) c->blocks_per_sm.push_back(std::max(1, cpk_max_resident_blocks(v)));
   *out = c;
   return CP_OK;
 }
@@ -724,7 +730,8 @@ int cp_world_create(cp_ctx* c, const cp_world_desc* d, int32_t* world_id) {
   std::vector<DHull> hulls;
   std::vector<DFace> faces;
   std::vector<float> hverts, hedges;
-  std::vector<int> hfi, hconn;
+  std::vector<double> hvd, hed;
+  std::vector<int> hfi, hconn, hcanon;
   for (int s = 0; s < ns; s++) {
     const cp_shape_desc& sd = d->shapes[s];
     if (sd.material < -1 || sd.material >= nm) return fail(CP_ERR_ARG, "shape %d: material out of range", s);
@@ -746,12 +753,39 @@ int cp_world_create(cp_ctx* c, const cp_world_desc* d, int32_t* world_id) {
     if (st) return st;
     o.bsr = shape_bsr(sd, &h);
     DHull dh;
+    std::memset(&dh, 0, sizeof(dh));
     dh.v0 = (int)hverts.size() / 4; dh.nv = (int)h.verts.size();
     dh.f0 = (int)faces.size(); dh.nf = (int)h.faces.size();
     dh.e0 = (int)hedges.size() / 4; dh.ne = (int)h.edges.size();
-    dh.has_axes = h.has_axes; dh.pad = 0;
-    for (auto& v : h.verts) { hverts.push_back(v.x); hverts.push_back(v.y); hverts.push_back(v.z); hverts.push_back(0.f); }
-    for (auto& e : h.edges) { hedges.push_back(e.x); hedges.push_back(e.y); hedges.push_back(e.z); hedges.push_back(0.f); }
+    dh.has_axes = h.has_axes;
+    dh.is_box = sd.type == CP_SHAPE_BOX;
+    dh.he[0] = sd.half_extents[0]; dh.he[1] = sd.half_extents[1]; dh.he[2] = sd.half_extents[2];
+    for (auto& v : h.verts) {
+      hverts.push_back(v.x); hverts.push_back(v.y); hverts.push_back(v.z); hverts.push_back(0.f);
+      hvd.push_back(v.x); hvd.push_back(v.y); hvd.push_back(v.z); hvd.push_back(0.0);
+    }
+    for (auto& e : h.edges) {
+      hedges.push_back(e.x); hedges.push_back(e.y); hedges.push_back(e.z); hedges.push_back(0.f);
+      hed.push_back(e.x); hed.push_back(e.y); hed.push_back(e.z); hed.push_back(0.0);
+    }
+    // canonical entries: those whose exact negation does not occur earlier
+    auto negated = [](const h3& a, const h3& b) { return a.x == -b.x && a.y == -b.y && a.z == -b.z; };
+    std::vector<int> fcanon(h.faces.size());
+    dh.cf0 = (int)hcanon.size();
+    for (size_t f = 0; f < h.faces.size(); f++) {
+      fcanon[f] = (int)f;
+      for (size_t g = 0; g < f; g++)
+        if (fcanon[g] == (int)g && negated(h.normals[f], h.normals[g])) { fcanon[f] = (int)g; break; }
+      if (fcanon[f] == (int)f) hcanon.push_back((int)f);
+    }
+    dh.ncf = (int)hcanon.size() - dh.cf0;
+    dh.ce0 = (int)hcanon.size();
+    for (size_t e = 0; e < h.edges.size(); e++) {
+      bool dup = false;
+      for (size_t g = 0; g < e && !dup; g++) dup = negated(h.edges[e], h.edges[g]);
+      if (!dup) hcanon.push_back((int)e);
+    }
+    dh.nce = (int)hcanon.size() - dh.ce0;
     for (size_t f = 0; f < h.faces.size(); f++) {
       DFace F;
       std::memset(&F, 0, sizeof(F));
@@ -768,7 +802,9 @@ int cp_world_create(cp_ctx* c, const cp_world_desc* d, int32_t* world_id) {
       for (int x : conn) hconn.push_back(x);
       F.nc = (int)conn.size();
       F.normal[0] = h.normals[f].x; F.normal[1] = h.normals[f].y; F.normal[2] = h.normals[f].z;
+      F.dnormal[0] = h.normals[f].x; F.dnormal[1] = h.normals[f].y; F.dnormal[2] = h.normals[f].z;
       F.plane_const = -dot3(h.normals[f], h.verts[h.faces[f][0]]);  // getPlaneConstantOfFace
+      F.canon = fcanon[f];
       faces.push_back(F);
     }
     o.hull = (int)hulls.size();
@@ -883,6 +919,9 @@ int cp_world_create(cp_ctx* c, const cp_world_desc* d, int32_t* world_id) {
   size_t o_hv = L.take(sizeof(float) * (hverts.size() + 4));
   size_t o_he = L.take(sizeof(float) * (hedges.size() + 4));
   size_t o_hfi = L.take(sizeof(int) * (hfi.size() + 1));
+  size_t o_hvd = L.take(sizeof(double) * (hvd.size() + 4));
+  size_t o_hed = L.take(sizeof(double) * (hed.size() + 4));
+  size_t o_hcn = L.take(sizeof(int) * (hcanon.size() + 1));
   size_t o_hc = L.take(sizeof(int) * (hconn.size() + 1));
   size_t o_m = L.take(sizeof(DMaterial) * (nm + 1));
   size_t o_ct = L.take(sizeof(int) * cmt.size());
@@ -900,6 +939,9 @@ int cp_world_create(cp_ctx* c, const cp_world_desc* d, int32_t* world_id) {
   if (!hverts.empty()) std::memcpy(&host[o_hv], hverts.data(), sizeof(float) * hverts.size());
   if (!hedges.empty()) std::memcpy(&host[o_he], hedges.data(), sizeof(float) * hedges.size());
   if (!hfi.empty()) std::memcpy(&host[o_hfi], hfi.data(), sizeof(int) * hfi.size());
+  if (!hvd.empty()) std::memcpy(&host[o_hvd], hvd.data(), sizeof(double) * hvd.size());
+  if (!hed.empty()) std::memcpy(&host[o_hed], hed.data(), sizeof(double) * hed.size());
+  if (!hcanon.empty()) std::memcpy(&host[o_hcn], hcanon.data(), sizeof(int) * hcanon.size());
   if (!hconn.empty()) std::memcpy(&host[o_hc], hconn.data(), sizeof(int) * hconn.size());
   if (nm) std::memcpy(&host[o_m], mats.data(), sizeof(DMaterial) * nm);
   std::memcpy(&host[o_ct], cmt.data(), sizeof(int) * cmt.size());
@@ -928,6 +970,9 @@ int cp_world_create(cp_ctx* c, const cp_world_desc* d, int32_t* world_id) {
   dw.hedges = (float*)(base + o_he);
   dw.haxes = nullptr;
   dw.hfi = (int*)(base + o_hfi);
+  dw.hvd = (double*)(base + o_hvd);
+  dw.hed = (double*)(base + o_hed);
+  dw.hcanon = (int*)(base + o_hcn);
   dw.hconn = (int*)(base + o_hc);
   dw.mats = (DMaterial*)(base + o_m);
   dw.cm_table = (int*)(base + o_ct);
@@ -1114,16 +1159,26 @@ int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t n
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return c->worlds[a].nb > c->worlds[b].nb; });
   int st = ensure_ids(c, n);
   if (st) return st;
-  const int grid = std::max(1, std::min(n, c->sms * c->blocks_per_sm));
-  bool reuse = c->graph && c->graph_ids == order && c->graph_dt == dt && c->graph_steps == nsteps;
+  // autotuning: while variants are untimed for this world set, each call runs
+  // its steps with the next untimed variant (results do not depend on it)
+  if (c->tune_ids != order) {
+    c->tune_ids = order;
+    c->tune_ms.assign(cpk_num_variants(), 0.0);
+    c->tune_next = 0;
+    c->best = -1;
+  }
+  const bool tuning = c->best < 0;
+  const int variant = tuning ? c->tune_next : c->best;
+  const int grid = std::max(1, std::min(n, c->sms * c->blocks_per_sm[variant]));
+  bool reuse = !tuning && c->graph && c->graph_ids == order && c->graph_dt == dt && c->graph_steps == nsteps;
   CUDA_TRY(cudaMemcpyAsync(c->d_ids, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
-  if (!reuse) {
+  if (!reuse && !tuning) {
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     cudaGraph_t g;
     CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 0; s < nsteps; s++) {
-      cudaError_t e = cpk_launch_step(c->d_worlds, c->d_ids, n, dt, c->d_queue, grid, c->stream);
+      cudaError_t e = cpk_launch_step(c->d_worlds, c->d_ids, n, dt, c->d_queue, grid, c->stream, variant);
       if (e != cudaSuccess) {
         cudaStreamEndCapture(c->stream, &g);
         return fail(CP_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
@@ -1142,7 +1197,11 @@ int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t n
   std::vector<long long> before(4 * (size_t)n), after(4 * (size_t)n);
   CUDA_TRY(cudaMemcpyAsync(before.data(), c->d_status, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
-  CUDA_TRY(cudaGraphLaunch(c->graph, c->stream));
+  if (tuning) {
+    for (int s = 0; s < nsteps; s++) CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_ids, n, dt, c->d_queue, grid, c->stream, variant));
+  } else {
+    CUDA_TRY(cudaGraphLaunch(c->graph, c->stream));
+  }
   CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
   c->launches += 2LL * nsteps + 1;
   CUDA_TRY(cpk_gather_status(c->d_worlds, c->d_ids, n, c->d_status, c->stream));
@@ -1152,6 +1211,12 @@ int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t n
   CUDA_TRY(cudaEventElapsedTime(&gms, c->ev0, c->ev1));
   c->graph_ms += gms;
   c->graph_step_launches += nsteps;
+  if (tuning) {
+    c->tune_ms[variant] = gms / nsteps;
+    if (++c->tune_next == cpk_num_variants()) {
+      c->best = (int)(std::min_element(c->tune_ms.begin(), c->tune_ms.end()) - c->tune_ms.begin());
+    }
+  }
   c->launches += 1;
   for (int i = 0; i < n; i++) {
     if (after[4 * i] != 0) {  // overflowed part way: grow and finish on the plain path
@@ -1243,6 +1308,26 @@ int cp_get_stream(cp_ctx* c, void** stream) {
   if (!c || !stream) return fail(CP_ERR_ARG, "null argument");
   *stream = (void*)c->stream;
   return CP_OK;
+}
+
+int cp_phase_profile(cp_ctx* c, double* cycles, int32_t n) {
+  if (!c || !cycles || n < CP_NUM_PHASES) return fail(CP_ERR_ARG, "need room for %d phases", CP_NUM_PHASES);
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  unsigned long long v[CP_NUM_PHASES];
+  CUDA_TRY(cpk_phase_cycles(v, true));
+  for (int i = 0; i < CP_NUM_PHASES; i++) cycles[i] = (double)v[i];
+  return CP_OK;
+}
+
+int cp_autotune_info(cp_ctx* c, int32_t* variant, int32_t* threads, double* ms, int32_t n) {
+  if (!c || !variant || !threads) return fail(CP_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lock(c->mu);
+  *variant = c->best;
+  *threads = c->best >= 0 ? cpk_variant_threads(c->best) : 0;
+  for (int i = 0; ms && i < n && i < (int)c->tune_ms.size(); i++) ms[i] = c->tune_ms[i];
+  return cpk_num_variants();
 }
 
 int cp_batch_profile(cp_ctx* c, double* graph_ms, int64_t* step_launches) {

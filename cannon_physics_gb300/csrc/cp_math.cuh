@@ -18,6 +18,36 @@
 
 struct f3 { float x, y, z; };
 struct q4 { float x, y, z, w; };
+struct d3 { double x, y, z; };  // a Vector3 held as binary64 (each value exactly a binary32)
+
+// (double)(float)x without the F2F conversions: for results in binary32's
+// normal range the 29 low mantissa bits are rounded off on the integer pipe
+// (round to nearest, ties to even; a carry into the exponent is the correct
+// next binade).  Zeros, subnormals, values that could overflow, infinities
+// and NaNs take the conversion path.  GB300 issues F2F.F32.F64 at its
+// binary64 rate, about 1/60 of the integer rate.
+DI double r32(double x) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+  if (e - 897u < 253u) {  // 2^-126 <= |x| < 2^127
+    u += 0x0FFFFFFFull + ((u >> 29) & 1ull);
+    u &= ~0x1FFFFFFFull;
+    return __longlong_as_double((long long)u);
+  }
+  if ((u << 1) == 0) return x;  // +-0
+  return (double)__double2float_rn(x);
+}
+DI d3 d3of(f3 v) { return d3{(double)v.x, (double)v.y, (double)v.z}; }
+DI d3 ldd3(const double* p) { return d3{p[0], p[1], p[2]}; }
+DI void std3(double* p, d3 v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
+DI double ddot(d3 a, d3 b) {
+  double s = a.x * b.x;
+  s = s + a.y * b.y;
+  s = s + a.z * b.z;
+  return s;
+}
+// addScaledVector with the binary32 store: a + s * v, rounded
+DI d3 dadd_scaled(d3 a, double s, d3 v) { return d3{r32(a.x + s * v.x), r32(a.y + s * v.y), r32(a.z + s * v.z)}; }
 
 DI f3 mkf3(double x, double y, double z) { return f3{(float)x, (float)y, (float)z}; }
 DI f3 ld3(const float* p) { return f3{p[0], p[1], p[2]}; }

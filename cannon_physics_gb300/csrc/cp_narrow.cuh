@@ -314,196 +314,6 @@ DI int plane_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rs
   return n;
 }
 
-// ---- convex-convex (convex_polyhedron.dart:189-587,843-883) ----
-
-struct HullPose {
-  DHull H;
-  f3 x;
-  q4 q;
-  f3 origin;  // Transform.pointToLocalFrame(pos, quat, 0): the same for every axis
-};
-
-// ConvexPolyhedron.project
-DI void project(const DWorld& W, const HullPose& h, f3 axis, double& mx, double& mn) {
-  f3 la = vector_to_local(h.q, axis);
-  double addv = dot(h.origin, la);
-  double max = dot(hv(W, h.H.v0), la), min = max;
-  for (int i = 1; i < h.H.nv; i++) {
-    double v = dot(hv(W, h.H.v0 + i), la);
-    if (v > max) max = v;
-    if (v < min) min = v;
-  }
-  min -= addv;
-  max -= addv;
-  if (min > max) { double t = min; min = max; max = t; }
-  mx = max;
-  mn = min;
-}
-
-// testSepAxis; false when the hulls are separated along `axis`
-DI bool test_sep_axis(const DWorld& W, const HullPose& A, const HullPose& B, f3 axis, double& depth) {
-  double maxA, minA, maxB, minB;
-  project(W, A, axis, maxA, minA);
-  project(W, B, axis, maxB, minB);
-  if (maxA < minB || maxB < minA) return false;
-  double d0 = maxA - minB, d1 = maxB - minA;
-  depth = d0 < d1 ? d0 : d1;
-  return true;
-}
-
-// findSeparatingAxis: face normals of A (when A has uniqueAxes), face normals
-// of B (when B has uniqueAxes), then every edge-pair cross product; the first
-// smallest depth wins; the axis is flipped to point from B towards A.
-DI bool find_separating_axis(const DWorld& W, const HullPose& A, const HullPose& B, const f3* wnA, const f3* wnB, f3& target) {
-  double dmin = __longlong_as_double(0x7ff0000000000000LL);
-  double d;
-  if (A.H.has_axes)
-    for (int i = 0; i < A.H.nf; i++) {
-      if (!test_sep_axis(W, A, B, wnA[i], d)) return false;
-      if (d < dmin) { dmin = d; target = wnA[i]; }
-    }
-  if (B.H.has_axes)
-    for (int i = 0; i < B.H.nf; i++) {
-      if (!test_sep_axis(W, A, B, wnB[i], d)) return false;
-      if (d < dmin) { dmin = d; target = wnB[i]; }
-    }
-  f3 weB[CP_MAX_HULL_VERTS];
-  int neB = B.H.ne;
-  for (int e1 = 0; e1 < neB; e1++) weB[e1] = vmult(B.q, ld3(W.hedges + 4 * (B.H.e0 + e1)));
-  for (int e0 = 0; e0 < A.H.ne; e0++) {
-    f3 we0 = vmult(A.q, ld3(W.hedges + 4 * (A.H.e0 + e0)));
-    for (int e1 = 0; e1 < neB; e1++) {
-      f3 cr = cross(we0, weB[e1]);
-      if (!almost_zero(cr)) {
-        cr = normalized(cr);
-        if (!test_sep_axis(W, A, B, cr, d)) return false;
-        if (d < dmin) { dmin = d; target = cr; }
-      }
-    }
-  }
-  f3 deltaC = sub(B.x, A.x);
-  if (dot(deltaC, target) > 0.0) target = neg(target);
-  return true;
-}
-
-// clipFaceAgainstPlane
-DI int clip_face_against_plane(const f3* in, int nin, f3* out, f3 n, double c) {
-  if (nin < 2) return 0;
-  int nout = 0;
-  f3 first = in[nin - 1];
-  double nDotFirst = dot(n, first) + c;
-  for (int vi = 0; vi < nin; vi++) {
-    f3 last = in[vi];
-    double nDotLast = dot(n, last) + c;
-    if (nDotFirst < 0) {
-      if (nDotLast < 0) {
-        if (nout < CP_MAX_CLIP) out[nout] = last;
-        nout++;
-      } else {
-        if (nout < CP_MAX_CLIP) out[nout] = lerp(first, last, nDotFirst / (nDotFirst - nDotLast));
-        nout++;
-      }
-    } else if (nDotLast < 0) {
-      if (nout < CP_MAX_CLIP) out[nout] = lerp(first, last, nDotFirst / (nDotFirst - nDotLast));
-      nout++;
-      if (nout < CP_MAX_CLIP) out[nout] = last;
-      nout++;
-    }
-    first = last;
-    nDotFirst = nDotLast;
-  }
-  return nout;
-}
-
-// narrow_phase.dart:1981-2043 convexConvex, with clipAgainstHull /
-// clipFaceAgainstHull (convex_polyhedron.dart:189-227,417-541)
-DI int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qA, q4 qB, int& start) {
-  const DWorld& W = *C.W;
-  const DShape& SA = W.shapes[shA];
-  const DShape& SB = W.shapes[shB];
-  if (distance_to(xA, xB) > SA.bsr + SB.bsr) return 0;
-  HullPose A, B;
-  A.H = W.hulls[SA.hull]; A.x = xA; A.q = qA; A.origin = point_to_local(xA, qA, f3{0.f, 0.f, 0.f});
-  B.H = W.hulls[SB.hull]; B.x = xB; B.q = qB; B.origin = point_to_local(xB, qB, f3{0.f, 0.f, 0.f});
-  if (A.H.nf > CP_MAX_HULL_VERTS || B.H.nf > CP_MAX_HULL_VERTS || B.H.ne > CP_MAX_HULL_VERTS) {
-    atomicOr(C.overflow, ST_HULL_OVERFLOW);
-    return 0;
-  }
-  f3 wnA[CP_MAX_HULL_VERTS], wnB[CP_MAX_HULL_VERTS];
-  for (int i = 0; i < A.H.nf; i++) wnA[i] = vmult(qA, ld3(W.faces[A.H.f0 + i].normal));
-  for (int i = 0; i < B.H.nf; i++) wnB[i] = vmult(qB, ld3(W.faces[B.H.f0 + i].normal));
-  f3 sep{0.f, 0.f, 0.f};
-  if (!find_separating_axis(W, A, B, wnA, wnB, sep)) return 0;
-  // clipAgainstHull: face of B most aligned with the axis
-  int cfb = -1;
-  double dmax = __longlong_as_double(0xfff0000000000000LL);
-  for (int f = 0; f < B.H.nf; f++) {
-    double d = dot(wnB[f], sep);
-    if (d > dmax) { dmax = d; cfb = f; }
-  }
-  if (cfb < 0) return 0;
-  f3 bufA[CP_MAX_CLIP], bufB[CP_MAX_CLIP];
-  const DFace FB = W.faces[B.H.f0 + cfb];
-  if (FB.n > CP_MAX_CLIP) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
-  int nin = FB.n;
-  for (int i = 0; i < nin; i++) bufA[i] = add(vmult(qB, hv(W, B.H.v0 + W.hfi[FB.i0 + i])), xB);
-  // clipFaceAgainstHull: face of A most anti-aligned with the axis
-  int cfa = -1;
-  double dmin = __longlong_as_double(0x7ff0000000000000LL);
-  for (int f = 0; f < A.H.nf; f++) {
-    double d = dot(wnA[f], sep);
-    if (d < dmin) { dmin = d; cfa = f; }
-  }
-  if (cfa < 0) return 0;
-  const DFace FA = W.faces[A.H.f0 + cfa];
-  f3* pin = bufA;
-  f3* pout = bufB;
-  for (int i = 0; i < FA.n; i++) {
-    int other = FA.nc > i ? W.hconn[FA.c0 + i] : 0;
-    const DFace FO = W.faces[A.H.f0 + other];
-    f3 pn = wnA[other];
-    double planeEqWS = FO.plane_const - dot(pn, xA);
-    int nout = clip_face_against_plane(pin, nin, pout, pn, planeEqWS);
-    if (nout > CP_MAX_CLIP) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
-    f3* t = pin; pin = pout; pout = t;
-    nin = nout;
-  }
-  f3 pn = wnA[cfa];
-  double planeEqWS = FA.plane_const - dot(pn, xA);
-  double depth[CP_MAX_CLIP];
-  int n = 0;
-  for (int i = 0; i < nin; i++) {
-    double dd = dot(pn, pin[i]) + planeEqWS;
-    if (dd <= -100.0) dd = -100.0;
-    depth[i] = dd;
-    if (dd <= 100.0 && dd <= 1e-6) n++;
-  }
-  if (n == 0) return 0;
-  start = reserve(C, n);
-  if (start < 0) return n;
-  const DBody& BA = W.bodies[bA];
-  const DBody& BB = W.bodies[bB];
-  f3 ni = neg(sep);
-  int k = 0;
-  for (int i = 0; i < nin; i++) {
-    double dd = depth[i];
-    if (dd <= 100.0 && dd <= 1e-6) {
-      ContactOut g;
-      g.ni = ni;
-      f3 q = scale(neg(pn), dd);
-      g.ri = add(pin[i], q);
-      g.rj = pin[i];
-      g.ri = sub(g.ri, xA);
-      g.rj = sub(g.rj, xB);
-      g.ri = rel(g.ri, xA, BA);
-      g.rj = rel(g.rj, xB, BB);
-      fill_contact(C, W.ctmp[start + k], bA, bB, shA, shB, rsi, rsj, g);
-      k++;
-    }
-  }
-  return n;
-}
-
 // Resolver choice of narrow_phase.dart:116-238,476-489,706-710.  The shape
 // with the lower ShapeType index goes first (for equal types the call is the
 // swapped one); (rsi, rsj) stay in getContacts order.

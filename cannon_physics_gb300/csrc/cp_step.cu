@@ -18,12 +18,19 @@
 
 #include "cp_kernels.h"
 #include "cp_narrow.cuh"
+#include "cp_cc.cuh"
 #include "cp_types.h"
 
-#define BT 256
-#define NWARP (BT / 32)
+#define BT blockDim.x
+#define NWARP (blockDim.x >> 5)
+
+// Per-phase SM cycles summed over blocks (World.profile's breakdown,
+// world_class.dart:27-41); read with cp_phase_profile.
+__device__ unsigned long long g_phase_cycles[CP_NUM_PHASES];
 
 struct __align__(16) Smem {
+  long long t_last;
+  long long t_acc[CP_NUM_PHASES];
   DWorld W;
   DWorldParams P;
   int warp[32];
@@ -852,8 +859,8 @@ DI void ph_solve_prep(Smem& S) {
     }
     s.im_solve = im;
     s.active = (im != 0.0) || any_iw;
-    st3(s.vl, f3{0.f, 0.f, 0.f});
-    st3(s.wl, f3{0.f, 0.f, 0.f});
+    std3(s.vl, d3{0.0, 0.0, 0.0});
+    std3(s.wl, d3{0.0, 0.0, 0.0});
     st3(s.imf, scale(ld3(b.force), im));
     st3(s.iit, mvmult(iw, ld3(b.torque)));
   }
@@ -922,8 +929,8 @@ DI void assemble_row(const Smem& S, const RowGeom& G, DRow& R, double h) {
   C += dot(iMaR, gaR);
   C += dot(iMbR, gbR);
   C = C + G.eps;
-  st3(R.gaS, gaS); st3(R.gaR, gaR); st3(R.gbS, gbS); st3(R.gbR, gbR);
-  st3(R.iMaR, iMaR); st3(R.iMbR, iMbR);
+  std3(R.gaS, d3of(gaS)); std3(R.gaR, d3of(gaR)); std3(R.gbS, d3of(gbS)); std3(R.gbR, d3of(gbR));
+  std3(R.iMaR, d3of(iMaR)); std3(R.iMbR, d3of(iMbR));
   R.B = B;
   R.invC = 1.0 / C;
   R.eps = G.eps;
@@ -1060,25 +1067,23 @@ DI void ph_levels(Smem& S) {
 DI double gs_row(const DWorld& W, DRow& R) {
   DBodyScr& A = W.bscr[R.bi];
   DBodyScr& B = W.bscr[R.bj];
-  f3 vla = ld3(A.vl), wla = ld3(A.wl), vlb = ld3(B.vl), wlb = ld3(B.wl);
-  double gwl = (dot(vla, ld3(R.gaS)) + dot(wla, ld3(R.gaR))) + (dot(vlb, ld3(R.gbS)) + dot(wlb, ld3(R.gbR)));
+  d3 vla = ldd3(A.vl), wla = ldd3(A.wl), vlb = ldd3(B.vl), wlb = ldd3(B.wl);
+  double gwl = (ddot(vla, ldd3(R.gaS)) + ddot(wla, ldd3(R.gaR))) + (ddot(vlb, ldd3(R.gbS)) + ddot(wlb, ldd3(R.gbR)));
   double lj = R.lambda;
   double dl = R.invC * (R.B - gwl - R.eps * lj);
   if (lj + dl < R.minF) dl = R.minF - lj;
   else if (lj + dl > R.maxF) dl = R.maxF - lj;
   R.lambda = lj + dl;
-  if (A.active) {
-    st3(A.vl, add_scaled(vla, R.imA * dl, ld3(R.gaS)));
-  }
+  if (A.active) std3(A.vl, dadd_scaled(vla, R.imA * dl, ldd3(R.gaS)));
   if (B.active) {
     // re-read: bi == bj is possible for a constraint between a body and itself
-    f3 v = R.bi == R.bj ? ld3(B.vl) : vlb;
-    st3(B.vl, add_scaled(v, R.imB * dl, ld3(R.gbS)));
+    d3 v = R.bi == R.bj ? ldd3(B.vl) : vlb;
+    std3(B.vl, dadd_scaled(v, R.imB * dl, ldd3(R.gbS)));
   }
-  if (A.active) st3(A.wl, add_scaled(wla, dl, ld3(R.iMaR)));
+  if (A.active) std3(A.wl, dadd_scaled(wla, dl, ldd3(R.iMaR)));
   if (B.active) {
-    f3 w = R.bi == R.bj ? ld3(B.wl) : wlb;
-    st3(B.wl, add_scaled(w, dl, ld3(R.iMbR)));
+    d3 w = R.bi == R.bj ? ldd3(B.wl) : wlb;
+    std3(B.wl, dadd_scaled(w, dl, ldd3(R.iMbR)));
   }
   return dl > 0.0 ? dl : -dl;
 }
@@ -1134,12 +1139,10 @@ DI void ph_solve_apply(Smem& S, double h) {
   for (int i = threadIdx.x; i < S.P.nb; i += BT) {
     DBody& b = W.bodies[i];
     DBodyScr& s = W.bscr[i];
-    f3 vl = mul(ld3(s.vl), ld3(b.lin_factor));
+    f3 vl = mul(f3{(float)s.vl[0], (float)s.vl[1], (float)s.vl[2]}, ld3(b.lin_factor));
     st3(b.vel, add(ld3(b.vel), vl));
-    f3 wl = mul(ld3(s.wl), ld3(b.ang_factor));
+    f3 wl = mul(f3{(float)s.wl[0], (float)s.wl[1], (float)s.wl[2]}, ld3(b.ang_factor));
     st3(b.avel, add(ld3(b.avel), wl));
-    st3(s.vl, vl);
-    st3(s.wl, wl);
   }
   double invDt = 1 / h;
   for (int r = threadIdx.x; r < S.n_rows; r += BT) W.rows[r].mult = W.rows[r].lambda * invDt;
@@ -1215,41 +1218,60 @@ DI void ph_integrate(Smem& S, double dt) {
 
 // ---------------------------------------------------------------------------
 
+DI void tick(Smem& S, int phase) {
+  if (threadIdx.x == 0) {
+    long long t = clock64();
+    S.t_acc[phase] += t - S.t_last;
+    S.t_last = t;
+  }
+}
+
 DI void step_world(Smem& S, double dt) {
   if (threadIdx.x == 0) {
     S.overflow = 0;
     S.n_pairs = S.n_contacts = S.n_rows = S.n_levels = 0;
     S.n_fric = S.n_cand = 0;
+    S.t_last = clock64();
   }
   __syncthreads();
   ph_prepare(S);
+  tick(S, 0);
   if (S.P.broadphase == CP_BROAD_SAP) ph_broad_sap(S);
   else if (S.P.broadphase == CP_BROAD_GRID) ph_broad_grid(S);
   else ph_broad_naive(S);
   if (S.overflow) return;
   if (S.P.n_nocollide > 0) ph_nocollide(S);
+  tick(S, 1);
   ph_narrow(S);
+  tick(S, 2);
   if (S.overflow) return;
   ph_rows_list(S);
   if (S.overflow) return;
   // ---- body state changes from here on ----
   ph_contacts_post(S);
   ph_solve_prep(S);
+  tick(S, 3);
   ph_rows_assemble(S, dt);
+  tick(S, 4);
   if (S.n_rows > 0) {
     ph_levels(S);
+    tick(S, 5);
     ph_solve(S, dt);
+    tick(S, 6);
     ph_solve_apply(S, dt);
   } else if (threadIdx.x == 0) {
     S.P.last_iterations = 0;
   }
   __syncthreads();
   ph_integrate(S, dt);
+  tick(S, 7);
 }
 
-__global__ void __launch_bounds__(BT, 1) k_step_worlds(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n,
-                                                       double dt, int* __restrict__ queue) {
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_step_worlds(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n,
+                                                              double dt, int* __restrict__ queue) {
   __shared__ Smem S;
+  if (threadIdx.x < CP_NUM_PHASES) S.t_acc[threadIdx.x] = 0;
   for (;;) {
     if (threadIdx.x == 0) S.wi = atomicAdd(queue, 1);
     __syncthreads();
@@ -1279,6 +1301,7 @@ __global__ void __launch_bounds__(BT, 1) k_step_worlds(const DWorld* __restrict_
     }
     __syncthreads();
   }
+  if (threadIdx.x < CP_NUM_PHASES) atomicAdd(&g_phase_cycles[threadIdx.x], (unsigned long long)S.t_acc[threadIdx.x]);
 }
 
 __global__ void k_gather_status(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n, long long* out) {
@@ -1351,18 +1374,44 @@ cudaError_t cpk_gather_poses(const DWorld* d_worlds, const int* d_ids, const lon
   return cudaGetLastError();
 }
 
-int cpk_block_threads() { return BT; }
+
+cudaError_t cpk_phase_cycles(unsigned long long* out, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(unsigned long long) * CP_NUM_PHASES);
+  if (e == cudaSuccess && reset) {
+    unsigned long long z[CP_NUM_PHASES] = {0};
+    e = cudaMemcpyToSymbol(g_phase_cycles, z, sizeof(z));
+  }
+  return e;
+}
+
+// Kernel variants (block threads, minimum resident blocks per SM): the
+// register budget, and with it the number of blocks that hide each other's
+// barrier waits, differs between them.  All compute identical results.
+struct Variant {
+  void (*fn)(const DWorld*, const int*, int, double, int*);
+  int threads;
+  int minb;
+};
+static const Variant kVariants[] = {
+    {k_step_worlds<256, 1>, 256, 1}, {k_step_worlds<128, 2>, 128, 2}, {k_step_worlds<128, 4>, 128, 4},
+    {k_step_worlds<64, 8>, 64, 8},   {k_step_worlds<256, 2>, 256, 2},
+};
+
+int cpk_num_variants() { return (int)(sizeof(kVariants) / sizeof(kVariants[0])); }
+
+int cpk_variant_threads(int v) { return kVariants[v].threads; }
 
 cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, int n, double dt, int* d_queue, int grid,
-                            cudaStream_t stream) {
+                            cudaStream_t stream, int variant) {
   cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
   if (e != cudaSuccess) return e;
-  k_step_worlds<<<grid, BT, 0, stream>>>(d_worlds, d_ids, n, dt, d_queue);
+  const Variant& V = kVariants[variant];
+  V.fn<<<grid, V.threads, 0, stream>>>(d_worlds, d_ids, n, dt, d_queue);
   return cudaGetLastError();
 }
 
-int cpk_max_resident_blocks() {
+int cpk_max_resident_blocks(int variant) {
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_worlds, BT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kVariants[variant].fn, kVariants[variant].threads, 0);
   return nb;
 }

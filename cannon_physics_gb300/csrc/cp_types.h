@@ -16,6 +16,7 @@
 #define CP_MAX_FACE_VERTS 16
 #define CP_MAX_CLIP 48
 #define CP_MAX_PAIR_CONTACTS 32
+#define CP_NUM_PHASES 8
 
 // body flags
 #define BF_ALLOW_SLEEP 1
@@ -73,13 +74,17 @@ struct __align__(16) DShape {
 // in the reference: the connected faces of each face and -n.v0.
 struct __align__(16) DHull {
   int v0, nv, f0, nf;        // vertices [v0, v0+nv), faces [f0, f0+nf)
-  int e0, ne, has_axes, pad; // unique edges [e0, e0+ne)
+  int e0, ne, has_axes, is_box;  // unique edges [e0, e0+ne); is_box: vertices are (+-he)
+  int cf0, ncf, ce0, nce;    // canonical faces / edges: hcanon[cf0 ..), hcanon[ce0 ..)
+  double he[4];              // box half extents (binary32 values)
 };
 struct __align__(16) DFace {
   int i0, n;     // vertex indices hfi[i0 .. i0+n)
   int c0, nc;    // connected faces hconn[c0 .. c0+nc)
   float normal[4];
+  double dnormal[4];   // the same normal in binary64
   double plane_const;
+  int canon, pad[3];   // the face whose normal is this one's exact negation (earlier), or itself
 };
 
 struct DMaterial { double friction, restitution; };
@@ -108,9 +113,11 @@ struct __align__(16) DContact {
   double slip;  // mug * reducedMass
 };
 
+// A solver row.  The Jacobian entries are binary32 values (JacobianElement
+// stores Vector3s) held exactly in binary64, so the sweeps need no conversions.
 struct __align__(16) DRow {
-  float gaS[4], gaR[4], gbS[4], gbR[4];
-  float iMaR[4], iMbR[4];  // invInertiaWorldSolve * rotational Jacobians (the addToWlambda temp)
+  double gaS[3], gaR[3], gbS[3], gbR[3];
+  double iMaR[3], iMbR[3];  // invInertiaWorldSolve * rotational Jacobians (the addToWlambda temp)
   double B, invC, eps, minF, maxF, lambda;
   double imA, imB;          // invMassSolve of bi, bj
   double mult;              // Equation.multiplier = lambda / h
@@ -120,8 +127,8 @@ struct __align__(16) DRow {
 struct __align__(16) DBodyScr {
   float xs[4];   // shape world position
   float qs[4];   // shape world orientation
-  float vl[4];   // vlambda
-  float wl[4];   // wlambda
+  double vl[4];  // vlambda (binary32 values held in binary64)
+  double wl[4];  // wlambda
   float imf[4];  // force * invMassSolve (computeGiMf)
   float iit[4];  // invInertiaWorldSolve * torque
   double im_solve;
@@ -152,6 +159,9 @@ struct DWorld {
   DFace* faces;
   float* hverts;   // float4 per vertex
   float* hedges;   // float4 per unique edge
+  double* hvd;     // vertices, binary64 (4 per vertex)
+  double* hed;     // unique edges, binary64 (4 per edge)
+  int* hcanon;     // canonical face / edge index lists
   float* haxes;    // unused by the step (uniqueAxes only gate face tests)
   int* hfi;        // face vertex indices
   int* hconn;      // connected faces

@@ -52,6 +52,8 @@ def lib():
         L.cp_kernel_launches.restype = C.c_int64
         L.cp_get_stream.argtypes = [vp, vp]
         L.cp_batch_profile.argtypes = [vp, vp, vp]
+        L.cp_phase_profile.argtypes = [vp, vp, i32]
+        L.cp_autotune_info.argtypes = [vp, vp, vp, vp, i32]
         _lib = L
     return _lib
 
@@ -93,6 +95,20 @@ class Context:
         s = C.c_void_p()
         check(lib().cp_get_stream(self.h, C.byref(s)), "cp_get_stream")
         return s.value
+
+    PHASES = ("prepare", "broadphase", "narrowphase", "rows_wake_prep", "assemble", "levels", "gs_sweeps", "integrate")
+
+    def phase_profile(self):
+        """SM cycles per step phase (summed over blocks) since the last call."""
+        out = np.zeros(len(self.PHASES), np.float64)
+        check(lib().cp_phase_profile(self.h, out.ctypes.data, len(out)), "cp_phase_profile")
+        return dict(zip(self.PHASES, out.tolist()))
+
+    def autotune_info(self):
+        v, t = C.c_int32(), C.c_int32()
+        ms = np.zeros(16)
+        n = lib().cp_autotune_info(self.h, C.byref(v), C.byref(t), ms.ctypes.data, 16)
+        return {"variant": v.value, "threads": t.value, "ms_per_variant": ms[:n].round(3).tolist()}
 
     def batch_profile(self):
         """(device ms, step launches) of batched graphs since the last call."""

@@ -281,6 +281,20 @@ int64_t cp_kernel_launches(cp_ctx* ctx);
  * can order their own work or time with events on it. */
 int cp_get_stream(cp_ctx* ctx, void** stream);
 
+/* The batch autotuner's choice: every kernel variant (threads per block and
+ * register budget) gives identical results, so the first cp_batch_step calls
+ * on a world set each time one variant on the live steps and later calls use
+ * the fastest.  Writes the chosen variant (-1 while tuning), its block size
+ * and up to n per-variant ms/step; returns the number of variants. */
+int cp_autotune_info(cp_ctx* ctx, int32_t* variant, int32_t* threads, double* ms, int32_t n);
+
+/* The World.profile breakdown (world_class.dart:27-41) of every step since
+ * the previous call, as SM cycles summed over thread blocks, in 8 slots:
+ * prepare, broadphase, narrowphase, contact rows + wake-ups + solve set-up,
+ * row assembly (computeB / computeC), solver levels, Gauss-Seidel sweeps,
+ * velocity update + integrate + sleep.  Shares, not wall time. */
+int cp_phase_profile(cp_ctx* ctx, double* cycles, int32_t n);
+
 /* Device time (CUDA events on the context stream) of the batched-step graph
  * launches since the previous call, and how many step launches they held. */
 int cp_batch_profile(cp_ctx* ctx, double* graph_ms, int64_t* step_launches);

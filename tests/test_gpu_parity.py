@@ -86,14 +86,18 @@ def test_edge_scenes(ctx, name):
 
 
 def test_dense_cluster_grows_capacities(ctx):
-    """300 spheres in a 2 m cube overlap far more than the initial pair and
+    """300 spheres in a 1.2 m cube overlap far more than the initial pair and
     contact capacities; the step reports the overflow, the world's scratch is
     regrown and the step re-run, with results still equal to the oracle."""
     sc = scenes.spheres_on_plane(300)
     rng = scenes.SplitMix64(99)
-    sc.bodies["position"][1:] = (rng.uniform(900).reshape(300, 3) * 2.0 + np.array([-1.0, 0.6, -1.0]))
-    info = run_parity(ctx, sc, 5)
-    assert info.num_pairs > 4 * 301 + 64
+    sc.bodies["position"][1:] = (rng.uniform(900).reshape(300, 3) * 1.2 + np.array([-0.6, 0.6, -0.6]))
+    engine.setup_scene(sc)
+    probe = ctx.world(sc)
+    probe.step()
+    assert probe.info().num_pairs > 4 * 301 + 64  # above the initial pair capacity
+    probe.destroy()
+    run_parity(ctx, sc, 5)
 
 
 def test_batched_equals_plain_and_oracle(ctx):
