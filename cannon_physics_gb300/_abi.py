@@ -209,7 +209,8 @@ class StepInfo(C.Structure):
         ("iterations", C.c_int32),
         ("status", C.c_int32),
         ("num_bodies", C.c_int32),
-        ("profile_ms", C.c_double * 4),
+        ("num_levels", C.c_int32),
+        ("pad", C.c_int32),
     ]
 
 

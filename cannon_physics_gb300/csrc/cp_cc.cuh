@@ -161,11 +161,65 @@ DI int dclip_face_against_plane(const d3* in, int nin, d3* out, d3 n, double c) 
   return nout;
 }
 
+// binary32 projection radius of a hull about its center along unit axis a
+DI float proj_radius32(const DWorld& W, const DHull& H, q4 q, const f3* ax, f3 a) {
+  if (H.is_box) {
+    return fabsf(dot32(a, ax[0])) * (float)H.he[0] + fabsf(dot32(a, ax[1])) * (float)H.he[1] +
+           fabsf(dot32(a, ax[2])) * (float)H.he[2];
+  }
+  f3 la = rot32(q4{-q.x, -q.y, -q.z, q.w}, a);
+  float m = 0.f;
+  for (int i = 0; i < H.nv; i++) {
+    const float* v = W.hverts + 4 * (H.v0 + i);
+    m = fmaxf(m, fabsf(la.x * v[0] + la.y * v[1] + la.z * v[2]));
+  }
+  return m;
+}
+
+// true when one of the axes findSeparatingAxis tests (canonical face
+// normals, edge crosses that are not almost zero) separates the hulls by a
+// clear margin in binary32: then the reference's SAT reports separation too.
+DI bool hulls_apart32(const DWorld& W, const DHull& A, const DHull& B, f3 xA, f3 xB, q4 qA, q4 qB, float rsum) {
+  f3 axA[3] = {rot32(qA, f3{1.f, 0.f, 0.f}), rot32(qA, f3{0.f, 1.f, 0.f}), rot32(qA, f3{0.f, 0.f, 1.f})};
+  f3 axB[3] = {rot32(qB, f3{1.f, 0.f, 0.f}), rot32(qB, f3{0.f, 1.f, 0.f}), rot32(qB, f3{0.f, 0.f, 1.f})};
+  f3 d = f3{xB.x - xA.x, xB.y - xA.y, xB.z - xA.z};
+  const float margin = 1e-4f * (rsum + fabsf(d.x) + fabsf(d.y) + fabsf(d.z)) + 1e-6f;
+  for (int side = 0; side < 2; side++) {
+    const DHull& H = side ? B : A;
+    if (!H.has_axes) continue;
+    q4 q = side ? qB : qA;
+    for (int k = 0; k < H.ncf; k++) {
+      const float* n = W.faces[H.f0 + W.hcanon[H.cf0 + k]].normal;
+      f3 a = rot32(q, f3{n[0], n[1], n[2]});
+      float dist = fabsf(dot32(a, d));
+      if (dist > proj_radius32(W, A, qA, axA, a) + proj_radius32(W, B, qB, axB, a) + margin) return true;
+    }
+  }
+  for (int k0 = 0; k0 < A.nce; k0++) {
+    const float* e0 = W.hedges + 4 * (A.e0 + W.hcanon[A.ce0 + k0]);
+    f3 we0 = rot32(qA, f3{e0[0], e0[1], e0[2]});
+    for (int k1 = 0; k1 < B.nce; k1++) {
+      const float* e1 = W.hedges + 4 * (B.e0 + W.hcanon[B.ce0 + k1]);
+      f3 we1 = rot32(qB, f3{e1[0], e1[1], e1[2]});
+      f3 cr = f3{we0.y * we1.z - we0.z * we1.y, we0.z * we1.x - we0.x * we1.z, we0.x * we1.y - we0.y * we1.x};
+      if (fmaxf(fabsf(cr.x), fmaxf(fabsf(cr.y), fabsf(cr.z))) < 1e-4f) continue;  // near the almostZero skip
+      float l = len32(cr);
+      f3 a = f3{cr.x / l, cr.y / l, cr.z / l};
+      float dist = fabsf(dot32(a, d));
+      if (dist > proj_radius32(W, A, qA, axA, a) + proj_radius32(W, B, qB, axB, a) + margin) return true;
+    }
+  }
+  return false;
+}
+
 DI int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xAf, f3 xBf, q4 qAf, q4 qBf, int& start) {
   const DWorld& W = *C.W;
   const DShape& SA = W.shapes[shA];
   const DShape& SB = W.shapes[shB];
   if (distance_to(xAf, xBf) > SA.bsr + SB.bsr) return 0;
+  if (W.hulls[SA.hull].nf <= CP_MAX_HULL_VERTS && W.hulls[SB.hull].nf <= CP_MAX_HULL_VERTS &&
+      hulls_apart32(W, W.hulls[SA.hull], W.hulls[SB.hull], xAf, xBf, qAf, qBf, (float)(SA.bsr + SB.bsr)))
+    return 0;
   DHullPose A, B;
   A.H = W.hulls[SA.hull]; A.x = d3of(xAf); A.q = d4of(qAf);
   B.H = W.hulls[SB.hull]; B.x = d3of(xBf); B.q = d4of(qBf);

@@ -310,6 +310,7 @@ struct cp_ctx {
   int tune_next = 0;
   int best = -1;
   std::vector<int> tune_ids;
+  int forced = -1;
   long long launches = 0;
   std::mutex mu;
   // batched host I/O
@@ -327,6 +328,7 @@ struct cp_ctx {
   std::vector<int> graph_ids;
   double graph_dt = 0;
   int graph_steps = 0;
+  int graph_variant = -1;
 };
 
 namespace {
@@ -1069,6 +1071,7 @@ int cp_world_get_info(cp_ctx* c, int32_t id, cp_step_info* out) {
   out->iterations = p.last_iterations;
   out->status = p.status;
   out->num_bodies = p.nb;
+  out->num_levels = p.num_levels;
   return CP_OK;
 }
 
@@ -1167,10 +1170,11 @@ int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t n
     c->tune_next = 0;
     c->best = -1;
   }
-  const bool tuning = c->best < 0;
-  const int variant = tuning ? c->tune_next : c->best;
+  const bool tuning = c->forced < 0 && c->best < 0;
+  const int variant = c->forced >= 0 ? c->forced : (tuning ? c->tune_next : c->best);
   const int grid = std::max(1, std::min(n, c->sms * c->blocks_per_sm[variant]));
-  bool reuse = !tuning && c->graph && c->graph_ids == order && c->graph_dt == dt && c->graph_steps == nsteps;
+  bool reuse = !tuning && c->graph && c->graph_ids == order && c->graph_dt == dt && c->graph_steps == nsteps &&
+               c->graph_variant == variant;
   CUDA_TRY(cudaMemcpyAsync(c->d_ids, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
   if (!reuse && !tuning) {
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
@@ -1191,6 +1195,7 @@ int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t n
     c->graph_ids = order;
     c->graph_dt = dt;
     c->graph_steps = nsteps;
+    c->graph_variant = variant;
   }
   // step numbers before the launch, to finish worlds whose step overflowed
   CUDA_TRY(cpk_gather_status(c->d_worlds, c->d_ids, n, c->d_status, c->stream));
@@ -1328,6 +1333,13 @@ int cp_autotune_info(cp_ctx* c, int32_t* variant, int32_t* threads, double* ms, 
   *threads = c->best >= 0 ? cpk_variant_threads(c->best) : 0;
   for (int i = 0; ms && i < n && i < (int)c->tune_ms.size(); i++) ms[i] = c->tune_ms[i];
   return cpk_num_variants();
+}
+
+int cp_set_variant(cp_ctx* c, int32_t v) {
+  if (!c || v < -1 || v >= cpk_num_variants()) return fail(CP_ERR_ARG, "variant %d out of range", v);
+  std::lock_guard<std::mutex> lock(c->mu);
+  c->forced = v;
+  return CP_OK;
 }
 
 int cp_batch_profile(cp_ctx* c, double* graph_ms, int64_t* step_launches) {

@@ -314,6 +314,47 @@ DI int plane_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rs
   return n;
 }
 
+// ---- binary32 "no contact" certificates --------------------------------
+// Each test below returns true only when the pair certainly produces no
+// contact in the reference's binary64 arithmetic: it evaluates a necessary
+// condition for a contact in binary32 and demands a relative margin of
+// 1e-4 (the binary32 estimate is within ~1e-6 of the binary64 values), so the
+// exact resolver, which would return no contacts, can be skipped.
+
+DI f3 rot32(q4 q, f3 v) {  // binary32 rotation (approximate)
+  float ix = q.w * v.x + q.y * v.z - q.z * v.y;
+  float iy = q.w * v.y + q.z * v.x - q.x * v.z;
+  float iz = q.w * v.z + q.x * v.y - q.y * v.x;
+  float iw = -q.x * v.x - q.y * v.y - q.z * v.z;
+  return f3{ix * q.w - iw * q.x - iy * q.z + iz * q.y, iy * q.w - iw * q.y - iz * q.x + ix * q.z,
+            iz * q.w - iw * q.z - ix * q.y + iy * q.x};
+}
+DI float dot32(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+DI float len32(f3 a) { return sqrtf(dot32(a, a)); }
+
+// plane (xP, qP) vs a body whose shape lies within distance rB of xB: a
+// contact needs a point of the shape on or behind the plane
+// (spherePlane :797, planeConvex :1877)
+DI bool plane_far(f3 xP, q4 qP, f3 xB, float rB) {
+  f3 n = rot32(qP, f3{0.f, 0.f, 1.f});
+  f3 d = f3{xB.x - xP.x, xB.y - xP.y, xB.z - xP.z};
+  float h = dot32(n, d);
+  float margin = 1e-4f * (rB + fabsf(d.x) + fabsf(d.y) + fabsf(d.z)) + 1e-6f;
+  return h > rB + margin;
+}
+
+// sphere (center c, radius R) vs box: every contact sphereBox makes (side,
+// corner or edge, narrow_phase.dart:852-1034) has the sphere center closer
+// than R to the box
+DI bool sphere_box_far(f3 c, float R, f3 xB, q4 qB, const float* he) {
+  f3 d = f3{c.x - xB.x, c.y - xB.y, c.z - xB.z};
+  f3 p = rot32(q4{-qB.x, -qB.y, -qB.z, qB.w}, d);
+  float ox = fmaxf(fabsf(p.x) - he[0], 0.f), oy = fmaxf(fabsf(p.y) - he[1], 0.f), oz = fmaxf(fabsf(p.z) - he[2], 0.f);
+  float dist = sqrtf(ox * ox + oy * oy + oz * oz);
+  float margin = 1e-4f * (R + he[0] + he[1] + he[2] + fabsf(d.x) + fabsf(d.y) + fabsf(d.z)) + 1e-6f;
+  return dist > R + margin;
+}
+
 // Resolver choice of narrow_phase.dart:116-238,476-489,706-710.  The shape
 // with the lower ShapeType index goes first (for equal types the call is the
 // swapped one); (rsi, rsj) stay in getContacts order.

@@ -647,6 +647,10 @@ DI void narrow_pair(Smem& S, int k, bool heavy_pass) {
     int shA = swap ? bj.shape : bi.shape, shB = swap ? bi.shape : bj.shape;
     f3 xA = swap ? xj : xi, xB = swap ? xi : xj;
     q4 qA = swap ? qj : qi, qB = swap ? qi : qj;
+    // binary32 no-contact certificates (see cp_narrow.cuh)
+    if (rk == RK_SP && plane_far(xB, qB, xA, (float)W.shapes[shA].radius)) break;
+    if ((rk == RK_PB || rk == RK_PC) && plane_far(xA, qA, xB, (float)W.shapes[shB].bsr)) break;
+    if (rk == RK_SB && sphere_box_far(xA, (float)W.shapes[shA].radius, xB, qB, W.shapes[shB].he)) break;
     switch (rk) {
       case RK_SS: cnt = sphere_sphere(C, bA, bB, shA, shB, rsi, rsj, xA, xB, start); break;
       case RK_SP: cnt = sphere_plane(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qB, start); break;
@@ -1028,22 +1032,27 @@ DI void ph_rows_assemble(Smem& S, double h) {
 // dynamic body with it.  Bodies with zero solve mass and inertia
 // (static, sleeping, kinematic) keep vlambda = wlambda = +0 exactly, so they
 // order nothing.
-DI void ph_levels(Smem& S) {
+#define CP_SMEM_LEVEL_BODIES 2048
+
+DI void ph_levels(Smem& S, int* s_last) {
   const DWorld& W = S.W;
   const int nrows = S.n_rows;
   const int nb = S.P.nb;
-  for (int i = threadIdx.x; i < nb; i += BT) W.bscr[i].last_level = -1;
+  const bool smem = nb <= CP_SMEM_LEVEL_BODIES;
+  // last[b] = level of the latest row on dynamic body b, or -2 for bodies with
+  // zero solve mass and inertia (they order nothing)
+  int* last = smem ? s_last : W.level_cursor;
+  for (int i = threadIdx.x; i < nb; i += BT) last[i] = W.bscr[i].active ? -1 : -2;
   __syncthreads();
   if (threadIdx.x == 0) {
     int nl = 0;
     for (int r = 0; r < nrows; r++) {
       int a = W.rows[r].bi, b = W.rows[r].bj;
-      int aa = W.bscr[a].active, ba = W.bscr[b].active;
-      int la = aa ? W.bscr[a].last_level : -1;
-      int lb = ba ? W.bscr[b].last_level : -1;
+      int la = last[a], lb = last[b];
       int l = (la > lb ? la : lb) + 1;
-      if (aa) W.bscr[a].last_level = l;
-      if (ba) W.bscr[b].last_level = l;
+      if (l < 0) l = 0;
+      if (la != -2) last[a] = l;
+      if (lb != -2) last[b] = l;
       W.level_of[r] = l;
       if (l + 1 > nl) nl = l + 1;
     }
@@ -1068,7 +1077,12 @@ DI double gs_row(const DWorld& W, DRow& R) {
   DBodyScr& A = W.bscr[R.bi];
   DBodyScr& B = W.bscr[R.bj];
   d3 vla = ldd3(A.vl), wla = ldd3(A.wl), vlb = ldd3(B.vl), wlb = ldd3(B.wl);
-  double gwl = (ddot(vla, ldd3(R.gaS)) + ddot(wla, ldd3(R.gaR))) + (ddot(vlb, ldd3(R.gbS)) + ddot(wlb, ldd3(R.gbR)));
+  // A body with zero solve mass and inertia keeps vlambda = wlambda = +0, so
+  // its half of G*Wlambda is a signed zero and adding it changes no nonzero
+  // sum; a zero sum can only change sign, which no later store observes.
+  double ga = A.active ? ddot(vla, ldd3(R.gaS)) + ddot(wla, ldd3(R.gaR)) : 0.0;
+  double gb = B.active ? ddot(vlb, ldd3(R.gbS)) + ddot(wlb, ldd3(R.gbR)) : 0.0;
+  double gwl = A.active && B.active ? ga + gb : (A.active ? ga : gb);
   double lj = R.lambda;
   double dl = R.invC * (R.B - gwl - R.eps * lj);
   if (lj + dl < R.minF) dl = R.minF - lj;
@@ -1226,7 +1240,7 @@ DI void tick(Smem& S, int phase) {
   }
 }
 
-DI void step_world(Smem& S, double dt) {
+DI void step_world(Smem& S, int* s_last, double dt) {
   if (threadIdx.x == 0) {
     S.overflow = 0;
     S.n_pairs = S.n_contacts = S.n_rows = S.n_levels = 0;
@@ -1254,7 +1268,7 @@ DI void step_world(Smem& S, double dt) {
   ph_rows_assemble(S, dt);
   tick(S, 4);
   if (S.n_rows > 0) {
-    ph_levels(S);
+    ph_levels(S, s_last);
     tick(S, 5);
     ph_solve(S, dt);
     tick(S, 6);
@@ -1271,6 +1285,7 @@ template <int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_step_worlds(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n,
                                                               double dt, int* __restrict__ queue) {
   __shared__ Smem S;
+  __shared__ int s_last[CP_SMEM_LEVEL_BODIES];
   if (threadIdx.x < CP_NUM_PHASES) S.t_acc[threadIdx.x] = 0;
   for (;;) {
     if (threadIdx.x == 0) S.wi = atomicAdd(queue, 1);
@@ -1283,7 +1298,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step_worlds(const DWorld* __r
     }
     __syncthreads();
     if (S.P.status == 0) {
-      step_world(S, dt);
+      step_world(S, s_last, dt);
       if (threadIdx.x == 0) {
         DWorldParams* gp = S.W.P;
         gp->num_pairs = S.n_pairs;

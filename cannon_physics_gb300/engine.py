@@ -54,6 +54,7 @@ def lib():
         L.cp_batch_profile.argtypes = [vp, vp, vp]
         L.cp_phase_profile.argtypes = [vp, vp, i32]
         L.cp_autotune_info.argtypes = [vp, vp, vp, vp, i32]
+        L.cp_set_variant.argtypes = [vp, i32]
         _lib = L
     return _lib
 
@@ -109,6 +110,10 @@ class Context:
         ms = np.zeros(16)
         n = lib().cp_autotune_info(self.h, C.byref(v), C.byref(t), ms.ctypes.data, 16)
         return {"variant": v.value, "threads": t.value, "ms_per_variant": ms[:n].round(3).tolist()}
+
+    def set_variant(self, v):
+        """Pin the batched kernel variant, or -1 to autotune."""
+        check(lib().cp_set_variant(self.h, v), "cp_set_variant")
 
     def batch_profile(self):
         """(device ms, step launches) of batched graphs since the last call."""

@@ -195,7 +195,8 @@ typedef struct cp_step_info {
   double time;
   int32_t num_pairs, num_contacts, num_rows, iterations;
   int32_t status, num_bodies;
-  double profile_ms[4];             /* broadphase+narrowphase, rows, solve, integrate (plain path only) */
+  int32_t num_levels;               /* dependency levels of the last solve (rows of a level share no dynamic body) */
+  int32_t pad;
 } cp_step_info;
 
 typedef struct cp_config {
@@ -287,6 +288,10 @@ int cp_get_stream(cp_ctx* ctx, void** stream);
  * the fastest.  Writes the chosen variant (-1 while tuning), its block size
  * and up to n per-variant ms/step; returns the number of variants. */
 int cp_autotune_info(cp_ctx* ctx, int32_t* variant, int32_t* threads, double* ms, int32_t n);
+
+/* Pin the batched kernel variant (0 .. number of variants - 1), or -1 to
+ * return to autotuning. */
+int cp_set_variant(cp_ctx* ctx, int32_t variant);
 
 /* The World.profile breakdown (world_class.dart:27-41) of every step since
  * the previous call, as SM cycles summed over thread blocks, in 8 slots:

@@ -123,6 +123,26 @@ def test_batched_equals_plain_and_oracle(ctx):
         w.destroy()
 
 
+def test_every_kernel_variant_gives_the_same_bits(ctx):
+    """The autotuner may switch kernel variants between steps: every variant
+    (block size, register budget) must produce identical state."""
+    scs = [scenes.column_world(int(n), 4000 + i, "sphere_box") for i, n in enumerate(scenes.batch_sizes(24, 6000))]
+    for s in scs:
+        engine.setup_scene(s)
+    results = []
+    nvar = ctx.autotune_info()["ms_per_variant"]
+    count = len(nvar) if nvar else 5
+    for v in range(count):
+        ws = [ctx.world(s) for s in scs]
+        ctx.set_variant(v)
+        ctx.batch_step(ws, 1 / 60, 30)
+        results.append(b"".join(w.bodies().tobytes() for w in ws))
+        for w in ws:
+            w.destroy()
+    ctx.set_variant(-1)
+    assert all(r == results[0] for r in results[1:])
+
+
 def test_bad_arguments_raise(ctx):
     sc = engine.setup_scene(scenes.spheres_on_plane(4))
     w = ctx.world(sc)
