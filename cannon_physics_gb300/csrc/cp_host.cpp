@@ -23,10 +23,11 @@
 #include <vector>
 
 #include "../../include/cannon_gpu.h"
+#include "cp_internal.h"
 #include "cp_kernels.h"
 #include "cp_types.h"
 
-namespace {
+namespace cpi {
 
 thread_local std::string g_err;
 
@@ -39,6 +40,12 @@ int fail(int code, const char* fmt, ...) {
   g_err = buf;
   return code;
 }
+
+}  // namespace cpi
+
+using namespace cpi;
+
+namespace {
 
 #define CUDA_TRY(x)                                                                         \
   do {                                                                                      \
@@ -264,72 +271,7 @@ void shape_aabb(const cp_shape_desc& d, const Hull* h, const h3& pos, const hq& 
   }
 }
 
-// ---------------------------------------------------------------------------
-// device allocation layout
-
-struct Layout {
-  size_t off = 0;
-  size_t take(size_t bytes) {
-    size_t o = (off + 255) & ~(size_t)255;
-    off = o + bytes;
-    return o;
-  }
-};
-
-struct WorldRec {
-  bool live = false;
-  char* state = nullptr;   // device: params, bodies, shapes, hulls, materials, constraints, sap order, damping
-  char* scratch = nullptr; // device: per-step lists
-  DWorld dw{};
-  int nb = 0, nshapes = 0, nmat = 0, ncm = 0, ncons = 0, ncon_rows = 0;
-  int broadphase = 0, nbins = 0;
-  int pairs_cap = 0, contacts_cap = 0, rows_cap = 0, bins_cap = 0;
-  double dt_cached = -1.0;
-  std::vector<double> lin_damp, ang_damp;
-  std::vector<DContactMaterial> cms;  // host copy for SPOOK updates
-};
-
 }  // namespace
-
-struct cp_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::vector<WorldRec> worlds;
-  DWorld* d_worlds = nullptr;
-  int d_worlds_cap = 0;
-  int* d_ids = nullptr;
-  int d_ids_cap = 0;
-  int* d_queue = nullptr;
-  int* d_one = nullptr;  // world id of the plain path
-  long long* d_status = nullptr;
-  int d_status_cap = 0;
-  int sms = 0;
-  std::vector<int> blocks_per_sm;  // per kernel variant
-  // autotuner: one timed step per kernel variant, then the fastest
-  std::vector<double> tune_ms;
-  int tune_next = 0;
-  int best = -1;
-  std::vector<int> tune_ids;
-  int forced = -1;
-  long long launches = 0;
-  std::mutex mu;
-  // batched host I/O
-  int* d_io_ids = nullptr;
-  long long* d_io_first = nullptr;
-  int io_cap = 0;
-  float* d_io = nullptr;
-  long long io_floats = 0;
-  std::vector<int> io_ids;  // ids whose offsets are on the device
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  double graph_ms = 0.0;
-  long long graph_step_launches = 0;
-  // batched-step graph cache
-  cudaGraphExec_t graph = nullptr;
-  std::vector<int> graph_ids;
-  double graph_dt = 0;
-  int graph_steps = 0;
-  int graph_variant = -1;
-};
 
 namespace {
 
@@ -356,9 +298,9 @@ int pow2_at_least(int v) {
   return p;
 }
 
-// (re)allocate the scratch of a world for its current capacities
-int alloc_scratch(WorldRec& w) {
-  if (w.scratch) { cudaFree(w.scratch); w.scratch = nullptr; }
+// Layout of a world's scratch for its current capacities; returns its size
+// and, when `base` is given, points the world's scratch arrays into it.
+size_t scratch_layout(WorldRec& w, char* base) {
   const int nb = w.nb, cc = w.contacts_cap, rc = w.rows_cap;
   const int pc = std::max(w.pairs_cap, nb);  // SAP also keeps one count per list position in the pair arrays
   const int cand_cap = 3 * cc + w.ncon_rows + 1;
@@ -389,10 +331,7 @@ int alloc_scratch(WorldRec& w) {
   size_t o_ba = L.take(sizeof(float) * (w.broadphase == CP_BROAD_GRID ? 3 * 4096 : 1));
   size_t o_hk = L.take(sizeof(long long) * hash_cap);
   size_t o_hw = L.take(sizeof(int) * hash_cap);
-  char* base = nullptr;
-  cudaError_t e = cudaMalloc(&base, L.off);
-  if (e != cudaSuccess) return fail(CP_ERR_OOM, "scratch allocation of %zu bytes failed: %s", L.off, cudaGetErrorString(e));
-  w.scratch = base;
+  if (!base) return L.off;
   DWorld& d = w.dw;
   d.bscr = (DBodyScr*)(base + o_bscr);
   d.sap_tmp = (int*)(base + o_tmp);
@@ -419,8 +358,40 @@ int alloc_scratch(WorldRec& w) {
   d.hkeys = (long long*)(base + o_hk);
   d.hvals = (int*)(base + o_hw);
   d.hash_cap = hash_cap;
+  return L.off;
+}
+
+// Device memory of a world: from the context's pool when it has one (stream
+// ordered on the context's stream), else cudaMalloc.
+int dev_alloc(cp_ctx* c, void** p, size_t bytes, const char* what) {
+  *p = nullptr;
+  cudaError_t e = c->pool ? cudaMallocFromPoolAsync(p, bytes, c->pool, c->stream) : cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(CP_ERR_OOM, "%s: allocation of %zu bytes failed: %s", what, bytes, cudaGetErrorString(e));
+  }
   return CP_OK;
 }
+
+void dev_free(cp_ctx* c, void* p, bool pooled) {
+  if (!p) return;
+  if (pooled) cudaFreeAsync(p, c->stream);
+  else cudaFree(p);
+}
+
+// (re)allocate the scratch of a world for its current capacities
+int alloc_scratch(cp_ctx* c, WorldRec& w) {
+  if (w.scratch) { dev_free(c, w.scratch, w.pooled); w.scratch = nullptr; }
+  w.scratch_bytes = scratch_layout(w, nullptr);
+  char* base = nullptr;
+  int st = dev_alloc(c, (void**)&base, w.scratch_bytes, "world scratch");
+  if (st) return st;
+  w.scratch = base;
+  scratch_layout(w, base);
+  return CP_OK;
+}
+
 
 void body_to_device(const cp_body_desc& s, DBody& b) {
   std::memset(&b, 0, sizeof(b));
@@ -535,7 +506,7 @@ int grow(cp_ctx* c, int id, int status) {
   if (status & ST_ROWS_OVERFLOW) w.rows_cap *= 2;
   if (status & ST_BINS_OVERFLOW) w.bins_cap *= 2;
   if (w.pairs_cap > (1 << 28) || w.contacts_cap > (1 << 28) || w.rows_cap > (1 << 28)) return fail(CP_ERR_CAPACITY, "capacity limit");
-  int st = alloc_scratch(w);
+  int st = alloc_scratch(c, w);
   if (st) return st;
   DWorldParams p;
   st = read_params(c, w, p);
@@ -556,10 +527,22 @@ int ensure_ids(cp_ctx* c, int n) {
     int cap = std::max(256, 2 * n);
     CUDA_TRY(cudaMalloc(&c->d_ids, sizeof(int) * cap));
     CUDA_TRY(cudaMalloc(&c->d_status, sizeof(long long) * 4 * cap));
+    if (c->d_gstart) cudaFree(c->d_gstart);
+    CUDA_TRY(cudaMalloc(&c->d_gstart, sizeof(int) * (cap + 1)));
     c->d_ids_cap = cap;
     c->d_status_cap = cap;
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   }
+  return CP_OK;
+}
+
+// Reports a failed index check of the solve kernel (the kernel skipped the
+// access) as an error of the call that launched it.
+int kernel_check() {
+  int chk[4];
+  CUDA_TRY(cpk_read_check(chk));
+  if (chk[0] != 0)
+    return fail(CP_ERR_CUDA, "solve kernel index check %d failed: world %d, index %d, bound %d", chk[0], chk[1], chk[2], chk[3]);
   return CP_OK;
 }
 
@@ -575,8 +558,9 @@ int plain_steps(cp_ctx* c, int id, double dt, int nsteps) {
   for (int guard = 0; guard < 64; guard++) {
     long long done = p.stepnumber;
     for (long long s = done; s < target; s++) {
-      CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_one, 1, dt, c->d_queue, 1, c->stream, w.nb > 512 ? 0 : 2));
-      c->launches += 2;
+      CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_one, c->d_one_group, 1, dt, c->d_queue, 1, 1, c->stream,
+                               w.nb > 512 ? 0 : c->plain_variant, 1));
+      c->launches += 3;
     }
     st = read_params(c, w, p);
     if (st) return st;
@@ -586,6 +570,8 @@ int plain_steps(cp_ctx* c, int id, double dt, int nsteps) {
     st = read_params(c, w, p);
     if (st) return st;
   }
+  st = kernel_check();
+  if (st) return st;
   if (p.status != 0 || p.stepnumber != target) return fail(CP_ERR_CAPACITY, "world %d could not complete its steps", id);
   return CP_OK;
 }
@@ -671,8 +657,13 @@ int cp_create(const cp_config* cfg, cp_ctx** out) {
   cp_ctx* c = new cp_ctx();
   c->device = dev;
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&c->d_queue, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_queue, 2 * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_one, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_one_group, 2 * sizeof(int));
+  if (e == cudaSuccess) {
+    int og[2] = {0, 1};
+    e = cudaMemcpy(c->d_one_group, og, sizeof(og), cudaMemcpyHostToDevice);
+  }
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
@@ -680,7 +671,12 @@ int cp_create(const cp_config* cfg, cp_ctx** out) {
     delete c;
     return fail(CP_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
   }
-  for (int v = 0; v < cpk_num_variants(); v++) c->blocks_per_sm.push_back(std::max(1, cpk_max_resident_blocks(v)));
+  for (int v = 0; v < cpk_num_variants(); v++) {
+    int bp = 0, bs = 0;
+    cpk_max_resident_blocks(v, &bp, &bs);
+    c->blocks_pre.push_back(std::max(1, bp));
+    c->blocks_solve.push_back(std::max(1, bs));
+  }
   *out = c;
   return CP_OK;
 }
@@ -690,14 +686,18 @@ int cp_destroy(cp_ctx* c) {
   cudaSetDevice(c->device);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   for (auto& w : c->worlds) {
-    if (w.state) cudaFree(w.state);
-    if (w.scratch) cudaFree(w.scratch);
+    if (w.state) dev_free(c, w.state, w.pooled);
+    if (w.scratch) dev_free(c, w.scratch, w.pooled);
   }
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->pool) cudaMemPoolDestroy(c->pool);
   if (c->d_worlds) cudaFree(c->d_worlds);
   if (c->d_ids) cudaFree(c->d_ids);
   if (c->d_status) cudaFree(c->d_status);
   if (c->d_queue) cudaFree(c->d_queue);
   if (c->d_one) cudaFree(c->d_one);
+  if (c->d_one_group) cudaFree(c->d_one_group);
+  if (c->d_gstart) cudaFree(c->d_gstart);
   if (c->d_io_ids) cudaFree(c->d_io_ids);
   if (c->d_io_first) cudaFree(c->d_io_first);
   if (c->d_io) cudaFree(c->d_io);
@@ -708,10 +708,12 @@ int cp_destroy(cp_ctx* c) {
   return CP_OK;
 }
 
-int cp_world_create(cp_ctx* c, const cp_world_desc* d, int32_t* world_id) {
-  if (!c || !d || !world_id) return fail(CP_ERR_ARG, "null argument");
-  std::lock_guard<std::mutex> lock(c->mu);
-  cudaSetDevice(c->device);
+}  // extern "C"
+
+namespace cpi {
+
+int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
+  if (!d) return fail(CP_ERR_ARG, "null world descriptor");
   if (d->num_bodies < 0 || d->num_shapes < 0 || d->num_materials < 0 || d->num_contact_materials < 0 || d->num_constraints < 0)
     return fail(CP_ERR_ARG, "negative count");
   if ((d->num_bodies && !d->bodies) || (d->num_shapes && !d->shapes) || (d->num_materials && !d->materials) ||
@@ -886,6 +888,7 @@ int cp_world_create(cp_ctx* c, const cp_world_desc* d, int32_t* world_id) {
   DWorldParams P;
   std::memset(&P, 0, sizeof(P));
   P.time = d->time; P.tolerance = d->solver_tolerance; P.dt_cached = -1; P.stepnumber = d->stepnumber;
+  P.step_limit = LLONG_MAX;
   for (int k = 0; k < 3; k++) {
     P.gravity[k] = d->gravity[k]; P.fgrav[k] = d->friction_gravity[k];
     P.grid_min[k] = d->grid_aabb_min[k]; P.grid_max[k] = d->grid_aabb_max[k];
@@ -956,45 +959,131 @@ int cp_world_create(cp_ctx* c, const cp_world_desc* d, int32_t* world_id) {
     if (order[i] < 0 || order[i] >= nb) return fail(CP_ERR_ARG, "sap_axis_list[%d] out of range", i);
   }
   if (nb) std::memcpy(&host[o_so], order.data(), sizeof(int) * nb);
-  cudaError_t e = cudaMalloc(&w.state, L.off);
-  if (e != cudaSuccess) return fail(CP_ERR_OOM, "world allocation of %zu bytes failed: %s", L.off, cudaGetErrorString(e));
-  e = cudaMemcpy(w.state, host.data(), L.off, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) { cudaFree(w.state); return fail(CP_ERR_CUDA, "world upload: %s", cudaGetErrorString(e)); }
+  w.state_bytes = L.off;
+  w.scratch_bytes = scratch_layout(w, nullptr);
+  out.off = StateOffsets{o_P, o_b, o_s, o_h, o_f, o_hv, o_he, o_hfi, o_hvd, o_hed, o_hcn, o_hc,
+                         o_m, o_ct, o_cm, o_cn, o_nc, o_dp, o_so};
+  out.w = std::move(w);
+  out.host = std::move(host);
+  return CP_OK;
+}
+
+int commit_world(cp_ctx* c, PreparedWorld& p, int* world_id) {
+  WorldRec& w = p.w;
+  const StateOffsets& o = p.off;
+  int st = dev_alloc(c, (void**)&w.state, w.state_bytes, "world state");
+  if (st) return st;
+  w.pooled = c->pool != nullptr;
+  cudaError_t e = cudaMemcpyAsync(w.state, p.host.data(), w.state_bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    dev_free(c, w.state, w.pooled);
+    return fail(CP_ERR_CUDA, "world upload: %s", cudaGetErrorString(e));
+  }
   char* base = w.state;
   DWorld& dw = w.dw;
   std::memset(&dw, 0, sizeof(dw));
-  dw.P = (DWorldParams*)(base + o_P);
-  dw.bodies = (DBody*)(base + o_b);
-  dw.shapes = (DShape*)(base + o_s);
-  dw.hulls = (DHull*)(base + o_h);
-  dw.faces = (DFace*)(base + o_f);
-  dw.hverts = (float*)(base + o_hv);
-  dw.hedges = (float*)(base + o_he);
+  dw.P = (DWorldParams*)(base + o.P);
+  dw.bodies = (DBody*)(base + o.bodies);
+  dw.shapes = (DShape*)(base + o.shapes);
+  dw.hulls = (DHull*)(base + o.hulls);
+  dw.faces = (DFace*)(base + o.faces);
+  dw.hverts = (float*)(base + o.hverts);
+  dw.hedges = (float*)(base + o.hedges);
   dw.haxes = nullptr;
-  dw.hfi = (int*)(base + o_hfi);
-  dw.hvd = (double*)(base + o_hvd);
-  dw.hed = (double*)(base + o_hed);
-  dw.hcanon = (int*)(base + o_hcn);
-  dw.hconn = (int*)(base + o_hc);
-  dw.mats = (DMaterial*)(base + o_m);
-  dw.cm_table = (int*)(base + o_ct);
-  dw.cms = (DContactMaterial*)(base + o_cm);
-  dw.cons = (DConstraint*)(base + o_cn);
-  dw.nocollide = (int*)(base + o_nc);
-  dw.dpow = (double*)(base + o_dp);
-  dw.sap_order = (int*)(base + o_so);
-  int st = alloc_scratch(w);
-  if (st) { cudaFree(w.state); return st; }
+  dw.hfi = (int*)(base + o.hfi);
+  dw.hvd = (double*)(base + o.hvd);
+  dw.hed = (double*)(base + o.hed);
+  dw.hcanon = (int*)(base + o.hcanon);
+  dw.hconn = (int*)(base + o.hconn);
+  dw.mats = (DMaterial*)(base + o.mats);
+  dw.cm_table = (int*)(base + o.cm_table);
+  dw.cms = (DContactMaterial*)(base + o.cms);
+  dw.cons = (DConstraint*)(base + o.cons);
+  dw.nocollide = (int*)(base + o.nocollide);
+  dw.dpow = (double*)(base + o.dpow);
+  dw.sap_order = (int*)(base + o.sap_order);
+  st = alloc_scratch(c, w);
+  if (st) { dev_free(c, w.state, w.pooled); w.state = nullptr; return st; }
   w.live = true;
   int id = -1;
   for (size_t i = 0; i < c->worlds.size(); i++)
     if (!c->worlds[i].live) { id = (int)i; break; }
   if (id < 0) { id = (int)c->worlds.size(); c->worlds.emplace_back(); }
   c->worlds[id] = std::move(w);
+  p.host.clear();
   st = upload_world_entry(c, id);
   if (st) return st;
   *world_id = id;
   return CP_OK;
+}
+
+int destroy_world(cp_ctx* c, int id) {
+  WorldRec& w = c->worlds[id];
+  if (!w.pooled) cudaStreamSynchronize(c->stream);
+  if (w.state) dev_free(c, w.state, w.pooled);
+  if (w.scratch) dev_free(c, w.scratch, w.pooled);
+  w = WorldRec();
+  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  return CP_OK;
+}
+
+int read_bodies(cp_ctx* c, int id, cp_body_desc* out) {
+  WorldRec& w = c->worlds[id];
+  if (w.nb == 0) return CP_OK;
+  std::vector<DBody> b(w.nb);
+  CUDA_TRY(cudaMemcpyAsync(b.data(), w.dw.bodies, sizeof(DBody) * w.nb, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < w.nb; i++) body_from_device(b[i], out[i]);
+  return CP_OK;
+}
+
+int read_info(cp_ctx* c, int id, cp_step_info* out) {
+  DWorldParams p;
+  int st = read_params(c, c->worlds[id], p);
+  if (st) return st;
+  std::memset(out, 0, sizeof(*out));
+  out->stepnumber = p.stepnumber;
+  out->time = p.time;
+  out->num_pairs = p.num_pairs;
+  out->num_contacts = p.num_contacts;
+  out->num_rows = p.num_rows;
+  out->iterations = p.last_iterations;
+  out->status = p.status;
+  out->num_bodies = p.nb;
+  out->num_levels = p.num_levels;
+  return CP_OK;
+}
+
+int enable_pool(cp_ctx* c) {
+  if (c->pool) return CP_OK;
+  cudaMemPoolProps props;
+  std::memset(&props, 0, sizeof(props));
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = c->device;
+  CUDA_TRY(cudaMemPoolCreate(&c->pool, &props));
+  // keep freed blocks for reuse instead of returning them at each synchronisation
+  unsigned long long keep = ~0ull;
+  CUDA_TRY(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  return CP_OK;
+}
+
+const char* last_error() { return g_err.c_str(); }
+
+}  // namespace cpi
+
+extern "C" {
+
+int cp_world_create(cp_ctx* c, const cp_world_desc* d, int32_t* world_id) {
+  if (!c || !d || !world_id) return fail(CP_ERR_ARG, "null argument");
+  PreparedWorld p;
+  int st = prepare_world(d, p);
+  if (st) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  return commit_world(c, p, world_id);
 }
 
 int cp_world_destroy(cp_ctx* c, int32_t id) {
@@ -1002,13 +1091,7 @@ int cp_world_destroy(cp_ctx* c, int32_t id) {
   if (st) return st;
   std::lock_guard<std::mutex> lock(c->mu);
   cudaSetDevice(c->device);
-  cudaStreamSynchronize(c->stream);
-  WorldRec& w = c->worlds[id];
-  if (w.state) cudaFree(w.state);
-  if (w.scratch) cudaFree(w.scratch);
-  w = WorldRec();
-  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
-  return CP_OK;
+  return destroy_world(c, id);
 }
 
 int cp_world_step(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
@@ -1026,12 +1109,7 @@ int cp_world_get_bodies(cp_ctx* c, int32_t id, cp_body_desc* out, int32_t n) {
   std::lock_guard<std::mutex> lock(c->mu);
   WorldRec& w = c->worlds[id];
   if ((!out && n > 0) || n != w.nb) return fail(CP_ERR_ARG, "expected %d bodies", w.nb);
-  if (w.nb == 0) return CP_OK;
-  std::vector<DBody> b(w.nb);
-  CUDA_TRY(cudaMemcpyAsync(b.data(), w.dw.bodies, sizeof(DBody) * w.nb, cudaMemcpyDeviceToHost, c->stream));
-  CUDA_TRY(cudaStreamSynchronize(c->stream));
-  for (int i = 0; i < w.nb; i++) body_from_device(b[i], out[i]);
-  return CP_OK;
+  return read_bodies(c, id, out);
 }
 
 int cp_world_set_bodies(cp_ctx* c, int32_t id, const cp_body_desc* in, int32_t n) {
@@ -1059,20 +1137,7 @@ int cp_world_get_info(cp_ctx* c, int32_t id, cp_step_info* out) {
   if (st) return st;
   if (!out) return fail(CP_ERR_ARG, "null out");
   std::lock_guard<std::mutex> lock(c->mu);
-  DWorldParams p;
-  st = read_params(c, c->worlds[id], p);
-  if (st) return st;
-  std::memset(out, 0, sizeof(*out));
-  out->stepnumber = p.stepnumber;
-  out->time = p.time;
-  out->num_pairs = p.num_pairs;
-  out->num_contacts = p.num_contacts;
-  out->num_rows = p.num_rows;
-  out->iterations = p.last_iterations;
-  out->status = p.status;
-  out->num_bodies = p.nb;
-  out->num_levels = p.num_levels;
-  return CP_OK;
+  return read_info(c, id, out);
 }
 
 int cp_world_get_pairs(cp_ctx* c, int32_t id, int32_t* p1, int32_t* p2, int32_t cap, int32_t* count) {
@@ -1147,11 +1212,11 @@ int cp_world_get_sap_order(cp_ctx* c, int32_t id, int32_t* out, int32_t n) {
   return CP_OK;
 }
 
-int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t nsteps) {
-  if (!c || (n > 0 && !ids) || n < 0 || nsteps < 0 || !(dt > 0)) return fail(CP_ERR_ARG, "bad arguments");
-  if (n == 0 || nsteps == 0) return CP_OK;
-  std::lock_guard<std::mutex> lock(c->mu);
-  cudaSetDevice(c->device);
+}  // extern "C"
+
+namespace cpi {
+
+int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool use_graph) {
   for (int i = 0; i < n; i++) {
     if (ids[i] < 0 || ids[i] >= (int)c->worlds.size() || !c->worlds[ids[i]].live) return fail(CP_ERR_ARG, "no world %d", ids[i]);
     int st = ensure_dt(c, c->worlds[ids[i]], dt);
@@ -1164,25 +1229,58 @@ int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t n
   if (st) return st;
   // autotuning: while variants are untimed for this world set, each call runs
   // its steps with the next untimed variant (results do not depend on it)
-  if (c->tune_ids != order) {
+  // A second tuning round once the worlds have settled into contact: early
+  // steps (bodies in free fall) favour other variants than contact-heavy ones.
+  if (use_graph && c->tune_ids != order) {
     c->tune_ids = order;
+    c->tune_calls = 0;
+  }
+  // A round times every pre-solve kernel variant with solve variant 0, then
+  // every solve variant with the fastest pre-solve variant.
+  const int npre = cpk_num_pre_variants(), nsol = cpk_num_solve_variants();
+  if (use_graph && (c->tune_calls == 0 || c->tune_calls == 48)) {
     c->tune_ms.assign(cpk_num_variants(), 0.0);
+    c->tune_plan.clear();
+    for (int p = 0; p < npre; p++) c->tune_plan.push_back(p * nsol);
     c->tune_next = 0;
     c->best = -1;
   }
-  const bool tuning = c->forced < 0 && c->best < 0;
-  const int variant = c->forced >= 0 ? c->forced : (tuning ? c->tune_next : c->best);
-  const int grid = std::max(1, std::min(n, c->sms * c->blocks_per_sm[variant]));
-  bool reuse = !tuning && c->graph && c->graph_ids == order && c->graph_dt == dt && c->graph_steps == nsteps &&
+  if (use_graph) c->tune_calls++;
+  // Without a graph (world sets that change from call to call) nothing is
+  // tuned: the forced variant, else the tuned one, else the plain default.
+  const bool tuning = use_graph && c->forced < 0 && c->best < 0;
+  const int variant = c->forced >= 0 ? c->forced : (tuning ? c->tune_plan[c->tune_next] : (c->best >= 0 ? c->best : c->plain_variant));
+  // groups of consecutive worlds (the order is by size) up to group_bodies
+  std::vector<int> gstart(1, 0);
+  {
+    int cnt = 0, bodies = 0;
+    for (int i = 0; i < n; i++) {
+      int nb = c->worlds[order[i]].nb;
+      if (cnt > 0 && (cnt == CP_GROUP_MAX_WORLDS || bodies + nb > c->group_bodies)) {
+        gstart.push_back(i);
+        cnt = 0;
+        bodies = 0;
+      }
+      cnt++;
+      bodies += nb;
+    }
+    gstart.push_back(n);
+  }
+  const int ngroups = (int)gstart.size() - 1;
+  const int grid_pre = std::max(1, std::min(n, c->sms * c->blocks_pre[variant]));
+  const int grid_solve = std::max(1, std::min(ngroups, c->sms * c->blocks_solve[variant]));
+  bool reuse = use_graph && !tuning && c->graph && c->graph_ids == order && c->graph_dt == dt && c->graph_steps == nsteps &&
                c->graph_variant == variant;
   CUDA_TRY(cudaMemcpyAsync(c->d_ids, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
-  if (!reuse && !tuning) {
+  CUDA_TRY(cudaMemcpyAsync(c->d_gstart, gstart.data(), sizeof(int) * gstart.size(), cudaMemcpyHostToDevice, c->stream));
+  if (use_graph && !reuse && !tuning) {
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     cudaGraph_t g;
     CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 0; s < nsteps; s++) {
-      cudaError_t e = cpk_launch_step(c->d_worlds, c->d_ids, n, dt, c->d_queue, grid, c->stream, variant);
+      cudaError_t e = cpk_launch_step(c->d_worlds, c->d_ids, c->d_gstart, ngroups, dt, c->d_queue, grid_pre, grid_solve, c->stream,
+                                      variant, n);
       if (e != cudaSuccess) {
         cudaStreamEndCapture(c->stream, &g);
         return fail(CP_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
@@ -1202,31 +1300,49 @@ int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t n
   std::vector<long long> before(4 * (size_t)n), after(4 * (size_t)n);
   CUDA_TRY(cudaMemcpyAsync(before.data(), c->d_status, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
-  if (tuning) {
-    for (int s = 0; s < nsteps; s++) CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_ids, n, dt, c->d_queue, grid, c->stream, variant));
+  if (tuning || !use_graph) {
+    for (int s = 0; s < nsteps; s++)
+      CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_ids, c->d_gstart, ngroups, dt, c->d_queue, grid_pre, grid_solve, c->stream,
+                               variant, n));
   } else {
     CUDA_TRY(cudaGraphLaunch(c->graph, c->stream));
   }
   CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
-  c->launches += 2LL * nsteps + 1;
+  c->launches += 3LL * nsteps + 1;
   CUDA_TRY(cpk_gather_status(c->d_worlds, c->d_ids, n, c->d_status, c->stream));
   CUDA_TRY(cudaMemcpyAsync(after.data(), c->d_status, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
+  st = kernel_check();
+  if (st) return st;
   float gms = 0.f;
   CUDA_TRY(cudaEventElapsedTime(&gms, c->ev0, c->ev1));
   c->graph_ms += gms;
   c->graph_step_launches += nsteps;
   if (tuning) {
     c->tune_ms[variant] = gms / nsteps;
-    if (++c->tune_next == cpk_num_variants()) {
-      c->best = (int)(std::min_element(c->tune_ms.begin(), c->tune_ms.end()) - c->tune_ms.begin());
+    if (++c->tune_next == (int)c->tune_plan.size()) {
+      auto fastest = [&]() {
+        int b = c->tune_plan[0];
+        for (int v : c->tune_plan)
+          if (c->tune_ms[v] < c->tune_ms[b]) b = v;
+        return b;
+      };
+      int b = fastest();
+      if ((int)c->tune_plan.size() == npre) {  // first half done: now the solve variants
+        c->tune_plan.clear();
+        for (int sv = 0; sv < nsol; sv++) c->tune_plan.push_back((b / nsol) * nsol + sv);
+        c->tune_next = 1;  // (b, solve 0) is timed already
+      } else {
+        c->best = b;
+      }
     }
   }
   c->launches += 1;
   for (int i = 0; i < n; i++) {
     if (after[4 * i] != 0) {  // overflowed part way: grow and finish on the plain path
       int id = order[i];
-      long long left = before[4 * i + 1] + nsteps - after[4 * i + 1];
+      const long long limit = c->worlds[id].step_limit;
+      long long left = std::min(before[4 * i + 1] + nsteps, limit) - after[4 * i + 1];
       st = grow(c, id, (int)after[4 * i]);
       if (st) return st;
       st = plain_steps(c, id, dt, (int)left);
@@ -1234,6 +1350,18 @@ int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t n
     }
   }
   return CP_OK;
+}
+
+}  // namespace cpi
+
+extern "C" {
+
+int cp_batch_step(cp_ctx* c, const int32_t* ids, int32_t n, double dt, int32_t nsteps) {
+  if (!c || (n > 0 && !ids) || n < 0 || nsteps < 0 || !(dt > 0)) return fail(CP_ERR_ARG, "bad arguments");
+  if (n == 0 || nsteps == 0) return CP_OK;
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  return step_worlds(c, ids, n, dt, nsteps, true);
 }
 
 }  // extern "C"
@@ -1320,9 +1448,17 @@ int cp_phase_profile(cp_ctx* c, double* cycles, int32_t n) {
   std::lock_guard<std::mutex> lock(c->mu);
   cudaSetDevice(c->device);
   CUDA_TRY(cudaStreamSynchronize(c->stream));
-  unsigned long long v[CP_NUM_PHASES];
+  unsigned long long v[CP_PROFILE_SLOTS];
   CUDA_TRY(cpk_phase_cycles(v, true));
-  for (int i = 0; i < CP_NUM_PHASES; i++) cycles[i] = (double)v[i];
+  for (int i = 0; i < n && i < CP_PROFILE_SLOTS; i++) cycles[i] = (double)v[i];
+  return CP_OK;
+}
+
+int cp_set_group_bodies(cp_ctx* c, int32_t bodies) {
+  if (!c || bodies < 0) return fail(CP_ERR_ARG, "bad group size");
+  std::lock_guard<std::mutex> lock(c->mu);
+  c->group_bodies = bodies;
+  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   return CP_OK;
 }
 

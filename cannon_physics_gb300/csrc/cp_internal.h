@@ -1,0 +1,131 @@
+// cp_internal.h -- host-side records shared by the C ABI (cp_host.cpp) and
+// the request server (cp_serve.cpp).  Not part of the public interface.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cannon_gpu.h"
+#include "cp_kernels.h"
+#include "cp_types.h"
+
+namespace cpi {
+
+// Sub-arrays of one device allocation, each 256-byte aligned.
+struct Layout {
+  size_t off = 0;
+  size_t take(size_t bytes) {
+    size_t o = (off + 255) & ~(size_t)255;
+    off = o + bytes;
+    return o;
+  }
+};
+
+struct WorldRec {
+  bool live = false;
+  char* state = nullptr;   // device: params, bodies, shapes, hulls, materials, constraints, sap order, damping
+  char* scratch = nullptr; // device: per-step lists
+  size_t state_bytes = 0, scratch_bytes = 0;
+  bool pooled = false;     // state and scratch come from the context's memory pool
+  DWorld dw{};
+  int nb = 0, nshapes = 0, nmat = 0, ncm = 0, ncons = 0, ncon_rows = 0;
+  int broadphase = 0, nbins = 0;
+  int pairs_cap = 0, contacts_cap = 0, rows_cap = 0, bins_cap = 0;
+  long long step_limit = LLONG_MAX;  // the kernels leave the world alone at this step number
+  double dt_cached = -1.0;
+  std::vector<double> lin_damp, ang_damp;
+  std::vector<DContactMaterial> cms;  // host copy for SPOOK updates
+};
+
+// Offsets of the state sub-arrays inside a world's state allocation.
+struct StateOffsets {
+  size_t P, bodies, shapes, hulls, faces, hverts, hedges, hfi, hvd, hed, hcanon, hconn;
+  size_t mats, cm_table, cms, cons, nocollide, dpow, sap_order;
+};
+
+// A world checked and laid out on the host, ready to be copied to the device:
+// everything cp_world_create does except the device work.
+struct PreparedWorld {
+  WorldRec w;
+  std::vector<char> host;  // image of the state allocation
+  StateOffsets off{};
+};
+
+// Records the message of a failing call for cp_last_error (thread-local)
+// and returns `code`.
+int fail(int code, const char* fmt, ...);
+const char* last_error();
+
+}  // namespace cpi
+
+struct cp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // When set, world allocations come from this stream-ordered pool (no
+  // device-wide synchronisation on allocate or free).
+  cudaMemPool_t pool = nullptr;
+  std::vector<cpi::WorldRec> worlds;
+  DWorld* d_worlds = nullptr;
+  int d_worlds_cap = 0;
+  int* d_ids = nullptr;
+  int d_ids_cap = 0;
+  int* d_queue = nullptr;
+  int* d_one = nullptr;  // world id of the plain path
+  int* d_one_group = nullptr;  // {0, 1}: the plain path's single group
+  int* d_gstart = nullptr;  // batched path: group boundaries into d_ids
+  int ngroups = 0;
+  int group_bodies = 640;   // a group gathers consecutive (similar-size) worlds up to this many bodies
+  int plain_variant = 2 * cpk_num_solve_variants();  // (pre 128x4, solve 128x4) for single small worlds
+  long long* d_status = nullptr;
+  int d_status_cap = 0;
+  int sms = 0;
+  std::vector<int> blocks_pre, blocks_solve;  // resident blocks per SM, per kernel variant
+  // autotuner: one timed step per kernel variant, then the fastest
+  std::vector<double> tune_ms;   // ms/step per (pre, solve) variant pair timed so far
+  std::vector<int> tune_plan;    // variant pairs still to time in this round
+  int tune_next = 0;
+  int best = -1;
+  std::vector<int> tune_ids;
+  long long tune_calls = 0;  // batched calls on this world set
+  int forced = -1;
+  long long launches = 0;
+  std::mutex mu;
+  // batched host I/O
+  int* d_io_ids = nullptr;
+  long long* d_io_first = nullptr;
+  int io_cap = 0;
+  float* d_io = nullptr;
+  long long io_floats = 0;
+  std::vector<int> io_ids;  // ids whose offsets are on the device
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double graph_ms = 0.0;
+  long long graph_step_launches = 0;
+  // batched-step graph cache
+  cudaGraphExec_t graph = nullptr;
+  std::vector<int> graph_ids;
+  double graph_dt = 0;
+  int graph_steps = 0;
+  int graph_variant = -1;
+};
+
+namespace cpi {
+
+// All of these expect the context's mutex to be held by the caller, except
+// prepare_world, which touches no context.
+int prepare_world(const cp_world_desc* d, PreparedWorld& out);
+int commit_world(cp_ctx* c, PreparedWorld& p, int* world_id);
+int destroy_world(cp_ctx* c, int id);
+// Steps a world set `nsteps` times; worlds stop at their step limit.  With
+// `use_graph` the launch sequence is captured and replayed while the set, dt
+// and step count repeat; without it the kernels are launched directly.
+int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool use_graph);
+int read_bodies(cp_ctx* c, int id, cp_body_desc* out);
+int read_info(cp_ctx* c, int id, cp_step_info* out);
+// Creates the context's memory pool (release threshold: never) if absent.
+int enable_pool(cp_ctx* c);
+
+}  // namespace cpi

@@ -5,14 +5,20 @@
 
 #include "cp_types.h"
 
+#define CP_GROUP_MAX_WORLDS 8
 // kernel variants (threads per block, min blocks per SM) the autotuner picks from
+// (pre-solve kernel, solve kernel) variant pairs, numbered 0 .. cpk_num_variants()-1
 int cpk_num_variants();
+int cpk_num_pre_variants();
+int cpk_num_solve_variants();
 int cpk_variant_threads(int variant);
-int cpk_max_resident_blocks(int variant);
-// One World.step for each of the n worlds ids[0..n) of the world table, by a
-// persistent grid of `grid` blocks pulling worlds from *d_queue.
-cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, int n, double dt, int* d_queue, int grid,
-                            cudaStream_t stream, int variant);
+void cpk_max_resident_blocks(int variant, int* pre, int* solve);
+// One World.step for the n worlds ids[0..n): the pre-solve kernel (one world
+// per block, grid_pre persistent blocks) then the solve kernel (groups of
+// worlds ids[gstart[g] .. gstart[g+1]), grid_solve persistent blocks); two
+// queue counters at d_queue.
+cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, const int* d_gstart, int ngroups, double dt, int* d_queue,
+                            int grid_pre, int grid_solve, cudaStream_t stream, int variant, int n);
 // status, stepnumber and counts of the listed worlds, gathered into out[4*i..]
 cudaError_t cpk_gather_status(const DWorld* d_worlds, const int* d_ids, int n, long long* d_out, cudaStream_t stream);
 // clear the status of the listed worlds
@@ -23,6 +29,12 @@ cudaError_t cpk_scatter_forces(const DWorld* d_worlds, const int* d_ids, const l
                                cudaStream_t stream);
 cudaError_t cpk_gather_poses(const DWorld* d_worlds, const int* d_ids, const long long* d_first, int n, float* d_out,
                              cudaStream_t stream);
-// per-phase cycles summed over blocks: prepare, broadphase, narrowphase,
-// rows+wake+solve prep, row assembly, levels, GS sweeps, apply+integrate
+// CP_PROFILE_SLOTS counters: per-phase cycles summed over blocks (prepare,
+// broadphase, narrowphase, rows+wake+solve prep, row assembly, levels, GS
+// sweeps, apply+integrate), then 16 per-resolver thread-cycle sums and 16
+// per-resolver call counts (slots 10..12: pairs settled by a binary32
+// no-contact certificate for sphere-plane, plane-hull, sphere-box)
 cudaError_t cpk_phase_cycles(unsigned long long* out, bool reset);
+// First failed index check of the solve kernel since the last read, as
+// {code, world id, index, bound} (code 0: none); clears it once read.
+cudaError_t cpk_read_check(int out[4]);

@@ -27,10 +27,15 @@
 // Per-phase SM cycles summed over blocks (World.profile's breakdown,
 // world_class.dart:27-41); read with cp_phase_profile.
 __device__ unsigned long long g_phase_cycles[CP_NUM_PHASES];
+// per narrowphase resolver kind: summed thread cycles and calls
+__device__ unsigned long long g_res_cycles[16];
+__device__ unsigned long long g_res_calls[16];
 
 struct __align__(16) Smem {
   long long t_last;
   long long t_acc[CP_NUM_PHASES];
+  unsigned long long r_cyc[16];
+  unsigned int r_cnt[16];
   DWorld W;
   DWorldParams P;
   int warp[32];
@@ -91,6 +96,8 @@ DI int block_scan_array(Smem& S, int* a, int n) {
       }
     carry += tot;
   }
+  // every caller reads elements written by other threads
+  __syncthreads();
   return carry;
 }
 
@@ -647,10 +654,15 @@ DI void narrow_pair(Smem& S, int k, bool heavy_pass) {
     int shA = swap ? bj.shape : bi.shape, shB = swap ? bi.shape : bj.shape;
     f3 xA = swap ? xj : xi, xB = swap ? xi : xj;
     q4 qA = swap ? qj : qi, qB = swap ? qi : qj;
+    const long long t_res = clock64();
     // binary32 no-contact certificates (see cp_narrow.cuh)
-    if (rk == RK_SP && plane_far(xB, qB, xA, (float)W.shapes[shA].radius)) break;
-    if ((rk == RK_PB || rk == RK_PC) && plane_far(xA, qA, xB, (float)W.shapes[shB].bsr)) break;
-    if (rk == RK_SB && sphere_box_far(xA, (float)W.shapes[shA].radius, xB, qB, W.shapes[shB].he)) break;
+    if ((rk == RK_SP && plane_far(xB, qB, xA, (float)W.shapes[shA].radius)) ||
+        ((rk == RK_PB || rk == RK_PC) && plane_far(xA, qA, xB, (float)W.shapes[shB].bsr)) ||
+        (rk == RK_SB && sphere_box_far(xA, (float)W.shapes[shA].radius, xB, qB, W.shapes[shB].he))) {
+      atomicAdd(&S.r_cyc[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], (unsigned long long)(clock64() - t_res));
+      atomicAdd(&S.r_cnt[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], 1u);
+      break;
+    }
     switch (rk) {
       case RK_SS: cnt = sphere_sphere(C, bA, bB, shA, shB, rsi, rsj, xA, xB, start); break;
       case RK_SP: cnt = sphere_plane(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qB, start); break;
@@ -662,6 +674,8 @@ DI void narrow_pair(Smem& S, int k, bool heavy_pass) {
       case RK_BC: cnt = convex_convex(C, bA, bB, shA, shB, shA, shB, xA, xB, qA, qB, start); break;
       default: cnt = convex_convex(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qA, qB, start); break;
     }
+    atomicAdd(&S.r_cyc[rk], (unsigned long long)(clock64() - t_res));
+    atomicAdd(&S.r_cnt[rk], 1u);
   } while (0);
   W.pair_cnt[k] = cnt;
   W.pair_tstart[k] = start;
@@ -1102,51 +1116,6 @@ DI double gs_row(const DWorld& W, DRow& R) {
   return dl > 0.0 ? dl : -dl;
 }
 
-DI void ph_solve(Smem& S, double h) {
-  const DWorld& W = S.W;
-  const int nrows = S.n_rows;
-  const int nl = S.n_levels;
-  const int maxIter = S.P.iterations;
-  const double tol2 = S.P.tolerance * S.P.tolerance;
-  int iter = 0;
-  for (iter = 0; iter != maxIter; iter++) {
-    double part = 0.0;
-    for (int l = 0; l < nl; l++) {
-      int e = W.level_start[l + 1];
-      for (int x = W.level_start[l] + threadIdx.x; x < e; x += BT) {
-        int r = W.level_rows[x];
-        double a = gs_row(W, W.rows[r]);
-        W.absdl[r] = a;
-        part += a;
-      }
-      __syncthreads();
-    }
-    // deltalambdaTot is the sum in row order.  The block sum has the same
-    // terms in another order; both are within 2(n-1)u of the exact sum
-    // (non-negative terms), so unless tol^2 falls inside that band the
-    // comparison is decided by the block sum; otherwise thread 0 adds the
-    // terms in row order.
-    double sp = block_sum(S, part);
-    if (threadIdx.x == 0) {
-      double band = 2.2 * (double)nrows * 1.1102230246251565e-16;
-      double hi = sp * (1.0 + band), lo = sp * (1.0 - band);
-      int conv;
-      if (hi * hi * (1.0 + 4.5e-16) < tol2) conv = 1;
-      else if (lo * lo * (1.0 - 4.5e-16) >= tol2 && lo >= 0.0) conv = 0;
-      else {
-        double t = 0.0;
-        for (int r = 0; r < nrows; r++) t += W.absdl[r];
-        conv = t * t < tol2;
-      }
-      S.converged = conv;
-    }
-    __syncthreads();
-    if (S.converged) break;
-  }
-  if (threadIdx.x == 0) S.P.last_iterations = iter;
-  __syncthreads();
-}
-
 // Add result to velocity; multipliers (gs_solver.dart:157-176)
 DI void ph_solve_apply(Smem& S, double h) {
   const DWorld& W = S.W;
@@ -1240,7 +1209,9 @@ DI void tick(Smem& S, int phase) {
   }
 }
 
-DI void step_world(Smem& S, int* s_last, double dt) {
+// Everything of World.internalStep up to the solver's sweeps; returns false
+// when a capacity overflow stopped the step before any body state changed.
+DI bool step_pre(Smem& S, int* s_last, double dt) {
   if (threadIdx.x == 0) {
     S.overflow = 0;
     S.n_pairs = S.n_contacts = S.n_rows = S.n_levels = 0;
@@ -1253,40 +1224,159 @@ DI void step_world(Smem& S, int* s_last, double dt) {
   if (S.P.broadphase == CP_BROAD_SAP) ph_broad_sap(S);
   else if (S.P.broadphase == CP_BROAD_GRID) ph_broad_grid(S);
   else ph_broad_naive(S);
-  if (S.overflow) return;
+  if (S.overflow) return false;
   if (S.P.n_nocollide > 0) ph_nocollide(S);
   tick(S, 1);
   ph_narrow(S);
   tick(S, 2);
-  if (S.overflow) return;
+  if (S.overflow) return false;
   ph_rows_list(S);
-  if (S.overflow) return;
+  if (S.overflow) return false;
   // ---- body state changes from here on ----
   ph_contacts_post(S);
   ph_solve_prep(S);
   tick(S, 3);
   ph_rows_assemble(S, dt);
   tick(S, 4);
-  if (S.n_rows > 0) {
-    ph_levels(S, s_last);
-    tick(S, 5);
-    ph_solve(S, dt);
-    tick(S, 6);
-    ph_solve_apply(S, dt);
-  } else if (threadIdx.x == 0) {
-    S.P.last_iterations = 0;
-  }
-  __syncthreads();
-  ph_integrate(S, dt);
-  tick(S, 7);
+  if (S.n_rows > 0) ph_levels(S, s_last);
+  tick(S, 5);
+  return true;
 }
 
+// A group of worlds in one block: the state one world keeps between its
+// pre-solve phases and its post-solve phases.
+#define CP_GROUP_MAX 8
+struct __align__(16) Slot {
+  DWorld W;
+  DWorldParams P;
+  int n_pairs, n_contacts, n_rows, n_levels;
+  int ok, done, iters, id;
+};
+
+// The solve kernel checks every index it derives from a world's level lists
+// before it uses it.  A failed check skips the access and records the first
+// failure here as {code, world id, index, bound}; the host reads and clears
+// it after each launch sequence and reports it as an error.
+__device__ int g_check[4];
+
+DI bool index_ok(int code, int world, int idx, int bound) {
+  if ((unsigned)idx < (unsigned)bound) return true;
+  if (atomicCAS(&g_check[0], 0, code) == 0) {
+    g_check[1] = world;
+    g_check[2] = idx;
+    g_check[3] = bound;
+  }
+  return false;
+}
+
+// GSSolver sweeps (gs_solver.dart:122-155) of all worlds of a group at once:
+// level l of every unfinished world runs between the same two barriers, so a
+// barrier waits for many independent rows instead of a few.  Each world keeps
+// its own iteration count and convergence test.
+DI void joint_solve(Smem& S, Slot* slots, int K) {
+  __shared__ double s_part[CP_GROUP_MAX][32];
+  __shared__ int s_conv[CP_GROUP_MAX];
+  for (int sweep = 0;; sweep++) {
+    int active = 0, Lmax = 0;
+    for (int k = 0; k < K; k++) {
+      const Slot& sl = slots[k];
+      if (sl.ok && !sl.done && sl.n_rows > 0) {
+        active |= 1 << k;
+        Lmax = max(Lmax, sl.n_levels);
+      }
+    }
+    if (!active) break;
+    double part[CP_GROUP_MAX];
+#pragma unroll
+    for (int k = 0; k < CP_GROUP_MAX; k++) part[k] = 0.0;
+    for (int l = 0; l < Lmax; l++) {
+      int base[CP_GROUP_MAX], cnt[CP_GROUP_MAX];
+      int total = 0;
+#pragma unroll
+      for (int k = 0; k < CP_GROUP_MAX; k++) {
+        cnt[k] = 0;
+        base[k] = 0;
+        if (k < K && (active >> k & 1) && l < slots[k].n_levels) {
+          const Slot& sl = slots[k];
+          int b = sl.W.level_start[l], e = sl.W.level_start[l + 1];
+          // a level is a non-empty sub-range of [0, n_rows)
+          if (index_ok(1, sl.id, b, sl.n_rows) && index_ok(2, sl.id, e - 1 - b, sl.n_rows - b)) {
+            base[k] = b;
+            cnt[k] = e - b;
+          }
+        }
+        total += cnt[k];
+      }
+      for (int x = threadIdx.x; x < total; x += BT) {
+        int k = 0, off = x;
+        while (k < K - 1 && off >= cnt[k]) { off -= cnt[k]; k++; }
+        const Slot& sl = slots[k];
+        const DWorld& W = sl.W;
+        if (!index_ok(3, sl.id, off, cnt[k])) continue;
+        int r = W.level_rows[base[k] + off];
+        if (!index_ok(4, sl.id, r, sl.n_rows)) continue;
+        DRow& R = W.rows[r];
+        if (!index_ok(5, sl.id, R.bi, sl.P.nb) || !index_ok(6, sl.id, R.bj, sl.P.nb)) continue;
+        double a = gs_row(W, R);
+        W.absdl[r] = a;
+#pragma unroll
+        for (int kk = 0; kk < CP_GROUP_MAX; kk++)
+          if (kk == k) part[kk] += a;
+      }
+      __syncthreads();
+    }
+    // per-world convergence: (sum of |dlambda| in row order)^2 < tol^2, with
+    // the order-free block sum deciding unless it lies within the rounding
+    // band of the threshold (then the ordered sum decides)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < CP_GROUP_MAX; k++) {
+      double v = part[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) s_part[k][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+      const int k = threadIdx.x;
+      Slot& sl = slots[k];
+      if (active >> k & 1) {
+        double sp = 0.0;
+        for (int w = 0; w < (int)NWARP; w++) sp += s_part[k][w];
+        const int nrows = sl.n_rows;
+        const double tol2 = sl.P.tolerance * sl.P.tolerance;
+        double band = 2.2 * (double)nrows * 1.1102230246251565e-16;
+        double hi = sp * (1.0 + band), lo = sp * (1.0 - band);
+        int conv;
+        if (hi * hi * (1.0 + 4.5e-16) < tol2) conv = 1;
+        else if (lo * lo * (1.0 - 4.5e-16) >= tol2 && lo >= 0.0) conv = 0;
+        else {
+          double t = 0.0;
+          for (int r = 0; r < nrows; r++) t += sl.W.absdl[r];
+          conv = t * t < tol2;
+        }
+        if (conv) {
+          sl.done = 1;
+          sl.iters = sweep;
+        } else if (sweep + 1 >= sl.P.iterations) {
+          sl.done = 1;
+          sl.iters = sl.P.iterations;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Kernel 1 of a step: one world per block, everything up to the solver's
+// sweeps (pairs, contacts, rows, levels).  Register-hungry (the resolvers).
 template <int THREADS, int MINB>
-__global__ void __launch_bounds__(THREADS, MINB) k_step_worlds(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n,
-                                                              double dt, int* __restrict__ queue) {
+__global__ void __launch_bounds__(THREADS, MINB) k_step_pre(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n,
+                                                           double dt, int* __restrict__ queue) {
   __shared__ Smem S;
   __shared__ int s_last[CP_SMEM_LEVEL_BODIES];
   if (threadIdx.x < CP_NUM_PHASES) S.t_acc[threadIdx.x] = 0;
+  if (threadIdx.x < 16) { S.r_cyc[threadIdx.x] = 0; S.r_cnt[threadIdx.x] = 0; }
   for (;;) {
     if (threadIdx.x == 0) S.wi = atomicAdd(queue, 1);
     __syncthreads();
@@ -1297,26 +1387,81 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step_worlds(const DWorld* __r
       S.P = *S.W.P;
     }
     __syncthreads();
-    if (S.P.status == 0) {
-      step_world(S, s_last, dt);
+    if (S.P.status == 0 && S.P.stepnumber < S.P.step_limit) {
+      bool ok = step_pre(S, s_last, dt);
       if (threadIdx.x == 0) {
         DWorldParams* gp = S.W.P;
         gp->num_pairs = S.n_pairs;
         gp->num_contacts = S.n_contacts;
-        gp->num_rows = S.n_rows;
-        gp->num_levels = S.n_levels;
-        if (S.overflow) {
-          gp->status = S.overflow;
-        } else {
-          gp->last_iterations = S.P.last_iterations;
-          gp->stepnumber = S.P.stepnumber + 1;
-          gp->time = S.P.time + dt;
-        }
+        gp->num_rows = ok ? S.n_rows : 0;
+        gp->num_levels = ok ? S.n_levels : 0;
+        if (!ok) gp->status = S.overflow;
       }
     }
     __syncthreads();
   }
   if (threadIdx.x < CP_NUM_PHASES) atomicAdd(&g_phase_cycles[threadIdx.x], (unsigned long long)S.t_acc[threadIdx.x]);
+  if (threadIdx.x < 16) {
+    atomicAdd(&g_res_cycles[threadIdx.x], S.r_cyc[threadIdx.x]);
+    atomicAdd(&g_res_calls[threadIdx.x], (unsigned long long)S.r_cnt[threadIdx.x]);
+  }
+}
+
+// Kernel 2 of a step: the solver sweeps, velocity update, integration and
+// sleep for groups of worlds (ids[gstart[g] .. gstart[g+1])).  The sweeps of a
+// group share barriers (joint_solve); this kernel needs few registers, so
+// many blocks share an SM and hide the binary64 latency of each other's rows.
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_step_solve(const DWorld* __restrict__ worlds, const int* __restrict__ ids,
+                                                             const int* __restrict__ gstart, int ngroups, double dt,
+                                                             int* __restrict__ queue) {
+  __shared__ Smem S;
+  __shared__ Slot slots[CP_GROUP_MAX];
+  if (threadIdx.x < CP_NUM_PHASES) S.t_acc[threadIdx.x] = 0;
+  for (;;) {
+    if (threadIdx.x == 0) S.wi = atomicAdd(queue, 1);
+    __syncthreads();
+    const int g = S.wi;
+    if (g >= ngroups) break;
+    const int k0 = gstart[g];
+    int K = gstart[g + 1] - k0;
+    if (!index_ok(7, -1, K - 1, CP_GROUP_MAX)) K = 0;
+    if (threadIdx.x < K) {
+      Slot& sl = slots[threadIdx.x];
+      sl.id = ids[k0 + threadIdx.x];
+      sl.W = worlds[sl.id];
+      sl.P = *sl.W.P;
+      sl.ok = sl.P.status == 0 && sl.P.stepnumber < sl.P.step_limit;
+      sl.n_rows = sl.ok ? sl.P.num_rows : 0;
+      sl.n_levels = sl.P.num_levels;
+      sl.done = 0;
+      sl.iters = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) S.t_last = clock64();
+    joint_solve(S, slots, K);
+    tick(S, 6);
+    for (int k = 0; k < K; k++) {
+      if (!slots[k].ok) continue;
+      if (threadIdx.x == 0) {
+        S.W = slots[k].W;
+        S.P = slots[k].P;
+        S.n_rows = slots[k].n_rows;
+      }
+      __syncthreads();
+      if (S.n_rows > 0) ph_solve_apply(S, dt);
+      ph_integrate(S, dt);
+      if (threadIdx.x == 0) {
+        DWorldParams* gp = S.W.P;
+        gp->last_iterations = slots[k].iters;
+        gp->stepnumber = S.P.stepnumber + 1;
+        gp->time = S.P.time + dt;
+      }
+      tick(S, 7);
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x == 6 || threadIdx.x == 7) atomicAdd(&g_phase_cycles[threadIdx.x], (unsigned long long)S.t_acc[threadIdx.x]);
 }
 
 __global__ void k_gather_status(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n, long long* out) {
@@ -1390,43 +1535,76 @@ cudaError_t cpk_gather_poses(const DWorld* d_worlds, const int* d_ids, const lon
 }
 
 
-cudaError_t cpk_phase_cycles(unsigned long long* out, bool reset) {
-  cudaError_t e = cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(unsigned long long) * CP_NUM_PHASES);
-  if (e == cudaSuccess && reset) {
-    unsigned long long z[CP_NUM_PHASES] = {0};
-    e = cudaMemcpyToSymbol(g_phase_cycles, z, sizeof(z));
+cudaError_t cpk_read_check(int out[4]) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_check, sizeof(int) * 4);
+  if (e == cudaSuccess && out[0] != 0) {
+    int z[4] = {0, 0, 0, 0};
+    e = cudaMemcpyToSymbol(g_check, z, sizeof(z));
   }
   return e;
 }
 
-// Kernel variants (block threads, minimum resident blocks per SM): the
-// register budget, and with it the number of blocks that hide each other's
-// barrier waits, differs between them.  All compute identical results.
-struct Variant {
+cudaError_t cpk_phase_cycles(unsigned long long* out, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(unsigned long long) * CP_NUM_PHASES);
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(out + CP_NUM_PHASES, g_res_cycles, sizeof(unsigned long long) * 16);
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(out + CP_NUM_PHASES + 16, g_res_calls, sizeof(unsigned long long) * 16);
+  if (e == cudaSuccess && reset) {
+    unsigned long long z[16] = {0};
+    e = cudaMemcpyToSymbol(g_phase_cycles, z, sizeof(unsigned long long) * CP_NUM_PHASES);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_res_cycles, z, sizeof(z));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_res_calls, z, sizeof(z));
+  }
+  return e;
+}
+
+// Kernel variants (block threads, minimum resident blocks per SM) for each
+// of the two kernels: the register budget, and with it the number of blocks
+// that hide each other's waits, differs between them.  All compute
+// identical results.
+struct PreVariant {
   void (*fn)(const DWorld*, const int*, int, double, int*);
   int threads;
   int minb;
 };
-static const Variant kVariants[] = {
-    {k_step_worlds<256, 1>, 256, 1}, {k_step_worlds<128, 2>, 128, 2}, {k_step_worlds<128, 4>, 128, 4},
-    {k_step_worlds<64, 8>, 64, 8},   {k_step_worlds<256, 2>, 256, 2},
+struct SolveVariant {
+  void (*fn)(const DWorld*, const int*, const int*, int, double, int*);
+  int threads;
+  int minb;
 };
+static const PreVariant kPre[] = {
+    {k_step_pre<256, 1>, 256, 1}, {k_step_pre<128, 2>, 128, 2}, {k_step_pre<128, 4>, 128, 4},
+    {k_step_pre<64, 8>, 64, 8},   {k_step_pre<256, 2>, 256, 2},
+};
+static const SolveVariant kSolve[] = {
+    {k_step_solve<128, 4>, 128, 4}, {k_step_solve<128, 8>, 128, 8}, {k_step_solve<256, 4>, 256, 4},
+};
+static const int kNumPre = sizeof(kPre) / sizeof(kPre[0]);
+static const int kNumSolve = sizeof(kSolve) / sizeof(kSolve[0]);
 
-int cpk_num_variants() { return (int)(sizeof(kVariants) / sizeof(kVariants[0])); }
+int cpk_num_variants() { return kNumPre * kNumSolve; }
+int cpk_num_pre_variants() { return kNumPre; }
+int cpk_num_solve_variants() { return kNumSolve; }
 
-int cpk_variant_threads(int v) { return kVariants[v].threads; }
+int cpk_variant_threads(int v) { return kPre[v / kNumSolve].threads; }
 
-cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, int n, double dt, int* d_queue, int grid,
-                            cudaStream_t stream, int variant) {
-  cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
+cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, const int* d_gstart, int ngroups, double dt, int* d_queue,
+                            int grid_pre, int grid_solve, cudaStream_t stream, int variant, int n) {
+  cudaError_t e = cudaMemsetAsync(d_queue, 0, 2 * sizeof(int), stream);
   if (e != cudaSuccess) return e;
-  const Variant& V = kVariants[variant];
-  V.fn<<<grid, V.threads, 0, stream>>>(d_worlds, d_ids, n, dt, d_queue);
+  const PreVariant& P = kPre[variant / kNumSolve];
+  const SolveVariant& V = kSolve[variant % kNumSolve];
+  P.fn<<<grid_pre, P.threads, 0, stream>>>(d_worlds, d_ids, n, dt, d_queue);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  V.fn<<<grid_solve, V.threads, 0, stream>>>(d_worlds, d_ids, d_gstart, ngroups, dt, d_queue + 1);
   return cudaGetLastError();
 }
 
-int cpk_max_resident_blocks(int variant) {
-  int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kVariants[variant].fn, kVariants[variant].threads, 0);
-  return nb;
+void cpk_max_resident_blocks(int variant, int* pre, int* solve) {
+  const PreVariant& P = kPre[variant / kNumSolve];
+  const SolveVariant& V = kSolve[variant % kNumSolve];
+  *pre = 0;
+  *solve = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(pre, P.fn, P.threads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(solve, V.fn, V.threads, 0);
 }

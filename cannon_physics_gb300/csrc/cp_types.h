@@ -17,6 +17,7 @@
 #define CP_MAX_CLIP 48
 #define CP_MAX_PAIR_CONTACTS 32
 #define CP_NUM_PHASES 8
+#define CP_PROFILE_SLOTS (CP_NUM_PHASES + 32)
 
 // body flags
 #define BF_ALLOW_SLEEP 1
@@ -149,6 +150,7 @@ struct __align__(16) DWorldParams {
   int pairs_cap, contacts_cap, rows_cap, bins_cap;
   int grid_plane_done, n_nocollide, pad[2];
   float grid_plane_n[4];
+  long long step_limit;  // the step kernels leave the world alone once stepnumber reaches this
 };
 
 struct DWorld {

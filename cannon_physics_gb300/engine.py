@@ -55,6 +55,7 @@ def lib():
         L.cp_phase_profile.argtypes = [vp, vp, i32]
         L.cp_autotune_info.argtypes = [vp, vp, vp, vp, i32]
         L.cp_set_variant.argtypes = [vp, i32]
+        L.cp_set_group_bodies.argtypes = [vp, i32]
         _lib = L
     return _lib
 
@@ -99,16 +100,27 @@ class Context:
 
     PHASES = ("prepare", "broadphase", "narrowphase", "rows_wake_prep", "assemble", "levels", "gs_sweeps", "integrate")
 
-    def phase_profile(self):
-        """SM cycles per step phase (summed over blocks) since the last call."""
-        out = np.zeros(len(self.PHASES), np.float64)
+    RESOLVERS = ("", "sphere_sphere", "sphere_plane", "sphere_box", "sphere_convex", "plane_box", "plane_convex", "box_box",
+                 "box_convex", "convex_convex", "cert_sphere_plane", "cert_plane_hull", "cert_sphere_box")
+
+    def phase_profile(self, resolvers=False):
+        """SM cycles per step phase (summed over blocks) since the last call;
+        with resolvers=True also {resolver: (thread cycles, calls)}."""
+        out = np.zeros(40, np.float64)
         check(lib().cp_phase_profile(self.h, out.ctypes.data, len(out)), "cp_phase_profile")
-        return dict(zip(self.PHASES, out.tolist()))
+        ph = dict(zip(self.PHASES, out[:8].tolist()))
+        if not resolvers:
+            return ph
+        res = {name: (out[8 + i], out[24 + i]) for i, name in enumerate(self.RESOLVERS) if name and out[24 + i] > 0}
+        return ph, res
+
+    def set_group_bodies(self, n):
+        check(lib().cp_set_group_bodies(self.h, n), "cp_set_group_bodies")
 
     def autotune_info(self):
         v, t = C.c_int32(), C.c_int32()
-        ms = np.zeros(16)
-        n = lib().cp_autotune_info(self.h, C.byref(v), C.byref(t), ms.ctypes.data, 16)
+        ms = np.zeros(64)
+        n = lib().cp_autotune_info(self.h, C.byref(v), C.byref(t), ms.ctypes.data, 64)
         return {"variant": v.value, "threads": t.value, "ms_per_variant": ms[:n].round(3).tolist()}
 
     def set_variant(self, v):

@@ -1,0 +1,433 @@
+// GpuWorld: a drop-in World whose internalStep runs on a GB300 through
+// libcannon_gpu.so.
+//
+// The scene is built with the reference's own API (World, Body, Sphere, Box,
+// Plane, ConvexPolyhedron, Cylinder, Material, ContactMaterial,
+// PointToPointConstraint, HingeConstraint, DistanceConstraint, GSSolver).
+// On the first step, and after markDirty(), the bodies, shapes, materials and
+// constraints are packed into a cp_world_desc and uploaded; every step after
+// that is one cp_world_step call followed by a write-back of the fields that
+// World.internalStep changes (lib/world/world_class.dart:433-701): position,
+// quaternion, velocity, angular velocity, previous pose, world inertia,
+// AABB, sleep state, time of the last sleepy state, forces (cleared).
+//
+// This file is written for a maintainer; it is not compiled in this
+// repository (no Dart or Flutter SDK is present).  The C side checks every
+// descriptor and returns a status; a failing status throws a StateError with
+// the library's message.
+import 'dart:ffi';
+
+import 'package:cannon_physics/cannon_physics.dart';
+import 'package:ffi/ffi.dart';
+
+import 'src/cannon_gpu_ffi.dart';
+
+class GpuWorld extends World {
+  GpuWorld({
+    super.gravity,
+    super.frictionGravity,
+    super.allowSleep,
+    super.broadphase,
+    super.solver,
+    super.quatNormalizeFast,
+    super.quatNormalizeSkip,
+    this.libraryPath = 'libcannon_gpu.so',
+    this.device = 0,
+  });
+
+  final String libraryPath;
+  final int device;
+
+  CannonGpu? _api;
+  Pointer<CpCtx> _ctx = nullptr;
+  int _worldId = -1;
+  bool _dirty = true;
+  Pointer<CpBodyDesc> _bodyBuf = nullptr;
+  int _bodyCap = 0;
+
+  /// Call after adding or removing bodies, shapes, materials or constraints,
+  /// or after changing a body field other than the ones a step writes.
+  void markDirty() => _dirty = true;
+
+  CannonGpu get _lib {
+    final api = _api ??= CannonGpu(DynamicLibrary.open(libraryPath));
+    if (_ctx == nullptr) {
+      if (api.abiVersion() != cpAbiVersion) {
+        throw StateError('libcannon_gpu ABI ${api.abiVersion()} != $cpAbiVersion');
+      }
+      final cfg = calloc<CpConfig>();
+      final out = calloc<Pointer<CpCtx>>();
+      try {
+        cfg.ref.device = device;
+        _check(api.create(cfg, out));
+        _ctx = out.value;
+      } finally {
+        calloc.free(cfg);
+        calloc.free(out);
+      }
+    }
+    return api;
+  }
+
+  void _check(int status) {
+    if (status != cpOk) throw StateError('cannon_gpu: ${_api!.errorText()}');
+  }
+
+  @override
+  void internalStep(double dt) {
+    final api = _lib;
+    if (_dirty) _upload(api);
+    // Body fields the app may have changed between steps (forces, velocities,
+    // kinematic poses) travel with every step.
+    _packBodies();
+    _check(api.worldSetBodies(_ctx, _worldId, _bodyBuf, bodies.length));
+    _check(api.worldStep(_ctx, _worldId, dt, 1));
+    _check(api.worldGetBodies(_ctx, _worldId, _bodyBuf, bodies.length));
+    _unpackBodies();
+    final info = calloc<CpStepInfo>();
+    try {
+      _check(api.worldGetInfo(_ctx, _worldId, info));
+      stepnumber = info.ref.stepnumber;
+      time = info.ref.time;
+    } finally {
+      calloc.free(info);
+    }
+    this.dt = dt;
+  }
+
+  /// Releases the device world and the context.
+  void dispose() {
+    final api = _api;
+    if (api == null) return;
+    if (_worldId >= 0) api.worldDestroy(_ctx, _worldId);
+    if (_ctx != nullptr) api.destroy(_ctx);
+    if (_bodyBuf != nullptr) calloc.free(_bodyBuf);
+    _worldId = -1;
+    _ctx = nullptr;
+    _bodyBuf = nullptr;
+  }
+
+  // ---------------------------------------------------------------- packing
+
+  static int _shapeType(Shape s) {
+    switch (s.type) {
+      case ShapeType.sphere:
+        return cpShapeSphere;
+      case ShapeType.plane:
+        return cpShapePlane;
+      case ShapeType.box:
+        return cpShapeBox;
+      case ShapeType.convex:
+        return cpShapeConvex;
+      case ShapeType.cylinder:
+        return cpShapeCylinder;
+      default:
+        throw UnsupportedError('GpuWorld: shape type ${s.type} is not on the GPU path');
+    }
+  }
+
+  void _ensureBodyBuf() {
+    if (_bodyCap >= bodies.length) return;
+    if (_bodyBuf != nullptr) calloc.free(_bodyBuf);
+    _bodyCap = bodies.length < 16 ? 16 : bodies.length;
+    _bodyBuf = calloc<CpBodyDesc>(_bodyCap);
+  }
+
+  void _upload(CannonGpu api) {
+    if (_worldId >= 0) {
+      _check(api.worldDestroy(_ctx, _worldId));
+      _worldId = -1;
+    }
+    if (narrowphase.enableFrictionReduction) {
+      throw UnsupportedError('GpuWorld: enableFrictionReduction is not on the GPU path');
+    }
+    final arena = Arena();
+    try {
+      // materials: every Material reachable from shapes, bodies and contact
+      // materials, in first-seen order
+      final mats = <Material>[];
+      int matIndex(Material? m) {
+        if (m == null) return -1;
+        final i = mats.indexOf(m);
+        if (i >= 0) return i;
+        mats.add(m);
+        return mats.length - 1;
+      }
+
+      final shapes = arena<CpShapeDesc>(bodies.isEmpty ? 1 : bodies.length);
+      final vertexBuffers = <Pointer<Float>>[];
+      _ensureBodyBuf();
+      for (var i = 0; i < bodies.length; i++) {
+        final b = bodies[i];
+        if (b.shapes.length != 1) {
+          throw UnsupportedError('GpuWorld: body $i has ${b.shapes.length} shapes; the GPU path takes one');
+        }
+        final s = b.shapes[0];
+        final d = shapes[i];
+        d.type = _shapeType(s);
+        d.collisionFilterGroup = s.collisionFilterGroup;
+        d.collisionFilterMask = s.collisionFilterMask;
+        d.collisionResponse = s.collisionResponse ? 1 : 0;
+        d.material = matIndex(s.material);
+        d.boundingSphereRadius = s.boundingSphereRadius;
+        if (s is Sphere) d.radius = s.radius;
+        if (s is Box) {
+          d.halfExtents[0] = s.halfExtents.x;
+          d.halfExtents[1] = s.halfExtents.y;
+          d.halfExtents[2] = s.halfExtents.z;
+        }
+        if (s is Cylinder) {
+          d.radiusTop = s.radiusTop;
+          d.radiusBottom = s.radiusBottom;
+          d.height = s.height;
+          d.numSegments = s.numSegments;
+        } else if (s is ConvexPolyhedron) {
+          final nv = s.vertices.length;
+          final verts = arena<Float>(3 * nv);
+          for (var k = 0; k < nv; k++) {
+            verts[3 * k] = s.vertices[k].x;
+            verts[3 * k + 1] = s.vertices[k].y;
+            verts[3 * k + 2] = s.vertices[k].z;
+          }
+          final nf = s.faces.length;
+          final sizes = arena<Int32>(nf);
+          var total = 0;
+          for (var f = 0; f < nf; f++) {
+            sizes[f] = s.faces[f].length;
+            total += s.faces[f].length;
+          }
+          final idx = arena<Int32>(total);
+          var o = 0;
+          for (final face in s.faces) {
+            for (final v in face) {
+              idx[o++] = v;
+            }
+          }
+          d.numVertices = nv;
+          d.numFaces = nf;
+          d.vertices = verts;
+          d.faceSizes = sizes;
+          d.faceIndices = idx;
+          final axes = s.uniqueAxes;
+          if (axes != null) {
+            final ax = arena<Float>(3 * axes.length);
+            for (var k = 0; k < axes.length; k++) {
+              ax[3 * k] = axes[k].x;
+              ax[3 * k + 1] = axes[k].y;
+              ax[3 * k + 2] = axes[k].z;
+            }
+            d.hasAxes = 1;
+            d.numAxes = axes.length;
+            d.axes = ax;
+          }
+          vertexBuffers.add(verts);
+        }
+        _check(api.shapeSetup(d));
+        matIndex(b.material);
+      }
+      _packBodies(materialIndex: matIndex);
+
+      final cmats = arena<CpContactMaterial>(contactmaterials.isEmpty ? 1 : contactmaterials.length);
+      for (var k = 0; k < contactmaterials.length; k++) {
+        final cm = contactmaterials[k];
+        _fillContactMaterial(cmats[k], cm, matIndex(cm.materials[0]), matIndex(cm.materials[1]));
+      }
+      final mtab = arena<CpMaterial>(mats.isEmpty ? 1 : mats.length);
+      for (var k = 0; k < mats.length; k++) {
+        mtab[k].friction = mats[k].friction;
+        mtab[k].restitution = mats[k].restitution;
+      }
+
+      final cons = arena<CpConstraintDesc>(constraints.isEmpty ? 1 : constraints.length);
+      for (var k = 0; k < constraints.length; k++) {
+        _fillConstraint(cons[k], constraints[k]);
+      }
+
+      final w = arena<CpWorldDesc>();
+      final r = w.ref;
+      r.numBodies = bodies.length;
+      r.numShapes = bodies.length;
+      r.numMaterials = mats.length;
+      r.numContactMaterials = contactmaterials.length;
+      r.numConstraints = constraints.length;
+      r.allowSleep = allowSleep ? 1 : 0;
+      r.quatNormalizeSkip = quatNormalizeSkip;
+      r.quatNormalizeFast = quatNormalizeFast ? 1 : 0;
+      r.solverIterations = solver.iterations;
+      r.solverTolerance = solver is GSSolver ? (solver as GSSolver).tolerance : 1e-7;
+      r.useBoundingBoxes = broadphase.useBoundingBoxes ? 1 : 0;
+      final bp = broadphase;
+      if (bp is SAPBroadphase) {
+        r.broadphase = cpBroadSap;
+        r.sapAxis = bp.axisIndex.index;
+      } else if (bp is GridBroadphase) {
+        r.broadphase = cpBroadGrid;
+        r.gridN[0] = bp.nx;
+        r.gridN[1] = bp.ny;
+        r.gridN[2] = bp.nz;
+        r.gridAabbMin[0] = bp.aabbMin.x;
+        r.gridAabbMin[1] = bp.aabbMin.y;
+        r.gridAabbMin[2] = bp.aabbMin.z;
+        r.gridAabbMax[0] = bp.aabbMax.x;
+        r.gridAabbMax[1] = bp.aabbMax.y;
+        r.gridAabbMax[2] = bp.aabbMax.z;
+      } else {
+        r.broadphase = cpBroadNaive;
+      }
+      r.stepnumber = stepnumber;
+      r.time = time;
+      r.gravity[0] = gravity.x;
+      r.gravity[1] = gravity.y;
+      r.gravity[2] = gravity.z;
+      final fg = frictionGravity;
+      if (fg != null) {
+        r.hasFrictionGravity = 1;
+        r.frictionGravity[0] = fg.x;
+        r.frictionGravity[1] = fg.y;
+        r.frictionGravity[2] = fg.z;
+      }
+      r.bodies = _bodyBuf;
+      r.shapes = shapes;
+      r.materials = mtab;
+      r.contactMaterials = cmats;
+      r.constraints = cons;
+      r.sapAxisList = nullptr;
+      _fillContactMaterial(r.defaultContactMaterial, defaultContactMaterial, -1, -1);
+
+      final id = arena<Int32>();
+      _check(api.worldCreate(_ctx, w, id));
+      _worldId = id.value;
+      _dirty = false;
+    } finally {
+      arena.releaseAll();
+    }
+  }
+
+  static void _fillContactMaterial(CpContactMaterial d, ContactMaterial cm, int a, int b) {
+    d.materialA = a;
+    d.materialB = b;
+    d.friction = cm.friction;
+    d.restitution = cm.restitution;
+    d.contactStiffness = cm.contactEquationStiffness;
+    d.contactRelaxation = cm.contactEquationRelaxation;
+    d.frictionStiffness = cm.frictionEquationStiffness;
+    d.frictionRelaxation = cm.frictionEquationRelaxation;
+  }
+
+  void _fillConstraint(CpConstraintDesc d, Constraint c) {
+    d.bodyA = bodies.indexOf(c.bodyA);
+    d.bodyB = bodies.indexOf(c.bodyB);
+    d.collideConnected = c.collideConnected ? 1 : 0;
+    final eq = c.equations.first;
+    d.spookStiffness = eq.stiffness;
+    d.spookRelaxation = eq.relaxation;
+    d.spookTimeStep = 1 / 60;
+    d.maxForce = eq.maxForce;
+    if (c is HingeConstraint) {
+      d.type = cpConHinge;
+      _set3(d.pivotA, c.pivotA);
+      _set3(d.pivotB, c.pivotB);
+      _set3(d.axisA, c.axisA);
+      _set3(d.axisB, c.axisB);
+      d.motorEnabled = c.motorEquation.enabled ? 1 : 0;
+      d.motorTargetVelocity = c.motorTargetVelocity ?? 0;
+      d.motorMaxForce = c.motorEquation.maxForce;
+    } else if (c is PointToPointConstraint) {
+      d.type = cpConPointToPoint;
+      _set3(d.pivotA, c.pivotA);
+      _set3(d.pivotB, c.pivotB);
+    } else if (c is DistanceConstraint) {
+      d.type = cpConDistance;
+      d.distance = c.distance;
+    } else {
+      throw UnsupportedError('GpuWorld: ${c.runtimeType} is not on the GPU path');
+    }
+  }
+
+  static void _set3(Array<Float> a, Vector3 v) {
+    a[0] = v.x;
+    a[1] = v.y;
+    a[2] = v.z;
+  }
+
+  void _packBodies({int Function(Material?)? materialIndex}) {
+    _ensureBodyBuf();
+    for (var i = 0; i < bodies.length; i++) {
+      final b = bodies[i];
+      final d = _bodyBuf[i];
+      _set3(d.position, b.position);
+      d.quaternion[0] = b.quaternion.x;
+      d.quaternion[1] = b.quaternion.y;
+      d.quaternion[2] = b.quaternion.z;
+      d.quaternion[3] = b.quaternion.w;
+      _set3(d.velocity, b.velocity);
+      _set3(d.angularVelocity, b.angularVelocity);
+      _set3(d.force, b.force);
+      _set3(d.torque, b.torque);
+      _set3(d.linearFactor, b.linearFactor);
+      _set3(d.angularFactor, b.angularFactor);
+      _set3(d.invInertia, b.invInertia);
+      for (var k = 0; k < 9; k++) {
+        d.invInertiaWorld[k] = b.invInertiaWorld.storage[k];
+      }
+      _set3(d.aabbLower, b.aabb.lowerBound);
+      _set3(d.aabbUpper, b.aabb.upperBound);
+      _set3(d.shapeOffset, b.shapeOffsets[0]);
+      final so = b.shapeOrientations[0];
+      d.shapeOrientation[0] = so.x;
+      d.shapeOrientation[1] = so.y;
+      d.shapeOrientation[2] = so.z;
+      d.shapeOrientation[3] = so.w;
+      _set3(d.previousPosition, b.previousPosition);
+      d.previousQuaternion[0] = b.previousQuaternion.x;
+      d.previousQuaternion[1] = b.previousQuaternion.y;
+      d.previousQuaternion[2] = b.previousQuaternion.z;
+      d.previousQuaternion[3] = b.previousQuaternion.w;
+      d.mass = b.mass;
+      d.invMass = b.invMass;
+      d.linearDamping = b.linearDamping;
+      d.angularDamping = b.angularDamping;
+      d.sleepSpeedLimit = b.sleepSpeedLimit;
+      d.sleepTimeLimit = b.sleepTimeLimit.toDouble();
+      d.timeLastSleepy = b.timeLastSleepy.toDouble();
+      d.boundingRadius = b.boundingRadius;
+      d.type = b.type.index;
+      d.sleepState = b.sleepState.index;
+      d.allowSleep = b.allowSleep ? 1 : 0;
+      d.wakeUpAfterNarrowphase = b.wakeUpAfterNarrowphase ? 1 : 0;
+      d.collisionFilterGroup = b.collisionFilterGroup;
+      d.collisionFilterMask = b.collisionFilterMask;
+      d.collisionResponse = b.collisionResponse ? 1 : 0;
+      d.isTrigger = b.isTrigger ? 1 : 0;
+      if (materialIndex != null) d.material = materialIndex(b.material);
+      d.shape = i;
+      d.fixedRotation = b.fixedRotation ? 1 : 0;
+      d.aabbNeedsUpdate = b.aabbNeedsUpdate ? 1 : 0;
+    }
+  }
+
+  void _unpackBodies() {
+    for (var i = 0; i < bodies.length; i++) {
+      final b = bodies[i];
+      final d = _bodyBuf[i];
+      b.position.setValues(d.position[0], d.position[1], d.position[2]);
+      b.quaternion.setValues(d.quaternion[0], d.quaternion[1], d.quaternion[2], d.quaternion[3]);
+      b.velocity.setValues(d.velocity[0], d.velocity[1], d.velocity[2]);
+      b.angularVelocity.setValues(d.angularVelocity[0], d.angularVelocity[1], d.angularVelocity[2]);
+      b.force.setZero();
+      b.torque.setZero();
+      b.previousPosition.setValues(d.previousPosition[0], d.previousPosition[1], d.previousPosition[2]);
+      b.previousQuaternion.setValues(
+          d.previousQuaternion[0], d.previousQuaternion[1], d.previousQuaternion[2], d.previousQuaternion[3]);
+      for (var k = 0; k < 9; k++) {
+        b.invInertiaWorld.storage[k] = d.invInertiaWorld[k];
+      }
+      b.aabb.lowerBound.setValues(d.aabbLower[0], d.aabbLower[1], d.aabbLower[2]);
+      b.aabb.upperBound.setValues(d.aabbUpper[0], d.aabbUpper[1], d.aabbUpper[2]);
+      b.aabbNeedsUpdate = d.aabbNeedsUpdate != 0;
+      b.sleepState = BodySleepStates.values[d.sleepState];
+      b.timeLastSleepy = d.timeLastSleepy;
+      b.wakeUpAfterNarrowphase = d.wakeUpAfterNarrowphase != 0;
+    }
+  }
+}

@@ -1,0 +1,223 @@
+// dart:ffi mirror of include/cannon_gpu.h.
+//
+// Struct layouts follow the C header field by field; the C side checks the
+// ABI version at load time (cp_abi_version).  Nothing here allocates device
+// memory: the library owns it, and every pointer passed in is read or written
+// only during the call.
+import 'dart:ffi';
+
+const int cpAbiVersion = 1;
+
+const int cpOk = 0;
+const int cpErrArg = 1;
+const int cpErrCapacity = 2;
+const int cpErrNonfinite = 3;
+const int cpErrTimeout = 4;
+const int cpErrOom = 5;
+const int cpErrCuda = 6;
+const int cpErrUnsupported = 7;
+
+const int cpShapeSphere = 0, cpShapePlane = 1, cpShapeBox = 2, cpShapeConvex = 3, cpShapeCylinder = 4;
+const int cpBroadNaive = 0, cpBroadSap = 1, cpBroadGrid = 2;
+const int cpConPointToPoint = 0, cpConHinge = 1, cpConDistance = 2;
+
+final class CpShapeDesc extends Struct {
+  @Int32() external int type;
+  @Int32() external int collisionFilterGroup;
+  @Int32() external int collisionFilterMask;
+  @Int32() external int collisionResponse;
+  @Int32() external int material;
+  @Int32() external int numSegments;
+  @Double() external double radius;
+  @Double() external double radiusTop;
+  @Double() external double radiusBottom;
+  @Double() external double height;
+  @Array(3) external Array<Float> halfExtents;
+  @Int32() external int numVertices;
+  @Int32() external int numFaces;
+  @Int32() external int numAxes;
+  @Int32() external int hasAxes;
+  external Pointer<Float> vertices;
+  external Pointer<Int32> faceSizes;
+  external Pointer<Int32> faceIndices;
+  external Pointer<Float> axes;
+  @Double() external double boundingSphereRadius;
+}
+
+final class CpBodyDesc extends Struct {
+  @Array(3) external Array<Float> position;
+  @Array(4) external Array<Float> quaternion;
+  @Array(3) external Array<Float> velocity;
+  @Array(3) external Array<Float> angularVelocity;
+  @Array(3) external Array<Float> force;
+  @Array(3) external Array<Float> torque;
+  @Array(3) external Array<Float> linearFactor;
+  @Array(3) external Array<Float> angularFactor;
+  @Array(3) external Array<Float> invInertia;
+  @Array(9) external Array<Float> invInertiaWorld;
+  @Array(3) external Array<Float> aabbLower;
+  @Array(3) external Array<Float> aabbUpper;
+  @Array(3) external Array<Float> shapeOffset;
+  @Array(4) external Array<Float> shapeOrientation;
+  @Array(3) external Array<Float> previousPosition;
+  @Array(4) external Array<Float> previousQuaternion;
+  @Double() external double mass;
+  @Double() external double invMass;
+  @Double() external double linearDamping;
+  @Double() external double angularDamping;
+  @Double() external double sleepSpeedLimit;
+  @Double() external double sleepTimeLimit;
+  @Double() external double timeLastSleepy;
+  @Double() external double boundingRadius;
+  @Int32() external int type;
+  @Int32() external int sleepState;
+  @Int32() external int allowSleep;
+  @Int32() external int wakeUpAfterNarrowphase;
+  @Int32() external int collisionFilterGroup;
+  @Int32() external int collisionFilterMask;
+  @Int32() external int collisionResponse;
+  @Int32() external int isTrigger;
+  @Int32() external int material;
+  @Int32() external int shape;
+  @Int32() external int fixedRotation;
+  @Int32() external int aabbNeedsUpdate;
+}
+
+final class CpMaterial extends Struct {
+  @Double() external double friction;
+  @Double() external double restitution;
+}
+
+final class CpContactMaterial extends Struct {
+  @Int32() external int materialA;
+  @Int32() external int materialB;
+  @Double() external double friction;
+  @Double() external double restitution;
+  @Double() external double contactStiffness;
+  @Double() external double contactRelaxation;
+  @Double() external double frictionStiffness;
+  @Double() external double frictionRelaxation;
+}
+
+final class CpConstraintDesc extends Struct {
+  @Int32() external int type;
+  @Int32() external int bodyA;
+  @Int32() external int bodyB;
+  @Int32() external int collideConnected;
+  @Int32() external int motorEnabled;
+  @Int32() external int pad0;
+  @Array(3) external Array<Float> pivotA;
+  @Array(3) external Array<Float> pivotB;
+  @Array(3) external Array<Float> axisA;
+  @Array(3) external Array<Float> axisB;
+  @Double() external double distance;
+  @Double() external double maxForce;
+  @Double() external double motorTargetVelocity;
+  @Double() external double motorMaxForce;
+  @Double() external double spookStiffness;
+  @Double() external double spookRelaxation;
+  @Double() external double spookTimeStep;
+}
+
+final class CpWorldDesc extends Struct {
+  @Int32() external int numBodies;
+  @Int32() external int numShapes;
+  @Int32() external int numMaterials;
+  @Int32() external int numContactMaterials;
+  @Int32() external int numConstraints;
+  @Int32() external int allowSleep;
+  @Int32() external int quatNormalizeSkip;
+  @Int32() external int quatNormalizeFast;
+  @Int32() external int solverIterations;
+  @Int32() external int broadphase;
+  @Int32() external int useBoundingBoxes;
+  @Int32() external int sapAxis;
+  @Array(3) external Array<Int32> gridN;
+  @Int32() external int enableFrictionReduction;
+  @Int32() external int hasFrictionGravity;
+  @Int32() external int stepnumber;
+  @Double() external double solverTolerance;
+  @Double() external double time;
+  @Array(3) external Array<Float> gravity;
+  @Array(3) external Array<Float> frictionGravity;
+  @Array(3) external Array<Float> gridAabbMin;
+  @Array(3) external Array<Float> gridAabbMax;
+  external Pointer<CpBodyDesc> bodies;
+  external Pointer<CpShapeDesc> shapes;
+  external Pointer<CpMaterial> materials;
+  external Pointer<CpContactMaterial> contactMaterials;
+  external Pointer<CpConstraintDesc> constraints;
+  external Pointer<Int32> sapAxisList;
+  external CpContactMaterial defaultContactMaterial;
+}
+
+final class CpStepInfo extends Struct {
+  @Int64() external int stepnumber;
+  @Double() external double time;
+  @Int32() external int numPairs;
+  @Int32() external int numContacts;
+  @Int32() external int numRows;
+  @Int32() external int iterations;
+  @Int32() external int status;
+  @Int32() external int numBodies;
+  @Int32() external int numLevels;
+  @Int32() external int pad;
+}
+
+final class CpConfig extends Struct {
+  @Int32() external int device;
+  @Int32() external int blockThreads;
+  @Int64() external int arenaBytes;
+}
+
+final class CpCtx extends Opaque {}
+
+/// The entry points of libcannon_gpu.so that the drop-in uses.
+class CannonGpu {
+  CannonGpu(DynamicLibrary lib)
+      : abiVersion = lib.lookupFunction<Int32 Function(), int Function()>('cp_abi_version'),
+        lastError = lib.lookupFunction<Pointer<Uint8> Function(), Pointer<Uint8> Function()>('cp_last_error'),
+        shapeSetup = lib.lookupFunction<Int32 Function(Pointer<CpShapeDesc>), int Function(Pointer<CpShapeDesc>)>(
+            'cp_shape_setup'),
+        bodySetup = lib.lookupFunction<
+            Int32 Function(Pointer<CpShapeDesc>, Int32, Pointer<CpBodyDesc>, Int32),
+            int Function(Pointer<CpShapeDesc>, int, Pointer<CpBodyDesc>, int)>('cp_body_setup'),
+        create = lib.lookupFunction<Int32 Function(Pointer<CpConfig>, Pointer<Pointer<CpCtx>>),
+            int Function(Pointer<CpConfig>, Pointer<Pointer<CpCtx>>)>('cp_create'),
+        destroy = lib.lookupFunction<Int32 Function(Pointer<CpCtx>), int Function(Pointer<CpCtx>)>('cp_destroy'),
+        worldCreate = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Pointer<CpWorldDesc>, Pointer<Int32>),
+            int Function(Pointer<CpCtx>, Pointer<CpWorldDesc>, Pointer<Int32>)>('cp_world_create'),
+        worldDestroy = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32), int Function(Pointer<CpCtx>, int)>(
+            'cp_world_destroy'),
+        worldStep = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Double, Int32),
+            int Function(Pointer<CpCtx>, int, double, int)>('cp_world_step'),
+        worldGetBodies = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Pointer<CpBodyDesc>, Int32),
+            int Function(Pointer<CpCtx>, int, Pointer<CpBodyDesc>, int)>('cp_world_get_bodies'),
+        worldSetBodies = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Pointer<CpBodyDesc>, Int32),
+            int Function(Pointer<CpCtx>, int, Pointer<CpBodyDesc>, int)>('cp_world_set_bodies'),
+        worldGetInfo = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Pointer<CpStepInfo>),
+            int Function(Pointer<CpCtx>, int, Pointer<CpStepInfo>)>('cp_world_get_info');
+
+  final int Function() abiVersion;
+  final Pointer<Uint8> Function() lastError;
+  final int Function(Pointer<CpShapeDesc>) shapeSetup;
+  final int Function(Pointer<CpShapeDesc>, int, Pointer<CpBodyDesc>, int) bodySetup;
+  final int Function(Pointer<CpConfig>, Pointer<Pointer<CpCtx>>) create;
+  final int Function(Pointer<CpCtx>) destroy;
+  final int Function(Pointer<CpCtx>, Pointer<CpWorldDesc>, Pointer<Int32>) worldCreate;
+  final int Function(Pointer<CpCtx>, int) worldDestroy;
+  final int Function(Pointer<CpCtx>, int, double, int) worldStep;
+  final int Function(Pointer<CpCtx>, int, Pointer<CpBodyDesc>, int) worldGetBodies;
+  final int Function(Pointer<CpCtx>, int, Pointer<CpBodyDesc>, int) worldSetBodies;
+  final int Function(Pointer<CpCtx>, int, Pointer<CpStepInfo>) worldGetInfo;
+
+  /// The thread-local message of the last failing call.
+  String errorText() {
+    final p = lastError();
+    final bytes = <int>[];
+    for (var i = 0; p[i] != 0; i++) {
+      bytes.add(p[i]);
+    }
+    return String.fromCharCodes(bytes);
+  }
+}

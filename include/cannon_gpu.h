@@ -297,8 +297,17 @@ int cp_set_variant(cp_ctx* ctx, int32_t variant);
  * the previous call, as SM cycles summed over thread blocks, in 8 slots:
  * prepare, broadphase, narrowphase, contact rows + wake-ups + solve set-up,
  * row assembly (computeB / computeC), solver levels, Gauss-Seidel sweeps,
- * velocity update + integrate + sleep.  Shares, not wall time. */
+ * velocity update + integrate + sleep.  Shares, not wall time.  With n >= 40
+ * it also writes 16 narrowphase-resolver thread-cycle sums and 16 call
+ * counts (resolver kinds: 1 sphere-sphere, 2 sphere-plane, 3 sphere-box,
+ * 4 sphere-convex, 5 plane-box, 6 plane-convex, 7 box-box, 8 box-convex,
+ * 9 convex-convex; 10-12 pairs settled by a binary32 no-contact test). */
 int cp_phase_profile(cp_ctx* ctx, double* cycles, int32_t n);
+
+/* Batched path: worlds are handed to thread blocks in groups of consecutive
+ * (similar-size) worlds holding up to `bodies` bodies (at most 8 worlds);
+ * the solver sweeps of a group share barriers.  0 = one world per group. */
+int cp_set_group_bodies(cp_ctx* ctx, int32_t bodies);
 
 /* Device time (CUDA events on the context stream) of the batched-step graph
  * launches since the previous call, and how many step launches they held. */

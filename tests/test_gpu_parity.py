@@ -123,6 +123,27 @@ def test_batched_equals_plain_and_oracle(ctx):
         w.destroy()
 
 
+def test_large_batch_equals_plain(ctx):
+    """2048 worlds of the batched workload, 70 steps in two calls (the second
+    replays the captured graph): a sample of worlds must match stepping each
+    alone.  At this size every block of the persistent kernels handles many
+    worlds in a row, which is where a missing barrier between phases shows."""
+    scs = scenes.batch_worlds(2048, 1000)
+    for s in scs:
+        engine.setup_scene(s)
+    ws = [ctx.world(s) for s in scs]
+    ctx.batch_step(ws, 1 / 60, 35)
+    ctx.batch_step(ws, 1 / 60, 35)
+    sample = list(range(0, 2048, 97)) + [2047]
+    for i in sample:
+        p = ctx.world(scs[i])
+        p.step(1 / 60, 70)
+        assert p.bodies().tobytes() == ws[i].bodies().tobytes(), scs[i].name
+        p.destroy()
+    for w in ws:
+        w.destroy()
+
+
 def test_every_kernel_variant_gives_the_same_bits(ctx):
     """The autotuner may switch kernel variants between steps: every variant
     (block size, register budget) must produce identical state."""
@@ -130,12 +151,12 @@ def test_every_kernel_variant_gives_the_same_bits(ctx):
     for s in scs:
         engine.setup_scene(s)
     results = []
-    nvar = ctx.autotune_info()["ms_per_variant"]
-    count = len(nvar) if nvar else 5
+    count = len(ctx.autotune_info()["ms_per_variant"])
+    assert count >= 8
     for v in range(count):
         ws = [ctx.world(s) for s in scs]
         ctx.set_variant(v)
-        ctx.batch_step(ws, 1 / 60, 30)
+        ctx.batch_step(ws, 1 / 60, 12)
         results.append(b"".join(w.bodies().tobytes() for w in ws))
         for w in ws:
             w.destroy()
