@@ -299,8 +299,8 @@ int pow2_at_least(int v) {
 }
 
 // Layout of a world's scratch for its current capacities; returns its size
-// and, when `base` is given, points the world's scratch arrays into it.
-size_t scratch_layout(WorldRec& w, char* base) {
+// and, when `base` is given, points the scratch arrays of `d` into it.
+size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   const int nb = w.nb, cc = w.contacts_cap, rc = w.rows_cap;
   const int pc = std::max(w.pairs_cap, nb);  // SAP also keeps one count per list position in the pair arrays
   const int cand_cap = 3 * cc + w.ncon_rows + 1;
@@ -332,7 +332,6 @@ size_t scratch_layout(WorldRec& w, char* base) {
   size_t o_hk = L.take(sizeof(long long) * hash_cap);
   size_t o_hw = L.take(sizeof(int) * hash_cap);
   if (!base) return L.off;
-  DWorld& d = w.dw;
   d.bscr = (DBodyScr*)(base + o_bscr);
   d.sap_tmp = (int*)(base + o_tmp);
   d.pair_a = (int*)(base + o_pa);
@@ -360,6 +359,8 @@ size_t scratch_layout(WorldRec& w, char* base) {
   d.hash_cap = hash_cap;
   return L.off;
 }
+
+size_t scratch_layout(WorldRec& w, char* base) { return scratch_layout_into(w, w.dw, base); }
 
 // Device memory of a world: from the context's pool when it has one (stream
 // ordered on the context's stream), else cudaMalloc.
@@ -1101,6 +1102,91 @@ int cp_world_step(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
   std::lock_guard<std::mutex> lock(c->mu);
   cudaSetDevice(c->device);
   return plain_steps(c, id, dt, nsteps);
+}
+
+}  // extern "C"
+
+namespace {
+
+// ensure_dt without a host allocation: the damping powers go up in chunks
+// through a stack buffer (each chunk copy is synchronous, so the buffer can
+// be reused), and the contact materials are updated in place.
+int ensure_dt_static(cp_ctx* c, WorldRec& w, double dt) {
+  if (w.dt_cached == dt) return CP_OK;
+  double buf[512];
+  for (int i0 = 0; i0 < w.nb; i0 += 256) {
+    const int n = std::min(256, w.nb - i0);
+    for (int i = 0; i < n; i++) {
+      buf[2 * i] = std::pow(1.0 - w.lin_damp[i0 + i], dt);
+      buf[2 * i + 1] = std::pow(1.0 - w.ang_damp[i0 + i], dt);
+    }
+    CUDA_TRY(cudaMemcpyAsync(w.dw.dpow + 2 * i0, buf, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+  }
+  for (auto& m : w.cms) {
+    spook(m.cs, m.cr, dt, m.ca, m.cb, m.ceps);
+    spook(m.fs, m.fr, dt, m.fa, m.fb, m.feps);
+  }
+  CUDA_TRY(cudaMemcpyAsync(w.dw.cms, w.cms.data(), sizeof(DContactMaterial) * w.cms.size(), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  w.dt_cached = dt;
+  return CP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Steps a world with the static step scratch of cp_step.cu in place of the
+// world's own scratch.  The static array holds, from its start: a one-entry
+// world table (this world's descriptor with its scratch pointers moved into
+// the array), the work list {0} and group bounds {0, 1}, then the scratch.
+int cp_world_step_static(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
+  int st = check_world(c, id);
+  if (st) return st;
+  if (nsteps < 0 || !(dt > 0)) return fail(CP_ERR_ARG, "need dt > 0 and nsteps >= 0");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  CUDA_TRY(cpk_static_scratch(c->device, &arena, &arena_bytes));
+  WorldRec& w = c->worlds[id];
+  Layout L;
+  const size_t o_rec = L.take(sizeof(DWorld));
+  const size_t o_ids = L.take(3 * sizeof(int));
+  const size_t o_scr = L.take(0);
+  DWorld dw = w.dw;
+  const size_t need = o_scr + scratch_layout_into(w, dw, nullptr);
+  if (need > arena_bytes)
+    return fail(CP_ERR_CAPACITY, "world %d needs %zu bytes of step scratch; the static scratch holds %zu (use cp_world_step)",
+                id, need, arena_bytes);
+  if (nsteps == 0) return CP_OK;
+  char* base = (char*)arena;
+  scratch_layout_into(w, dw, base + o_scr);
+  const int hdr[3] = {0, 0, 1};  // work list {world 0}, group bounds {0, 1}
+  st = ensure_dt_static(c, w, dt);
+  if (st) return st;
+  CUDA_TRY(cudaMemcpyAsync(base + o_rec, &dw, sizeof(DWorld), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(base + o_ids, hdr, sizeof(hdr), cudaMemcpyHostToDevice, c->stream));
+  const DWorld* d_world = (const DWorld*)(base + o_rec);
+  const int* d_list = (const int*)(base + o_ids);
+  const int variant = w.nb > 512 ? 0 : c->plain_variant;
+  for (int s = 0; s < nsteps; s++) {
+    CUDA_TRY(cpk_launch_step(d_world, d_list, d_list + 1, 1, dt, c->d_queue, 1, 1, c->stream, variant, 1));
+    c->launches += 3;
+  }
+  DWorldParams p;
+  st = read_params(c, w, p);  // synchronises the stream: the host buffers above are no longer in use
+  if (st) return st;
+  st = kernel_check();
+  if (st) return st;
+  if (p.status != 0) {
+    const int zero = 0;
+    CUDA_TRY(cudaMemcpy(&w.dw.P->status, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    return fail(CP_ERR_CAPACITY, "world %d: step %lld overflowed a capacity (status %d); the world is left before that step",
+                id, p.stepnumber + 1, p.status);
+  }
+  return CP_OK;
 }
 
 int cp_world_get_bodies(cp_ctx* c, int32_t id, cp_body_desc* out, int32_t n) {

@@ -35,6 +35,10 @@ cudaError_t cpk_gather_poses(const DWorld* d_worlds, const int* d_ids, const lon
 // per-resolver call counts (slots 10..12: pairs settled by a binary32
 // no-contact certificate for sphere-plane, plane-hull, sphere-box)
 cudaError_t cpk_phase_cycles(unsigned long long* out, bool reset);
+// Address and size of the static step scratch on `device`, which must be the
+// current device; the first call per device looks the address up.
+#define CP_MAX_DEVICES 64
+cudaError_t cpk_static_scratch(int device, void** ptr, size_t* bytes);
 // First failed index check of the solve kernel since the last read, as
 // {code, world id, index, bound} (code 0: none); clears it once read.
 cudaError_t cpk_read_check(int out[4]);

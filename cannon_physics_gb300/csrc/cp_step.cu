@@ -16,6 +16,8 @@
 // step then returns with a status bit set and the state untouched.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "cp_kernels.h"
 #include "cp_narrow.cuh"
 #include "cp_cc.cuh"
@@ -1534,6 +1536,37 @@ cudaError_t cpk_gather_poses(const DWorld* d_worlds, const int* d_ids, const lon
   return cudaGetLastError();
 }
 
+
+// ---------------------------------------------------------------------------
+// Static step scratch for cp_world_step_static: a file-scope device array, so
+// stepping through it needs no device allocation.  Its address is taken once
+// per device, with that device current, by the first cpk_static_scratch call.
+static __device__ __align__(256) unsigned char g_static_scratch[CP_STATIC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_static_mu;
+void* g_static_addr[CP_MAX_DEVICES] = {};
+}  // namespace
+
+cudaError_t cpk_static_scratch(int device, void** ptr, size_t* bytes) {
+  *ptr = nullptr;
+  *bytes = 0;
+  if (device < 0 || device >= CP_MAX_DEVICES) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_addr[device]) {
+    int cur = -1;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess) return e;
+    if (cur != device) return cudaErrorInvalidDevice;
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return e;
+    g_static_addr[device] = p;
+  }
+  *ptr = g_static_addr[device];
+  *bytes = sizeof(g_static_scratch);
+  return cudaSuccess;
+}
 
 cudaError_t cpk_read_check(int out[4]) {
   cudaError_t e = cudaMemcpyFromSymbol(out, g_check, sizeof(int) * 4);

@@ -240,6 +240,47 @@ int cp_world_destroy(cp_ctx* ctx, int32_t world_id);
  * (world_class.dart:392-399,433-701). */
 int cp_world_step(cp_ctx* ctx, int32_t world_id, double dt, int32_t nsteps);
 
+/* cp_world_step without any allocation.  It has no counterpart in the
+ * reference (Dart allocates as it pleases).
+ *
+ * Who needs it: callers that must not allocate device memory while they
+ * step.  One example is a frame loop with a hard deadline, where
+ * cudaMalloc / cudaFree can synchronise the whole device.  Another is a
+ * server whose device memory was fixed when a request was admitted.
+ * cp_world_step may allocate: when a step overflows the world's pair,
+ * contact or row capacity, it regrows the world's scratch and re-runs the
+ * step.
+ *
+ * What it does: it gives the same results as cp_world_step, bit for bit.
+ * The per-step lists (pairs, contacts, rows, levels, solver scratch) live
+ * in one file-scope device array of CP_STATIC_SCRATCH_BYTES (64 MiB), not
+ * in the world's own scratch.
+ *
+ * Limits:
+ *  - A world whose lists, at its current capacities, need more than that
+ *    array is rejected with CP_ERR_CAPACITY before anything runs.  This is
+ *    roughly 8 KB per body: a 4096-body world fits, 10,000 bodies do not.
+ *  - A step that overflows a capacity is not regrown.  The world's bodies
+ *    are left as they were at the start of that step (only their cached
+ *    AABBs may be refreshed), its status is cleared, and the call returns
+ *    CP_ERR_CAPACITY.  cp_world_step can then take that step and grow the
+ *    capacities.
+ *
+ * Set-up: the first call on a device takes the array's address with
+ * cudaGetSymbolAddress, with that device current.  Make that first call
+ * before any stream capture.
+ *
+ * Start state: nothing in the array needs to start at zero.  Every step
+ * writes each list before reading it.  The work-queue counters the kernels
+ * take work from are cleared before every step.
+ *
+ * Concurrency: every context on a device shares the one array.  Calls whose
+ * GPU work overlaps race on it; for example, calls on two contexts of one
+ * device, which run on different streams.  Calls on one context never
+ * overlap: they are serialised on its stream. */
+#define CP_STATIC_SCRATCH_BYTES (64u * 1024u * 1024u)
+int cp_world_step_static(cp_ctx* ctx, int32_t world_id, double dt, int32_t nsteps);
+
 /* Read back / overwrite body state (Body fields). */
 int cp_world_get_bodies(cp_ctx* ctx, int32_t world_id, cp_body_desc* out, int32_t n);
 int cp_world_set_bodies(cp_ctx* ctx, int32_t world_id, const cp_body_desc* in, int32_t n);
