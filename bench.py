@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=10)
     ap.add_argument("--cpu-sample", type=int, default=16, help="every k-th world goes into the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-rate", type=float, default=2000.0, help="served form: Poisson arrival rate, requests/s")
+    ap.add_argument("--serve-window", type=float, default=1.0, help="served form: seconds of arrivals")
+    ap.add_argument("--serve-tick", type=int, default=4, help="served form: steps per tick")
+    ap.add_argument("--no-serve", action="store_true")
     return ap.parse_args()
 
 
@@ -164,6 +168,82 @@ def cpu_baseline(scenes_list, every, warmup, steps, threads=None):
     return {"value": bodies * steps / sec, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{len(sample)} of the worlds (every {every}th, {bodies} bodies), steps {warmup}..{warmup + steps - 1}, "
                       "one world per thread"}
+
+
+def run_served(args, device):
+    """The served form: Poisson arrivals of rollout requests (worlds of
+    floor(exp(U[ln 16, ln 4096])) bodies in the 40/40/20 sphere/box/cylinder
+    mix, horizons U{1..240}, dt 1/60) submitted on their arrival times to a
+    continuous-batching server with a 150 GB HBM budget.  Latency is
+    submission to result ready; throughput is completed body-steps over the
+    span from the first submission to the last completion."""
+    import threading
+    from cannon_physics_gb300 import engine, scenes
+    from cannon_physics_gb300 import serve as S
+    reqs = scenes.serve_requests(rate=args.serve_rate, window=args.serve_window, seed=77)
+    built = [engine.setup_scene(scenes.request_world(r)) for r in reqs]
+    srv = S.Server(device=device, hbm_budget=150e9, steps_per_tick=args.serve_tick)
+    warm = engine.setup_scene(scenes.request_world(scenes.Request(0.0, 64, 2, 5)))
+    t = srv.submit(warm, warm.dt, 2)
+    srv.wait(t)
+    srv.result(t)
+    srv.stats(reset=True)
+    tickets = [None] * len(reqs)
+    lag = [0.0]
+
+    def submitter():
+        t0 = time.perf_counter()
+        for i, (r, sc) in enumerate(zip(reqs, built)):
+            delay = t0 + r.arrival - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            else:
+                lag[0] = max(lag[0], -delay)
+            tickets[i] = srv.submit(sc, sc.dt, r.horizon)
+
+    clocks = Clocks(device)
+    clocks.start()
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    for t in tickets:
+        if srv.wait(t) != S.DONE:
+            raise RuntimeError(f"served request {t} did not complete")
+        srv.result(t)
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    offered = sum(sc.num_bodies * r.horizon for r, sc in zip(reqs, built))
+    # the plain per-request path: a sample of the same requests, each alone
+    # through cp_world_step
+    ctx = engine.Context(device=device)
+    sample = list(range(0, len(reqs), max(1, len(reqs) // 12)))[:12]
+    t0 = time.perf_counter()
+    plain_bs = 0
+    for i in sample:
+        w = ctx.world(built[i])
+        w.step(built[i].dt, reqs[i].horizon)
+        w.bodies()
+        w.destroy()
+        plain_bs += built[i].num_bodies * reqs[i].horizon
+    plain_sec = time.perf_counter() - t0
+    ctx.close()
+    value = st["body_steps"] / st["span_s"]
+    plain = plain_bs / plain_sec
+    return {
+        "workload": f"Poisson arrivals at {args.serve_rate:g} req/s for {args.serve_window:g} s ({len(reqs)} requests), "
+                    "worlds floor(exp(U[ln 16, ln 4096])) bodies + Plane, 40/40/20 Sphere/Box/Cylinder(10), NaiveBroadphase, "
+                    "GSSolver 10 iterations, dt 1/60, horizons U{1..240}; HBM budget 150 GB",
+        "value": value, "unit": UNIT, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+        "max_ms": st["max_ms"], "requests": len(reqs), "completed": st["completed"],
+        "offered_body_steps_per_s": offered / args.serve_window, "span_s": st["span_s"],
+        "submit_lag_max_s": lag[0], "ticks": st["ticks"], "steps_per_tick": args.serve_tick,
+        "bytes_peak_gb": st["bytes_peak"] / 1e9,
+        "plain_per_request": {"value": plain, "unit": UNIT,
+                              "sample": f"{len(sample)} of the requests, each alone through cp_world_step ({plain_bs} body-steps)"},
+        "served_over_plain": value / plain,
+        "clocks": clk,
+    }
 
 
 def run_ours(args):
@@ -276,7 +356,7 @@ def run_ours(args):
         "plain": plain,
         "batched_over_plain": value / ws / plain["value"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "kernel": "k_step_worlds",
+                     "peak_kind": peak_kind, "kernel": "k_step_pre + k_step_solve (one step)",
                      "alg_bytes_per_body_step": ALG_BYTES_PER_BODY_STEP, "kernel_ms": kernel_ms,
                      "traffic": None if traffic_per_bs is None else traffic_per_bs * total,
                      "note": "the step is bound by binary64 issue on GB300, not HBM; see DESIGN.md"},
@@ -285,10 +365,12 @@ def run_ours(args):
         "autotune": dict(ctx.autotune_info(), warmup_calls=args.warmup + tune_calls),
         "phase_share": {k: round(v / max(sum(phases.values()), 1.0), 4) for k, v in phases.items()},
     }
+    ctx.close()
+    if not args.no_serve:
+        line["served"] = run_served(args, local)
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(scs, args.cpu_sample, args.warmup, args.steps)
     print(json.dumps(line), flush=True)
-    ctx.close()
 
 
 def run_reference(args):

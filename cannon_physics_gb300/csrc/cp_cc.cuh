@@ -212,14 +212,226 @@ DI bool hulls_apart32(const DWorld& W, const DHull& A, const DHull& B, f3 xA, f3
   return false;
 }
 
-DI int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xAf, f3 xBf, q4 qAf, q4 qBf, int& start) {
+// ---------------------------------------------------------------------------
+// findSeparatingAxis with a binary32 filter.
+//
+// Pass 1 estimates, in binary32, the depth testSepAxis would return on every
+// axis of the reference's list (canonical face normals of A, of B, then the
+// edge crosses), with an absolute error bound E.  An axis estimated below -E
+// separates the hulls for certain: the reference returns false too (at that
+// axis or an earlier one).  Otherwise U = min(estimate + E) bounds the
+// smallest true depth from above, and U >= 0.
+// Pass 2 walks the list again in the reference's order and evaluates in
+// binary64, exactly as the reference does, only the axes whose estimate is
+// within E of U from below (d - E <= U: candidates for the first strict
+// minimum; this includes every axis that might separate, since U >= 0) and
+// the edge pairs whose binary32 cross product is too short for a reliable
+// direction (near-parallel edges, where the reference's almostZero test
+// decides).  An axis left out has a true depth above the true minimum and
+// above zero, so it neither separates the hulls nor is chosen; the chosen
+// axis and the separation verdict are the reference's, bit for bit.
+//
+// E: both evaluations round binary32 inputs; projections carry errors of a
+// few ulps of |x| + extent, and an edge axis built from a cross product of
+// length >= SAT_EDGE_MIN has a direction error of at most ~1.2e-5.  E =
+// 1e-4 (|xA|1 + |xB|1 + rA + rB) + 1e-6 is a wide margin over both.
+#define SAT_EDGE_MIN 0.05f
+
+// binary32 [lo, hi] of a hull's projection on unit world axis a
+DI void proj32(const DWorld& W, const DHull& H, f3 x, q4 q, const f3* ax, f3 a, float& lo, float& hi) {
+  const float c = dot32(a, x);
+  if (H.is_box) {
+    const float r = fabsf(dot32(a, ax[0])) * (float)H.he[0] + fabsf(dot32(a, ax[1])) * (float)H.he[1] +
+                    fabsf(dot32(a, ax[2])) * (float)H.he[2];
+    lo = c - r;
+    hi = c + r;
+    return;
+  }
+  const f3 la = rot32(q4{-q.x, -q.y, -q.z, q.w}, a);
+  float mn = __int_as_float(0x7f800000), mx = -mn;
+  for (int i = 0; i < H.nv; i++) {
+    const float* v = W.hverts + 4 * (H.v0 + i);
+    const float p = la.x * v[0] + la.y * v[1] + la.z * v[2];
+    mn = fminf(mn, p);
+    mx = fmaxf(mx, p);
+  }
+  lo = c + mn;
+  hi = c + mx;
+}
+
+struct Sat32 {
+  const DWorld* W;
+  const DHull *A, *B;
+  f3 xA, xB;
+  q4 qA, qB;
+  f3 axA[3], axB[3];  // box axes in the world frame
+  float E;
+  DI float depth(f3 a) const {
+    float loA, hiA, loB, hiB;
+    proj32(*W, *A, xA, qA, axA, a, loA, hiA);
+    proj32(*W, *B, xB, qB, axB, a, loB, hiB);
+    return fminf(hiA - loB, hiB - loA);
+  }
+  DI f3 face(const DHull& H, q4 q, int k) const {
+    const float* n = W->faces[H.f0 + W->hcanon[H.cf0 + k]].normal;
+    return rot32(q, f3{n[0], n[1], n[2]});
+  }
+  DI f3 edge(const DHull& H, q4 q, int k) const {
+    const float* e = W->hedges + 4 * (H.e0 + W->hcanon[H.ce0 + k]);
+    return rot32(q, f3{e[0], e[1], e[2]});
+  }
+};
+
+DI f3 cross32(f3 a, f3 b) { return f3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+DI float maxabs32(f3 a) { return fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))); }
+
+// Pass 1; returns false when an axis separates the hulls for certain.
+DI bool sat32_bound(const Sat32& S, float& U) {
+  U = __int_as_float(0x7f800000);
+  const DHull& A = *S.A;
+  const DHull& B = *S.B;
+  if (A.has_axes)
+    for (int k = 0; k < A.ncf; k++) {
+      float d = S.depth(S.face(A, S.qA, k));
+      if (d < -S.E) return false;
+      U = fminf(U, d + S.E);
+    }
+  if (B.has_axes)
+    for (int k = 0; k < B.ncf; k++) {
+      float d = S.depth(S.face(B, S.qB, k));
+      if (d < -S.E) return false;
+      U = fminf(U, d + S.E);
+    }
+  for (int k0 = 0; k0 < A.nce; k0++) {
+    const f3 e0 = S.edge(A, S.qA, k0);
+    for (int k1 = 0; k1 < B.nce; k1++) {
+      const f3 cr = cross32(e0, S.edge(B, S.qB, k1));
+      if (maxabs32(cr) < SAT_EDGE_MIN) continue;  // decided exactly in pass 2
+      const float l = len32(cr);
+      float d = S.depth(f3{cr.x / l, cr.y / l, cr.z / l});
+      if (d < -S.E) return false;
+      U = fminf(U, d + S.E);
+    }
+  }
+  return true;
+}
+
+// Pass 2: the reference's loop over the candidate axes only.
+DI bool sat64_candidates(const DWorld& W, const DHullPose& A, const DHullPose& B, const d3* wnA, const d3* wnB,
+                         const Sat32& S, float U, d3& target) {
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  double d;
+  if (A.H.has_axes)
+    for (int k = 0; k < A.H.ncf; k++) {
+      if (S.depth(S.face(A.H, S.qA, k)) - S.E > U) continue;
+      const d3 ax = wnA[W.hcanon[A.H.cf0 + k]];
+      if (!dtest_sep_axis(W, A, B, ax, d)) return false;
+      if (d < dmin) { dmin = d; target = ax; }
+    }
+  if (B.H.has_axes)
+    for (int k = 0; k < B.H.ncf; k++) {
+      if (S.depth(S.face(B.H, S.qB, k)) - S.E > U) continue;
+      const d3 ax = wnB[W.hcanon[B.H.cf0 + k]];
+      if (!dtest_sep_axis(W, A, B, ax, d)) return false;
+      if (d < dmin) { dmin = d; target = ax; }
+    }
+  for (int k0 = 0; k0 < A.H.nce; k0++) {
+    const f3 e0 = S.edge(A.H, S.qA, k0);
+    bool have0 = false;
+    d3 we0;
+    for (int k1 = 0; k1 < B.H.nce; k1++) {
+      const f3 cr32 = cross32(e0, S.edge(B.H, S.qB, k1));
+      if (maxabs32(cr32) >= SAT_EDGE_MIN) {
+        const float l = len32(cr32);
+        if (S.depth(f3{cr32.x / l, cr32.y / l, cr32.z / l}) - S.E > U) continue;
+      }
+      if (!have0) {
+        we0 = dvmult(A.q, ldd3(W.hed + 4 * (A.H.e0 + W.hcanon[A.H.ce0 + k0])));
+        have0 = true;
+      }
+      d3 cr = dcross(we0, dvmult(B.q, ldd3(W.hed + 4 * (B.H.e0 + W.hcanon[B.H.ce0 + k1]))));
+      if (dalmost_zero(cr)) continue;
+      cr = dnormalized(cr);
+      if (!dtest_sep_axis(W, A, B, cr, d)) return false;
+      if (d < dmin) { dmin = d; target = cr; }
+    }
+  }
+  d3 deltaC = dsub(B.x, A.x);
+  if (ddot(deltaC, target) > 0.0) target = dneg(target);
+  return true;
+}
+
+// Pass 2 with the candidates first gathered into a short list (indices into
+// the reference's axis order: A faces, B faces, then edge pairs k0-major).
+// Lanes of a warp hold different candidates; walking each lane's list in
+// rounds runs the binary64 axis test of all lanes together instead of once
+// per distinct list position.  More than SAT_MAXC candidates: the walk of
+// the whole list (sat64_candidates) decides.
+#define SAT_MAXC 8
+DI bool sat64_compact(const DWorld& W, const DHullPose& A, const DHullPose& B, const d3* wnA, const d3* wnB,
+                      const Sat32& S, float U, d3& target) {
+  int cand[SAT_MAXC];
+  int nc = 0;
+  bool over = false;
+  const int nfa = A.H.has_axes ? A.H.ncf : 0, nfb = B.H.has_axes ? B.H.ncf : 0;
+  for (int k = 0; k < nfa; k++)
+    if (!(S.depth(S.face(A.H, S.qA, k)) - S.E > U)) { if (nc < SAT_MAXC) cand[nc++] = k; else over = true; }
+  for (int k = 0; k < nfb; k++)
+    if (!(S.depth(S.face(B.H, S.qB, k)) - S.E > U)) { if (nc < SAT_MAXC) cand[nc++] = nfa + k; else over = true; }
+  for (int k0 = 0; k0 < A.H.nce; k0++) {
+    const f3 e0 = S.edge(A.H, S.qA, k0);
+    for (int k1 = 0; k1 < B.H.nce; k1++) {
+      const f3 cr32 = cross32(e0, S.edge(B.H, S.qB, k1));
+      if (maxabs32(cr32) >= SAT_EDGE_MIN) {
+        const float l = len32(cr32);
+        if (S.depth(f3{cr32.x / l, cr32.y / l, cr32.z / l}) - S.E > U) continue;
+      }
+      if (nc < SAT_MAXC) cand[nc++] = nfa + nfb + k0 * B.H.nce + k1; else over = true;
+    }
+  }
+  if (over) return sat64_candidates(W, A, B, wnA, wnB, S, U, target);
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  double d;
+  for (int j = 0; j < nc; j++) {
+    const int idx = cand[j];
+    d3 ax;
+    if (idx < nfa) {
+      ax = wnA[W.hcanon[A.H.cf0 + idx]];
+    } else if (idx < nfa + nfb) {
+      ax = wnB[W.hcanon[B.H.cf0 + idx - nfa]];
+    } else {
+      const int e = idx - nfa - nfb, k0 = e / B.H.nce, k1 = e - k0 * B.H.nce;
+      const d3 we0 = dvmult(A.q, ldd3(W.hed + 4 * (A.H.e0 + W.hcanon[A.H.ce0 + k0])));
+      const d3 cr = dcross(we0, dvmult(B.q, ldd3(W.hed + 4 * (B.H.e0 + W.hcanon[B.H.ce0 + k1]))));
+      if (dalmost_zero(cr)) continue;
+      ax = dnormalized(cr);
+    }
+    if (!dtest_sep_axis(W, A, B, ax, d)) return false;
+    if (d < dmin) { dmin = d; target = ax; }
+  }
+  d3 deltaC = dsub(B.x, A.x);
+  if (ddot(deltaC, target) > 0.0) target = dneg(target);
+  return true;
+}
+
+// one out-of-line copy: the resolver is large and is reached from several
+// dispatch cases; inlining it at each bloats the step kernel's instruction footprint
+__device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xAf, f3 xBf, q4 qAf, q4 qBf, int& start) {
   const DWorld& W = *C.W;
   const DShape& SA = W.shapes[shA];
   const DShape& SB = W.shapes[shB];
   if (distance_to(xAf, xBf) > SA.bsr + SB.bsr) return 0;
-  if (W.hulls[SA.hull].nf <= CP_MAX_HULL_VERTS && W.hulls[SB.hull].nf <= CP_MAX_HULL_VERTS &&
-      hulls_apart32(W, W.hulls[SA.hull], W.hulls[SB.hull], xAf, xBf, qAf, qBf, (float)(SA.bsr + SB.bsr)))
-    return 0;
+  Sat32 S32;
+  S32.W = &W;
+  S32.A = &W.hulls[SA.hull];
+  S32.B = &W.hulls[SB.hull];
+  S32.xA = xAf; S32.xB = xBf; S32.qA = qAf; S32.qB = qBf;
+  S32.axA[0] = rot32(qAf, f3{1.f, 0.f, 0.f}); S32.axA[1] = rot32(qAf, f3{0.f, 1.f, 0.f}); S32.axA[2] = rot32(qAf, f3{0.f, 0.f, 1.f});
+  S32.axB[0] = rot32(qBf, f3{1.f, 0.f, 0.f}); S32.axB[1] = rot32(qBf, f3{0.f, 1.f, 0.f}); S32.axB[2] = rot32(qBf, f3{0.f, 0.f, 1.f});
+  S32.E = 1e-4f * (fabsf(xAf.x) + fabsf(xAf.y) + fabsf(xAf.z) + fabsf(xBf.x) + fabsf(xBf.y) + fabsf(xBf.z) +
+                   (float)(SA.bsr + SB.bsr)) + 1e-6f;
+  float U;
+  if (!sat32_bound(S32, U)) return 0;
   DHullPose A, B;
   A.H = W.hulls[SA.hull]; A.x = d3of(xAf); A.q = d4of(qAf);
   B.H = W.hulls[SB.hull]; B.x = d3of(xBf); B.q = d4of(qBf);
@@ -239,7 +451,7 @@ DI int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int r
     wnB[f] = dvmult(B.q, ldd3(W.faces[B.H.f0 + f].dnormal));
   }
   d3 sep = d3{0.0, 0.0, 0.0};
-  if (!dfind_separating_axis(W, A, B, wnA, wnB, sep)) return 0;
+  if (!sat64_compact(W, A, B, wnA, wnB, S32, U, sep)) return 0;
   // clipAgainstHull: face of B most aligned with the axis
   int cfb = -1;
   double dmax = __longlong_as_double(0xfff0000000000000LL);

@@ -1337,12 +1337,16 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
   const bool tuning = use_graph && c->forced < 0 && c->best < 0;
   const int variant = c->forced >= 0 ? c->forced : (tuning ? c->tune_plan[c->tune_next] : (c->best >= 0 ? c->best : c->plain_variant));
   // groups of consecutive worlds (the order is by size) up to group_bodies
+  // per 128 solve threads: a narrower solve block takes a smaller group, so
+  // its levels still fill its lanes without long barrier waits
   std::vector<int> gstart(1, 0);
   {
-    int cnt = 0, bodies = 0;
+    const long long limit = (long long)c->group_bodies * cpk_solve_threads(variant) / 128;
+    int cnt = 0;
+    long long bodies = 0;
     for (int i = 0; i < n; i++) {
       int nb = c->worlds[order[i]].nb;
-      if (cnt > 0 && (cnt == CP_GROUP_MAX_WORLDS || bodies + nb > c->group_bodies)) {
+      if (cnt > 0 && (cnt == CP_GROUP_MAX_WORLDS || bodies + nb > limit)) {
         gstart.push_back(i);
         cnt = 0;
         bodies = 0;

@@ -12,6 +12,8 @@ int cpk_num_variants();
 int cpk_num_pre_variants();
 int cpk_num_solve_variants();
 int cpk_variant_threads(int variant);
+// threads per block of the solve kernel of a variant
+int cpk_solve_threads(int variant);
 void cpk_max_resident_blocks(int variant, int* pre, int* solve);
 // One World.step for the n worlds ids[0..n): the pre-solve kernel (one world
 // per block, grid_pre persistent blocks) then the solve kernel (groups of

@@ -91,7 +91,9 @@ DI int sphere_plane(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rs
 }
 
 // narrow_phase.dart:816-1038 (box.dart:99-115 for the side vectors)
-DI int sphere_box(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
+// one out-of-line copy: the resolver is large and is reached from several
+// dispatch cases; inlining it at each bloats the step kernel's instruction footprint
+__device__ __noinline__ int sphere_box(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
   const DWorld& W = *C.W;
   const DShape& sb = W.shapes[shB];
   double R = W.shapes[shA].radius;
@@ -208,7 +210,9 @@ DI bool point_in_polygon(const f3* verts, int N, f3 normal, f3 p) {
 DI f3 hv(const DWorld& W, int i) { return ld3(W.hverts + 4 * i); }
 
 // narrow_phase.dart:1039-1257
-DI int sphere_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
+// one out-of-line copy: the resolver is large and is reached from several
+// dispatch cases; inlining it at each bloats the step kernel's instruction footprint
+__device__ __noinline__ int sphere_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
   const DWorld& W = *C.W;
   const DHull H = W.hulls[W.shapes[shB].hull];
   double R = W.shapes[shA].radius;
@@ -277,7 +281,9 @@ DI int sphere_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int r
 }
 
 // narrow_phase.dart:1847-1915 (planeBox forwards here with its own shapes)
-DI int plane_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qA, q4 qB, int& start) {
+// one out-of-line copy: the resolver is large and is reached from several
+// dispatch cases; inlining it at each bloats the step kernel's instruction footprint
+__device__ __noinline__ int plane_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qA, q4 qB, int& start) {
   const DWorld& W = *C.W;
   const DHull H = W.hulls[W.shapes[shB].hull];
   f3 wn = vmult(qA, f3{0.f, 0.f, 1.f});

@@ -1248,6 +1248,7 @@ DI bool step_pre(Smem& S, int* s_last, double dt) {
 // A group of worlds in one block: the state one world keeps between its
 // pre-solve phases and its post-solve phases.
 #define CP_GROUP_MAX 8
+#define CP_SOLVE_MAX_WARPS 8  // solve kernels run at most 256 threads per block
 struct __align__(16) Slot {
   DWorld W;
   DWorldParams P;
@@ -1276,7 +1277,7 @@ DI bool index_ok(int code, int world, int idx, int bound) {
 // barrier waits for many independent rows instead of a few.  Each world keeps
 // its own iteration count and convergence test.
 DI void joint_solve(Smem& S, Slot* slots, int K) {
-  __shared__ double s_part[CP_GROUP_MAX][32];
+  __shared__ double s_part[CP_GROUP_MAX][CP_SOLVE_MAX_WARPS];
   __shared__ int s_conv[CP_GROUP_MAX];
   for (int sweep = 0;; sweep++) {
     int active = 0, Lmax = 0;
@@ -1417,6 +1418,7 @@ template <int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_step_solve(const DWorld* __restrict__ worlds, const int* __restrict__ ids,
                                                              const int* __restrict__ gstart, int ngroups, double dt,
                                                              int* __restrict__ queue) {
+  static_assert(THREADS <= 32 * CP_SOLVE_MAX_WARPS, "solve block too wide");
   __shared__ Smem S;
   __shared__ Slot slots[CP_GROUP_MAX];
   if (threadIdx.x < CP_NUM_PHASES) S.t_acc[threadIdx.x] = 0;
@@ -1606,10 +1608,11 @@ struct SolveVariant {
 };
 static const PreVariant kPre[] = {
     {k_step_pre<256, 1>, 256, 1}, {k_step_pre<128, 2>, 128, 2}, {k_step_pre<128, 4>, 128, 4},
-    {k_step_pre<64, 8>, 64, 8},   {k_step_pre<256, 2>, 256, 2},
+    {k_step_pre<64, 8>, 64, 8},   {k_step_pre<256, 2>, 256, 2}, {k_step_pre<32, 16>, 32, 16},
 };
 static const SolveVariant kSolve[] = {
     {k_step_solve<128, 4>, 128, 4}, {k_step_solve<128, 8>, 128, 8}, {k_step_solve<256, 4>, 256, 4},
+    {k_step_solve<32, 32>, 32, 32},
 };
 static const int kNumPre = sizeof(kPre) / sizeof(kPre[0]);
 static const int kNumSolve = sizeof(kSolve) / sizeof(kSolve[0]);
@@ -1619,6 +1622,7 @@ int cpk_num_pre_variants() { return kNumPre; }
 int cpk_num_solve_variants() { return kNumSolve; }
 
 int cpk_variant_threads(int v) { return kPre[v / kNumSolve].threads; }
+int cpk_solve_threads(int v) { return kSolve[v % kNumSolve].threads; }
 
 cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, const int* d_gstart, int ngroups, double dt, int* d_queue,
                             int grid_pre, int grid_solve, cudaStream_t stream, int variant, int n) {

@@ -354,6 +354,65 @@ int cp_set_group_bodies(cp_ctx* ctx, int32_t bodies);
  * launches since the previous call, and how many step launches they held. */
 int cp_batch_profile(cp_ctx* ctx, double* graph_ms, int64_t* step_launches);
 
+/* ---- served form ---------------------------------------------------------
+ *
+ * No counterpart in the reference.  A request server on one device: a
+ * request is one world plus a horizon (nsteps steps at dt).  The server keeps
+ * admitted worlds resident in HBM and admits queued requests (first come,
+ * first served) while their state and step scratch fit `hbm_budget_bytes`.
+ * Every admitted world advances up to `steps_per_tick` steps per launch
+ * sequence, together with all other admitted worlds, so requests that arrive
+ * while others run share the device with them (continuous batching).  A
+ * world stops at its own horizon.  Its result is the same, bit for bit, as
+ * stepping it alone with cp_world_step.
+ *
+ * The server owns its own context and thread; submit, poll, wait, result,
+ * cancel and stats may be called from any thread. */
+typedef struct cp_server cp_server;
+
+typedef struct cp_serve_config {
+  int32_t device;
+  int32_t steps_per_tick;           /* 0 = 2 */
+  int64_t hbm_budget_bytes;         /* device memory admitted worlds may hold at once */
+  int64_t max_active_bodies;        /* 0 = no cap; else admission also stops at this many bodies stepping */
+  int32_t variant;                  /* kernel variant pair, -1 = default */
+  int32_t group_bodies;             /* world grouping of the solve kernel, 0 = default */
+} cp_serve_config;
+
+/* request states */
+#define CP_REQ_PENDING   0
+#define CP_REQ_ACTIVE    1
+#define CP_REQ_DONE      2
+#define CP_REQ_FAILED    3
+#define CP_REQ_CANCELLED 4
+
+typedef struct cp_serve_stats {
+  int64_t submitted, admitted, completed, failed, cancelled;
+  int64_t pending, active, ticks;
+  int64_t bytes_in_use, bytes_peak, bytes_budget;
+  int64_t body_steps;               /* bodies x steps of the completed requests */
+  double span_s;                    /* first submission to last completion */
+  double device_s;                  /* time inside step launch sequences */
+  double p50_ms, p99_ms, mean_ms, max_ms;  /* latency: submission to result ready */
+} cp_serve_stats;
+
+int cp_serve_start(const cp_serve_config* cfg, cp_server** out);
+int cp_serve_stop(cp_server* server);
+/* Copies the world during the call.  CP_ERR_CAPACITY if the world alone needs
+ * more than the whole budget. */
+int cp_serve_submit(cp_server* server, const cp_world_desc* desc, double dt, int32_t nsteps, int64_t* ticket);
+int cp_serve_poll(cp_server* server, int64_t ticket, int32_t* state);
+/* Blocks until the request finished (done, failed or cancelled);
+ * timeout_s < 0 waits without limit, else CP_ERR_TIMEOUT when it runs out. */
+int cp_serve_wait(cp_server* server, int64_t ticket, double timeout_s, int32_t* state);
+/* Copies a finished request's bodies and final step info and releases it. */
+int cp_serve_result(cp_server* server, int64_t ticket, cp_body_desc* out, int32_t n, cp_step_info* info);
+/* A queued request is dropped; an admitted one is retired at the end of the
+ * current tick without a result. */
+int cp_serve_cancel(cp_server* server, int64_t ticket);
+/* Counters and latency percentiles since the previous reset. */
+int cp_serve_get_stats(cp_server* server, cp_serve_stats* out, int32_t reset);
+
 const char* cp_last_error(void);
 int cp_abi_version(void);
 

@@ -10,6 +10,7 @@ import pytest
 
 from cannon_physics_gb300 import _abi as A
 from cannon_physics_gb300 import engine, scenes
+from cannon_physics_gb300 import serve as S
 from oracle import oracle_py as O
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -46,7 +47,8 @@ def test_ctypes_layouts_match_the_c_header(tmp_path):
         pytest.skip("no C compiler")
     structs = [("cp_body_desc", A.BodyDesc), ("cp_shape_desc", A.ShapeDesc), ("cp_world_desc", A.WorldDesc),
                ("cp_contact", A.Contact), ("cp_row", A.Row), ("cp_constraint_desc", A.ConstraintDesc),
-               ("cp_contact_material", A.ContactMaterial), ("cp_step_info", A.StepInfo), ("cp_config", A.Config)]
+               ("cp_contact_material", A.ContactMaterial), ("cp_step_info", A.StepInfo), ("cp_config", A.Config),
+               ("cp_serve_config", S.ServeConfig), ("cp_serve_stats", S.ServeStats)]
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "cannon_gpu.h"', "int main(void) {"]
     expect = []
     for cname, py in structs:
