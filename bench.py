@@ -128,9 +128,9 @@ def peaks():
 
 
 def profiled_traffic():
-    """DRAM bytes per body-step of the step kernel from the committed ncu summary
-    (profiles/k_step_worlds_batch.txt: 'dram_bytes_per_body_step: X')."""
-    path = os.path.join(ROOT, "profiles", "k_step_worlds_batch.txt")
+    """DRAM bytes per body-step of the two step kernels from the committed ncu
+    summary (profiles/step_kernels_traffic.txt: 'dram_bytes_per_body_step: X')."""
+    path = os.path.join(ROOT, "profiles", "step_kernels_traffic.txt")
     try:
         for ln in open(path):
             if ln.startswith("dram_bytes_per_body_step:"):
@@ -359,7 +359,7 @@ def run_ours(args):
                      "peak_kind": peak_kind, "kernel": "k_step_pre + k_step_solve (one step)",
                      "alg_bytes_per_body_step": ALG_BYTES_PER_BODY_STEP, "kernel_ms": kernel_ms,
                      "traffic": None if traffic_per_bs is None else traffic_per_bs * total,
-                     "note": "the step is bound by binary64 issue on GB300, not HBM; see DESIGN.md"},
+                     "note": "bound by binary64 issue (64 cycles per warp instruction per sub-partition on GB300), barriers and load latency, not HBM bandwidth; traffic is DRAM bytes of one step from the committed ncu capture, scaled by bodies"},
         "gpu_launches": launches,
         "clocks": clk,
         "autotune": dict(ctx.autotune_info(), warmup_calls=args.warmup + tune_calls),
