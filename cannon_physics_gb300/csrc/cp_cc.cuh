@@ -23,15 +23,15 @@
 
 struct d4 { double x, y, z, w; };
 
-DI d4 d4of(q4 q) { return d4{(double)q.x, (double)q.y, (double)q.z, (double)q.w}; }
+DI d4 d4of(q4 q) { return d4{F(q.x), F(q.y), F(q.z), F(q.w)}; }
 
-DI d3 dvmult(d4 q, d3 v) {  // Quat.vmult with the Vector3 store
+DI d3 dvmult(d4 q, d3 v) {  // Quat.vmult with the Vector3 store (q, v binary32 values)
   double x = v.x, y = v.y, z = v.z;
   double qx = q.x, qy = q.y, qz = q.z, qw = q.w;
-  double ix = qw * x + qy * z - qz * y;
-  double iy = qw * y + qz * x - qx * z;
-  double iz = qw * z + qx * y - qy * x;
-  double iw = -qx * x - qy * y - qz * z;
+  double ix = fma_ff(-qz, y, fma_ff(qy, z, qw * x));
+  double iy = fma_ff(-qx, z, fma_ff(qz, x, qw * y));
+  double iz = fma_ff(-qy, x, fma_ff(qx, y, qw * z));
+  double iw = fma_ff(-qz, z, fma_ff(-qy, y, -qx * x));
   return d3{r32(ix * qw + iw * -qx + iy * -qz - iz * -qy), r32(iy * qw + iw * -qy + iz * -qx - ix * -qz),
             r32(iz * qw + iw * -qz + ix * -qy - iy * -qx)};
 }
@@ -39,8 +39,8 @@ DI d3 dneg(d3 v) { return d3{-v.x, -v.y, -v.z}; }
 DI d3 dadd(d3 a, d3 b) { return d3{r32(a.x + b.x), r32(a.y + b.y), r32(a.z + b.z)}; }
 DI d3 dsub(d3 a, d3 b) { return d3{r32(a.x - b.x), r32(a.y - b.y), r32(a.z - b.z)}; }
 DI d3 dscale(d3 a, double s) { return d3{r32(s * a.x), r32(s * a.y), r32(s * a.z)}; }
-DI d3 dcross(d3 a, d3 v) {
-  return d3{r32(a.y * v.z - a.z * v.y), r32(a.z * v.x - a.x * v.z), r32(a.x * v.y - a.y * v.x)};
+DI d3 dcross(d3 a, d3 v) {  // binary32 values: each difference of exact products rounds once
+  return d3{r32(fma_ff(a.y, v.z, -(a.z * v.y))), r32(fma_ff(a.z, v.x, -(a.x * v.z))), r32(fma_ff(a.x, v.y, -(a.y * v.x)))};
 }
 DI d3 dnormalized(d3 v) {
   double l = sqrt(ddot(v, v));

@@ -313,6 +313,7 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   size_t o_pc = L.take(sizeof(int) * (pc + 1));
   size_t o_pt = L.take(sizeof(int) * (pc + 1));
   size_t o_hv = L.take(sizeof(int) * (pc + 1));
+  size_t o_hv2 = L.take(sizeof(int) * (pc + 16 * 32 + 1));
   size_t o_ct = L.take(sizeof(DContact) * (cc + 1));
   size_t o_co = L.take(sizeof(DContact) * (cc + 1));
   size_t o_cs = L.take(sizeof(int) * (cc + 1));
@@ -323,6 +324,11 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   size_t o_lr = L.take(sizeof(int) * (rc + 1));
   size_t o_ls = L.take(sizeof(int) * (rc + 2));
   size_t o_lc = L.take(sizeof(int) * (rc + 2));
+  const int swc = rc + 1;
+  size_t o_swj = L.take(sizeof(float) * 4 * 5 * (size_t)swc);
+  size_t o_swd = L.take(sizeof(double) * 2 * 4 * (size_t)swc);
+  size_t o_swb = L.take(sizeof(int) * 2 * (size_t)swc);
+  size_t o_swo = L.take(sizeof(int) * (size_t)swc);
   size_t o_sk = L.take(sizeof(float) * (nb + 1));
   const int nbins = w.broadphase == CP_BROAD_GRID ? w.nbins : 0;
   size_t o_bc = L.take(sizeof(int) * (nbins + 2));
@@ -339,6 +345,7 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   d.pair_cnt = (int*)(base + o_pc);
   d.pair_tstart = (int*)(base + o_pt);
   d.heavy = (int*)(base + o_hv);
+  d.heavy2 = (int*)(base + o_hv2);
   d.ctmp = (DContact*)(base + o_ct);
   d.contacts = (DContact*)(base + o_co);
   d.cscr = (int*)(base + o_cs);
@@ -357,6 +364,11 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   d.hkeys = (long long*)(base + o_hk);
   d.hvals = (int*)(base + o_hw);
   d.hash_cap = hash_cap;
+  d.sw_j = (float4*)(base + o_swj);
+  d.sw_d = (double2*)(base + o_swd);
+  d.sw_b = (int2*)(base + o_swb);
+  d.sw_orig = (int*)(base + o_swo);
+  d.sw_cap = swc;
   return L.off;
 }
 
@@ -560,7 +572,7 @@ int plain_steps(cp_ctx* c, int id, double dt, int nsteps) {
     long long done = p.stepnumber;
     for (long long s = done; s < target; s++) {
       CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_one, c->d_one_group, 1, dt, c->d_queue, 1, 1, c->stream,
-                               w.nb > 512 ? 0 : c->plain_variant, 1));
+                               w.nb > 512 ? 0 : c->plain_variant, 1, w.nb));
       c->launches += 3;
     }
     st = read_params(c, w, p);
@@ -1172,7 +1184,7 @@ int cp_world_step_static(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
   const int* d_list = (const int*)(base + o_ids);
   const int variant = w.nb > 512 ? 0 : c->plain_variant;
   for (int s = 0; s < nsteps; s++) {
-    CUDA_TRY(cpk_launch_step(d_world, d_list, d_list + 1, 1, dt, c->d_queue, 1, 1, c->stream, variant, 1));
+    CUDA_TRY(cpk_launch_step(d_world, d_list, d_list + 1, 1, dt, c->d_queue, 1, 1, c->stream, variant, 1, w.nb));
     c->launches += 3;
   }
   DWorldParams p;
@@ -1336,12 +1348,13 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
   // tuned: the forced variant, else the tuned one, else the plain default.
   const bool tuning = use_graph && c->forced < 0 && c->best < 0;
   const int variant = c->forced >= 0 ? c->forced : (tuning ? c->tune_plan[c->tune_next] : (c->best >= 0 ? c->best : c->plain_variant));
-  // groups of consecutive worlds (the order is by size) up to group_bodies
-  // per 128 solve threads: a narrower solve block takes a smaller group, so
-  // its levels still fill its lanes without long barrier waits
+  // groups of consecutive worlds (the order is by size): up to group_bodies
+  // per 128 threads of a block-wide solve kernel (a narrower block takes a
+  // smaller group, so its levels still fill its lanes), or up to group_bodies
+  // per warp for the warp-centric one
   std::vector<int> gstart(1, 0);
   {
-    const long long limit = (long long)c->group_bodies * cpk_solve_threads(variant) / 128;
+    const long long limit = cpk_solve_group_limit(variant, c->group_bodies);
     int cnt = 0;
     long long bodies = 0;
     for (int i = 0; i < n; i++) {
@@ -1357,7 +1370,8 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
     gstart.push_back(n);
   }
   const int ngroups = (int)gstart.size() - 1;
-  const int grid_pre = std::max(1, std::min(n, c->sms * c->blocks_pre[variant]));
+  const int max_nb = c->worlds[order[0]].nb;  // the order is by size
+  const int grid_pre = std::max(1, std::min(n, c->sms * cpk_pre_blocks_per_sm(variant, max_nb)));
   const int grid_solve = std::max(1, std::min(ngroups, c->sms * c->blocks_solve[variant]));
   bool reuse = use_graph && !tuning && c->graph && c->graph_ids == order && c->graph_dt == dt && c->graph_steps == nsteps &&
                c->graph_variant == variant;
@@ -1370,7 +1384,7 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
     CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 0; s < nsteps; s++) {
       cudaError_t e = cpk_launch_step(c->d_worlds, c->d_ids, c->d_gstart, ngroups, dt, c->d_queue, grid_pre, grid_solve, c->stream,
-                                      variant, n);
+                                      variant, n, max_nb);
       if (e != cudaSuccess) {
         cudaStreamEndCapture(c->stream, &g);
         return fail(CP_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
@@ -1393,7 +1407,7 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
   if (tuning || !use_graph) {
     for (int s = 0; s < nsteps; s++)
       CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_ids, c->d_gstart, ngroups, dt, c->d_queue, grid_pre, grid_solve, c->stream,
-                               variant, n));
+                               variant, n, max_nb));
   } else {
     CUDA_TRY(cudaGraphLaunch(c->graph, c->stream));
   }

@@ -14,13 +14,19 @@ int cpk_num_solve_variants();
 int cpk_variant_threads(int variant);
 // threads per block of the solve kernel of a variant
 int cpk_solve_threads(int variant);
+// bodies per world group of a variant's solve kernel for the configured group size
+int cpk_solve_group_limit(int variant, int group_bodies);
 void cpk_max_resident_blocks(int variant, int* pre, int* solve);
 // One World.step for the n worlds ids[0..n): the pre-solve kernel (one world
 // per block, grid_pre persistent blocks) then the solve kernel (groups of
 // worlds ids[gstart[g] .. gstart[g+1]), grid_solve persistent blocks); two
 // queue counters at d_queue.
+// max_nb: the most bodies of any world in the launch (sizes the pre kernel's
+// shared level table)
 cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, const int* d_gstart, int ngroups, double dt, int* d_queue,
-                            int grid_pre, int grid_solve, cudaStream_t stream, int variant, int n);
+                            int grid_pre, int grid_solve, cudaStream_t stream, int variant, int n, int max_nb);
+// resident blocks per SM of a variant's pre kernel for that largest world
+int cpk_pre_blocks_per_sm(int variant, int max_nb);
 // status, stepnumber and counts of the listed worlds, gathered into out[4*i..]
 cudaError_t cpk_gather_status(const DWorld* d_worlds, const int* d_ids, int n, long long* d_out, cudaStream_t stream);
 // clear the status of the listed worlds

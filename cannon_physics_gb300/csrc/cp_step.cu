@@ -45,6 +45,8 @@ struct __align__(16) Smem {
   int n_pairs, n_contacts, n_heavy, n_rows;
   int n_fric, n_cand, n_levels, cursor;
   int overflow, converged, wi, pad;
+  int kcnt[16], kpos[16];  // narrowphase: heavy pairs per resolver kind, segment cursors
+  int cursor2, pad2[3];
 };
 
 // ---------------------------------------------------------------------------
@@ -639,7 +641,7 @@ DI void narrow_pair(Smem& S, int k, bool heavy_pass) {
     int rk = swap ? resolver_kind(sj.type, si.type) : resolver_kind(si.type, sj.type);
     if (rk == RK_NONE) break;
     if (is_heavy(rk) != heavy_pass) {
-      if (!heavy_pass) W.heavy[atomicAdd(&S.n_heavy, 1)] = k;
+      if (!heavy_pass) W.heavy[atomicAdd(&S.n_heavy, 1)] = (int)(((unsigned)rk << 28) | (unsigned)k);  // k < 2^28
       return;
     }
     if (!((si.mask & sj.group) != 0 && (sj.mask & si.group) != 0)) break;
@@ -690,8 +692,35 @@ DI void ph_narrow(Smem& S) {
   __syncthreads();
   for (int k = threadIdx.x; k < np; k += BT) narrow_pair(S, k, false);
   __syncthreads();
+  // heavy pairs by resolver kind, each kind's segment starting on a warp
+  // boundary: a warp then runs one resolver instead of interleaving several
+  // (a binary64 warp instruction costs the same with one active lane or 32)
   const int nh = S.n_heavy;
-  for (int h = threadIdx.x; h < nh; h += BT) narrow_pair(S, W.heavy[h], true);
+  if (threadIdx.x < 16) S.kcnt[threadIdx.x] = 0;
+  __syncthreads();
+  for (int h = threadIdx.x; h < nh; h += BT) atomicAdd(&S.kcnt[(unsigned)W.heavy[h] >> 28], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int o = 0;
+    for (int r = 0; r < 16; r++) {
+      S.kpos[r] = o;
+      o += (S.kcnt[r] + 31) & ~31;
+    }
+    S.cursor2 = o;
+  }
+  __syncthreads();
+  const int nhp = S.cursor2;
+  for (int h = threadIdx.x; h < nhp; h += BT) W.heavy2[h] = -1;
+  __syncthreads();
+  for (int h = threadIdx.x; h < nh; h += BT) {
+    const unsigned e = (unsigned)W.heavy[h];
+    W.heavy2[atomicAdd(&S.kpos[e >> 28], 1)] = (int)(e & 0x0FFFFFFFu);
+  }
+  __syncthreads();
+  for (int h = threadIdx.x; h < nhp; h += BT) {
+    const int k = W.heavy2[h];
+    if (k >= 0) narrow_pair(S, k, true);
+  }
   __syncthreads();
   // order: contacts of pair k follow those of pairs < k
   for (int k = threadIdx.x; k < np; k += BT) W.heavy[k] = W.pair_cnt[k];
@@ -949,8 +978,8 @@ DI void assemble_row(const Smem& S, const RowGeom& G, DRow& R, double h) {
   C += dot(iMaR, gaR);
   C += dot(iMbR, gbR);
   C = C + G.eps;
-  std3(R.gaS, d3of(gaS)); std3(R.gaR, d3of(gaR)); std3(R.gbS, d3of(gbS)); std3(R.gbR, d3of(gbR));
-  std3(R.iMaR, d3of(iMaR)); std3(R.iMbR, d3of(iMbR));
+  st3(R.gaS, gaS); st3(R.gaR, gaR); st3(R.gbS, gbS); st3(R.gbR, gbR);
+  st3(R.iMaR, iMaR); st3(R.iMbR, iMbR);
   R.B = B;
   R.invC = 1.0 / C;
   R.eps = G.eps;
@@ -1048,32 +1077,47 @@ DI void ph_rows_assemble(Smem& S, double h) {
 // dynamic body with it.  Bodies with zero solve mass and inertia
 // (static, sleeping, kinematic) keep vlambda = wlambda = +0 exactly, so they
 // order nothing.
-#define CP_SMEM_LEVEL_BODIES 2048
+// Rows are walked in order by one thread (the level of a row depends on
+// every earlier row on its bodies), from shared memory: all threads stage the
+// (bi, bj) pairs of a chunk of rows, thread 0 assigns their levels against a
+// per-body table in shared memory (worlds of up to last_cap bodies; larger
+// worlds keep the table in global scratch), and all threads write the levels
+// back.
+#define CP_LEVEL_CHUNK 512
+// largest per-body level table kept in shared memory (33 KB; with the row
+// chunk the dynamic shared memory stays under the 48 KB default limit)
+#define CP_SMEM_LEVEL_MAX 8448
 
-DI void ph_levels(Smem& S, int* s_last) {
+DI void ph_levels(Smem& S, int* s_last, int last_cap, int2* s_pairs) {
   const DWorld& W = S.W;
   const int nrows = S.n_rows;
   const int nb = S.P.nb;
-  const bool smem = nb <= CP_SMEM_LEVEL_BODIES;
   // last[b] = level of the latest row on dynamic body b, or -2 for bodies with
   // zero solve mass and inertia (they order nothing)
-  int* last = smem ? s_last : W.level_cursor;
+  int* last = nb <= last_cap ? s_last : W.level_cursor;
   for (int i = threadIdx.x; i < nb; i += BT) last[i] = W.bscr[i].active ? -1 : -2;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int nl = 0;
-    for (int r = 0; r < nrows; r++) {
-      int a = W.rows[r].bi, b = W.rows[r].bj;
-      int la = last[a], lb = last[b];
-      int l = (la > lb ? la : lb) + 1;
-      if (l < 0) l = 0;
-      if (la != -2) last[a] = l;
-      if (lb != -2) last[b] = l;
-      W.level_of[r] = l;
-      if (l + 1 > nl) nl = l + 1;
+  int nlev = 0;  // thread 0
+  for (int c0 = 0; c0 < nrows; c0 += CP_LEVEL_CHUNK) {
+    const int n = min(CP_LEVEL_CHUNK, nrows - c0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += BT) s_pairs[i] = make_int2(W.rows[c0 + i].bi, W.rows[c0 + i].bj);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < n; i++) {
+        const int2 p = s_pairs[i];
+        const int la = last[p.x], lb = last[p.y];
+        int l = (la > lb ? la : lb) + 1;
+        if (l < 0) l = 0;
+        if (la != -2) last[p.x] = l;
+        if (lb != -2) last[p.y] = l;
+        s_pairs[i].x = l;
+        if (l + 1 > nlev) nlev = l + 1;
+      }
     }
-    S.n_levels = nl;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += BT) W.level_of[c0 + i] = s_pairs[i].x;
   }
+  if (threadIdx.x == 0) S.n_levels = nlev;
   __syncthreads();
   const int nl = S.n_levels;
   for (int l = threadIdx.x; l <= nl; l += BT) W.level_start[l] = 0;
@@ -1085,119 +1129,190 @@ DI void ph_levels(Smem& S, int* s_last) {
   __syncthreads();
   for (int r = threadIdx.x; r < nrows; r += BT) W.level_rows[atomicAdd(&W.level_cursor[W.level_of[r]], 1)] = r;
   __syncthreads();
+  // the rows in level order for the sweeps
+  const int cap = W.sw_cap;
+  for (int p = threadIdx.x; p < nrows; p += BT) {
+    const int r = W.level_rows[p];
+    const DRow& R = W.rows[r];
+    W.sw_j[p] = make_float4(R.gaS[0], R.gaS[1], R.gaS[2], R.gaR[0]);
+    W.sw_j[cap + p] = make_float4(R.gaR[1], R.gaR[2], R.gbS[0], R.gbS[1]);
+    W.sw_j[2 * cap + p] = make_float4(R.gbS[2], R.gbR[0], R.gbR[1], R.gbR[2]);
+    W.sw_j[3 * cap + p] = make_float4(R.iMaR[0], R.iMaR[1], R.iMaR[2], R.iMbR[0]);
+    W.sw_j[4 * cap + p] = make_float4(R.iMbR[1], R.iMbR[2], 0.f, 0.f);
+    W.sw_d[p] = make_double2(R.B, R.invC);
+    W.sw_d[cap + p] = make_double2(R.eps, R.lambda);
+    W.sw_d[2 * cap + p] = make_double2(R.imA, R.imB);
+    W.sw_d[3 * cap + p] = make_double2(R.minF, R.maxF);
+    W.sw_b[p] = make_int2(R.bi, R.bj);
+    W.sw_orig[p] = r;
+  }
+  __syncthreads();
 }
 
 // One row of one sweep (gs_solver.dart:127-148 with Equation.computeGWlambda
 // and addToWlambda, equation_class.dart:95-169)
-DI double gs_row(const DWorld& W, DRow& R) {
-  DBodyScr& A = W.bscr[R.bi];
-  DBodyScr& B = W.bscr[R.bj];
-  d3 vla = ldd3(A.vl), wla = ldd3(A.wl), vlb = ldd3(B.vl), wlb = ldd3(B.wl);
-  // A body with zero solve mass and inertia keeps vlambda = wlambda = +0, so
-  // its half of G*Wlambda is a signed zero and adding it changes no nonzero
-  // sum; a zero sum can only change sign, which no later store observes.
-  double ga = A.active ? ddot(vla, ldd3(R.gaS)) + ddot(wla, ldd3(R.gaR)) : 0.0;
-  double gb = B.active ? ddot(vlb, ldd3(R.gbS)) + ddot(wlb, ldd3(R.gbR)) : 0.0;
-  double gwl = A.active && B.active ? ga + gb : (A.active ? ga : gb);
-  double lj = R.lambda;
-  double dl = R.invC * (R.B - gwl - R.eps * lj);
-  if (lj + dl < R.minF) dl = R.minF - lj;
-  else if (lj + dl > R.maxF) dl = R.maxF - lj;
-  R.lambda = lj + dl;
-  if (A.active) std3(A.vl, dadd_scaled(vla, R.imA * dl, ldd3(R.gaS)));
-  if (B.active) {
-    // re-read: bi == bj is possible for a constraint between a body and itself
-    d3 v = R.bi == R.bj ? ldd3(B.vl) : vlb;
-    std3(B.vl, dadd_scaled(v, R.imB * dl, ldd3(R.gbS)));
-  }
-  if (A.active) std3(A.wl, dadd_scaled(wla, dl, ldd3(R.iMaR)));
-  if (B.active) {
-    d3 w = R.bi == R.bj ? ldd3(B.wl) : wlb;
-    std3(B.wl, dadd_scaled(w, dl, ldd3(R.iMbR)));
+// binary32 value to binary64 on the integer pipe: exact, and free of the
+// F2F conversion that occupies the binary64 pipe on GB300.  Normal numbers
+// and zeros take the integer path; subnormals and non-finite values convert
+// the ordinary way.
+DI double f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e - 1u < 254u)
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+  if ((u << 1) == 0u) return __longlong_as_double((long long)sign);
+  return (double)f;
+}
+DI d3 f2d3(float x, float y, float z) { return d3{f2d(x), f2d(y), f2d(z)}; }
+
+// dot product of two vectors of binary32 values in the reference's order
+// ((x + y) + z): every product is exact in binary64, so a fused multiply-add
+// rounds each partial sum exactly as the separate multiply and add do
+DI double ddot_f(d3 a, d3 b) { return __fma_rn(a.z, b.z, __fma_rn(a.y, b.y, a.x * b.x)); }
+
+// One row of a GSSolver sweep (gs_solver.dart:122-155) at level position p.
+// A body with zero solve mass and inertia keeps vlambda = wlambda = +0, so
+// its half of G*Wlambda is a signed zero and adding it changes no nonzero
+// sum; a zero sum can only change sign, which no later store observes.
+DI double gs_row_sw(const DWorld& W, int p, int2 bb) {
+  const int cap = W.sw_cap;
+  const float4 j0 = W.sw_j[p], j1 = W.sw_j[cap + p], j2 = W.sw_j[2 * cap + p];
+  const double2 d0 = W.sw_d[p], d1 = W.sw_d[cap + p], d3b = W.sw_d[3 * cap + p];
+  DBodyScr& A = W.bscr[bb.x];
+  DBodyScr& B = W.bscr[bb.y];
+  const d3 gaS = f2d3(j0.x, j0.y, j0.z), gaR = f2d3(j0.w, j1.x, j1.y);
+  const d3 gbS = f2d3(j1.z, j1.w, j2.x), gbR = f2d3(j2.y, j2.z, j2.w);
+  const d3 vla = ldd3(A.vl), wla = ldd3(A.wl), vlb = ldd3(B.vl), wlb = ldd3(B.wl);
+  const double ga = A.active ? ddot_f(vla, gaS) + ddot_f(wla, gaR) : 0.0;
+  const double gb = B.active ? ddot_f(vlb, gbS) + ddot_f(wlb, gbR) : 0.0;
+  const double gwl = A.active && B.active ? ga + gb : (A.active ? ga : gb);
+  const double lj = d1.y;
+  double dl = d0.y * (d0.x - gwl - d1.x * lj);
+  if (lj + dl < d3b.x) dl = d3b.x - lj;
+  else if (lj + dl > d3b.y) dl = d3b.y - lj;
+  W.sw_d[cap + p].y = lj + dl;
+  if (A.active || B.active) {
+    const double2 im = W.sw_d[2 * cap + p];
+    const float4 j3 = W.sw_j[3 * cap + p], j4 = W.sw_j[4 * cap + p];
+    if (A.active) {
+      std3(A.vl, dadd_scaled(vla, im.x * dl, gaS));
+      std3(A.wl, dadd_scaled(wla, dl, f2d3(j3.x, j3.y, j3.z)));
+    }
+    if (B.active) {
+      // re-read: bi == bj is possible for a constraint between a body and itself
+      const bool same = bb.x == bb.y;
+      const d3 v = same ? ldd3(B.vl) : vlb;
+      const d3 w = same ? ldd3(B.wl) : wlb;
+      std3(B.vl, dadd_scaled(v, im.y * dl, gbS));
+      std3(B.wl, dadd_scaled(w, dl, f2d3(j3.w, j4.x, j4.y)));
+    }
   }
   return dl > 0.0 ? dl : -dl;
 }
 
 // Add result to velocity; multipliers (gs_solver.dart:157-176)
+// binary64 holding a binary32 value -> binary32, on the integer pipe (the
+// reverse of f2d); other values convert the ordinary way
+DI float d2f(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
+  if (e - 897u < 254u && (u & 0x1fffffffull) == 0)
+    return __uint_as_float(sign | ((e - 896u) << 23) | (unsigned)((u >> 29) & 0x7fffffu));
+  if ((u << 1) == 0) return __uint_as_float(sign);
+  return (float)x;
+}
+
+DI void apply_body(const DWorld& W, int i) {
+  DBody& b = W.bodies[i];
+  DBodyScr& s = W.bscr[i];
+  f3 vl = mul(f3{d2f(s.vl[0]), d2f(s.vl[1]), d2f(s.vl[2])}, ld3(b.lin_factor));
+  st3(b.vel, add(ld3(b.vel), vl));
+  f3 wl = mul(f3{d2f(s.wl[0]), d2f(s.wl[1]), d2f(s.wl[2])}, ld3(b.ang_factor));
+  st3(b.avel, add(ld3(b.avel), wl));
+}
+
+DI void apply_row(const DWorld& W, int p, double invDt) {
+  DRow& R = W.rows[W.sw_orig[p]];
+  const double lam = W.sw_d[W.sw_cap + p].y;
+  R.lambda = lam;
+  R.mult = lam * invDt;
+}
+
 DI void ph_solve_apply(Smem& S, double h) {
   const DWorld& W = S.W;
-  for (int i = threadIdx.x; i < S.P.nb; i += BT) {
-    DBody& b = W.bodies[i];
-    DBodyScr& s = W.bscr[i];
-    f3 vl = mul(f3{(float)s.vl[0], (float)s.vl[1], (float)s.vl[2]}, ld3(b.lin_factor));
-    st3(b.vel, add(ld3(b.vel), vl));
-    f3 wl = mul(f3{(float)s.wl[0], (float)s.wl[1], (float)s.wl[2]}, ld3(b.ang_factor));
-    st3(b.avel, add(ld3(b.avel), wl));
-  }
-  double invDt = 1 / h;
-  for (int r = threadIdx.x; r < S.n_rows; r += BT) W.rows[r].mult = W.rows[r].lambda * invDt;
+  for (int i = threadIdx.x; i < S.P.nb; i += BT) apply_body(W, i);
+  const double invDt = 1 / h;
+  for (int p = threadIdx.x; p < S.n_rows; p += BT) apply_row(W, p, invDt);
   __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
 // damping, integrate, clearForces, sleepTick (world_class.dart:647-700,
 // rigid_body.dart:263-300,627-680)
+DI void integrate_body(const DWorld& W, const DWorldParams& P, int i, double dt, bool qn, double time) {
+  DBody& b = W.bodies[i];
+  f3 v = ld3(b.vel), w = ld3(b.avel);
+  if (b.type == CP_BODY_DYNAMIC) {
+    v = scale(v, W.dpow[2 * i]);
+    w = scale(w, W.dpow[2 * i + 1]);
+  }
+  f3 p = ld3(b.pos);
+  q4 q = ld4q(b.quat);
+  st3(b.prev_pos, p);
+  st4q(b.prev_quat, q);
+  if ((b.type == CP_BODY_DYNAMIC || b.type == CP_BODY_KINEMATIC) && b.sleep_state != CP_SLEEPING) {
+    double iMdt = b.inv_mass * dt;
+    f3 lf = ld3(b.lin_factor), af = ld3(b.ang_factor);
+    f3 f = ld3(b.force), t = ld3(b.torque);
+    v.x = (float)(v.x + f.x * iMdt * lf.x);
+    v.y = (float)(v.y + f.y * iMdt * lf.y);
+    v.z = (float)(v.z + f.z * iMdt * lf.z);
+    const float* e = b.iw;
+    double tx = (double)t.x * af.x, ty = (double)t.y * af.y, tz = (double)t.z * af.z;
+    w.x = (float)(w.x + dt * (e[0] * tx + e[1] * ty + e[2] * tz));
+    w.y = (float)(w.y + dt * (e[3] * tx + e[4] * ty + e[5] * tz));
+    w.z = (float)(w.z + dt * (e[6] * tx + e[7] * ty + e[8] * tz));
+    p.x = (float)(p.x + v.x * dt);
+    p.y = (float)(p.y + v.y * dt);
+    p.z = (float)(p.z + v.z * dt);
+    q = qintegrate(q, w, dt, af);
+    if (qn) q = P.qn_fast ? qnormalize_fast(q) : qnormalize(q);
+    st3(b.pos, p);
+    st4q(b.quat, q);
+    b.flags |= BF_AABB_DIRTY;
+    f3 I = ld3(b.inv_inertia);
+    if (!(I.x == I.y && I.y == I.z)) inertia_world(q, I, b.iw);
+  }
+  st3(b.force, f3{0.f, 0.f, 0.f});
+  st3(b.torque, f3{0.f, 0.f, 0.f});
+  if (P.allow_sleep && (b.flags & BF_ALLOW_SLEEP)) {
+    int st = b.sleep_state;
+    double s2 = length2(v) + length2(w);
+    double lim2 = b.sleep_speed_limit * b.sleep_speed_limit;
+    if (st == CP_AWAKE && s2 < lim2) {
+      b.sleep_state = CP_SLEEPY;
+      b.time_last_sleepy = time;
+    } else if (st == CP_SLEEPY && s2 > lim2) {
+      b.sleep_state = CP_AWAKE;
+      b.flags &= ~BF_WAKE;
+    } else if (st == CP_SLEEPY && time - b.time_last_sleepy > b.sleep_time_limit) {
+      b.sleep_state = CP_SLEEPING;
+      v = f3{0.f, 0.f, 0.f};
+      w = f3{0.f, 0.f, 0.f};
+      b.flags &= ~BF_WAKE;
+    }
+  }
+  st3(b.vel, v);
+  st3(b.avel, w);
+
+}
+
 DI void ph_integrate(Smem& S, double dt) {
-  const DWorld& W = S.W;
   const DWorldParams& P = S.P;
   const bool qn = (P.stepnumber % (long long)(P.qn_skip + 1)) == 0;
-  const double time = P.time;
-  for (int i = threadIdx.x; i < P.nb; i += BT) {
-    DBody& b = W.bodies[i];
-    f3 v = ld3(b.vel), w = ld3(b.avel);
-    if (b.type == CP_BODY_DYNAMIC) {
-      v = scale(v, W.dpow[2 * i]);
-      w = scale(w, W.dpow[2 * i + 1]);
-    }
-    f3 p = ld3(b.pos);
-    q4 q = ld4q(b.quat);
-    st3(b.prev_pos, p);
-    st4q(b.prev_quat, q);
-    if ((b.type == CP_BODY_DYNAMIC || b.type == CP_BODY_KINEMATIC) && b.sleep_state != CP_SLEEPING) {
-      double iMdt = b.inv_mass * dt;
-      f3 lf = ld3(b.lin_factor), af = ld3(b.ang_factor);
-      f3 f = ld3(b.force), t = ld3(b.torque);
-      v.x = (float)(v.x + f.x * iMdt * lf.x);
-      v.y = (float)(v.y + f.y * iMdt * lf.y);
-      v.z = (float)(v.z + f.z * iMdt * lf.z);
-      const float* e = b.iw;
-      double tx = (double)t.x * af.x, ty = (double)t.y * af.y, tz = (double)t.z * af.z;
-      w.x = (float)(w.x + dt * (e[0] * tx + e[1] * ty + e[2] * tz));
-      w.y = (float)(w.y + dt * (e[3] * tx + e[4] * ty + e[5] * tz));
-      w.z = (float)(w.z + dt * (e[6] * tx + e[7] * ty + e[8] * tz));
-      p.x = (float)(p.x + v.x * dt);
-      p.y = (float)(p.y + v.y * dt);
-      p.z = (float)(p.z + v.z * dt);
-      q = qintegrate(q, w, dt, af);
-      if (qn) q = P.qn_fast ? qnormalize_fast(q) : qnormalize(q);
-      st3(b.pos, p);
-      st4q(b.quat, q);
-      b.flags |= BF_AABB_DIRTY;
-      f3 I = ld3(b.inv_inertia);
-      if (!(I.x == I.y && I.y == I.z)) inertia_world(q, I, b.iw);
-    }
-    st3(b.force, f3{0.f, 0.f, 0.f});
-    st3(b.torque, f3{0.f, 0.f, 0.f});
-    if (P.allow_sleep && (b.flags & BF_ALLOW_SLEEP)) {
-      int st = b.sleep_state;
-      double s2 = length2(v) + length2(w);
-      double lim2 = b.sleep_speed_limit * b.sleep_speed_limit;
-      if (st == CP_AWAKE && s2 < lim2) {
-        b.sleep_state = CP_SLEEPY;
-        b.time_last_sleepy = time;
-      } else if (st == CP_SLEEPY && s2 > lim2) {
-        b.sleep_state = CP_AWAKE;
-        b.flags &= ~BF_WAKE;
-      } else if (st == CP_SLEEPY && time - b.time_last_sleepy > b.sleep_time_limit) {
-        b.sleep_state = CP_SLEEPING;
-        v = f3{0.f, 0.f, 0.f};
-        w = f3{0.f, 0.f, 0.f};
-        b.flags &= ~BF_WAKE;
-      }
-    }
-    st3(b.vel, v);
-    st3(b.avel, w);
-  }
+  for (int i = threadIdx.x; i < P.nb; i += BT) integrate_body(S.W, P, i, dt, qn, P.time);
   __syncthreads();
 }
 
@@ -1213,7 +1328,7 @@ DI void tick(Smem& S, int phase) {
 
 // Everything of World.internalStep up to the solver's sweeps; returns false
 // when a capacity overflow stopped the step before any body state changed.
-DI bool step_pre(Smem& S, int* s_last, double dt) {
+DI bool step_pre(Smem& S, int* s_last, int last_cap, int2* s_pairs, double dt) {
   if (threadIdx.x == 0) {
     S.overflow = 0;
     S.n_pairs = S.n_contacts = S.n_rows = S.n_levels = 0;
@@ -1240,7 +1355,7 @@ DI bool step_pre(Smem& S, int* s_last, double dt) {
   tick(S, 3);
   ph_rows_assemble(S, dt);
   tick(S, 4);
-  if (S.n_rows > 0) ph_levels(S, s_last);
+  if (S.n_rows > 0) ph_levels(S, s_last, last_cap, s_pairs);
   tick(S, 5);
   return true;
 }
@@ -1316,11 +1431,12 @@ DI void joint_solve(Smem& S, Slot* slots, int K) {
         const Slot& sl = slots[k];
         const DWorld& W = sl.W;
         if (!index_ok(3, sl.id, off, cnt[k])) continue;
-        int r = W.level_rows[base[k] + off];
+        const int p = base[k] + off;
+        const int r = W.sw_orig[p];
         if (!index_ok(4, sl.id, r, sl.n_rows)) continue;
-        DRow& R = W.rows[r];
-        if (!index_ok(5, sl.id, R.bi, sl.P.nb) || !index_ok(6, sl.id, R.bj, sl.P.nb)) continue;
-        double a = gs_row(W, R);
+        const int2 bb = W.sw_b[p];
+        if (!index_ok(5, sl.id, bb.x, sl.P.nb) || !index_ok(6, sl.id, bb.y, sl.P.nb)) continue;
+        double a = gs_row_sw(W, p, bb);
         W.absdl[r] = a;
 #pragma unroll
         for (int kk = 0; kk < CP_GROUP_MAX; kk++)
@@ -1373,11 +1489,15 @@ DI void joint_solve(Smem& S, Slot* slots, int K) {
 
 // Kernel 1 of a step: one world per block, everything up to the solver's
 // sweeps (pairs, contacts, rows, levels).  Register-hungry (the resolvers).
+// Dynamic shared memory: CP_LEVEL_CHUNK row pairs, then the level table of
+// up to last_cap bodies.
 template <int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_step_pre(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n,
-                                                           double dt, int* __restrict__ queue) {
+                                                           double dt, int* __restrict__ queue, int last_cap) {
   __shared__ Smem S;
-  __shared__ int s_last[CP_SMEM_LEVEL_BODIES];
+  extern __shared__ int2 s_dyn[];
+  int2* s_pairs = s_dyn;
+  int* s_last = (int*)(s_dyn + CP_LEVEL_CHUNK);
   if (threadIdx.x < CP_NUM_PHASES) S.t_acc[threadIdx.x] = 0;
   if (threadIdx.x < 16) { S.r_cyc[threadIdx.x] = 0; S.r_cnt[threadIdx.x] = 0; }
   for (;;) {
@@ -1391,7 +1511,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step_pre(const DWorld* __rest
     }
     __syncthreads();
     if (S.P.status == 0 && S.P.stepnumber < S.P.step_limit) {
-      bool ok = step_pre(S, s_last, dt);
+      bool ok = step_pre(S, s_last, last_cap, s_pairs, dt);
       if (threadIdx.x == 0) {
         DWorldParams* gp = S.W.P;
         gp->num_pairs = S.n_pairs;
@@ -1466,6 +1586,186 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step_solve(const DWorld* __re
     }
   }
   if (threadIdx.x == 6 || threadIdx.x == 7) atomicAdd(&g_phase_cycles[threadIdx.x], (unsigned long long)S.t_acc[threadIdx.x]);
+}
+
+// ---------------------------------------------------------------------------
+// Kernel 2, warp-centric form.  Every warp takes a pool of up to
+// CP_GROUP_MAX worlds from the queue and runs their GSSolver sweeps with no
+// block barrier: each round fills the warp's 32 lanes with rows from the
+// current level of any of its worlds (rows of one level of one world share
+// no dynamic body, and rows of different worlds share nothing), and a world
+// moves on to its next level, or its next sweep, as soon as its current
+// level is done.  Every world still sees its rows level by level, sweep by
+// sweep, so results are those of the block form; the warp's lanes stay busy
+// instead of waiting for the slowest level of a block.
+#define WS_MAX_ROUNDS (1 << 26)
+
+template <int WARPS, int MINB>
+__global__ void __launch_bounds__(WARPS * 32, MINB) k_step_solve_w(const DWorld* __restrict__ worlds, const int* __restrict__ ids,
+                                                                  const int* __restrict__ gstart, int ngroups, double dt,
+                                                                  int* __restrict__ queue) {
+  __shared__ Slot s_slot[WARPS][CP_GROUP_MAX];
+  __shared__ int s_cur[WARPS][CP_GROUP_MAX];    // next level position to hand out
+  __shared__ int s_end[WARPS][CP_GROUP_MAX];    // end of the current level
+  __shared__ int s_lev[WARPS][CP_GROUP_MAX];    // current level
+  __shared__ int s_sweep[WARPS][CP_GROUP_MAX];  // current sweep
+  __shared__ int s_live[WARPS][CP_GROUP_MAX];   // 1: sweeping, 2: sweep just finished, 0: done
+  const unsigned FULL = 0xffffffffu;
+  const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Slot* sl = s_slot[wp];
+  int* cur = s_cur[wp];
+  int* end = s_end[wp];
+  int* lev = s_lev[wp];
+  int* swp = s_sweep[wp];
+  int* live = s_live[wp];
+  for (;;) {
+    int g = 0;
+    if (lane == 0) g = atomicAdd(queue, 1);
+    g = __shfl_sync(FULL, g, 0);
+    if (g >= ngroups) break;
+    const int k0 = gstart[g];
+    int K = gstart[g + 1] - k0;
+    if (!index_ok(7, -1, K - 1, CP_GROUP_MAX)) K = 0;
+    if (lane < K) {
+      Slot& t = sl[lane];
+      t.id = ids[k0 + lane];
+      t.W = worlds[t.id];
+      t.P = *t.W.P;
+      t.ok = t.P.status == 0 && t.P.stepnumber < t.P.step_limit;
+      t.n_rows = t.ok ? t.P.num_rows : 0;
+      t.n_levels = t.P.num_levels;
+      t.iters = 0;
+      int run = t.n_rows > 0 && t.P.iterations > 0 && t.n_levels > 0;
+      int b = 0, e = 0;
+      if (run) {
+        b = t.W.level_start[0];
+        e = t.W.level_start[1];
+        if (!index_ok(1, t.id, b, t.n_rows) || !index_ok(2, t.id, e - 1 - b, t.n_rows - b)) run = 0;
+      }
+      live[lane] = run;
+      lev[lane] = 0;
+      swp[lane] = 0;
+      cur[lane] = b;
+      end[lane] = e;
+    }
+    __syncwarp();
+    double part[CP_GROUP_MAX];
+#pragma unroll
+    for (int k = 0; k < CP_GROUP_MAX; k++) part[k] = 0.0;
+    for (int round = 0;; round++) {
+      // rows on offer: the rest of every live world's current level
+      int pre[CP_GROUP_MAX + 1];
+      pre[0] = 0;
+#pragma unroll
+      for (int k = 0; k < CP_GROUP_MAX; k++) pre[k + 1] = pre[k] + ((k < K && live[k] == 1) ? end[k] - cur[k] : 0);
+      const int total = pre[CP_GROUP_MAX];
+      if (total == 0) break;
+      if (round >= WS_MAX_ROUNDS) {
+        index_ok(8, sl[0].id, round, WS_MAX_ROUNDS);
+        break;
+      }
+      if (lane < total) {
+        int k = 0;
+        while (k < K - 1 && lane >= pre[k + 1]) k++;
+        const Slot& t = sl[k];
+        const DWorld& W = t.W;
+        const int p = cur[k] + lane - pre[k];
+        if (index_ok(3, t.id, p, t.n_rows)) {
+          const int r = W.sw_orig[p];
+          const int2 bb = W.sw_b[p];
+          if (index_ok(4, t.id, r, t.n_rows) && index_ok(5, t.id, bb.x, t.P.nb) && index_ok(6, t.id, bb.y, t.P.nb)) {
+            const double a = gs_row_sw(W, p, bb);
+            W.absdl[r] = a;
+#pragma unroll
+            for (int kk = 0; kk < CP_GROUP_MAX; kk++)
+              if (kk == k) part[kk] += a;
+          }
+        }
+      }
+      __syncwarp();
+      // the lanes took the first 32 rows on offer
+      if (lane < K && live[lane] == 1) {
+        const int k = lane;
+        const int take = min(end[k] - cur[k], max(0, 32 - pre[k]));
+        cur[k] += take;
+        if (cur[k] == end[k]) {
+          const Slot& t = sl[k];
+          if (lev[k] + 1 < t.n_levels) {
+            lev[k]++;
+            const int e = t.W.level_start[lev[k] + 1];
+            if (index_ok(2, t.id, e - 1 - cur[k], t.n_rows - cur[k])) end[k] = e;
+            else live[k] = 0;
+          } else {
+            live[k] = 2;
+          }
+        }
+      }
+      __syncwarp();
+      // worlds whose sweep just ended: (sum of |dlambda| in row order)^2 <
+      // tol^2, decided by the warp sum unless it lies within the rounding
+      // band of the threshold (then by the ordered sum)
+#pragma unroll
+      for (int k = 0; k < CP_GROUP_MAX; k++) {
+        if (k < K && live[k] == 2) {
+          double v = part[k];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+          part[k] = 0.0;
+          if (lane == 0) {
+            Slot& t = sl[k];
+            const int nrows = t.n_rows;
+            const double tol2 = t.P.tolerance * t.P.tolerance;
+            const double band = 2.2 * (double)nrows * 1.1102230246251565e-16;
+            const double hi = v * (1.0 + band), lo = v * (1.0 - band);
+            int conv;
+            if (hi * hi * (1.0 + 4.5e-16) < tol2) conv = 1;
+            else if (lo * lo * (1.0 - 4.5e-16) >= tol2 && lo >= 0.0) conv = 0;
+            else {
+              double sum = 0.0;
+              for (int r = 0; r < nrows; r++) sum += t.W.absdl[r];
+              conv = sum * sum < tol2;
+            }
+            const int sweep = swp[k];
+            if (conv) {
+              live[k] = 0;
+              t.iters = sweep;
+            } else if (sweep + 1 >= t.P.iterations) {
+              live[k] = 0;
+              t.iters = t.P.iterations;
+            } else {
+              swp[k] = sweep + 1;
+              lev[k] = 0;
+              cur[k] = t.W.level_start[0];
+              end[k] = t.W.level_start[1];
+              live[k] = 1;
+            }
+          }
+          __syncwarp();
+        }
+      }
+    }
+    // velocities, multipliers, integration and sleep of each world
+    const double invDt = 1 / dt;
+    for (int k = 0; k < K; k++) {
+      const Slot& t = sl[k];
+      if (!t.ok) continue;
+      const DWorld& W = t.W;
+      if (t.n_rows > 0) {
+        for (int i = lane; i < t.P.nb; i += 32) apply_body(W, i);
+        for (int p = lane; p < t.n_rows; p += 32) apply_row(W, p, invDt);
+      }
+      __syncwarp();
+      const bool qn = (t.P.stepnumber % (long long)(t.P.qn_skip + 1)) == 0;
+      for (int i = lane; i < t.P.nb; i += 32) integrate_body(W, t.P, i, dt, qn, t.P.time);
+      if (lane == 0) {
+        DWorldParams* gp = W.P;
+        gp->last_iterations = t.iters;
+        gp->stepnumber = t.P.stepnumber + 1;
+        gp->time = t.P.time + dt;
+      }
+      __syncwarp();
+    }
+  }
 }
 
 __global__ void k_gather_status(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n, long long* out) {
@@ -1597,7 +1897,7 @@ cudaError_t cpk_phase_cycles(unsigned long long* out, bool reset) {
 // that hide each other's waits, differs between them.  All compute
 // identical results.
 struct PreVariant {
-  void (*fn)(const DWorld*, const int*, int, double, int*);
+  void (*fn)(const DWorld*, const int*, int, double, int*, int);
   int threads;
   int minb;
 };
@@ -1605,14 +1905,16 @@ struct SolveVariant {
   void (*fn)(const DWorld*, const int*, const int*, int, double, int*);
   int threads;
   int minb;
+  int per_warp;  // each warp takes its own group (k_step_solve_w)
 };
 static const PreVariant kPre[] = {
     {k_step_pre<256, 1>, 256, 1}, {k_step_pre<128, 2>, 128, 2}, {k_step_pre<128, 4>, 128, 4},
     {k_step_pre<64, 8>, 64, 8},   {k_step_pre<256, 2>, 256, 2}, {k_step_pre<32, 16>, 32, 16},
 };
 static const SolveVariant kSolve[] = {
-    {k_step_solve<128, 4>, 128, 4}, {k_step_solve<128, 8>, 128, 8}, {k_step_solve<256, 4>, 256, 4},
-    {k_step_solve<32, 32>, 32, 32},
+    {k_step_solve<128, 4>, 128, 4, 0},     {k_step_solve<128, 8>, 128, 8, 0},     {k_step_solve<256, 4>, 256, 4, 0},
+    {k_step_solve<32, 32>, 32, 32, 0},     {k_step_solve<64, 16>, 64, 16, 0},     {k_step_solve_w<4, 4>, 128, 4, 1},
+    {k_step_solve_w<4, 8>, 128, 8, 1},     {k_step_solve_w<8, 4>, 256, 4, 1},
 };
 static const int kNumPre = sizeof(kPre) / sizeof(kPre[0]);
 static const int kNumSolve = sizeof(kSolve) / sizeof(kSolve[0]);
@@ -1623,14 +1925,31 @@ int cpk_num_solve_variants() { return kNumSolve; }
 
 int cpk_variant_threads(int v) { return kPre[v / kNumSolve].threads; }
 int cpk_solve_threads(int v) { return kSolve[v % kNumSolve].threads; }
+int cpk_solve_group_limit(int v, int group_bodies) {
+  const SolveVariant& V = kSolve[v % kNumSolve];
+  return V.per_warp ? group_bodies : (int)((long long)group_bodies * V.threads / 128);
+}
+
+// body capacity of the pre kernel's shared level table for a launch whose
+// largest world has max_nb bodies, and the dynamic shared memory it takes
+static int last_cap_for(int max_nb) { return max_nb < 1 ? 1 : (max_nb < CP_SMEM_LEVEL_MAX ? max_nb : CP_SMEM_LEVEL_MAX); }
+static size_t pre_smem(int last_cap) { return sizeof(int2) * CP_LEVEL_CHUNK + sizeof(int) * (size_t)last_cap; }
+
+int cpk_pre_blocks_per_sm(int variant, int max_nb) {
+  const PreVariant& P = kPre[variant / kNumSolve];
+  int b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, P.fn, P.threads, pre_smem(last_cap_for(max_nb)));
+  return b < 1 ? 1 : b;
+}
 
 cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, const int* d_gstart, int ngroups, double dt, int* d_queue,
-                            int grid_pre, int grid_solve, cudaStream_t stream, int variant, int n) {
+                            int grid_pre, int grid_solve, cudaStream_t stream, int variant, int n, int max_nb) {
   cudaError_t e = cudaMemsetAsync(d_queue, 0, 2 * sizeof(int), stream);
   if (e != cudaSuccess) return e;
   const PreVariant& P = kPre[variant / kNumSolve];
   const SolveVariant& V = kSolve[variant % kNumSolve];
-  P.fn<<<grid_pre, P.threads, 0, stream>>>(d_worlds, d_ids, n, dt, d_queue);
+  const int cap = last_cap_for(max_nb);
+  P.fn<<<grid_pre, P.threads, pre_smem(cap), stream>>>(d_worlds, d_ids, n, dt, d_queue, cap);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   V.fn<<<grid_solve, V.threads, 0, stream>>>(d_worlds, d_ids, d_gstart, ngroups, dt, d_queue + 1);
@@ -1642,6 +1961,6 @@ void cpk_max_resident_blocks(int variant, int* pre, int* solve) {
   const SolveVariant& V = kSolve[variant % kNumSolve];
   *pre = 0;
   *solve = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(pre, P.fn, P.threads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(pre, P.fn, P.threads, pre_smem(last_cap_for(512)));
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(solve, V.fn, V.threads, 0);
 }

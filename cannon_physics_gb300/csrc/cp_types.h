@@ -10,6 +10,8 @@
 #pragma once
 #include <cstdint>
 
+#include <vector_types.h>
+
 #include "../../include/cannon_gpu.h"
 
 #define CP_MAX_HULL_VERTS 32
@@ -115,10 +117,10 @@ struct __align__(16) DContact {
 };
 
 // A solver row.  The Jacobian entries are binary32 values (JacobianElement
-// stores Vector3s) held exactly in binary64, so the sweeps need no conversions.
+// stores Vector3s).
 struct __align__(16) DRow {
-  double gaS[3], gaR[3], gbS[3], gbR[3];
-  double iMaR[3], iMbR[3];  // invInertiaWorldSolve * rotational Jacobians (the addToWlambda temp)
+  float gaS[4], gaR[4], gbS[4], gbR[4];
+  float iMaR[4], iMbR[4];  // invInertiaWorldSolve * rotational Jacobians (the addToWlambda temp)
   double B, invC, eps, minF, maxF, lambda;
   double imA, imB;          // invMassSolve of bi, bj
   double mult;              // Equation.multiplier = lambda / h
@@ -182,6 +184,7 @@ struct DWorld {
   int* pair_cnt;
   int* pair_tstart;
   int* heavy;
+  int* heavy2;      // heavy pairs sorted by resolver kind (pairs + 16 * 32 slots)
   DContact* ctmp;
   DContact* contacts;
   int* cscr;       // per-contact scratch (contacts_cap + 1)
@@ -200,4 +203,15 @@ struct DWorld {
   long long* hkeys;  // pair de-duplication hash (hash_cap)
   int* hvals;
   int hash_cap;
+  // The solver rows again, in level order (position p = rank of the row in
+  // level_rows) and as separate arrays, so that the threads sweeping a level
+  // read consecutive memory: sw_j[f * sw_cap + p], f < 5, the 18 binary32
+  // Jacobian values (gaS, gaR, gbS, gbR, iMaR, iMbR); sw_d[f * sw_cap + p],
+  // f < 4: (B, invC), (eps, lambda), (imA, imB), (minF, maxF); sw_b: (bi, bj);
+  // sw_orig: the row index.
+  float4* sw_j;
+  double2* sw_d;
+  int2* sw_b;
+  int* sw_orig;
+  int sw_cap;
 };

@@ -259,7 +259,7 @@ int cp_world_step(cp_ctx* ctx, int32_t world_id, double dt, int32_t nsteps);
  * Limits:
  *  - A world whose lists, at its current capacities, need more than that
  *    array is rejected with CP_ERR_CAPACITY before anything runs.  This is
- *    roughly 8 KB per body: a 4096-body world fits, 10,000 bodies do not.
+ *    roughly 11 KB per body: a 4096-body world fits, 10,000 bodies do not.
  *  - A step that overflows a capacity is not regrown.  The world's bodies
  *    are left as they were at the start of that step (only their cached
  *    AABBs may be refreshed), its status is cleared, and the call returns
