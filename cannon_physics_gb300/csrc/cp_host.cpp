@@ -1558,6 +1558,15 @@ int cp_phase_profile(cp_ctx* c, double* cycles, int32_t n) {
   return CP_OK;
 }
 
+int cp_set_resolver_profile(cp_ctx* c, int32_t on) {
+  if (!c) return fail(CP_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  CUDA_TRY(cpk_set_resolver_profile(on));
+  return CP_OK;
+}
+
 int cp_set_group_bodies(cp_ctx* c, int32_t bodies) {
   if (!c || bodies < 0) return fail(CP_ERR_ARG, "bad group size");
   std::lock_guard<std::mutex> lock(c->mu);

@@ -43,6 +43,7 @@ cudaError_t cpk_gather_poses(const DWorld* d_worlds, const int* d_ids, const lon
 // per-resolver call counts (slots 10..12: pairs settled by a binary32
 // no-contact certificate for sphere-plane, plane-hull, sphere-box)
 cudaError_t cpk_phase_cycles(unsigned long long* out, bool reset);
+cudaError_t cpk_set_resolver_profile(int on);
 // Address and size of the static step scratch on `device`, which must be the
 // current device; the first call per device looks the address up.
 #define CP_MAX_DEVICES 64

@@ -90,67 +90,106 @@ DI int sphere_plane(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rs
   return 1;
 }
 
-// narrow_phase.dart:816-1038 (box.dart:99-115 for the side vectors)
+// binary32 helpers of the no-contact tests and plans (approximate: every
+// use carries an error margin)
+DI f3 rot32(q4 q, f3 v) {  // binary32 rotation (approximate)
+  float ix = q.w * v.x + q.y * v.z - q.z * v.y;
+  float iy = q.w * v.y + q.z * v.x - q.x * v.z;
+  float iz = q.w * v.z + q.x * v.y - q.y * v.x;
+  float iw = -q.x * v.x - q.y * v.y - q.z * v.z;
+  return f3{ix * q.w - iw * q.x - iy * q.z + iz * q.y, iy * q.w - iw * q.y - iz * q.x + ix * q.z,
+            iz * q.w - iw * q.z - ix * q.y + iy * q.x};
+}
+DI float dot32(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+DI float len32(f3 a) { return sqrtf(dot32(a, a)); }
+
+// True when the sphere clearly misses the box, decided in binary32.  Every
+// branch of the reference's sphereBox that makes a contact puts a point of the
+// box (a side point with |d1| < h1, |d2| < h2, a corner, or an edge point with
+// |t| < h) within R of the sphere centre, so a centre farther than R + E from
+// the box makes none.  The binary32 distance differs from the exact one by a
+// few ulps of the box size, of |b2s| and of the positions; E is a wide margin
+// over all three.
+DI bool sphere_box_far(f3 xA, float R, f3 xB, q4 qB, const float* he) {
+  const f3 b2s = f3{xA.x - xB.x, xA.y - xB.y, xA.z - xB.z};
+  const f3 p = rot32(q4{-qB.x, -qB.y, -qB.z, qB.w}, b2s);  // centre in the box frame
+  const float E = 1e-4f * (R + he[0] + he[1] + he[2] + fabsf(b2s.x) + fabsf(b2s.y) + fabsf(b2s.z)) +
+                  4e-7f * (fabsf(xA.x) + fabsf(xA.y) + fabsf(xA.z) + fabsf(xB.x) + fabsf(xB.y) + fabsf(xB.z)) + 1e-6f;
+  const float ox = fmaxf(fabsf(p.x) - he[0], 0.f), oy = fmaxf(fabsf(p.y) - he[1], 0.f), oz = fmaxf(fabsf(p.z) - he[2], 0.f);
+  const float lim = R + E;
+  return ox * ox + oy * oy + oz * oz > lim * lim;
+}
+
+DI f3 sb_side(const DShape& sb, q4 qB, int idx) {
+  const int a = idx % 3;
+  const float s = idx < 3 ? 1.f : -1.f;
+  return vmult(qB, f3{a == 0 ? s * sb.he[0] : 0.f, a == 1 ? s * sb.he[1] : 0.f, a == 2 ? s * sb.he[2] : 0.f});
+}
+
+// Narrowphase.sphereBox (narrow_phase.dart:816-1038), reached for pairs that
+// sphere_box_far does not settle: the reference's binary64 evaluation, with
+// one exact shortcut in the side test: side 3 + a is side a
+// negated (vmult is odd in its vector and round-to-nearest is symmetric) up to
+// the signs of zero components, so its length is that of side a and its dot
+// product with b2s is the negated one (or a zero, which the test treats alike);
+// the test needs three rotations, three lengths, three normals and three dot
+// products (which are also the reference's d1, d2).
 // one out-of-line copy: the resolver is large and is reached from several
 // dispatch cases; inlining it at each bloats the step kernel's instruction footprint
 __device__ __noinline__ int sphere_box(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
   const DWorld& W = *C.W;
   const DShape& sb = W.shapes[shB];
-  double R = W.shapes[shA].radius;
-  f3 sides[6];
-  sides[0] = vmult(qB, f3{sb.he[0], 0.f, 0.f});
-  sides[1] = vmult(qB, f3{0.f, sb.he[1], 0.f});
-  sides[2] = vmult(qB, f3{0.f, 0.f, sb.he[2]});
-  sides[3] = vmult(qB, f3{-sb.he[0], 0.f, 0.f});
-  sides[4] = vmult(qB, f3{0.f, -sb.he[1], 0.f});
-  sides[5] = vmult(qB, f3{0.f, 0.f, -sb.he[2]});
-  f3 b2s = sub(xA, xB);
-  f3 sideNs{0, 0, 0}, sideNs1{0, 0, 0}, sideNs2{0, 0, 0};
-  double sideH = 0, sideDot1 = 0, sideDot2 = 0, sideDist = 0;
-  bool haveDist = false;
-  int sidePen = 0;
+  const double R = W.shapes[shA].radius;
+  const f3 b2s = sub(xA, xB);
+  f3 sd[3], nrm[3];
+  double hl[3], pd[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    sd[a] = sb_side(sb, qB, a);
+    hl[a] = length(sd[a]);
+    nrm[a] = normalized(sd[a]);
+    pd[a] = dot(b2s, nrm[a]);
+  }
+  // sides: the penetrating side of smallest |d - h - R|, the first on ties
+  int best = -1;
+  double bestDist = 0;
   for (int idx = 0; idx < 6; idx++) {
-    f3 ns = sides[idx];
-    double h = length(ns);
-    ns = normalized(ns);
-    double d = dot(b2s, ns);
-    if (d < h + R && d > 0) {
-      f3 ns1 = sides[(idx + 1) % 3], ns2 = sides[(idx + 2) % 3];
-      double h1 = length(ns1), h2 = length(ns2);
-      ns1 = normalized(ns1);
-      ns2 = normalized(ns2);
-      double d1 = dot(b2s, ns1), d2 = dot(b2s, ns2);
-      if (d1 < h1 && d1 > -h1 && d2 < h2 && d2 > -h2) {
-        double dist = fabs(d - h - R);
-        if (!haveDist || dist < sideDist) {
-          haveDist = true;
-          sideDist = dist; sideDot1 = d1; sideDot2 = d2; sideH = h;
-          sideNs = ns; sideNs1 = ns1; sideNs2 = ns2;
-          sidePen++;
-        }
+    const int ax = idx % 3;
+    const double h = hl[ax], d = idx < 3 ? pd[ax] : -pd[ax];
+    if (!(d < h + R && d > 0)) continue;
+    const int i1 = (idx + 1) % 3, i2 = (idx + 2) % 3;
+    const double d1 = pd[i1], d2 = pd[i2], h1 = hl[i1], h2 = hl[i2];
+    if (d1 < h1 && d1 > -h1 && d2 < h2 && d2 > -h2) {
+      const double dist = fabs(d - h - R);
+      if (best < 0 || dist < bestDist) {
+        best = idx;
+        bestDist = dist;
       }
     }
   }
   ContactOut g;
   bool found = false;
-  if (sidePen != 0) {
+  if (best >= 0) {
     found = true;
-    g.ri = scale(sideNs, -R);
-    g.ni = neg(sideNs);
-    f3 t = scale(sideNs, sideH);
-    f3 t1 = scale(sideNs1, sideDot1);
-    t = add(t, t1);
-    f3 t2 = scale(sideNs2, sideDot2);
-    g.rj = add(t, t2);
+    const int ax = best % 3, i1 = (best + 1) % 3, i2 = (best + 2) % 3;
+    // side 3 + a is rotated from (-h, +0, +0) etc.: its zero components
+    // need not be the negated ones of side a, so it is formed as the
+    // reference forms it
+    const f3 ns = best < 3 ? nrm[ax] : normalized(sb_side(sb, qB, best));
+    g.ri = scale(ns, -R);
+    g.ni = neg(ns);
+    f3 t = scale(ns, hl[ax]);
+    t = add(t, scale(nrm[i1], pd[i1]));
+    g.rj = add(t, scale(nrm[i2], pd[i2]));
   }
   for (int j = 0; j != 2 && !found; j++)
     for (int k = 0; k != 2 && !found; k++)
       for (int l = 0; l != 2 && !found; l++) {
         f3 rj{0.f, 0.f, 0.f};
-        rj = j != 0 ? add(rj, sides[0]) : sub(rj, sides[0]);
-        rj = k != 0 ? add(rj, sides[1]) : sub(rj, sides[1]);
-        rj = l != 0 ? add(rj, sides[2]) : sub(rj, sides[2]);
-        f3 s2c = sub(add(xB, rj), xA);
+        rj = j != 0 ? add(rj, sd[0]) : sub(rj, sd[0]);
+        rj = k != 0 ? add(rj, sd[1]) : sub(rj, sd[1]);
+        rj = l != 0 ? add(rj, sd[2]) : sub(rj, sd[2]);
+        const f3 s2c = sub(add(xB, rj), xA);
         if (length2(s2c) < R * R) {
           found = true;
           g.ri = normalized(s2c);
@@ -159,24 +198,28 @@ __device__ __noinline__ int sphere_box(const NarrowCtx& C, int bA, int bB, int s
           g.rj = rj;
         }
       }
+  f3 sdn[3];
+  if (!found)
+    for (int a = 0; a < 3; a++) sdn[a] = sb_side(sb, qB, 3 + a);
   for (int j = 0; j != 6 && !found; j++)
     for (int k = 0; k != 6 && !found; k++) {
       if (j % 3 != k % 3) {
-        f3 edgeTangent = normalized(cross(sides[k], sides[j]));
-        f3 edgeCenter = add(sides[j], sides[k]);
-        f3 r = sub(sub(xA, edgeCenter), xB);
-        double orthonorm = dot(r, edgeTangent);
-        f3 orthogonal = scale(edgeTangent, orthonorm);
+        const f3 sj = j < 3 ? sd[j] : sdn[j - 3], sk = k < 3 ? sd[k] : sdn[k - 3];
+        const f3 edgeTangent = normalized(cross(sk, sj));
+        const f3 edgeCenter = add(sj, sk);
+        const f3 r = sub(sub(xA, edgeCenter), xB);
+        const double orthonorm = dot(r, edgeTangent);
+        const f3 orthogonal = scale(edgeTangent, orthonorm);
         int l = 0;
         while (l == j % 3 || l == k % 3) l++;
-        f3 dist = sub(sub(sub(xA, orthogonal), edgeCenter), xB);
-        double tdist = fabs(orthonorm);
-        double ndist = length(dist);
-        if (tdist < length(sides[l]) && ndist < R) {
+        const f3 dist = sub(sub(sub(xA, orthogonal), edgeCenter), xB);
+        const double tdist = fabs(orthonorm);
+        const double ndist = length(dist);
+        if (tdist < hl[l] && ndist < R) {
           found = true;
           g.rj = add(edgeCenter, orthogonal);
           g.ni = normalized(neg(dist));
-          f3 ri = sub(add(g.rj, xB), xA);
+          const f3 ri = sub(add(g.rj, xB), xA);
           g.ri = scale(normalized(ri), R);
         }
       }
@@ -327,16 +370,6 @@ __device__ __noinline__ int plane_convex(const NarrowCtx& C, int bA, int bB, int
 // 1e-4 (the binary32 estimate is within ~1e-6 of the binary64 values), so the
 // exact resolver, which would return no contacts, can be skipped.
 
-DI f3 rot32(q4 q, f3 v) {  // binary32 rotation (approximate)
-  float ix = q.w * v.x + q.y * v.z - q.z * v.y;
-  float iy = q.w * v.y + q.z * v.x - q.x * v.z;
-  float iz = q.w * v.z + q.x * v.y - q.y * v.x;
-  float iw = -q.x * v.x - q.y * v.y - q.z * v.z;
-  return f3{ix * q.w - iw * q.x - iy * q.z + iz * q.y, iy * q.w - iw * q.y - iz * q.x + ix * q.z,
-            iz * q.w - iw * q.z - ix * q.y + iy * q.x};
-}
-DI float dot32(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-DI float len32(f3 a) { return sqrtf(dot32(a, a)); }
 
 // plane (xP, qP) vs a body whose shape lies within distance rB of xB: a
 // contact needs a point of the shape on or behind the plane
@@ -347,18 +380,6 @@ DI bool plane_far(f3 xP, q4 qP, f3 xB, float rB) {
   float h = dot32(n, d);
   float margin = 1e-4f * (rB + fabsf(d.x) + fabsf(d.y) + fabsf(d.z)) + 1e-6f;
   return h > rB + margin;
-}
-
-// sphere (center c, radius R) vs box: every contact sphereBox makes (side,
-// corner or edge, narrow_phase.dart:852-1034) has the sphere center closer
-// than R to the box
-DI bool sphere_box_far(f3 c, float R, f3 xB, q4 qB, const float* he) {
-  f3 d = f3{c.x - xB.x, c.y - xB.y, c.z - xB.z};
-  f3 p = rot32(q4{-qB.x, -qB.y, -qB.z, qB.w}, d);
-  float ox = fmaxf(fabsf(p.x) - he[0], 0.f), oy = fmaxf(fabsf(p.y) - he[1], 0.f), oz = fmaxf(fabsf(p.z) - he[2], 0.f);
-  float dist = sqrtf(ox * ox + oy * oy + oz * oz);
-  float margin = 1e-4f * (R + he[0] + he[1] + he[2] + fabsf(d.x) + fabsf(d.y) + fabsf(d.z)) + 1e-6f;
-  return dist > R + margin;
 }
 
 // Resolver choice of narrow_phase.dart:116-238,476-489,706-710.  The shape

@@ -29,9 +29,12 @@
 // Per-phase SM cycles summed over blocks (World.profile's breakdown,
 // world_class.dart:27-41); read with cp_phase_profile.
 __device__ unsigned long long g_phase_cycles[CP_NUM_PHASES];
-// per narrowphase resolver kind: summed thread cycles and calls
+// per narrowphase resolver kind: summed thread cycles and calls, counted
+// only while g_res_profile is set (cpk_set_resolver_profile): the per-pair
+// shared-memory atomics cost a few per cent of a step
 __device__ unsigned long long g_res_cycles[16];
 __device__ unsigned long long g_res_calls[16];
+__device__ int g_res_profile;
 
 struct __align__(16) Smem {
   long long t_last;
@@ -42,6 +45,7 @@ struct __align__(16) Smem {
   DWorldParams P;
   int warp[32];
   double dwarp[32];
+  int rprof;  // g_res_profile at kernel start
   int n_pairs, n_contacts, n_heavy, n_rows;
   int n_fric, n_cand, n_levels, cursor;
   int overflow, converged, wi, pad;
@@ -658,13 +662,16 @@ DI void narrow_pair(Smem& S, int k, bool heavy_pass) {
     int shA = swap ? bj.shape : bi.shape, shB = swap ? bi.shape : bj.shape;
     f3 xA = swap ? xj : xi, xB = swap ? xi : xj;
     q4 qA = swap ? qj : qi, qB = swap ? qi : qj;
-    const long long t_res = clock64();
+    const bool rprof = S.rprof != 0;
+    const long long t_res = rprof ? clock64() : 0;
     // binary32 no-contact certificates (see cp_narrow.cuh)
     if ((rk == RK_SP && plane_far(xB, qB, xA, (float)W.shapes[shA].radius)) ||
         ((rk == RK_PB || rk == RK_PC) && plane_far(xA, qA, xB, (float)W.shapes[shB].bsr)) ||
         (rk == RK_SB && sphere_box_far(xA, (float)W.shapes[shA].radius, xB, qB, W.shapes[shB].he))) {
-      atomicAdd(&S.r_cyc[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], (unsigned long long)(clock64() - t_res));
-      atomicAdd(&S.r_cnt[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], 1u);
+      if (rprof) {
+        atomicAdd(&S.r_cyc[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], (unsigned long long)(clock64() - t_res));
+        atomicAdd(&S.r_cnt[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], 1u);
+      }
       break;
     }
     switch (rk) {
@@ -678,8 +685,10 @@ DI void narrow_pair(Smem& S, int k, bool heavy_pass) {
       case RK_BC: cnt = convex_convex(C, bA, bB, shA, shB, shA, shB, xA, xB, qA, qB, start); break;
       default: cnt = convex_convex(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qA, qB, start); break;
     }
-    atomicAdd(&S.r_cyc[rk], (unsigned long long)(clock64() - t_res));
-    atomicAdd(&S.r_cnt[rk], 1u);
+    if (rprof) {
+      atomicAdd(&S.r_cyc[rk], (unsigned long long)(clock64() - t_res));
+      atomicAdd(&S.r_cnt[rk], 1u);
+    }
   } while (0);
   W.pair_cnt[k] = cnt;
   W.pair_tstart[k] = start;
@@ -1500,6 +1509,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step_pre(const DWorld* __rest
   int* s_last = (int*)(s_dyn + CP_LEVEL_CHUNK);
   if (threadIdx.x < CP_NUM_PHASES) S.t_acc[threadIdx.x] = 0;
   if (threadIdx.x < 16) { S.r_cyc[threadIdx.x] = 0; S.r_cnt[threadIdx.x] = 0; }
+  if (threadIdx.x == 0) S.rprof = *(volatile int*)&g_res_profile;
   for (;;) {
     if (threadIdx.x == 0) S.wi = atomicAdd(queue, 1);
     __syncthreads();
@@ -1524,7 +1534,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step_pre(const DWorld* __rest
     __syncthreads();
   }
   if (threadIdx.x < CP_NUM_PHASES) atomicAdd(&g_phase_cycles[threadIdx.x], (unsigned long long)S.t_acc[threadIdx.x]);
-  if (threadIdx.x < 16) {
+  if (threadIdx.x < 16 && S.rprof) {
     atomicAdd(&g_res_cycles[threadIdx.x], S.r_cyc[threadIdx.x]);
     atomicAdd(&g_res_calls[threadIdx.x], (unsigned long long)S.r_cnt[threadIdx.x]);
   }
@@ -1890,6 +1900,11 @@ cudaError_t cpk_phase_cycles(unsigned long long* out, bool reset) {
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_res_calls, z, sizeof(z));
   }
   return e;
+}
+
+cudaError_t cpk_set_resolver_profile(int on) {
+  const int v = on ? 1 : 0;
+  return cudaMemcpyToSymbol(g_res_profile, &v, sizeof(v));
 }
 
 // Kernel variants (block threads, minimum resident blocks per SM) for each

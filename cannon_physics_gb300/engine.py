@@ -53,6 +53,7 @@ def lib():
         L.cp_get_stream.argtypes = [vp, vp]
         L.cp_batch_profile.argtypes = [vp, vp, vp]
         L.cp_phase_profile.argtypes = [vp, vp, i32]
+        L.cp_set_resolver_profile.argtypes = [vp, i32]
         L.cp_autotune_info.argtypes = [vp, vp, vp, vp, i32]
         L.cp_set_variant.argtypes = [vp, i32]
         L.cp_set_group_bodies.argtypes = [vp, i32]
@@ -113,6 +114,10 @@ class Context:
             return ph
         res = {name: (out[8 + i], out[24 + i]) for i, name in enumerate(self.RESOLVERS) if name and out[24 + i] > 0}
         return ph, res
+
+    def resolver_profile(self, on=True):
+        """Count per-resolver cycles and calls (off by default; per device)."""
+        check(lib().cp_set_resolver_profile(self.h, int(bool(on))), "cp_set_resolver_profile")
 
     def set_group_bodies(self, n):
         check(lib().cp_set_group_bodies(self.h, n), "cp_set_group_bodies")

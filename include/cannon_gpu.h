@@ -342,8 +342,16 @@ int cp_set_variant(cp_ctx* ctx, int32_t variant);
  * it also writes 16 narrowphase-resolver thread-cycle sums and 16 call
  * counts (resolver kinds: 1 sphere-sphere, 2 sphere-plane, 3 sphere-box,
  * 4 sphere-convex, 5 plane-box, 6 plane-convex, 7 box-box, 8 box-convex,
- * 9 convex-convex; 10-12 pairs settled by a binary32 no-contact test). */
+ * 9 convex-convex; 10-12 pairs settled by a binary32 no-contact test);
+ * those are counted only while cp_set_resolver_profile is on. */
 int cp_phase_profile(cp_ctx* ctx, double* cycles, int32_t n);
+
+/* Turn the per-resolver cycle and call counts on (1) or off (0, the
+ * default).  The switch is per device, not per context: it applies to every
+ * step launched on the context's device afterwards.  Counting costs a few per
+ * cent of a step.  No counterpart in the reference (its World.profile has no
+ * per-resolver breakdown). */
+int cp_set_resolver_profile(cp_ctx* ctx, int32_t on);
 
 /* Batched path: worlds are handed to thread blocks in groups of consecutive
  * (similar-size) worlds holding up to `bodies` bodies (at most 8 worlds);
