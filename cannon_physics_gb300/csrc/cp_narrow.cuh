@@ -402,4 +402,3 @@ DI int resolver_kind(int ta, int tb) {  // ta <= tb
   if (ta == 2) return tb == 2 ? RK_BB : RK_BC;
   return RK_CC;
 }
-DI bool is_heavy(int rk) { return rk >= RK_BB; }

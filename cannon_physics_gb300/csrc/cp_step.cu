@@ -46,7 +46,7 @@ struct __align__(16) Smem {
   int warp[32];
   double dwarp[32];
   int rprof;  // g_res_profile at kernel start
-  int n_pairs, n_contacts, n_heavy, n_rows;
+  int n_pairs, n_contacts, n_queued, n_rows;
   int n_fric, n_cand, n_levels, cursor;
   int overflow, converged, wi, pad;
   int kcnt[16], kpos[16];  // narrowphase: heavy pairs per resolver kind, segment cursors
@@ -627,69 +627,118 @@ DI int contact_material(const DWorld& W, const DWorldParams& P, int ma, int mb) 
   return W.cm_table[ma * P.nmat + mb];
 }
 
-DI void narrow_pair(Smem& S, int k, bool heavy_pass) {
+// A pair with both shapes in place: the bodies, shapes and poses a resolver
+// takes, in the order narrow_phase.dart:706-710 calls it.
+struct PairJob {
+  NarrowCtx C;
+  int rsi, rsj, bA, bB, shA, shB;
+  f3 xA, xB;
+  q4 qA, qB;
+};
+
+// Resolver kind of pair k and its job; RK_NONE when the pair makes no
+// contact for a reason that needs no resolver (no shape, a kinematic/static
+// pair, no resolver for the shape types, the collision filter, the bounding
+// spheres, or a binary32 no-contact certificate).  With tests == false the
+// pair is known to have passed them and only the job is filled.
+DI int pair_job(Smem& S, int k, PairJob& X, bool tests) {
   const DWorld& W = S.W;
   const DWorldParams& P = S.P;
-  int i = W.pair_a[k], j = W.pair_b[k];
+  const int i = W.pair_a[k], j = W.pair_b[k];
   const DBody& bi = W.bodies[i];
   const DBody& bj = W.bodies[j];
-  int cnt = 0, start = 0;
-  bool just_test = (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_STATIC) ||
-                   (bi.type == CP_BODY_STATIC && bj.type == CP_BODY_KINEMATIC) ||
-                   (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_KINEMATIC);
-  do {
-    if (bi.shape < 0 || bj.shape < 0 || just_test) break;
-    const DShape& si = W.shapes[bi.shape];
-    const DShape& sj = W.shapes[bj.shape];
-    bool swap = !(si.type < sj.type);
-    int rk = swap ? resolver_kind(sj.type, si.type) : resolver_kind(si.type, sj.type);
-    if (rk == RK_NONE) break;
-    if (is_heavy(rk) != heavy_pass) {
-      if (!heavy_pass) W.heavy[atomicAdd(&S.n_heavy, 1)] = (int)(((unsigned)rk << 28) | (unsigned)k);  // k < 2^28
-      return;
-    }
-    if (!((si.mask & sj.group) != 0 && (sj.mask & si.group) != 0)) break;
-    f3 xi = ld3(W.bscr[i].xs), xj = ld3(W.bscr[j].xs);
-    q4 qi = ld4q(W.bscr[i].qs), qj = ld4q(W.bscr[j].qs);
-    if (distance_to(xi, xj) > si.bsr + sj.bsr) break;
-    int cm = contact_material(W, P, si.material, sj.material);
-    if (cm < 0) cm = contact_material(W, P, bi.material, bj.material);
-    if (cm < 0) cm = 0;
-    NarrowCtx C;
-    C.W = &W; C.cursor = &S.cursor; C.cap = P.contacts_cap; C.overflow = &S.overflow; C.cm = cm; C.pair = k;
-    int rsi = bi.shape, rsj = bj.shape;
-    int bA = swap ? j : i, bB = swap ? i : j;
-    int shA = swap ? bj.shape : bi.shape, shB = swap ? bi.shape : bj.shape;
-    f3 xA = swap ? xj : xi, xB = swap ? xi : xj;
-    q4 qA = swap ? qj : qi, qB = swap ? qi : qj;
-    const bool rprof = S.rprof != 0;
-    const long long t_res = rprof ? clock64() : 0;
+  if (tests) {
+    const bool just_test = (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_STATIC) ||
+                           (bi.type == CP_BODY_STATIC && bj.type == CP_BODY_KINEMATIC) ||
+                           (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_KINEMATIC);
+    if (bi.shape < 0 || bj.shape < 0 || just_test) return RK_NONE;
+  }
+  const DShape& si = W.shapes[bi.shape];
+  const DShape& sj = W.shapes[bj.shape];
+  const bool swap = !(si.type < sj.type);
+  const int rk = swap ? resolver_kind(sj.type, si.type) : resolver_kind(si.type, sj.type);
+  if (tests && rk == RK_NONE) return RK_NONE;
+  if (tests && !((si.mask & sj.group) != 0 && (sj.mask & si.group) != 0)) return RK_NONE;
+  const f3 xi = ld3(W.bscr[i].xs), xj = ld3(W.bscr[j].xs);
+  if (tests && distance_to(xi, xj) > si.bsr + sj.bsr) return RK_NONE;
+  const q4 qi = ld4q(W.bscr[i].qs), qj = ld4q(W.bscr[j].qs);
+  X.xA = swap ? xj : xi;
+  X.xB = swap ? xi : xj;
+  X.qA = swap ? qj : qi;
+  X.qB = swap ? qi : qj;
+  X.shA = swap ? bj.shape : bi.shape;
+  X.shB = swap ? bi.shape : bj.shape;
+  if (tests) {
     // binary32 no-contact certificates (see cp_narrow.cuh)
-    if ((rk == RK_SP && plane_far(xB, qB, xA, (float)W.shapes[shA].radius)) ||
-        ((rk == RK_PB || rk == RK_PC) && plane_far(xA, qA, xB, (float)W.shapes[shB].bsr)) ||
-        (rk == RK_SB && sphere_box_far(xA, (float)W.shapes[shA].radius, xB, qB, W.shapes[shB].he))) {
-      if (rprof) {
+    const long long t_res = S.rprof ? clock64() : 0;
+    if ((rk == RK_SP && plane_far(X.xB, X.qB, X.xA, (float)W.shapes[X.shA].radius)) ||
+        ((rk == RK_PB || rk == RK_PC) && plane_far(X.xA, X.qA, X.xB, (float)W.shapes[X.shB].bsr)) ||
+        (rk == RK_SB && sphere_box_far(X.xA, (float)W.shapes[X.shA].radius, X.xB, X.qB, W.shapes[X.shB].he))) {
+      if (S.rprof) {
         atomicAdd(&S.r_cyc[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], (unsigned long long)(clock64() - t_res));
         atomicAdd(&S.r_cnt[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], 1u);
       }
-      break;
+      return RK_NONE;
     }
-    switch (rk) {
-      case RK_SS: cnt = sphere_sphere(C, bA, bB, shA, shB, rsi, rsj, xA, xB, start); break;
-      case RK_SP: cnt = sphere_plane(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qB, start); break;
-      case RK_SB: cnt = sphere_box(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qB, start); break;
-      case RK_SC: cnt = sphere_convex(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qB, start); break;
-      case RK_PB: cnt = plane_convex(C, bA, bB, shA, shB, shA, shB, xA, xB, qA, qB, start); break;
-      case RK_PC: cnt = plane_convex(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qA, qB, start); break;
-      case RK_BB: cnt = convex_convex(C, bA, bB, shA, shB, shA, shB, xA, xB, qA, qB, start); break;
-      case RK_BC: cnt = convex_convex(C, bA, bB, shA, shB, shA, shB, xA, xB, qA, qB, start); break;
-      default: cnt = convex_convex(C, bA, bB, shA, shB, rsi, rsj, xA, xB, qA, qB, start); break;
-    }
-    if (rprof) {
-      atomicAdd(&S.r_cyc[rk], (unsigned long long)(clock64() - t_res));
-      atomicAdd(&S.r_cnt[rk], 1u);
-    }
-  } while (0);
+  }
+  int cm = contact_material(W, P, si.material, sj.material);
+  if (cm < 0) cm = contact_material(W, P, bi.material, bj.material);
+  if (cm < 0) cm = 0;
+  X.C.W = &W; X.C.cursor = &S.cursor; X.C.cap = P.contacts_cap; X.C.overflow = &S.overflow; X.C.cm = cm; X.C.pair = k;
+  X.rsi = bi.shape;
+  X.rsj = bj.shape;
+  X.bA = swap ? j : i;
+  X.bB = swap ? i : j;
+  return rk;
+}
+
+DI int run_resolver(Smem& S, int rk, const PairJob& X, int& start) {
+  const NarrowCtx& C = X.C;
+  const long long t_res = S.rprof ? clock64() : 0;
+  int cnt;
+  switch (rk) {
+    case RK_SS: cnt = sphere_sphere(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, start); break;
+    case RK_SP: cnt = sphere_plane(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, X.qB, start); break;
+    case RK_SB: cnt = sphere_box(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, X.qB, start); break;
+    case RK_SC: cnt = sphere_convex(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, X.qB, start); break;
+    case RK_PB: cnt = plane_convex(C, X.bA, X.bB, X.shA, X.shB, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, start); break;
+    case RK_PC: cnt = plane_convex(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, X.qA, X.qB, start); break;
+    case RK_BB: cnt = convex_convex(C, X.bA, X.bB, X.shA, X.shB, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, start); break;
+    case RK_BC: cnt = convex_convex(C, X.bA, X.bB, X.shA, X.shB, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, start); break;
+    default: cnt = convex_convex(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, X.qA, X.qB, start); break;
+  }
+  if (S.rprof) {
+    atomicAdd(&S.r_cyc[rk], (unsigned long long)(clock64() - t_res));
+    atomicAdd(&S.r_cnt[rk], 1u);
+  }
+  return cnt;
+}
+
+// First pass over pair k: settles it without a resolver, or queues it under
+// its resolver kind.  Queued pairs run grouped by kind, each kind's segment
+// starting on a warp boundary, so a warp runs one resolver with all its lanes
+// instead of interleaving several with a few lanes each (a binary64 warp
+// instruction costs the same with one active lane or 32); settling first
+// keeps the pairs that need no resolver out of those warps.
+DI void narrow_first(Smem& S, int k) {
+  const DWorld& W = S.W;
+  PairJob X;
+  const int rk = pair_job(S, k, X, true);
+  if (rk != RK_NONE) {
+    W.heavy[atomicAdd(&S.n_queued, 1)] = (int)(((unsigned)rk << 28) | (unsigned)k);  // k < 2^28
+    return;
+  }
+  W.pair_cnt[k] = 0;
+  W.pair_tstart[k] = 0;
+}
+
+// Queued pair k of kind rk (its tests passed in the first pass).
+DI void narrow_queued(Smem& S, int k, int rk) {
+  const DWorld& W = S.W;
+  PairJob X;
+  pair_job(S, k, X, false);
+  int start = 0;
+  const int cnt = run_resolver(S, rk, X, start);
   W.pair_cnt[k] = cnt;
   W.pair_tstart[k] = start;
 }
@@ -697,14 +746,13 @@ DI void narrow_pair(Smem& S, int k, bool heavy_pass) {
 DI void ph_narrow(Smem& S) {
   const DWorld& W = S.W;
   const int np = S.n_pairs;
-  if (threadIdx.x == 0) { S.n_heavy = 0; S.cursor = 0; }
+  if (threadIdx.x == 0) { S.n_queued = 0; S.cursor = 0; }
   __syncthreads();
-  for (int k = threadIdx.x; k < np; k += BT) narrow_pair(S, k, false);
+  for (int k = threadIdx.x; k < np; k += BT) narrow_first(S, k);
   __syncthreads();
-  // heavy pairs by resolver kind, each kind's segment starting on a warp
-  // boundary: a warp then runs one resolver instead of interleaving several
-  // (a binary64 warp instruction costs the same with one active lane or 32)
-  const int nh = S.n_heavy;
+  // queued pairs by resolver kind, each kind's segment starting on a warp
+  // boundary
+  const int nh = S.n_queued;
   if (threadIdx.x < 16) S.kcnt[threadIdx.x] = 0;
   __syncthreads();
   for (int h = threadIdx.x; h < nh; h += BT) atomicAdd(&S.kcnt[(unsigned)W.heavy[h] >> 28], 1);
@@ -723,12 +771,12 @@ DI void ph_narrow(Smem& S) {
   __syncthreads();
   for (int h = threadIdx.x; h < nh; h += BT) {
     const unsigned e = (unsigned)W.heavy[h];
-    W.heavy2[atomicAdd(&S.kpos[e >> 28], 1)] = (int)(e & 0x0FFFFFFFu);
+    W.heavy2[atomicAdd(&S.kpos[e >> 28], 1)] = (int)e;
   }
   __syncthreads();
   for (int h = threadIdx.x; h < nhp; h += BT) {
-    const int k = W.heavy2[h];
-    if (k >= 0) narrow_pair(S, k, true);
+    const unsigned e = (unsigned)W.heavy2[h];  // 0xffffffff: padding (no kind 15)
+    if (e != 0xffffffffu) narrow_queued(S, (int)(e & 0x0FFFFFFFu), (int)(e >> 28));
   }
   __syncthreads();
   // order: contacts of pair k follow those of pairs < k

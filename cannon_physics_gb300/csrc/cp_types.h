@@ -183,8 +183,8 @@ struct DWorld {
   int* pair_b;
   int* pair_cnt;
   int* pair_tstart;
-  int* heavy;
-  int* heavy2;      // heavy pairs sorted by resolver kind (pairs + 16 * 32 slots)
+  int* heavy;       // pairs queued for a resolver, (kind << 28) | pair; later scan scratch
+  int* heavy2;      // queued pairs sorted by resolver kind (pairs + 16 * 32 slots)
   DContact* ctmp;
   DContact* contacts;
   int* cscr;       // per-contact scratch (contacts_cap + 1)
