@@ -37,6 +37,18 @@ DI double r32(double x) {
   if ((u << 1) == 0) return x;  // +-0
   return (double)__double2float_rn(x);
 }
+// binary64 -> nearest binary32 (ties to even) on the integer pipe, for the
+// same range as r32; other values convert the ordinary way
+DI float r32f(double x) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+  if (e - 897u < 253u) {
+    u += 0x0FFFFFFFull + ((u >> 29) & 1ull);
+    const unsigned e2 = (unsigned)(u >> 52) & 0x7ffu;  // a carry moves to the next binade
+    return __uint_as_float((unsigned)(u >> 32) & 0x80000000u | ((e2 - 896u) << 23) | ((unsigned)(u >> 29) & 0x7fffffu));
+  }
+  return (float)x;
+}
 // binary32 -> binary64 (exact) and binary64 -> nearest binary32.  Plain
 // conversions: on GB300 they issue on the binary64 pipe, which these kernels
 // do not saturate, and every integer-pipe replacement measured slower.

@@ -965,8 +965,8 @@ DI void ph_solve_prep(Smem& S) {
     }
     s.im_solve = im;
     s.active = (im != 0.0) || any_iw;
-    std3(s.vl, d3{0.0, 0.0, 0.0});
-    std3(s.wl, d3{0.0, 0.0, 0.0});
+    *(float4*)s.vl = make_float4(0.f, 0.f, 0.f, s.active ? 1.f : 0.f);  // w: solve flag
+    *(float4*)s.wl = make_float4(0.f, 0.f, 0.f, 0.f);
     st3(s.imf, scale(ld3(b.force), im));
     st3(s.iit, mvmult(iw, ld3(b.torque)));
   }
@@ -1232,38 +1232,86 @@ DI double ddot_f(d3 a, d3 b) { return __fma_rn(a.z, b.z, __fma_rn(a.y, b.y, a.x 
 // A body with zero solve mass and inertia keeps vlambda = wlambda = +0, so
 // its half of G*Wlambda is a signed zero and adding it changes no nonzero
 // sum; a zero sum can only change sign, which no later store observes.
-DI double gs_row_sw(const DWorld& W, int p, int2 bb) {
+DI d3 f2d3v(float4 v) { return f2d3(v.x, v.y, v.z); }
+// vlambda / wlambda update: addScaledVector with the binary32 store (w kept)
+DI float4 vstep(float4 v, double s, float gx, float gy, float gz) {
+  return make_float4(r32f(f2d(v.x) + s * f2d(gx)), r32f(f2d(v.y) + s * f2d(gy)), r32f(f2d(v.z) + s * f2d(gz)), v.w);
+}
+
+// Where a world's vlambda / wlambda live during its sweeps: vlambda of body
+// i at base[i * stride], wlambda at the next float4; vlambda.w is the body's
+// solve flag (1: it takes velocity updates).  Shared memory for a group that
+// fits, else the body scratch records in global memory.
+struct VelRef {
+  float4* base;
+  int stride;
+};
+DI float4* vl_of(VelRef V, int i) { return V.base + (size_t)i * V.stride; }
+DI VelRef vel_global(const DWorld& W) { return VelRef{(float4*)W.bscr[0].vl, (int)(sizeof(DBodyScr) / sizeof(float4))}; }
+
+// One row's record, loaded at once so that its loads share one latency.
+struct RowRec {
+  float4 j0, j1, j2, j3, j4;
+  double2 d0, d1, im, d3b;
+};
+DI RowRec load_row(const DWorld& W, int p) {
   const int cap = W.sw_cap;
-  const float4 j0 = W.sw_j[p], j1 = W.sw_j[cap + p], j2 = W.sw_j[2 * cap + p];
-  const double2 d0 = W.sw_d[p], d1 = W.sw_d[cap + p], d3b = W.sw_d[3 * cap + p];
-  DBodyScr& A = W.bscr[bb.x];
-  DBodyScr& B = W.bscr[bb.y];
-  const d3 gaS = f2d3(j0.x, j0.y, j0.z), gaR = f2d3(j0.w, j1.x, j1.y);
-  const d3 gbS = f2d3(j1.z, j1.w, j2.x), gbR = f2d3(j2.y, j2.z, j2.w);
-  const d3 vla = ldd3(A.vl), wla = ldd3(A.wl), vlb = ldd3(B.vl), wlb = ldd3(B.wl);
-  const double ga = A.active ? ddot_f(vla, gaS) + ddot_f(wla, gaR) : 0.0;
-  const double gb = B.active ? ddot_f(vlb, gbS) + ddot_f(wlb, gbR) : 0.0;
-  const double gwl = A.active && B.active ? ga + gb : (A.active ? ga : gb);
-  const double lj = d1.y;
-  double dl = d0.y * (d0.x - gwl - d1.x * lj);
-  if (lj + dl < d3b.x) dl = d3b.x - lj;
-  else if (lj + dl > d3b.y) dl = d3b.y - lj;
-  W.sw_d[cap + p].y = lj + dl;
-  if (A.active || B.active) {
-    const double2 im = W.sw_d[2 * cap + p];
-    const float4 j3 = W.sw_j[3 * cap + p], j4 = W.sw_j[4 * cap + p];
-    if (A.active) {
-      std3(A.vl, dadd_scaled(vla, im.x * dl, gaS));
-      std3(A.wl, dadd_scaled(wla, dl, f2d3(j3.x, j3.y, j3.z)));
-    }
-    if (B.active) {
-      // re-read: bi == bj is possible for a constraint between a body and itself
-      const bool same = bb.x == bb.y;
-      const d3 v = same ? ldd3(B.vl) : vlb;
-      const d3 w = same ? ldd3(B.wl) : wlb;
-      std3(B.vl, dadd_scaled(v, im.y * dl, gbS));
-      std3(B.wl, dadd_scaled(w, dl, f2d3(j3.w, j4.x, j4.y)));
-    }
+  RowRec R;
+  R.j0 = W.sw_j[p];
+  R.j1 = W.sw_j[cap + p];
+  R.j2 = W.sw_j[2 * cap + p];
+  R.j3 = W.sw_j[3 * cap + p];
+  R.j4 = W.sw_j[4 * cap + p];
+  R.d0 = W.sw_d[p];
+  R.d1 = W.sw_d[cap + p];
+  R.im = W.sw_d[2 * cap + p];
+  R.d3b = W.sw_d[3 * cap + p];
+  return R;
+}
+
+// dlambda of a row from its two halves of G*Wlambda (gs_solver.dart:138-150)
+DI double row_dl(const RowRec& R, double ga, bool aa, double gb, bool ab) {
+  const double gwl = aa && ab ? ga + gb : (aa ? ga : gb);
+  const double lj = R.d1.y;
+  double dl = R.d0.y * (R.d0.x - gwl - R.d1.x * lj);
+  if (lj + dl < R.d3b.x) dl = R.d3b.x - lj;
+  else if (lj + dl > R.d3b.y) dl = R.d3b.y - lj;
+  return dl;
+}
+DI double half_a(const RowRec& R, float4 v, float4 w) {
+  return ddot_f(f2d3v(v), f2d3(R.j0.x, R.j0.y, R.j0.z)) + ddot_f(f2d3v(w), f2d3(R.j0.w, R.j1.x, R.j1.y));
+}
+DI double half_b(const RowRec& R, float4 v, float4 w) {
+  return ddot_f(f2d3v(v), f2d3(R.j1.z, R.j1.w, R.j2.x)) + ddot_f(f2d3v(w), f2d3(R.j2.y, R.j2.z, R.j2.w));
+}
+DI void update_a(float4* pa, float4 v, float4 w, const RowRec& R, double dl) {
+  pa[0] = vstep(v, R.im.x * dl, R.j0.x, R.j0.y, R.j0.z);
+  pa[1] = vstep(w, dl, R.j3.x, R.j3.y, R.j3.z);
+}
+DI void update_b(float4* pb, float4 v, float4 w, const RowRec& R, double dl) {
+  pb[0] = vstep(v, R.im.y * dl, R.j1.z, R.j1.w, R.j2.x);
+  pb[1] = vstep(w, dl, R.j3.w, R.j4.x, R.j4.y);
+}
+
+// One row of a GSSolver sweep (gs_solver.dart:122-155) at level position p.
+// A body with zero solve mass and inertia keeps vlambda = wlambda = +0, so
+// its half of G*Wlambda is a signed zero and adding it changes no nonzero
+// sum; a zero sum can only change sign, which no later store observes.
+DI double gs_row_sw(const DWorld& W, VelRef V, int p, int2 bb) {
+  const RowRec R = load_row(W, p);
+  float4* pa = vl_of(V, bb.x);
+  float4* pb = vl_of(V, bb.y);
+  const float4 vla = pa[0], wla = pa[1], vlb = pb[0], wlb = pb[1];
+  const bool aa = vla.w != 0.f, ab = vlb.w != 0.f;
+  const double ga = aa ? half_a(R, vla, wla) : 0.0;
+  const double gb = ab ? half_b(R, vlb, wlb) : 0.0;
+  const double dl = row_dl(R, ga, aa, gb, ab);
+  W.sw_d[W.sw_cap + p].y = R.d1.y + dl;
+  if (aa) update_a(pa, vla, wla, R, dl);
+  if (ab) {
+    // re-read: bi == bj is possible for a constraint between a body and itself
+    const bool same = bb.x == bb.y;
+    update_b(pb, same ? pb[0] : vlb, same ? pb[1] : wlb, R, dl);
   }
   return dl > 0.0 ? dl : -dl;
 }
@@ -1284,9 +1332,9 @@ DI float d2f(double x) {
 DI void apply_body(const DWorld& W, int i) {
   DBody& b = W.bodies[i];
   DBodyScr& s = W.bscr[i];
-  f3 vl = mul(f3{d2f(s.vl[0]), d2f(s.vl[1]), d2f(s.vl[2])}, ld3(b.lin_factor));
+  f3 vl = mul(ld3(s.vl), ld3(b.lin_factor));
   st3(b.vel, add(ld3(b.vel), vl));
-  f3 wl = mul(f3{d2f(s.wl[0]), d2f(s.wl[1]), d2f(s.wl[2])}, ld3(b.ang_factor));
+  f3 wl = mul(ld3(s.wl), ld3(b.ang_factor));
   st3(b.avel, add(ld3(b.avel), wl));
 }
 
@@ -1448,9 +1496,59 @@ DI bool index_ok(int code, int world, int idx, int bound) {
 // level l of every unfinished world runs between the same two barriers, so a
 // barrier waits for many independent rows instead of a few.  Each world keeps
 // its own iteration count and convergence test.
-DI void joint_solve(Smem& S, Slot* slots, int K) {
+// Rows of a level handed to a thread: position p in the world's sweep
+// arrays and the row's body pair (checked where it is used), or k = -1.
+struct LevelRow {
+  int k, p;
+  int2 bb;
+};
+
+// The first row of level `slot` (a ring entry of per-world level bounds)
+// that falls to this thread (both halves of a split level take the same
+// rows), with its body pair loaded and the rest of its record prefetched to
+// L2.  Prepared one level ahead and consumed one level later, so that none
+// of these loads lies on a level's path.
+DI LevelRow level_row(const Slot* slots, int K, const int* lb, const int* lc) {
+  LevelRow R{-1, 0, make_int2(0, 0)};
+  int total = 0;
+  for (int k = 0; k < K; k++) total += lc[k];
+  const int half = BT >> 1;
+  int off = total <= half ? (int)threadIdx.x % half : (int)threadIdx.x, k = 0;
+  while (k < K && off >= lc[k]) { off -= lc[k]; k++; }
+  if (k >= K) return R;
+  const Slot& sl = slots[k];
+  const DWorld& W = sl.W;
+  const int p = lb[k] + off;
+  if (!index_ok(8, sl.id, p, sl.n_rows)) return R;
+  const int cap = W.sw_cap;
+#pragma unroll
+  for (int q = 0; q < 5; q++) asm volatile("prefetch.global.L2 [%0];" ::"l"(W.sw_j + q * cap + p));
+#pragma unroll
+  for (int q = 0; q < 4; q++) asm volatile("prefetch.global.L2 [%0];" ::"l"(W.sw_d + q * cap + p));
+  R.k = k;
+  R.p = p;
+  R.bb = W.sw_b[p];
+  return R;
+}
+DI bool row_bodies_ok(const Slot& sl, int2 bb) {
+  return index_ok(5, sl.id, bb.x, sl.P.nb) && index_ok(6, sl.id, bb.y, sl.P.nb);
+}
+
+// GSSolver sweeps (gs_solver.dart:122-155) of all worlds of a group at once:
+// level l of every unfinished world runs between the same two barriers, so a
+// barrier waits for many independent rows instead of a few.  Each world keeps
+// its own iteration count and convergence test.
+// s_acc: CP_GROUP_MAX * blockDim.x per-thread, per-world sums of |dlambda|
+// over a sweep (in shared memory: eight binary64 accumulators in registers
+// make the kernel spill); vref: where each world's vlambda / wlambda live.
+DI void joint_solve(Smem& S, Slot* slots, int K, double* s_acc, const VelRef* vref) {
   __shared__ double s_part[CP_GROUP_MAX][CP_SOLVE_MAX_WARPS];
-  __shared__ int s_conv[CP_GROUP_MAX];
+  // ring of per-world level bounds: during level l, entry (l+2)%3 is filled
+  // for level l+2 and entry (l+1)%3 (filled during level l-1) is read
+  __shared__ int s_lb[3][CP_GROUP_MAX], s_lc[3][CP_GROUP_MAX];
+  // halves of G*Wlambda exchanged between the two threads of a split row
+  __shared__ double s_gx[CP_SOLVE_MAX_WARPS * 32];
+  __shared__ int s_ax[CP_SOLVE_MAX_WARPS * 32];
   for (int sweep = 0;; sweep++) {
     int active = 0, Lmax = 0;
     for (int k = 0; k < K; k++) {
@@ -1461,44 +1559,126 @@ DI void joint_solve(Smem& S, Slot* slots, int K) {
       }
     }
     if (!active) break;
-    double part[CP_GROUP_MAX];
+    // level bounds of world threadIdx.x at level l (count 0 once its levels
+    // are done): loaded during one level, checked and published at its end
+    auto bounds_load = [&](int l, int& b0, int& e0) {
+      b0 = e0 = 0;
+      if (threadIdx.x < K && (active >> threadIdx.x & 1) && l < slots[threadIdx.x].n_levels) {
+        b0 = slots[threadIdx.x].W.level_start[l];
+        e0 = slots[threadIdx.x].W.level_start[l + 1];
+      }
+    };
+    auto bounds_store = [&](int l, int e, int b0, int e0) {
+      if (threadIdx.x < K) {
+        const int k = threadIdx.x;
+        const Slot& sl = slots[k];
+        int b = 0, c = 0;
+        // a level is a non-empty sub-range of [0, n_rows)
+        if ((active >> k & 1) && l < sl.n_levels && index_ok(1, sl.id, b0, sl.n_rows) &&
+            index_ok(2, sl.id, e0 - 1 - b0, sl.n_rows - b0)) {
+          b = b0;
+          c = e0 - b0;
+        }
+        s_lb[e][k] = b;
+        s_lc[e][k] = c;
+      }
+    };
+    {
+      int b0, e0, b1, e1;
+      bounds_load(0, b0, e0);
+      bounds_load(1, b1, e1);
+      bounds_store(0, 0, b0, e0);
+      bounds_store(1, 1, b1, e1);
+    }
+    __syncthreads();
+    LevelRow nxt = level_row(slots, K, s_lb[0], s_lc[0]);
 #pragma unroll
-    for (int k = 0; k < CP_GROUP_MAX; k++) part[k] = 0.0;
+    for (int k = 0; k < CP_GROUP_MAX; k++) s_acc[k * BT + threadIdx.x] = 0.0;
     for (int l = 0; l < Lmax; l++) {
-      int base[CP_GROUP_MAX], cnt[CP_GROUP_MAX];
+      const int e = l % 3;
+      const LevelRow cur = nxt;
+      int b2, e2;
+      bounds_load(l + 2, b2, e2);
+      nxt = level_row(slots, K, s_lb[(l + 1) % 3], s_lc[(l + 1) % 3]);
+      const int* lb = s_lb[e];
+      const int* lc = s_lc[e];
       int total = 0;
-#pragma unroll
-      for (int k = 0; k < CP_GROUP_MAX; k++) {
-        cnt[k] = 0;
-        base[k] = 0;
-        if (k < K && (active >> k & 1) && l < slots[k].n_levels) {
+      for (int k = 0; k < K; k++) total += lc[k];
+      const int half = BT >> 1;
+      if (total <= half) {
+        // split level (see gs_row_sw): row threadIdx.x % half, side 0 (bi)
+        // on threads [0, half), side 1 (bj) on [half, BT)
+        const int side = threadIdx.x >= half;
+        const int partner = side ? threadIdx.x - half : threadIdx.x + half;
+        const bool mine = (int)threadIdx.x - side * half < total && cur.k >= 0 && row_bodies_ok(slots[cur.k], cur.bb);
+        RowRec R;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f), w = v;
+        float4* pme = nullptr;
+        bool act = false;
+        double g = 0.0;
+        if (mine) {
+          R = load_row(slots[cur.k].W, cur.p);
+          pme = vl_of(vref[cur.k], side ? cur.bb.y : cur.bb.x);
+          v = pme[0];
+          w = pme[1];
+          act = v.w != 0.f;
+          if (act) g = side ? half_b(R, v, w) : half_a(R, v, w);
+        }
+        s_gx[threadIdx.x] = g;
+        s_ax[threadIdx.x] = act;
+        __syncthreads();
+        if (mine) {
+          const int k = cur.k;
           const Slot& sl = slots[k];
-          int b = sl.W.level_start[l], e = sl.W.level_start[l + 1];
-          // a level is a non-empty sub-range of [0, n_rows)
-          if (index_ok(1, sl.id, b, sl.n_rows) && index_ok(2, sl.id, e - 1 - b, sl.n_rows - b)) {
-            base[k] = b;
-            cnt[k] = e - b;
+          const DWorld& W = sl.W;
+          const double go = s_gx[partner];
+          const bool ao = s_ax[partner] != 0;
+          const double dl = side ? row_dl(R, go, ao, g, act) : row_dl(R, g, act, go, ao);
+          const bool same = cur.bb.x == cur.bb.y;
+          if (side == 0) {
+            W.sw_d[W.sw_cap + cur.p].y = R.d1.y + dl;
+            if (act) update_a(pme, v, w, R, dl);
+            if (same && ao) update_b(pme, pme[0], pme[1], R, dl);  // the same body, after its first update
+            const int r = W.sw_orig[cur.p];
+            if (index_ok(4, sl.id, r, sl.n_rows)) {
+              const double a = dl > 0.0 ? dl : -dl;
+              W.absdl[r] = a;
+              s_acc[k * BT + threadIdx.x] += a;
+            }
+          } else if (act && !same) {
+            update_b(pme, v, w, R, dl);
           }
         }
-        total += cnt[k];
+      } else {
+        for (int x = threadIdx.x; x < total; x += BT) {
+          int k, p;
+          int2 bb;
+          if (x == (int)threadIdx.x) {
+            if (cur.k < 0) continue;  // a failed index check (recorded)
+            k = cur.k;
+            p = cur.p;
+            bb = cur.bb;
+          } else {
+            int off = x;
+            k = 0;
+            while (k < K - 1 && off >= lc[k]) { off -= lc[k]; k++; }
+            const Slot& sl = slots[k];
+            if (!index_ok(3, sl.id, off, lc[k])) continue;
+            p = lb[k] + off;
+            if (!index_ok(8, sl.id, p, sl.n_rows)) continue;
+            bb = sl.W.sw_b[p];
+          }
+          const Slot& sl = slots[k];
+          if (!row_bodies_ok(sl, bb)) continue;
+          const DWorld& W = sl.W;
+          const int r = W.sw_orig[p];
+          if (!index_ok(4, sl.id, r, sl.n_rows)) continue;
+          double a = gs_row_sw(W, vref[k], p, bb);
+          W.absdl[r] = a;
+          s_acc[k * BT + threadIdx.x] += a;
+        }
       }
-      for (int x = threadIdx.x; x < total; x += BT) {
-        int k = 0, off = x;
-        while (k < K - 1 && off >= cnt[k]) { off -= cnt[k]; k++; }
-        const Slot& sl = slots[k];
-        const DWorld& W = sl.W;
-        if (!index_ok(3, sl.id, off, cnt[k])) continue;
-        const int p = base[k] + off;
-        const int r = W.sw_orig[p];
-        if (!index_ok(4, sl.id, r, sl.n_rows)) continue;
-        const int2 bb = W.sw_b[p];
-        if (!index_ok(5, sl.id, bb.x, sl.P.nb) || !index_ok(6, sl.id, bb.y, sl.P.nb)) continue;
-        double a = gs_row_sw(W, p, bb);
-        W.absdl[r] = a;
-#pragma unroll
-        for (int kk = 0; kk < CP_GROUP_MAX; kk++)
-          if (kk == k) part[kk] += a;
-      }
+      bounds_store(l + 2, (l + 2) % 3, b2, e2);
       __syncthreads();
     }
     // per-world convergence: (sum of |dlambda| in row order)^2 < tol^2, with
@@ -1507,7 +1687,7 @@ DI void joint_solve(Smem& S, Slot* slots, int K) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < CP_GROUP_MAX; k++) {
-      double v = part[k];
+      double v = s_acc[k * BT + threadIdx.x];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
       if (lane == 0) s_part[k][wid] = v;
@@ -1599,6 +1779,15 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step_solve(const DWorld* __re
   static_assert(THREADS <= 32 * CP_SOLVE_MAX_WARPS, "solve block too wide");
   __shared__ Smem S;
   __shared__ Slot slots[CP_GROUP_MAX];
+  __shared__ double s_acc[CP_GROUP_MAX * THREADS];
+  __shared__ VelRef s_vref[CP_GROUP_MAX];
+  __shared__ int s_voff[CP_GROUP_MAX];  // body offset in s_vel, -1: global memory
+  // vlambda / wlambda of the group's bodies while it sweeps (two float4 per
+  // body); a group with more bodies than fit keeps them in global memory
+  extern __shared__ float4 s_vel[];
+  unsigned dyn_bytes;
+  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn_bytes));
+  const int vcap = (int)(dyn_bytes / (2 * sizeof(float4)));
   if (threadIdx.x < CP_NUM_PHASES) S.t_acc[threadIdx.x] = 0;
   for (;;) {
     if (threadIdx.x == 0) S.wi = atomicAdd(queue, 1);
@@ -1620,8 +1809,45 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step_solve(const DWorld* __re
       sl.iters = 0;
     }
     __syncthreads();
+    if (threadIdx.x == 0) {
+      int vo = 0;
+      for (int k = 0; k < K; k++) {
+        const Slot& sl = slots[k];
+        if (sl.n_rows > 0 && vo + sl.P.nb <= vcap) {
+          s_voff[k] = vo;
+          s_vref[k] = VelRef{s_vel + 2 * vo, 2};
+          vo += sl.P.nb;
+        } else {
+          s_voff[k] = -1;
+          s_vref[k] = vel_global(sl.W);
+        }
+      }
+    }
+    __syncthreads();
+    for (int k = 0; k < K; k++) {
+      if (s_voff[k] < 0) continue;
+      const DWorld& W = slots[k].W;
+      float4* sv = s_vel + 2 * s_voff[k];
+      for (int i = threadIdx.x; i < slots[k].P.nb; i += BT) {
+        const float4* gv = (const float4*)W.bscr[i].vl;
+        sv[2 * i] = gv[0];
+        sv[2 * i + 1] = gv[1];
+      }
+    }
+    __syncthreads();
     if (threadIdx.x == 0) S.t_last = clock64();
-    joint_solve(S, slots, K);
+    joint_solve(S, slots, K, s_acc, s_vref);
+    for (int k = 0; k < K; k++) {
+      if (s_voff[k] < 0) continue;
+      const DWorld& W = slots[k].W;
+      const float4* sv = s_vel + 2 * s_voff[k];
+      for (int i = threadIdx.x; i < slots[k].P.nb; i += BT) {
+        float4* gv = (float4*)W.bscr[i].vl;
+        gv[0] = sv[2 * i];
+        gv[1] = sv[2 * i + 1];
+      }
+    }
+    __syncthreads();
     tick(S, 6);
     for (int k = 0; k < K; k++) {
       if (!slots[k].ok) continue;
@@ -1732,7 +1958,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) k_step_solve_w(const DWorld*
           const int r = W.sw_orig[p];
           const int2 bb = W.sw_b[p];
           if (index_ok(4, t.id, r, t.n_rows) && index_ok(5, t.id, bb.x, t.P.nb) && index_ok(6, t.id, bb.y, t.P.nb)) {
-            const double a = gs_row_sw(W, p, bb);
+            const double a = gs_row_sw(W, vel_global(W), p, bb);
             W.absdl[r] = a;
 #pragma unroll
             for (int kk = 0; kk < CP_GROUP_MAX; kk++)
@@ -1976,8 +2202,8 @@ static const PreVariant kPre[] = {
 };
 static const SolveVariant kSolve[] = {
     {k_step_solve<128, 4>, 128, 4, 0},     {k_step_solve<128, 8>, 128, 8, 0},     {k_step_solve<256, 4>, 256, 4, 0},
-    {k_step_solve<32, 32>, 32, 32, 0},     {k_step_solve<64, 16>, 64, 16, 0},     {k_step_solve_w<4, 4>, 128, 4, 1},
-    {k_step_solve_w<4, 8>, 128, 8, 1},     {k_step_solve_w<8, 4>, 256, 4, 1},
+    {k_step_solve<128, 6>, 128, 6, 0},     {k_step_solve<64, 16>, 64, 16, 0},     {k_step_solve_w<4, 4>, 128, 4, 1},
+    {k_step_solve<64, 12>, 64, 12, 0},     {k_step_solve_w<8, 4>, 256, 4, 1},
 };
 static const int kNumPre = sizeof(kPre) / sizeof(kPre[0]);
 static const int kNumSolve = sizeof(kSolve) / sizeof(kSolve[0]);
@@ -1998,6 +2224,13 @@ int cpk_solve_group_limit(int v, int group_bodies) {
 static int last_cap_for(int max_nb) { return max_nb < 1 ? 1 : (max_nb < CP_SMEM_LEVEL_MAX ? max_nb : CP_SMEM_LEVEL_MAX); }
 static size_t pre_smem(int last_cap) { return sizeof(int2) * CP_LEVEL_CHUNK + sizeof(int) * (size_t)last_cap; }
 
+// shared memory for the solve kernel's vlambda / wlambda: the bodies of a
+// default-size group (CP_SOLVE_VEL_BODIES per 128 threads)
+#define CP_SOLVE_VEL_BODIES 640
+static size_t solve_smem(const SolveVariant& V) {
+  return V.per_warp ? 0 : (size_t)CP_SOLVE_VEL_BODIES * V.threads / 128 * 2 * sizeof(float4);
+}
+
 int cpk_pre_blocks_per_sm(int variant, int max_nb) {
   const PreVariant& P = kPre[variant / kNumSolve];
   int b = 0;
@@ -2015,7 +2248,7 @@ cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, const int*
   P.fn<<<grid_pre, P.threads, pre_smem(cap), stream>>>(d_worlds, d_ids, n, dt, d_queue, cap);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  V.fn<<<grid_solve, V.threads, 0, stream>>>(d_worlds, d_ids, d_gstart, ngroups, dt, d_queue + 1);
+  V.fn<<<grid_solve, V.threads, solve_smem(V), stream>>>(d_worlds, d_ids, d_gstart, ngroups, dt, d_queue + 1);
   return cudaGetLastError();
 }
 
@@ -2025,5 +2258,7 @@ void cpk_max_resident_blocks(int variant, int* pre, int* solve) {
   *pre = 0;
   *solve = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(pre, P.fn, P.threads, pre_smem(last_cap_for(512)));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(solve, V.fn, V.threads, 0);
+  // static plus dynamic shared memory above 48 KB needs the kernel's opt-in
+  cudaFuncSetAttribute((const void*)V.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)solve_smem(V));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(solve, V.fn, V.threads, solve_smem(V));
 }

@@ -130,8 +130,8 @@ struct __align__(16) DRow {
 struct __align__(16) DBodyScr {
   float xs[4];   // shape world position
   float qs[4];   // shape world orientation
-  double vl[4];  // vlambda (binary32 values held in binary64)
-  double wl[4];  // wlambda
+  float vl[4];   // vlambda (x, y, z; w unused)
+  float wl[4];   // wlambda
   float imf[4];  // force * invMassSolve (computeGiMf)
   float iit[4];  // invInertiaWorldSolve * torque
   double im_solve;
