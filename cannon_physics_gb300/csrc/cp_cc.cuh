@@ -414,14 +414,14 @@ DI bool sat64_compact(const DWorld& W, const DHullPose& A, const DHullPose& B, c
   return true;
 }
 
-// one out-of-line copy: the resolver is large and is reached from several
-// dispatch cases; inlining it at each bloats the step kernel's instruction footprint
-__device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xAf, f3 xBf, q4 qAf, q4 qBf, int& start) {
-  const DWorld& W = *C.W;
+// Stage 1 of convexConvex: the bounding spheres (narrow_phase.dart:1994) and
+// the binary32 bound of findSeparatingAxis.  False: the reference finds no
+// contact for certain.  Cheap and run for every queued hull pair first, so
+// that the binary64 stage runs on the survivors in full warps.
+DI bool cc_stage1(const DWorld& W, int shA, int shB, f3 xAf, f3 xBf, q4 qAf, q4 qBf, Sat32& S32, float& U) {
   const DShape& SA = W.shapes[shA];
   const DShape& SB = W.shapes[shB];
-  if (distance_to(xAf, xBf) > SA.bsr + SB.bsr) return 0;
-  Sat32 S32;
+  if (distance_to(xAf, xBf) > SA.bsr + SB.bsr) return false;
   S32.W = &W;
   S32.A = &W.hulls[SA.hull];
   S32.B = &W.hulls[SB.hull];
@@ -430,28 +430,52 @@ __device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, in
   S32.axB[0] = rot32(qBf, f3{1.f, 0.f, 0.f}); S32.axB[1] = rot32(qBf, f3{0.f, 1.f, 0.f}); S32.axB[2] = rot32(qBf, f3{0.f, 0.f, 1.f});
   S32.E = 1e-4f * (fabsf(xAf.x) + fabsf(xAf.y) + fabsf(xAf.z) + fabsf(xBf.x) + fabsf(xBf.y) + fabsf(xBf.z) +
                    (float)(SA.bsr + SB.bsr)) + 1e-6f;
-  float U;
-  if (!sat32_bound(S32, U)) return 0;
+  return sat32_bound(S32, U);
+}
+
+// Narrowphase.convexConvex (narrow_phase.dart:1981-2043).  Lanes leave at
+// data-dependent points (the stage-1 test, the binary64 separating-axis
+// walk); a ballot over the lanes that entered together at each such point
+// regroups the survivors, so the clipping that follows issues its binary64
+// instructions once for all of them instead of once per group of lanes
+// that happened to leave a loop together.  Past the last ballot no lane
+// returns early (failures set a flag), so the survivors stay together.
+// One out-of-line copy: the resolver is large and is reached from several
+// dispatch cases; inlining it at each bloats the step kernel's instruction footprint.
+__device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xAf, f3 xBf, q4 qAf, q4 qBf, int& start) {
+  const DWorld& W = *C.W;
+  const DShape& SA = W.shapes[shA];
+  const DShape& SB = W.shapes[shB];
+  unsigned lanes = __activemask();
+  Sat32 S32;
+  float U = 0.f;
+  const bool near = cc_stage1(W, shA, shB, xAf, xBf, qAf, qBf, S32, U);
+  lanes = __ballot_sync(lanes, near);
+  if (!near) return 0;
   DHullPose A, B;
   A.H = W.hulls[SA.hull]; A.x = d3of(xAf); A.q = d4of(qAf);
   B.H = W.hulls[SB.hull]; B.x = d3of(xBf); B.q = d4of(qBf);
   A.origin = dvmult(d4{-A.q.x, -A.q.y, -A.q.z, A.q.w}, dsub(d3{0.0, 0.0, 0.0}, A.x));
   B.origin = dvmult(d4{-B.q.x, -B.q.y, -B.q.z, B.q.w}, dsub(d3{0.0, 0.0, 0.0}, B.x));
-  if (A.H.nf > CP_MAX_HULL_VERTS || B.H.nf > CP_MAX_HULL_VERTS || B.H.nce > CP_MAX_HULL_VERTS) {
-    atomicOr(C.overflow, ST_HULL_OVERFLOW);
-    return 0;
-  }
+  const bool fits = !(A.H.nf > CP_MAX_HULL_VERTS || B.H.nf > CP_MAX_HULL_VERTS || B.H.nce > CP_MAX_HULL_VERTS);
+  if (!fits) atomicOr(C.overflow, ST_HULL_OVERFLOW);
   d3 wnA[CP_MAX_HULL_VERTS], wnB[CP_MAX_HULL_VERTS];
-  for (int k = 0; k < A.H.ncf; k++) {
-    int f = W.hcanon[A.H.cf0 + k];
-    wnA[f] = dvmult(A.q, ldd3(W.faces[A.H.f0 + f].dnormal));
-  }
-  for (int k = 0; k < B.H.ncf; k++) {
-    int f = W.hcanon[B.H.cf0 + k];
-    wnB[f] = dvmult(B.q, ldd3(W.faces[B.H.f0 + f].dnormal));
-  }
   d3 sep = d3{0.0, 0.0, 0.0};
-  if (!sat64_compact(W, A, B, wnA, wnB, S32, U, sep)) return 0;
+  bool touch = false;
+  if (fits) {
+    for (int k = 0; k < A.H.ncf; k++) {
+      int f = W.hcanon[A.H.cf0 + k];
+      wnA[f] = dvmult(A.q, ldd3(W.faces[A.H.f0 + f].dnormal));
+    }
+    for (int k = 0; k < B.H.ncf; k++) {
+      int f = W.hcanon[B.H.cf0 + k];
+      wnB[f] = dvmult(B.q, ldd3(W.faces[B.H.f0 + f].dnormal));
+    }
+    touch = sat64_compact(W, A, B, wnA, wnB, S32, U, sep);
+  }
+  lanes = __ballot_sync(lanes, touch);
+  if (!touch) return 0;
+  bool fail = false;
   // clipAgainstHull: face of B most aligned with the axis
   int cfb = -1;
   double dmax = __longlong_as_double(0xfff0000000000000LL);
@@ -459,11 +483,14 @@ __device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, in
     double d = ddot(face_wn(W, B.H, wnB, f), sep);
     if (d > dmax) { dmax = d; cfb = f; }
   }
-  if (cfb < 0) return 0;
+  fail = cfb < 0;
   d3 bufA[CP_MAX_CLIP], bufB[CP_MAX_CLIP];
-  const DFace FB = W.faces[B.H.f0 + cfb];
-  if (FB.n > CP_MAX_CLIP) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
-  int nin = FB.n;
+  const DFace FB = W.faces[B.H.f0 + (fail ? 0 : cfb)];
+  if (!fail && FB.n > CP_MAX_CLIP) {
+    atomicOr(C.overflow, ST_HULL_OVERFLOW);
+    fail = true;
+  }
+  int nin = fail ? 0 : FB.n;
   for (int i = 0; i < nin; i++) bufA[i] = dadd(dvmult(B.q, hvd(W, B.H.v0 + W.hfi[FB.i0 + i])), B.x);
   // clipFaceAgainstHull: face of A most anti-aligned with the axis
   int cfa = -1;
@@ -472,20 +499,26 @@ __device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, in
     double d = ddot(face_wn(W, A.H, wnA, f), sep);
     if (d < dmin) { dmin = d; cfa = f; }
   }
-  if (cfa < 0) return 0;
-  const DFace FA = W.faces[A.H.f0 + cfa];
+  fail = fail || cfa < 0;
+  const DFace FA = W.faces[A.H.f0 + (cfa < 0 ? 0 : cfa)];
   d3* pin = bufA;
   d3* pout = bufB;
-  for (int i = 0; i < FA.n; i++) {
+  const int nplanes = fail ? 0 : FA.n;
+  for (int i = 0; i < nplanes && !fail; i++) {
     int other = FA.nc > i ? W.hconn[FA.c0 + i] : 0;
     d3 pn = face_wn(W, A.H, wnA, other);
     double planeEqWS = W.faces[A.H.f0 + other].plane_const - ddot(pn, A.x);
     int nout = dclip_face_against_plane(pin, nin, pout, pn, planeEqWS);
-    if (nout > CP_MAX_CLIP) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
+    if (nout > CP_MAX_CLIP) {
+      atomicOr(C.overflow, ST_HULL_OVERFLOW);
+      fail = true;
+    }
     d3* t = pin; pin = pout; pout = t;
     nin = nout;
   }
-  d3 pn = face_wn(W, A.H, wnA, cfa);
+  __syncwarp(lanes);
+  if (fail) nin = 0;
+  d3 pn = face_wn(W, A.H, wnA, cfa < 0 ? 0 : cfa);
   double planeEqWS = FA.plane_const - ddot(pn, A.x);
   double depth[CP_MAX_CLIP];
   int n = 0;

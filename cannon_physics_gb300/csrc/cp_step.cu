@@ -774,9 +774,35 @@ DI void ph_narrow(Smem& S) {
     W.heavy2[atomicAdd(&S.kpos[e >> 28], 1)] = (int)e;
   }
   __syncthreads();
+  if (threadIdx.x == 0) S.n_queued = 0;
+  __syncthreads();
+  // hull pairs (kinds RK_BB and up) first take convex_convex's cheap stage 1;
+  // the survivors are queued again (into W.heavy, free once sorted) and take
+  // the binary64 stage together, in full warps
   for (int h = threadIdx.x; h < nhp; h += BT) {
     const unsigned e = (unsigned)W.heavy2[h];  // 0xffffffff: padding (no kind 15)
-    if (e != 0xffffffffu) narrow_queued(S, (int)(e & 0x0FFFFFFFu), (int)(e >> 28));
+    if (e == 0xffffffffu) continue;
+    const int k = (int)(e & 0x0FFFFFFFu), rk = (int)(e >> 28);
+    if (rk >= RK_BB) {
+      PairJob X;
+      pair_job(S, k, X, false);
+      Sat32 S32;
+      float U;
+      if (cc_stage1(W, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, S32, U)) {
+        W.heavy[atomicAdd(&S.n_queued, 1)] = (int)e;
+      } else {
+        W.pair_cnt[k] = 0;
+        W.pair_tstart[k] = 0;
+      }
+    } else {
+      narrow_queued(S, k, rk);
+    }
+  }
+  __syncthreads();
+  const int nh2 = S.n_queued;
+  for (int h = threadIdx.x; h < nh2; h += BT) {
+    const unsigned e = (unsigned)W.heavy[h];
+    narrow_queued(S, (int)(e & 0x0FFFFFFFu), (int)(e >> 28));
   }
   __syncthreads();
   // order: contacts of pair k follow those of pairs < k
