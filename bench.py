@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--serve-window", type=float, default=1.0, help="served form: seconds of arrivals")
     ap.add_argument("--serve-tick", type=int, default=4, help="served form: steps per tick")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--variant", type=int, default=None,
+                    help="pin the batched kernel variant (no autotuning): the step kernels then launch in a known order, "
+                         "two per warm-up step, for profiling")
     return ap.parse_args()
 
 
@@ -266,13 +269,15 @@ def run_ours(args):
     batch = engine.Batch(ctx, worlds)
     total = batch.total
     ext = torch.cuda.ExternalStream(ctx.stream_handle())
+    if args.variant is not None:
+        ctx.set_variant(args.variant)
 
     for _ in range(args.warmup):
         batch.step(DT)
     # the autotuner times one kernel variant per batched call; it tunes again
     # once the worlds are in contact (call 48)
     tune_calls = 0
-    while (ctx.autotune_info()["variant"] < 0 or tune_calls < 48) and tune_calls < 80:
+    while args.variant is None and (ctx.autotune_info()["variant"] < 0 or tune_calls < 48) and tune_calls < 80:
         batch.step(DT)
         tune_calls += 1
     ctx.batch_profile()

@@ -141,17 +141,15 @@ DI int dclip_face_against_plane(const d3* in, int nin, d3* out, d3 n, double c) 
   for (int vi = 0; vi < nin; vi++) {
     d3 last = in[vi];
     double nDotLast = ddot(n, last) + c;
-    if (nDotFirst < 0) {
-      if (nDotLast < 0) {
-        if (nout < CP_MAX_CLIP) out[nout] = last;
-        nout++;
-      } else {
-        if (nout < CP_MAX_CLIP) out[nout] = dlerp(first, last, nDotFirst / (nDotFirst - nDotLast));
-        nout++;
-      }
-    } else if (nDotLast < 0) {
+    // the reference's four cases (first/last behind the plane or not) emit
+    // the crossing point when exactly one is behind, then `last` when it is
+    // behind; one code path for the crossing keeps the division out of two
+    // divergent branches
+    if ((nDotFirst < 0) != (nDotLast < 0)) {
       if (nout < CP_MAX_CLIP) out[nout] = dlerp(first, last, nDotFirst / (nDotFirst - nDotLast));
       nout++;
+    }
+    if (nDotLast < 0) {
       if (nout < CP_MAX_CLIP) out[nout] = last;
       nout++;
     }
