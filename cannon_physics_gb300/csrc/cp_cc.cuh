@@ -420,7 +420,9 @@ DI bool sat64_compact(const DWorld& W, const DHullPose& A, const DHullPose& B, c
 // the binary32 bound of findSeparatingAxis.  False: the reference finds no
 // contact for certain.  Cheap and run for every queued hull pair first, so
 // that the binary64 stage runs on the survivors in full warps.
-DI bool cc_stage1(const DWorld& W, int shA, int shB, f3 xAf, f3 xBf, q4 qAf, q4 qBf, Sat32& S32, float& U) {
+// The binary32 SAT context of a pair (world axes, error margin E); false
+// when the bounding spheres are apart.
+DI bool cc_setup32(const DWorld& W, int shA, int shB, f3 xAf, f3 xBf, q4 qAf, q4 qBf, Sat32& S32) {
   const DShape& SA = W.shapes[shA];
   const DShape& SB = W.shapes[shB];
   if (distance_to(xAf, xBf) > SA.bsr + SB.bsr) return false;
@@ -432,7 +434,10 @@ DI bool cc_stage1(const DWorld& W, int shA, int shB, f3 xAf, f3 xBf, q4 qAf, q4 
   S32.axB[0] = rot32(qBf, f3{1.f, 0.f, 0.f}); S32.axB[1] = rot32(qBf, f3{0.f, 1.f, 0.f}); S32.axB[2] = rot32(qBf, f3{0.f, 0.f, 1.f});
   S32.E = 4e-6f * (fabsf(xAf.x) + fabsf(xAf.y) + fabsf(xAf.z) + fabsf(xBf.x) + fabsf(xBf.y) + fabsf(xBf.z)) +
           4e-5f * (fabsf(xAf.x - xBf.x) + fabsf(xAf.y - xBf.y) + fabsf(xAf.z - xBf.z) + (float)(SA.bsr + SB.bsr)) + 1e-6f;
-  return sat32_bound(S32, U);
+  return true;
+}
+DI bool cc_stage1(const DWorld& W, int shA, int shB, f3 xAf, f3 xBf, q4 qAf, q4 qBf, Sat32& S32, float& U) {
+  return cc_setup32(W, shA, shB, xAf, xBf, qAf, qBf, S32) && sat32_bound(S32, U);
 }
 
 // Narrowphase.convexConvex (narrow_phase.dart:1981-2043).  Lanes leave at
@@ -444,14 +449,15 @@ DI bool cc_stage1(const DWorld& W, int shA, int shB, f3 xAf, f3 xBf, q4 qAf, q4 
 // returns early (failures set a flag), so the survivors stay together.
 // One out-of-line copy: the resolver is large and is reached from several
 // dispatch cases; inlining it at each bloats the step kernel's instruction footprint.
-__device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xAf, f3 xBf, q4 qAf, q4 qBf, int& start) {
+// U1: the bound U that stage 1 already found for this pair, or NaN.
+__device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xAf, f3 xBf, q4 qAf, q4 qBf, int& start, float U1) {
   const DWorld& W = *C.W;
   const DShape& SA = W.shapes[shA];
   const DShape& SB = W.shapes[shB];
   unsigned lanes = __activemask();
   Sat32 S32;
-  float U = 0.f;
-  const bool near = cc_stage1(W, shA, shB, xAf, xBf, qAf, qBf, S32, U);
+  float U = U1;
+  const bool near = U1 == U1 ? cc_setup32(W, shA, shB, xAf, xBf, qAf, qBf, S32) : cc_stage1(W, shA, shB, xAf, xBf, qAf, qBf, S32, U);
   lanes = __ballot_sync(lanes, near);
   if (!near) return 0;
   DHullPose A, B;

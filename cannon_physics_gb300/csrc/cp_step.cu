@@ -634,6 +634,7 @@ struct PairJob {
   int rsi, rsj, bA, bB, shA, shB;
   f3 xA, xB;
   q4 qA, qB;
+  float U1;  // hull pairs: stage 1's bound U, or NaN
 };
 
 // Resolver kind of pair k and its job; RK_NONE when the pair makes no
@@ -689,6 +690,7 @@ DI int pair_job(Smem& S, int k, PairJob& X, bool tests) {
   X.rsj = bj.shape;
   X.bA = swap ? j : i;
   X.bB = swap ? i : j;
+  X.U1 = __int_as_float(0x7fc00000);
   return rk;
 }
 
@@ -703,9 +705,9 @@ DI int run_resolver(Smem& S, int rk, const PairJob& X, int& start) {
     case RK_SC: cnt = sphere_convex(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, X.qB, start); break;
     case RK_PB: cnt = plane_convex(C, X.bA, X.bB, X.shA, X.shB, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, start); break;
     case RK_PC: cnt = plane_convex(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, X.qA, X.qB, start); break;
-    case RK_BB: cnt = convex_convex(C, X.bA, X.bB, X.shA, X.shB, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, start); break;
-    case RK_BC: cnt = convex_convex(C, X.bA, X.bB, X.shA, X.shB, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, start); break;
-    default: cnt = convex_convex(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, X.qA, X.qB, start); break;
+    case RK_BB: cnt = convex_convex(C, X.bA, X.bB, X.shA, X.shB, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, start, X.U1); break;
+    case RK_BC: cnt = convex_convex(C, X.bA, X.bB, X.shA, X.shB, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, start, X.U1); break;
+    default: cnt = convex_convex(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, X.qA, X.qB, start, X.U1); break;
   }
   if (S.rprof) {
     atomicAdd(&S.r_cyc[rk], (unsigned long long)(clock64() - t_res));
@@ -732,11 +734,13 @@ DI void narrow_first(Smem& S, int k) {
   W.pair_tstart[k] = 0;
 }
 
-// Queued pair k of kind rk (its tests passed in the first pass).
-DI void narrow_queued(Smem& S, int k, int rk) {
+// Queued pair k of kind rk (its tests passed in the first pass); U1: stage
+// 1's bound for a hull pair, or NaN.
+DI void narrow_queued(Smem& S, int k, int rk, float U1) {
   const DWorld& W = S.W;
   PairJob X;
   pair_job(S, k, X, false);
+  X.U1 = U1;
   int start = 0;
   const int cnt = run_resolver(S, rk, X, start);
   W.pair_cnt[k] = cnt;
@@ -789,20 +793,22 @@ DI void ph_narrow(Smem& S) {
       Sat32 S32;
       float U;
       if (cc_stage1(W, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, S32, U)) {
+        W.pair_tstart[k] = __float_as_int(U);  // until the binary64 stage sets it
         W.heavy[atomicAdd(&S.n_queued, 1)] = (int)e;
       } else {
         W.pair_cnt[k] = 0;
         W.pair_tstart[k] = 0;
       }
     } else {
-      narrow_queued(S, k, rk);
+      narrow_queued(S, k, rk, __int_as_float(0x7fc00000));
     }
   }
   __syncthreads();
   const int nh2 = S.n_queued;
   for (int h = threadIdx.x; h < nh2; h += BT) {
     const unsigned e = (unsigned)W.heavy[h];
-    narrow_queued(S, (int)(e & 0x0FFFFFFFu), (int)(e >> 28));
+    const int k = (int)(e & 0x0FFFFFFFu);
+    narrow_queued(S, k, (int)(e >> 28), __int_as_float(W.pair_tstart[k]));
   }
   __syncthreads();
   // order: contacts of pair k follow those of pairs < k
