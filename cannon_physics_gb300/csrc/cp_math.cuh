@@ -191,7 +191,7 @@ DI void inertia_world(q4 q, f3 I, float* out) {
   // x2 = x + x is exact, and x * x2 is a product of binary32 values times 2,
   // exact too: the sums below fuse like products of binary32 values
   const double x2 = x + x, y2 = y + y, z2 = z + z;
-  const double xx = x * x2, xy = x * y2, xz = x * z2, yy = y * y2, yz = y * z2, zz = z * z2;
+  const double xx = x * x2, xy = x * y2, xz = x * z2, yy = y * y2, yz = y * z2;  // z*z2 enters through the fused forms
   float m[9];
   m[0] = rf(1 - fma_ff(z, z2, yy)); m[1] = rf(fma_ff(-w, z2, xy)); m[2] = rf(fma_ff(w, y2, xz));
   m[3] = rf(fma_ff(w, z2, xy)); m[4] = rf(1 - fma_ff(z, z2, xx)); m[5] = rf(fma_ff(-w, x2, yz));
