@@ -539,11 +539,13 @@ int ensure_ids(cp_ctx* c, int n) {
     if (c->d_status) cudaFree(c->d_status);
     int cap = std::max(256, 2 * n);
     CUDA_TRY(cudaMalloc(&c->d_ids, sizeof(int) * cap));
-    CUDA_TRY(cudaMalloc(&c->d_status, sizeof(long long) * 4 * cap));
+    CUDA_TRY(cudaMalloc(&c->d_status, sizeof(long long) * 8 * cap));
     if (c->d_gstart) cudaFree(c->d_gstart);
     CUDA_TRY(cudaMalloc(&c->d_gstart, sizeof(int) * (cap + 1)));
     c->d_ids_cap = cap;
     c->d_status_cap = cap;
+    c->dev_order.clear();
+    c->dev_gstart.clear();
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   }
   return CP_OK;
@@ -1375,8 +1377,18 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
   const int grid_solve = std::max(1, std::min(ngroups, c->sms * c->blocks_solve[variant]));
   bool reuse = use_graph && !tuning && c->graph && c->graph_ids == order && c->graph_dt == dt && c->graph_steps == nsteps &&
                c->graph_variant == variant;
-  CUDA_TRY(cudaMemcpyAsync(c->d_ids, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(c->d_gstart, gstart.data(), sizeof(int) * gstart.size(), cudaMemcpyHostToDevice, c->stream));
+  // world list and groups: uploaded when they change (a repeated call on
+  // the same worlds reuses them, and its captured graph)
+  if (c->dev_order != order) {
+    CUDA_TRY(cudaMemcpyAsync(c->d_ids, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));  // the host vector may change before a pageable copy completes
+    c->dev_order = order;
+  }
+  if (c->dev_gstart != gstart) {
+    CUDA_TRY(cudaMemcpyAsync(c->d_gstart, gstart.data(), sizeof(int) * gstart.size(), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->dev_gstart = gstart;
+  }
   if (use_graph && !reuse && !tuning) {
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1399,10 +1411,11 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
     c->graph_steps = nsteps;
     c->graph_variant = variant;
   }
-  // step numbers before the launch, to finish worlds whose step overflowed
-  CUDA_TRY(cpk_gather_status(c->d_worlds, c->d_ids, n, c->d_status, c->stream));
-  std::vector<long long> before(4 * (size_t)n), after(4 * (size_t)n);
-  CUDA_TRY(cudaMemcpyAsync(before.data(), c->d_status, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
+  // step numbers before the launch, to finish worlds whose step overflowed;
+  // kept on the device and read only when some world overflowed
+  long long* d_before = c->d_status + 4 * (size_t)c->d_status_cap;
+  CUDA_TRY(cpk_gather_status(c->d_worlds, c->d_ids, n, d_before, c->stream));
+  std::vector<long long> after(4 * (size_t)n);
   CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
   if (tuning || !use_graph) {
     for (int s = 0; s < nsteps; s++)
@@ -1442,6 +1455,12 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
     }
   }
   c->launches += 1;
+  bool any = false;
+  for (int i = 0; i < n && !any; i++) any = after[4 * i] != 0;
+  if (!any) return CP_OK;
+  std::vector<long long> before(4 * (size_t)n);
+  CUDA_TRY(cudaMemcpyAsync(before.data(), d_before, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
   for (int i = 0; i < n; i++) {
     if (after[4 * i] != 0) {  // overflowed part way: grow and finish on the plain path
       int id = order[i];

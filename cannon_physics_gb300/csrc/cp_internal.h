@@ -80,8 +80,9 @@ struct cp_ctx {
   int ngroups = 0;
   int group_bodies = 640;   // a group gathers consecutive (similar-size) worlds up to this many bodies
   int plain_variant = 2 * cpk_num_solve_variants();  // (pre 128x4, solve 128x4) for single small worlds
-  long long* d_status = nullptr;
+  long long* d_status = nullptr;  // 4 per world after a batched call, then 4 per world before it
   int d_status_cap = 0;
+  std::vector<int> dev_order, dev_gstart;  // what d_ids and d_gstart hold
   int sms = 0;
   std::vector<int> blocks_pre, blocks_solve;  // resident blocks per SM, per kernel variant
   // autotuner: one timed step per kernel variant, then the fastest
