@@ -241,6 +241,7 @@ def run_served(args, device):
         "max_ms": st["max_ms"], "requests": len(reqs), "completed": st["completed"],
         "offered_body_steps_per_s": offered / args.serve_window, "span_s": st["span_s"],
         "submit_lag_max_s": lag[0], "ticks": st["ticks"], "steps_per_tick": args.serve_tick,
+        "step_s": st["device_s"],  # time the server thread spent in step launches (the rest: admission, uploads, results)
         "bytes_peak_gb": st["bytes_peak"] / 1e9,
         "plain_per_request": {"value": plain, "unit": UNIT,
                               "sample": f"{len(sample)} of the requests, each alone through cp_world_step ({plain_bs} body-steps)"},
