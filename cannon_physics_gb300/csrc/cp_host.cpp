@@ -575,7 +575,7 @@ int plain_steps(cp_ctx* c, int id, double dt, int nsteps) {
     for (long long s = done; s < target; s++) {
       CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_one, c->d_one_group, 1, dt, c->d_queue, 1, 1, c->stream,
                                w.nb > 512 ? 0 : c->plain_variant, 1, w.nb));
-      c->launches += 3;
+      c->launches += 2;  // the two step kernels (the queue reset is a memset)
     }
     st = read_params(c, w, p);
     if (st) return st;
@@ -1187,7 +1187,7 @@ int cp_world_step_static(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
   const int variant = w.nb > 512 ? 0 : c->plain_variant;
   for (int s = 0; s < nsteps; s++) {
     CUDA_TRY(cpk_launch_step(d_world, d_list, d_list + 1, 1, dt, c->d_queue, 1, 1, c->stream, variant, 1, w.nb));
-    c->launches += 3;
+    c->launches += 2;  // the two step kernels (the queue reset is a memset)
   }
   DWorldParams p;
   st = read_params(c, w, p);  // synchronises the stream: the host buffers above are no longer in use
@@ -1425,7 +1425,7 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
     CUDA_TRY(cudaGraphLaunch(c->graph, c->stream));
   }
   CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
-  c->launches += 3LL * nsteps + 1;
+  c->launches += 2LL * nsteps + 1;  // two step kernels per step and the status gather before them
   CUDA_TRY(cpk_gather_status(c->d_worlds, c->d_ids, n, c->d_status, c->stream));
   CUDA_TRY(cudaMemcpyAsync(after.data(), c->d_status, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
