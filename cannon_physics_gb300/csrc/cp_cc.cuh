@@ -543,6 +543,7 @@ __device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, in
   const DBody& BB = W.bodies[bB];
   d3 ni = dneg(sep);
   d3 pa = d3of(ld3(BA.pos)), pb = d3of(ld3(BB.pos));
+  const ContactHead head = contact_head(C, bA, bB, shA, shB, rsi, rsj);
   int k = 0;
   for (int i = 0; i < nin; i++) {
     double dd = depth[i];
@@ -558,7 +559,7 @@ __device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, in
       g.ni = f3{(float)ni.x, (float)ni.y, (float)ni.z};
       g.ri = f3{(float)ri.x, (float)ri.y, (float)ri.z};
       g.rj = f3{(float)rj.x, (float)rj.y, (float)rj.z};
-      fill_contact(C, W.ctmp[start + k], bA, bB, shA, shB, rsi, rsj, g);
+      put_contact(W.ctmp[start + k], head, g);
       k++;
     }
   }

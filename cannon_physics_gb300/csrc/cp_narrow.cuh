@@ -27,25 +27,44 @@ struct ContactOut {
 // narrow_phase.dart:492-528 createContactEquation: everything except the
 // geometry.  shA/shB are the shapes handed to the resolver (type order),
 // rsi/rsj the shapes ContactEquation.si/.sj end up holding.
-DI void fill_contact(const NarrowCtx& C, DContact& c, int bA, int bB, int shA, int shB, int rsi, int rsj, const ContactOut& g) {
+// The fields a pair's contacts share (Narrowphase.createContactEquation,
+// narrow_phase.dart:489-528): bodies, shapes, response flag, material and
+// restitution; computed once per pair, not once per contact.
+struct ContactHead {
+  int bi, bj, si, sj, enabled, pair, cm;
+  double restitution;
+};
+DI ContactHead contact_head(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj) {
   const DWorld& W = *C.W;
   const DBody& A = W.bodies[bA];
   const DBody& B = W.bodies[bB];
   const DShape& SA = W.shapes[shA];
   const DShape& SB = W.shapes[shB];
-  c.bi = bA; c.bj = bB; c.si = rsi; c.sj = rsj;
-  st3(c.ni, g.ni); st3(c.ri, g.ri); st3(c.rj, g.rj);
-  c.enabled = (A.flags & BF_RESPONSE) && (B.flags & BF_RESPONSE) && SA.response && SB.response;
-  c.pair = C.pair;
-  c.cm = C.cm;
-  c.frow = -1;
-  c.slip = 0.0;
+  ContactHead h;
+  h.bi = bA; h.bj = bB; h.si = rsi; h.sj = rsj;
+  h.enabled = (A.flags & BF_RESPONSE) && (B.flags & BF_RESPONSE) && SA.response && SB.response;
+  h.pair = C.pair;
+  h.cm = C.cm;
   double rest = W.cms[C.cm].restitution;
   int ma = SA.material >= 0 ? SA.material : A.material;
   int mb = SB.material >= 0 ? SB.material : B.material;
   if (ma >= 0 && mb >= 0 && W.mats[ma].restitution >= 0 && W.mats[mb].restitution >= 0)
     rest = W.mats[ma].restitution * W.mats[mb].restitution;
-  c.restitution = rest;
+  h.restitution = rest;
+  return h;
+}
+DI void put_contact(DContact& c, const ContactHead& h, const ContactOut& g) {
+  c.bi = h.bi; c.bj = h.bj; c.si = h.si; c.sj = h.sj;
+  st3(c.ni, g.ni); st3(c.ri, g.ri); st3(c.rj, g.rj);
+  c.enabled = h.enabled;
+  c.pair = h.pair;
+  c.cm = h.cm;
+  c.frow = -1;
+  c.slip = 0.0;
+  c.restitution = h.restitution;
+}
+DI void fill_contact(const NarrowCtx& C, DContact& c, int bA, int bB, int shA, int shB, int rsi, int rsj, const ContactOut& g) {
+  put_contact(c, contact_head(C, bA, bB, shA, shB, rsi, rsj), g);
 }
 
 DI int reserve(const NarrowCtx& C, int n) {
@@ -346,6 +365,8 @@ __device__ __noinline__ int plane_convex(const NarrowCtx& C, int bA, int bB, int
   if (start < 0) return n;
   const DBody& BA = W.bodies[bA];
   const DBody& BB = W.bodies[bB];
+  const f3 pA = ld3(BA.pos), pB = ld3(BB.pos);
+  const ContactHead head = contact_head(C, bA, bB, shA, shB, rsi, rsj);
   int k = 0;
   for (int i = 0; i < nv; i++) {
     if (dv[i] <= 0.0) {
@@ -354,9 +375,9 @@ __device__ __noinline__ int plane_convex(const NarrowCtx& C, int bA, int bB, int
       g.ri = sub(proj, xA);
       g.ni = wn;
       g.rj = sub(wv[i], xB);
-      g.ri = rel(g.ri, xA, BA);
-      g.rj = rel(g.rj, xB, BB);
-      fill_contact(C, W.ctmp[start + k], bA, bB, shA, shB, rsi, rsj, g);
+      g.ri = sub(add(g.ri, xA), pA);  // rel(): r + x - body.position
+      g.rj = sub(add(g.rj, xB), pB);
+      put_contact(W.ctmp[start + k], head, g);
       k++;
     }
   }
