@@ -143,6 +143,25 @@ def profiled_traffic():
     return None
 
 
+def profiled_fp64_ops():
+    """Binary64 add, multiply and fused multiply-add thread-instructions per
+    body-step of the two step kernels, from the committed ncu summary
+    (profiles/step_kernels_fp64.txt: 'binary64_ops_per_body_step: X')."""
+    path = os.path.join(ROOT, "profiles", "step_kernels_fp64.txt")
+    try:
+        for ln in open(path):
+            if ln.startswith("binary64_ops_per_body_step:"):
+                return float(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+# GB300's nominal binary64 rate: 1.25 TFLOP/s, i.e. 625 G fused multiply-adds
+# (thread-instructions) per second
+FP64_PEAK_G_PER_S = 625.0
+
+
 def build_worlds(n, seed):
     from cannon_physics_gb300 import scenes
     return scenes.batch_worlds(n, seed)
@@ -353,6 +372,7 @@ def run_ours(args):
     kernel_ms = graph_ms / max(graph_steps, 1)
     achieved = ALG_BYTES_PER_BODY_STEP * total / (kernel_ms / 1e3) / 1e9
     traffic_per_bs = profiled_traffic()
+    fp64_per_bs = profiled_fp64_ops()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -366,6 +386,12 @@ def run_ours(args):
                      "alg_bytes_per_body_step": ALG_BYTES_PER_BODY_STEP, "kernel_ms": kernel_ms,
                      "traffic": None if traffic_per_bs is None else traffic_per_bs * total,
                      "note": "bound by binary64 issue (64 cycles per warp instruction per sub-partition on GB300), barriers and load latency, not HBM bandwidth; traffic is DRAM bytes of one step from the committed ncu capture, scaled by bodies"},
+        "fp64": None if fp64_per_bs is None else {
+            "ops_per_body_step": fp64_per_bs, "achieved": fp64_per_bs * value / 1e9, "peak": FP64_PEAK_G_PER_S,
+            "unit": "G binary64 thread-instructions/s", "frac": fp64_per_bs * value / 1e9 / FP64_PEAK_G_PER_S,
+            "peak_kind": "nominal (1.25 TFLOP/s)",
+            "note": "add, multiply and fused multiply-add instructions per body-step from the committed ncu capture; "
+                    "the binary64 pipe itself is 41-52 % busy because most binary64 warp instructions run with part of their lanes"},
         "gpu_launches": launches,
         "clocks": clk,
         "autotune": dict(ctx.autotune_info(), warmup_calls=args.warmup + tune_calls),
