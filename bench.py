@@ -387,8 +387,8 @@ def run_ours(args):
                      "traffic": None if traffic_per_bs is None else traffic_per_bs * total,
                      "note": "bound by binary64 issue (64 cycles per warp instruction per sub-partition on GB300), barriers and load latency, not HBM bandwidth; traffic is DRAM bytes of one step from the committed ncu capture, scaled by bodies"},
         "fp64": None if fp64_per_bs is None else {
-            "ops_per_body_step": fp64_per_bs, "achieved": fp64_per_bs * value / 1e9, "peak": FP64_PEAK_G_PER_S,
-            "unit": "G binary64 thread-instructions/s", "frac": fp64_per_bs * value / 1e9 / FP64_PEAK_G_PER_S,
+            "ops_per_body_step": fp64_per_bs, "achieved": fp64_per_bs * value / ws / 1e9, "peak": FP64_PEAK_G_PER_S,
+            "unit": "G binary64 thread-instructions/s per GPU", "frac": fp64_per_bs * value / ws / 1e9 / FP64_PEAK_G_PER_S,
             "peak_kind": "nominal (1.25 TFLOP/s)",
             "note": "add, multiply and fused multiply-add instructions per body-step from the committed ncu capture; "
                     "the binary64 pipe itself is 41-52 % busy because most binary64 warp instructions run with part of their lanes"},
