@@ -73,6 +73,23 @@ def dist_info():
     return ws, rank, local
 
 
+def rank_seed(rank, worlds):
+    """Scene seed of a rank's world set: weak scaling, every rank steps its own
+    `worlds` independent worlds and no data crosses ranks."""
+    return 1000 + rank * worlds
+
+
+def reduce_over_ranks(x, ws, op, device):
+    """x reduced over the ranks ('max' for times, 'sum' for counts)."""
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 class Clocks:
     """nvidia-smi clock / throttle samples during the timed region."""
 
@@ -281,7 +298,7 @@ def run_ours(args):
     from cannon_physics_gb300 import engine
 
     B.build()
-    scs = build_worlds(args.worlds, 1000 + rank * args.worlds)  # weak scaling: each rank its own worlds
+    scs = build_worlds(args.worlds, rank_seed(rank, args.worlds))
     for s in scs:
         engine.setup_scene(s)
     ctx = engine.Context(device=local)
@@ -325,11 +342,9 @@ def run_ours(args):
     ms = e0.elapsed_time(e1)
     graph_ms, graph_steps = ctx.batch_profile()
     phases = ctx.phase_profile()
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = total * ws * args.steps / (ms / 1e3)
+    ms = reduce_over_ranks(ms, ws, "max", "cuda")
+    job_bodies = reduce_over_ranks(total, ws, "sum", "cuda")  # each rank its own worlds
+    value = job_bodies * args.steps / (ms / 1e3)
 
     # end to end through the C ABI with pinned host buffers
     ft = torch.zeros(total * 6, dtype=torch.float32, pin_memory=True)
@@ -343,11 +358,8 @@ def run_ours(args):
         batch.get_poses(poses.data_ptr())
     e2e_sec = time.perf_counter() - t0
     barrier()
-    if ws > 1:
-        t = torch.tensor([e2e_sec], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_sec = float(t.item())
-    e2e = {"value": total * ws * e2e_steps / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": total * 6 * 4,
+    e2e_sec = reduce_over_ranks(e2e_sec, ws, "max", "cuda")
+    e2e = {"value": job_bodies * e2e_steps / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": total * 6 * 4,
            "d2h_bytes_per_step": total * 13 * 4, "steps": e2e_steps}
     assert np.isfinite(poses.numpy()).all()
 
