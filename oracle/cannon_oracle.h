@@ -4,8 +4,9 @@
  * TEST INFRASTRUCTURE ONLY.  The oracle is a sequential C++ restatement of
  * cannon_physics' World.step (Dart, lib/world/world_class.dart:433-701 and
  * everything it calls).  Only tests/, __graft_entry__.smoke() and bench.py's
- * CPU-baseline leg may load it, as the checker.  Nothing in the
- * cannon_physics_gb300 package links or calls it.
+ * CPU-baseline legs load it, to compare the GPU path's results with and to
+ * time the CPU baseline.  Nothing in the cannon_physics_gb300 package links or
+ * calls it.
  *
  * Arithmetic contract ("mode R"): every scalar is an IEEE binary64 value and
  * every Vector3 / Quaternion / Matrix3 component is rounded to binary32 at the

@@ -1,7 +1,8 @@
 """ctypes front end of the CPU oracle -- test infrastructure only.
 
-Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, as
-the checker.  The cannon_physics_gb300 package never imports this module.
+Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs, to
+compare the GPU path's results with and to time the CPU baseline.  The
+cannon_physics_gb300 package never imports this module.
 """
 import ctypes as C
 
