@@ -316,7 +316,9 @@ int cp_batch_step(cp_ctx* ctx, const int32_t* world_ids, int32_t n, double dt, i
 int cp_batch_set_forces(cp_ctx* ctx, const int32_t* world_ids, int32_t n, const float* ft, int64_t total_bodies);
 int cp_batch_get_poses(cp_ctx* ctx, const int32_t* world_ids, int32_t n, float* out, int64_t total_bodies);
 
-/* Number of GPU kernel launches issued by this context so far. */
+/* Number of this library's GPU kernel launches issued by this context so far
+ * (two per batched or single-world step, plus the status and I/O kernels;
+ * memory copies and sets are not counted). */
 int64_t cp_kernel_launches(cp_ctx* ctx);
 
 /* The CUDA stream (cudaStream_t) all work of the context runs on, so callers
