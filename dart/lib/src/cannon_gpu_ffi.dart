@@ -196,7 +196,11 @@ class CannonGpu {
         worldSetBodies = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Pointer<CpBodyDesc>, Int32),
             int Function(Pointer<CpCtx>, int, Pointer<CpBodyDesc>, int)>('cp_world_set_bodies'),
         worldGetInfo = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Pointer<CpStepInfo>),
-            int Function(Pointer<CpCtx>, int, Pointer<CpStepInfo>)>('cp_world_get_info');
+            int Function(Pointer<CpCtx>, int, Pointer<CpStepInfo>)>('cp_world_get_info'),
+        worldStepStatic = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Double, Int32),
+            int Function(Pointer<CpCtx>, int, double, int)>('cp_world_step_static'),
+        batchStep = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Pointer<Int32>, Int32, Double, Int32),
+            int Function(Pointer<CpCtx>, Pointer<Int32>, int, double, int)>('cp_batch_step');
 
   final int Function() abiVersion;
   final Pointer<Uint8> Function() lastError;
@@ -210,6 +214,13 @@ class CannonGpu {
   final int Function(Pointer<CpCtx>, int, Pointer<CpBodyDesc>, int) worldGetBodies;
   final int Function(Pointer<CpCtx>, int, Pointer<CpBodyDesc>, int) worldSetBodies;
   final int Function(Pointer<CpCtx>, int, Pointer<CpStepInfo>) worldGetInfo;
+
+  /// `worldStep` without device allocation (fixed step scratch; a world too
+  /// large for it, or a step that overflows a list, returns CP_ERR_CAPACITY).
+  final int Function(Pointer<CpCtx>, int, double, int) worldStepStatic;
+
+  /// Many independent worlds stepped together: ids, count, dt, steps.
+  final int Function(Pointer<CpCtx>, Pointer<Int32>, int, double, int) batchStep;
 
   /// The thread-local message of the last failing call.
   String errorText() {
