@@ -43,6 +43,10 @@ METRIC = "body-steps/s batched vs plain on 1 GB300 at <=1e-9 rel; p50/p99 reques
 UNIT = "body-steps/s"
 ALG_BYTES_PER_BODY_STEP = 208  # binary32 state x,q,v,w and invInertiaWorld read+written, static per-body data read
 DT = 1.0 / 60.0
+# untimed steps before every arm's timed range: the columns have landed and
+# the worlds are in contact by then (the autotuner's second round ends near
+# call 62)
+PREROLL = 80
 
 
 def parse():
@@ -50,12 +54,15 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=120)
     ap.add_argument("--warmup", type=int, default=3, help="untimed steps before the autotuner's calls")
+    ap.add_argument("--preroll", type=int, default=PREROLL,
+                    help="every arm (GPU, e2e, plain, CPU baseline, reference) times steps preroll .. preroll+steps-1 "
+                         "of the same worlds; the warm-up and autotuner calls are part of the GPU arm's pre-roll")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--worlds", type=int, default=4096)
     ap.add_argument("--plain-worlds", type=int, default=48)
-    ap.add_argument("--plain-steps", type=int, default=10)
     ap.add_argument("--cpu-sample", type=int, default=16, help="every k-th world goes into the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the single-world configurations C1-C3")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="served form: Poisson arrival rate, requests/s")
     ap.add_argument("--serve-window", type=float, default=1.0, help="served form: seconds of arrivals")
     ap.add_argument("--serve-tick", type=int, default=4, help="served form: steps per tick")
@@ -192,21 +199,68 @@ def workload_config(n_worlds, total_bodies):
             "l2": "inputs larger than L2 (body state alone is ~240 MB)", "parity": "bit-exact vs oracle"}
 
 
-def cpu_baseline(scenes_list, every, warmup, steps, threads=None):
+def cpu_baseline(scenes_list, every, preroll, steps, threads=None):
     """The oracle port on the host cores, one world per thread, over the same
-    step range as the timed GPU region."""
+    step range as the timed GPU region (steps preroll .. preroll+steps-1)."""
     from oracle import oracle_py as O
     sample = scenes_list[::every]
     worlds = [O.OracleWorld(s) for s in sample]
     threads = threads or os.cpu_count() or 1
     bodies = sum(s.num_bodies for s in sample)
-    O.step_parallel(worlds, DT, warmup, threads)
+    O.step_parallel(worlds, DT, preroll, threads)
     t0 = time.perf_counter()
     O.step_parallel(worlds, DT, steps, threads)
     sec = time.perf_counter() - t0
     return {"value": bodies * steps / sec, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{len(sample)} of the worlds (every {every}th, {bodies} bodies), steps {warmup}..{warmup + steps - 1}, "
-                      "one world per thread"}
+            "timed_steps": [preroll, preroll + steps - 1],
+            "sample": f"{len(sample)} of the worlds (every {every}th, {bodies} bodies), steps {preroll}..{preroll + steps - 1}, "
+                      f"one world per thread, {threads} thread{'s' if threads > 1 else ''}"}
+
+
+# The single-world configurations, each timed through the plain drop-in
+# (one cp_world_step call per step, as GpuWorld.internalStep makes) and
+# through the oracle on one host thread from the same state: name, scene,
+# untimed pre-roll (mid-horizon, in contact), GPU steps timed, CPU steps timed
+PLAIN_CONFIGS = [
+    ("C1", "spheres_on_plane", "64 Sphere(0.5) on a Plane, NaiveBroadphase, GSSolver 10 iterations, dt 1/60", 300, 60, 60),
+    ("C2", "box_pile", "4096 Box (half-extents U[0.2,0.5]) pile in a 16x16 footprint, SAPBroadphase x, GSSolver 20 iterations, "
+                       "friction 0.4, dt 1/60", 150, 10, 3),
+    ("C3", "mixed_chains", "8192 bodies 40/40/20 Sphere/Box/Cylinder(10), 128 chains of 16 (P2P/Hinge/Distance), "
+                           "GridBroadphase cell 1, sleeping, GSSolver 15 iterations, dt 1/120", 120, 10, 3),
+]
+
+
+def plain_configs(ctx, only=None):
+    from cannon_physics_gb300 import engine, scenes
+    from oracle import oracle_py as O
+    out = {}
+    for name, make, desc, pre, k_gpu, k_cpu in PLAIN_CONFIGS:
+        if only and name not in only:
+            continue
+        sc = engine.setup_scene(getattr(scenes, make)())
+        w = ctx.world(sc)
+        w.step(sc.dt, pre)
+        t0 = time.perf_counter()
+        for _ in range(k_gpu):
+            w.step(sc.dt, 1)
+        gsec = time.perf_counter() - t0
+        inf = w.info()
+        ow = O.OracleWorld(O.setup_scene(getattr(scenes, make)()))
+        ow.load_state(w)
+        t0 = time.perf_counter()
+        ow.step(sc.dt, k_cpu)
+        csec = time.perf_counter() - t0
+        w.destroy()
+        g = sc.num_bodies * k_gpu / gsec
+        c = sc.num_bodies * k_cpu / csec
+        out[name] = {"workload": desc, "bodies": sc.num_bodies, "ms_per_step": gsec * 1e3 / k_gpu, "value": g, "unit": UNIT,
+                     "timed_steps": [pre, pre + k_gpu - 1], "pairs": inf.num_pairs, "contacts": inf.num_contacts,
+                     "rows": inf.num_rows, "levels": inf.num_levels,
+                     "cpu_1thread": {"ms_per_step": csec * 1e3 / k_cpu, "value": c, "kind": "port", "cores": 1,
+                                     "timed_steps": [pre, pre + k_cpu - 1],
+                                     "sample": "the oracle continued from the GPU world's state at the same step"},
+                     "gpu_over_cpu_1thread": g / c}
+    return out
 
 
 def run_served(args, device):
@@ -311,12 +365,24 @@ def run_ours(args):
 
     for _ in range(args.warmup):
         batch.step(DT)
+    calls = args.warmup
     # the autotuner times one kernel variant per batched call; it tunes again
     # once the worlds are in contact (call 48)
-    tune_calls = 0
-    while args.variant is None and (ctx.autotune_info()["variant"] < 0 or tune_calls < 48) and tune_calls < 80:
+    while args.variant is None and (ctx.autotune_info()["variant"] < 0 or calls < 48) and calls < args.preroll:
         batch.step(DT)
-        tune_calls += 1
+        calls += 1
+    if args.variant is None and ctx.autotune_info()["variant"] < 0:
+        raise SystemExit(f"--preroll {args.preroll} ends before the autotuner has chosen a kernel variant")
+    tune_calls = calls - args.warmup
+    while calls < args.preroll:
+        batch.step(DT)
+        calls += 1
+    timed = [args.preroll, args.preroll + args.steps - 1]
+    # a second copy of the worlds for the end-to-end leg, at the same step
+    e2e_worlds = [ctx.world(s) for s in scs]
+    e2e_batch = engine.Batch(ctx, e2e_worlds)
+    for _ in range(args.preroll):
+        e2e_batch.step(DT)
     ctx.batch_profile()
     ctx.phase_profile()
 
@@ -346,36 +412,44 @@ def run_ours(args):
     job_bodies = reduce_over_ranks(total, ws, "sum", "cuda")  # each rank its own worlds
     value = job_bodies * args.steps / (ms / 1e3)
 
-    # end to end through the C ABI with pinned host buffers
+    # end to end through the C ABI with pinned host buffers, on the second
+    # copy of the worlds over the same steps
     ft = torch.zeros(total * 6, dtype=torch.float32, pin_memory=True)
     poses = torch.empty(total * 13, dtype=torch.float32, pin_memory=True)
-    e2e_steps = max(3, args.steps // 4)
     barrier()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        batch.set_forces(ft.data_ptr())
-        batch.step(DT)
-        batch.get_poses(poses.data_ptr())
+    for _ in range(args.steps):
+        e2e_batch.set_forces(ft.data_ptr())
+        e2e_batch.step(DT)
+        e2e_batch.get_poses(poses.data_ptr())
     e2e_sec = time.perf_counter() - t0
     barrier()
     e2e_sec = reduce_over_ranks(e2e_sec, ws, "max", "cuda")
-    e2e = {"value": job_bodies * e2e_steps / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": total * 6 * 4,
-           "d2h_bytes_per_step": total * 13 * 4, "steps": e2e_steps}
+    e2e = {"value": job_bodies * args.steps / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": total * 6 * 4,
+           "d2h_bytes_per_step": total * 13 * 4, "steps": args.steps, "timed_steps": timed}
     assert np.isfinite(poses.numpy()).all()
+    for w in e2e_worlds:
+        w.destroy()
 
-    # plain single-world path on a sample of the same worlds (fresh copies)
+    # plain single-world path on a sample of the same worlds (fresh copies,
+    # same pre-roll, same timed steps), one cp_world_step call per step as
+    # GpuWorld.internalStep makes
     idx = np.linspace(0, len(scs) - 1, args.plain_worlds).astype(int)
     plain_worlds = [ctx.world(scs[i]) for i in idx]
     for w in plain_worlds:
-        w.step(DT, 1)
+        w.step(DT, args.preroll)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for w in plain_worlds:
-        w.step(DT, args.plain_steps)
+        for _ in range(args.steps):
+            w.step(DT, 1)
     plain_sec = time.perf_counter() - t0
     plain_bodies = sum(w.n for w in plain_worlds)
-    plain = {"value": plain_bodies * args.plain_steps / plain_sec, "unit": UNIT,
-             "sample": f"{len(plain_worlds)} worlds ({plain_bodies} bodies) x {args.plain_steps} steps, one cp_world_step per world"}
+    plain = {"value": plain_bodies * args.steps / plain_sec, "unit": UNIT, "timed_steps": timed,
+             "sample": f"{len(plain_worlds)} of the worlds ({plain_bodies} bodies), one cp_world_step call per step"}
+    for w in plain_worlds:
+        w.destroy()
+    configs = plain_configs(ctx) if not args.no_configs else None
 
     if rank != 0:
         ctx.close()
@@ -387,6 +461,7 @@ def run_ours(args):
     fp64_per_bs = profiled_fp64_ops()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "timed_steps": timed,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded SplitMix64 scenes; the reference publishes no benchmark scenes)",
         "config": workload_config(args.worlds, total),
@@ -406,14 +481,16 @@ def run_ours(args):
                     "the binary64 pipe itself is 41-52 % busy because most binary64 warp instructions run with part of their lanes"},
         "gpu_launches": launches,
         "clocks": clk,
-        "autotune": dict(ctx.autotune_info(), warmup_calls=args.warmup + tune_calls),
+        "autotune": dict(ctx.autotune_info(), warmup_calls=args.warmup, tune_calls=tune_calls, preroll=args.preroll),
+        "plain_configs": configs,
         "phase_share": {k: round(v / max(sum(phases.values()), 1.0), 4) for k, v in phases.items()},
     }
     ctx.close()
     if not args.no_serve:
         line["served"] = run_served(args, local)
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(scs, args.cpu_sample, args.warmup, args.steps)
+        line["cpu_baseline"] = cpu_baseline(scs, args.cpu_sample, args.preroll, args.steps)
+        line["cpu_baseline_1thread"] = cpu_baseline(scs, 4 * args.cpu_sample, args.preroll, args.steps, threads=1)
     print(json.dumps(line), flush=True)
 
 
@@ -428,18 +505,20 @@ def run_reference(args):
     worlds = [O.OracleWorld(s) for s in scs]
     threads = os.cpu_count() or 1
     total = sum(s.num_bodies for s in scs)
-    O.step_parallel(worlds, DT, args.warmup, threads)
+    O.step_parallel(worlds, DT, args.preroll, threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         O.step_parallel(worlds, DT, 1, threads)
     sec = time.perf_counter() - t0
     value = total * args.steps / sec
+    timed = [args.preroll, args.preroll + args.steps - 1]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "timed_steps": timed, "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args.worlds, total),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"all {args.worlds} worlds, every step; the Dart reference needs a Flutter SDK, "
-                                       "absent here and on the GPU box, so its C++ port (oracle/) runs it"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "timed_steps": timed,
+                             "sample": f"all {args.worlds} worlds, steps {timed[0]}..{timed[1]} after {args.preroll} untimed "
+                                       "steps; the Dart reference needs a Flutter SDK, absent here and on the GPU box, "
+                                       "so its C++ port (oracle/) runs it"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

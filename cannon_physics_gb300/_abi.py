@@ -92,6 +92,29 @@ class BodyDesc(C.Structure):
         ("shape", C.c_int32),
         ("fixed_rotation", C.c_int32),
         ("aabb_needs_update", C.c_int32),
+        ("interpolated_position", f3),
+        ("interpolated_quaternion", f4),
+        ("pad0", C.c_int32),
+    ]
+
+
+class BodyState(C.Structure):
+    _fields_ = [
+        ("position", f3),
+        ("quaternion", f4),
+        ("velocity", f3),
+        ("angular_velocity", f3),
+        ("force", f3),
+        ("torque", f3),
+        ("previous_position", f3),
+        ("previous_quaternion", f4),
+        ("interpolated_position", f3),
+        ("interpolated_quaternion", f4),
+        ("sleep_state", C.c_int32),
+        ("wake_up_after_narrowphase", C.c_int32),
+        ("aabb_needs_update", C.c_int32),
+        ("pad0", C.c_int32),
+        ("time_last_sleepy", C.c_double),
     ]
 
 
@@ -210,7 +233,8 @@ class StepInfo(C.Structure):
         ("status", C.c_int32),
         ("num_bodies", C.c_int32),
         ("num_levels", C.c_int32),
-        ("pad", C.c_int32),
+        ("substeps", C.c_int32),
+        ("accumulator", C.c_double),
     ]
 
 
@@ -247,6 +271,7 @@ def np_dtype(struct_cls):
 
 SHAPE_DTYPE = np_dtype(ShapeDesc)
 BODY_DTYPE = np_dtype(BodyDesc)
+BODY_STATE_DTYPE = np_dtype(BodyState)
 MATERIAL_DTYPE = np_dtype(Material)
 CONTACT_MATERIAL_DTYPE = np_dtype(ContactMaterial)
 CONSTRAINT_DTYPE = np_dtype(ConstraintDesc)
@@ -268,6 +293,7 @@ def default_bodies(n):
     b = np.zeros(n, dtype=BODY_DTYPE)
     b["quaternion"][:, 3] = 1.0
     b["previous_quaternion"][:, 3] = 1.0
+    b["interpolated_quaternion"][:, 3] = 1.0
     b["shape_orientation"][:, 3] = 1.0
     b["linear_factor"] = 1.0
     b["angular_factor"] = 1.0

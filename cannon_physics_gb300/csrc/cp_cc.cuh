@@ -450,7 +450,7 @@ DI bool cc_stage1(const DWorld& W, int shA, int shB, f3 xAf, f3 xBf, q4 qAf, q4 
 // One out-of-line copy: the resolver is large and is reached from several
 // dispatch cases; inlining it at each bloats the step kernel's instruction footprint.
 // U1: the bound U that stage 1 already found for this pair, or NaN.
-__device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xAf, f3 xBf, q4 qAf, q4 qBf, int& start, float U1) {
+static __device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xAf, f3 xBf, q4 qAf, q4 qBf, int& start, float U1) {
   const DWorld& W = *C.W;
   const DShape& SA = W.shapes[shA];
   const DShape& SB = W.shapes[shB];

@@ -13,8 +13,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -337,6 +339,10 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   size_t o_ba = L.take(sizeof(float) * (w.broadphase == CP_BROAD_GRID ? 3 * 4096 : 1));
   size_t o_hk = L.take(sizeof(long long) * hash_cap);
   size_t o_hw = L.take(sizeof(int) * hash_cap);
+  size_t o_wd = L.take(sizeof(DWide));
+  size_t o_wp = L.take(sizeof(int) * (CP_WIDE_SCAN_BLOCKS + 1));
+  size_t o_wv = L.take(sizeof(float) * 6 * (size_t)(nb + 1));
+  size_t o_wf = L.take((size_t)nb + 1);
   if (!base) return L.off;
   d.bscr = (DBodyScr*)(base + o_bscr);
   d.sap_tmp = (int*)(base + o_tmp);
@@ -369,6 +375,10 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   d.sw_b = (int2*)(base + o_swb);
   d.sw_orig = (int*)(base + o_swo);
   d.sw_cap = swc;
+  d.wide = (DWide*)(base + o_wd);
+  d.wpart = (int*)(base + o_wp);
+  d.wvel = (float*)(base + o_wv);
+  d.wflag = (unsigned char*)(base + o_wf);
   return L.off;
 }
 
@@ -402,6 +412,8 @@ int alloc_scratch(cp_ctx* c, WorldRec& w) {
   if (st) return st;
   w.scratch = base;
   scratch_layout(w, base);
+  // the wide path's index-check record must start clear
+  CUDA_TRY(cudaMemsetAsync(w.dw.wide, 0, sizeof(DWide), c->stream));
   return CP_OK;
 }
 
@@ -424,6 +436,8 @@ void body_to_device(const cp_body_desc& s, DBody& b) {
   std::memcpy(b.shape_quat, s.shape_orientation, 16);
   std::memcpy(b.prev_pos, s.previous_position, 12);
   std::memcpy(b.prev_quat, s.previous_quaternion, 16);
+  std::memcpy(b.interp_pos, s.interpolated_position, 12);
+  std::memcpy(b.interp_quat, s.interpolated_quaternion, 16);
   b.mass = s.mass; b.inv_mass = s.inv_mass;
   b.lin_damp = s.linear_damping; b.ang_damp = s.angular_damping;
   b.sleep_speed_limit = s.sleep_speed_limit; b.sleep_time_limit = s.sleep_time_limit;
@@ -455,6 +469,8 @@ void body_from_device(const DBody& b, cp_body_desc& s) {
   std::memcpy(s.shape_orientation, b.shape_quat, 16);
   std::memcpy(s.previous_position, b.prev_pos, 12);
   std::memcpy(s.previous_quaternion, b.prev_quat, 16);
+  std::memcpy(s.interpolated_position, b.interp_pos, 12);
+  std::memcpy(s.interpolated_quaternion, b.interp_quat, 16);
   s.mass = b.mass; s.inv_mass = b.inv_mass;
   s.linear_damping = b.lin_damp; s.angular_damping = b.ang_damp;
   s.sleep_speed_limit = b.sleep_speed_limit; s.sleep_time_limit = b.sleep_time_limit;
@@ -561,7 +577,34 @@ int kernel_check() {
   return CP_OK;
 }
 
-int plain_steps(cp_ctx* c, int id, double dt, int nsteps) {
+bool is_wide(const cp_ctx* c, const WorldRec& w) { return c->wide_bodies > 0 && w.nb >= c->wide_bodies; }
+
+WideShape wide_shape(const WorldRec& w) {
+  WideShape s;
+  s.nb = w.nb;
+  s.nbins = w.broadphase == CP_BROAD_GRID ? w.nbins : 0;
+  s.broadphase = w.broadphase;
+  s.n_nocollide = w.n_nocollide;
+  s.pairs_cap = w.pairs_cap;
+  s.contacts_cap = w.contacts_cap;
+  s.rows_cap = w.rows_cap;
+  s.bins_cap = w.bins_cap;
+  s.smem_vel = w.nb <= cpk_wide_smem_vel_max();
+  return s;
+}
+
+// Reports a failed index check of the wide sweep kernel (the kernel skipped
+// the access) as an error of the call that launched it.
+int wide_check(cp_ctx* c, const WorldRec& w, int id) {
+  int chk[4] = {0, 0, 0, 0};
+  CUDA_TRY(cpk_wide_check(w.dw, chk, c->stream));
+  if (chk[0] != 0)
+    return fail(CP_ERR_CUDA, "wide sweep kernel index check %d failed: world %d, index %d, bound %d", chk[0], id, chk[1], chk[2]);
+  return CP_OK;
+}
+
+// nsteps internal steps of one world; its time advances by time_inc per step
+int plain_steps(cp_ctx* c, int id, double dt, int nsteps, double time_inc) {
   WorldRec& w = c->worlds[id];
   int st = ensure_dt(c, w, dt);
   if (st) return st;
@@ -570,10 +613,14 @@ int plain_steps(cp_ctx* c, int id, double dt, int nsteps) {
   st = read_params(c, w, p);
   if (st) return st;
   long long target = p.stepnumber + nsteps;
+  const bool wide = is_wide(c, w);
   for (int guard = 0; guard < 64; guard++) {
     long long done = p.stepnumber;
-    for (long long s = done; s < target; s++) {
-      CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_one, c->d_one_group, 1, dt, c->d_queue, 1, 1, c->stream,
+    if (wide && target > done)
+      CUDA_TRY(cpk_launch_wide_steps(c->d_worlds + id, w.dw, wide_shape(w), dt, time_inc, (int)(target - done), c->stream,
+                                     &c->launches));
+    for (long long s = done; s < target && !wide; s++) {
+      CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_one, c->d_one_group, 1, dt, time_inc, c->d_queue, 1, 1, c->stream,
                                w.nb > 512 ? 0 : c->plain_variant, 1, w.nb));
       c->launches += 2;  // the two step kernels (the queue reset is a memset)
     }
@@ -585,7 +632,7 @@ int plain_steps(cp_ctx* c, int id, double dt, int nsteps) {
     st = read_params(c, w, p);
     if (st) return st;
   }
-  st = kernel_check();
+  st = wide ? wide_check(c, w, id) : kernel_check();
   if (st) return st;
   if (p.status != 0 || p.stepnumber != target) return fail(CP_ERR_CAPACITY, "world %d could not complete its steps", id);
   return CP_OK;
@@ -621,6 +668,8 @@ int cp_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc*
     if (b.shape >= num_shapes) return fail(CP_ERR_ARG, "body %d: shape %d out of range", k, b.shape);
     std::memcpy(b.previous_position, b.position, 12);
     std::memcpy(b.previous_quaternion, b.quaternion, 16);
+    std::memcpy(b.interpolated_position, b.position, 12);
+    std::memcpy(b.interpolated_quaternion, b.quaternion, 16);
     b.inv_mass = b.mass > 0 ? 1.0 / b.mass : 0;
     if (b.type < 0) b.type = b.mass <= 0.0 ? CP_BODY_STATIC : CP_BODY_DYNAMIC;
     h3 he = mk3(0, 0, 0);
@@ -716,6 +765,7 @@ int cp_destroy(cp_ctx* c) {
   if (c->d_io_ids) cudaFree(c->d_io_ids);
   if (c->d_io_first) cudaFree(c->d_io_first);
   if (c->d_io) cudaFree(c->d_io);
+  if (c->d_states) cudaFree(c->d_states);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -914,6 +964,7 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
   P.qn_fast = d->quat_normalize_fast != 0; P.has_fgrav = d->has_friction_gravity != 0;
   P.grid_nx = d->grid_n[0]; P.grid_ny = d->grid_n[1]; P.grid_nz = d->grid_n[2];
   P.n_nocollide = (int)nocollide.size() / 2;
+  w.n_nocollide = P.n_nocollide;
   if (d->sap_axis < 0 || d->sap_axis > 2) return fail(CP_ERR_ARG, "sap_axis %d", d->sap_axis);
   if (d->broadphase == CP_BROAD_GRID) {
     if (P.grid_nx <= 0 || P.grid_ny <= 0 || P.grid_nz <= 0) return fail(CP_ERR_ARG, "GridBroadphase: Each dimension's n must be >0");
@@ -1067,6 +1118,8 @@ int read_info(cp_ctx* c, int id, cp_step_info* out) {
   out->status = p.status;
   out->num_bodies = p.nb;
   out->num_levels = p.num_levels;
+  out->substeps = c->worlds[id].last_substeps;
+  out->accumulator = c->worlds[id].accumulator;
   return CP_OK;
 }
 
@@ -1115,7 +1168,72 @@ int cp_world_step(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
   if (nsteps < 0 || !(dt > 0)) return fail(CP_ERR_ARG, "need dt > 0 and nsteps >= 0");
   std::lock_guard<std::mutex> lock(c->mu);
   cudaSetDevice(c->device);
-  return plain_steps(c, id, dt, nsteps);
+  return plain_steps(c, id, dt, nsteps, dt);
+}
+
+int cp_world_internal_step(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
+  int st = check_world(c, id);
+  if (st) return st;
+  if (nsteps < 0 || !(dt > 0)) return fail(CP_ERR_ARG, "need dt > 0 and nsteps >= 0");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  return plain_steps(c, id, dt, nsteps, 0.0);
+}
+
+int cp_world_set_time(cp_ctx* c, int32_t id, double time, int64_t stepnumber, double accumulator) {
+  int st = check_world(c, id);
+  if (st) return st;
+  if (stepnumber < 0 || !std::isfinite(time) || !std::isfinite(accumulator))
+    return fail(CP_ERR_ARG, "need a finite time and accumulator and stepnumber >= 0");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  WorldRec& w = c->worlds[id];
+  const long long sn = stepnumber;
+  CUDA_TRY(cudaMemcpyAsync(&w.dw.P->time, &time, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(&w.dw.P->stepnumber, &sn, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  w.accumulator = accumulator;
+  return CP_OK;
+}
+
+// World.step(dt, timeSinceLastCalled, maxSubSteps), world_class.dart:400-430
+int cp_world_step_interpolated(cp_ctx* c, int32_t id, double dt, double since, int32_t max_sub_steps, int32_t* substeps) {
+  int st = check_world(c, id);
+  if (st) return st;
+  if (!(dt > 0) || max_sub_steps < 0 || !std::isfinite(since))
+    return fail(CP_ERR_ARG, "need dt > 0, a finite timeSinceLastCalled and maxSubSteps >= 0");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  WorldRec& w = c->worlds[id];
+  w.accumulator += since;
+  const auto t0 = std::chrono::steady_clock::now();
+  int n = 0;
+  while (w.accumulator >= dt && n < max_sub_steps) {
+    st = plain_steps(c, id, dt, 1, 0.0);  // returns with the stream synchronised
+    if (st) return st;
+    w.accumulator -= dt;
+    n++;
+    // the reference bails out once the sub-steps took longer than dt (its
+    // performance.now() is in milliseconds)
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (ms > dt * 1000) break;
+  }
+  // Dart's double %: the remainder with the divisor's magnitude, never negative
+  double r = std::fmod(w.accumulator, dt);
+  if (r < 0) r += dt;
+  if (r == 0) r = 0.0;
+  w.accumulator = r;
+  w.last_substeps = n;
+  if (substeps) *substeps = n;
+  CUDA_TRY(cpk_interpolate(c->d_worlds + id, w.nb, w.accumulator / dt, c->stream));
+  c->launches += 1;
+  DWorldParams p;
+  st = read_params(c, w, p);
+  if (st) return st;
+  const double t1 = p.time + since;
+  CUDA_TRY(cudaMemcpyAsync(&w.dw.P->time, &t1, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return CP_OK;
 }
 
 }  // extern "C"
@@ -1186,7 +1304,7 @@ int cp_world_step_static(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
   const int* d_list = (const int*)(base + o_ids);
   const int variant = w.nb > 512 ? 0 : c->plain_variant;
   for (int s = 0; s < nsteps; s++) {
-    CUDA_TRY(cpk_launch_step(d_world, d_list, d_list + 1, 1, dt, c->d_queue, 1, 1, c->stream, variant, 1, w.nb));
+    CUDA_TRY(cpk_launch_step(d_world, d_list, d_list + 1, 1, dt, dt, c->d_queue, 1, 1, c->stream, variant, 1, w.nb));
     c->launches += 2;  // the two step kernels (the queue reset is a memset)
   }
   DWorldParams p;
@@ -1195,10 +1313,30 @@ int cp_world_step_static(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
   st = kernel_check();
   if (st) return st;
   if (p.status != 0) {
-    const int zero = 0;
-    CUDA_TRY(cudaMemcpy(&w.dw.P->status, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    // The failed step's lists are partial: clear the status and report empty
+    // lists (num_pairs, num_contacts, num_rows and num_levels are consecutive
+    // ints of the parameter record).
+    static_assert(offsetof(DWorldParams, num_levels) == offsetof(DWorldParams, num_pairs) + 3 * sizeof(int), "layout");
+    CUDA_TRY(cudaMemsetAsync(&w.dw.P->status, 0, sizeof(int), c->stream));
+    CUDA_TRY(cudaMemsetAsync(&w.dw.P->num_pairs, 0, 4 * sizeof(int), c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
     return fail(CP_ERR_CAPACITY, "world %d: step %lld overflowed a capacity (status %d); the world is left before that step",
                 id, p.stepnumber + 1, p.status);
+  }
+  // The last step's pairs, contacts and rows (with their lambdas and
+  // multipliers) into the world's own scratch, where cp_world_get_pairs /
+  // get_contacts / get_rows read them.  Both layouts come from the same
+  // capacities, and every count is within them after a step without overflow.
+  if (nsteps > 0) {
+    if (p.num_pairs > 0) {
+      CUDA_TRY(cudaMemcpyAsync(w.dw.pair_a, dw.pair_a, sizeof(int) * p.num_pairs, cudaMemcpyDeviceToDevice, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(w.dw.pair_b, dw.pair_b, sizeof(int) * p.num_pairs, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    if (p.num_contacts > 0)
+      CUDA_TRY(cudaMemcpyAsync(w.dw.contacts, dw.contacts, sizeof(DContact) * p.num_contacts, cudaMemcpyDeviceToDevice, c->stream));
+    if (p.num_rows > 0)
+      CUDA_TRY(cudaMemcpyAsync(w.dw.rows, dw.rows, sizeof(DRow) * p.num_rows, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
   }
   return CP_OK;
 }
@@ -1229,6 +1367,61 @@ int cp_world_set_bodies(cp_ctx* c, int32_t id, const cp_body_desc* in, int32_t n
   CUDA_TRY(cudaMemcpyAsync(w.dw.bodies, b.data(), sizeof(DBody) * w.nb, cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   w.dt_cached = -1.0;
+  return CP_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+int ensure_states(cp_ctx* c, int n) {
+  if (n <= c->states_cap) return CP_OK;
+  const int cap = std::max(n, 2 * c->states_cap);
+  if (c->d_states) cudaFree(c->d_states);
+  c->d_states = nullptr;
+  c->states_cap = 0;
+  CUDA_TRY(cudaMalloc(&c->d_states, sizeof(cp_body_state) * (size_t)cap));
+  c->states_cap = cap;
+  return CP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cp_world_get_states(cp_ctx* c, int32_t id, cp_body_state* out, int32_t n) {
+  int st = check_world(c, id);
+  if (st) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  WorldRec& w = c->worlds[id];
+  if ((!out && n > 0) || n != w.nb) return fail(CP_ERR_ARG, "expected %d bodies", w.nb);
+  if (n == 0) return CP_OK;
+  st = ensure_states(c, n);
+  if (st) return st;
+  CUDA_TRY(cpk_states(c->d_worlds + id, n, c->d_states, 0, c->stream));
+  c->launches += 1;
+  CUDA_TRY(cudaMemcpyAsync(out, c->d_states, sizeof(cp_body_state) * n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return CP_OK;
+}
+
+int cp_world_set_states(cp_ctx* c, int32_t id, const cp_body_state* in, int32_t n) {
+  int st = check_world(c, id);
+  if (st) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  WorldRec& w = c->worlds[id];
+  if ((!in && n > 0) || n != w.nb) return fail(CP_ERR_ARG, "expected %d bodies", w.nb);
+  for (int i = 0; i < n; i++)
+    if (in[i].sleep_state < CP_AWAKE || in[i].sleep_state > CP_SLEEPING) return fail(CP_ERR_ARG, "body %d: bad sleep state", i);
+  if (n == 0) return CP_OK;
+  st = ensure_states(c, n);
+  if (st) return st;
+  CUDA_TRY(cudaMemcpyAsync(c->d_states, in, sizeof(cp_body_state) * n, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cpk_states(c->d_worlds + id, n, c->d_states, 1, c->stream));
+  c->launches += 1;
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
   return CP_OK;
 }
 
@@ -1395,7 +1588,7 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
     cudaGraph_t g;
     CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 0; s < nsteps; s++) {
-      cudaError_t e = cpk_launch_step(c->d_worlds, c->d_ids, c->d_gstart, ngroups, dt, c->d_queue, grid_pre, grid_solve, c->stream,
+      cudaError_t e = cpk_launch_step(c->d_worlds, c->d_ids, c->d_gstart, ngroups, dt, dt, c->d_queue, grid_pre, grid_solve, c->stream,
                                       variant, n, max_nb);
       if (e != cudaSuccess) {
         cudaStreamEndCapture(c->stream, &g);
@@ -1419,7 +1612,7 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
   CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
   if (tuning || !use_graph) {
     for (int s = 0; s < nsteps; s++)
-      CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_ids, c->d_gstart, ngroups, dt, c->d_queue, grid_pre, grid_solve, c->stream,
+      CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_ids, c->d_gstart, ngroups, dt, dt, c->d_queue, grid_pre, grid_solve, c->stream,
                                variant, n, max_nb));
   } else {
     CUDA_TRY(cudaGraphLaunch(c->graph, c->stream));
@@ -1468,7 +1661,7 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
       long long left = std::min(before[4 * i + 1] + nsteps, limit) - after[4 * i + 1];
       st = grow(c, id, (int)after[4 * i]);
       if (st) return st;
-      st = plain_steps(c, id, dt, (int)left);
+      st = plain_steps(c, id, dt, (int)left, dt);
       if (st) return st;
     }
   }
@@ -1583,6 +1776,14 @@ int cp_set_resolver_profile(cp_ctx* c, int32_t on) {
   cudaSetDevice(c->device);
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   CUDA_TRY(cpk_set_resolver_profile(on));
+  return CP_OK;
+}
+
+int cp_set_wide_bodies(cp_ctx* c, int32_t bodies) {
+  if (!c) return fail(CP_ERR_ARG, "null context");
+  if (bodies < 0) return fail(CP_ERR_ARG, "bodies must be >= 0");
+  std::lock_guard<std::mutex> lock(c->mu);
+  c->wide_bodies = bodies;
   return CP_OK;
 }
 

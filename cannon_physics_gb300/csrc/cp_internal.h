@@ -13,6 +13,8 @@
 #include "cp_kernels.h"
 #include "cp_types.h"
 
+#define CP_WIDE_BODIES_DEFAULT 1024
+
 namespace cpi {
 
 // Sub-arrays of one device allocation, each 256-byte aligned.
@@ -33,10 +35,13 @@ struct WorldRec {
   bool pooled = false;     // state and scratch come from the context's memory pool
   DWorld dw{};
   int nb = 0, nshapes = 0, nmat = 0, ncm = 0, ncons = 0, ncon_rows = 0;
+  int n_nocollide = 0;
   int broadphase = 0, nbins = 0;
   int pairs_cap = 0, contacts_cap = 0, rows_cap = 0, bins_cap = 0;
   long long step_limit = LLONG_MAX;  // the kernels leave the world alone at this step number
   double dt_cached = -1.0;
+  double accumulator = 0.0;  // World.accumulator of the interpolating World.step
+  int last_substeps = 0;     // internal steps of the last interpolating step
   std::vector<double> lin_damp, ang_damp;
   std::vector<DContactMaterial> cms;  // host copy for SPOOK updates
 };
@@ -80,6 +85,9 @@ struct cp_ctx {
   int ngroups = 0;
   int group_bodies = 640;   // a group gathers consecutive (similar-size) worlds up to this many bodies
   int plain_variant = 2 * cpk_num_solve_variants();  // (pre 128x4, solve 128x4) for single small worlds
+  // cp_world_step on a world of at least this many bodies runs the wide
+  // kernels (the world spread over the whole GPU); 0: never
+  int wide_bodies = CP_WIDE_BODIES_DEFAULT;
   long long* d_status = nullptr;  // 4 per world after a batched call, then 4 per world before it
   int d_status_cap = 0;
   std::vector<int> dev_order, dev_gstart;  // what d_ids and d_gstart hold
@@ -103,6 +111,9 @@ struct cp_ctx {
   long long io_floats = 0;
   std::vector<int> io_ids;  // ids whose offsets are on the device
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // staging of cp_world_get_states / set_states
+  cp_body_state* d_states = nullptr;
+  int states_cap = 0;
   double graph_ms = 0.0;
   long long graph_step_launches = 0;
   // batched-step graph cache

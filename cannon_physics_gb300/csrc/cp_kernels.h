@@ -23,8 +23,10 @@ void cpk_max_resident_blocks(int variant, int* pre, int* solve);
 // queue counters at d_queue.
 // max_nb: the most bodies of any world in the launch (sizes the pre kernel's
 // shared level table)
-cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, const int* d_gstart, int ngroups, double dt, int* d_queue,
-                            int grid_pre, int grid_solve, cudaStream_t stream, int variant, int n, int max_nb);
+// time_inc: added to each world's time per step (dt for World.step, 0 for
+// World.internalStep, which leaves the clock to its caller)
+cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, const int* d_gstart, int ngroups, double dt, double time_inc,
+                            int* d_queue, int grid_pre, int grid_solve, cudaStream_t stream, int variant, int n, int max_nb);
 // resident blocks per SM of a variant's pre kernel for that largest world
 int cpk_pre_blocks_per_sm(int variant, int max_nb);
 // status, stepnumber and counts of the listed worlds, gathered into out[4*i..]
@@ -37,6 +39,30 @@ cudaError_t cpk_scatter_forces(const DWorld* d_worlds, const int* d_ids, const l
                                cudaStream_t stream);
 cudaError_t cpk_gather_poses(const DWorld* d_worlds, const int* d_ids, const long long* d_first, int n, float* d_out,
                              cudaStream_t stream);
+// World.step's interpolation of one world (world_class.dart:420-428) at
+// t = accumulator / dt: interpolated pose, then previousQuaternion.normalize()
+cudaError_t cpk_interpolate(const DWorld* d_world, int nb, double t, cudaStream_t stream);
+// the per-step body fields of one world to (to_device = 1) or from the
+// packed records d_buf
+cudaError_t cpk_states(const DWorld* d_world, int nb, cp_body_state* d_buf, int to_device, cudaStream_t stream);
+// One large world over the whole GPU (cp_wide.cu): the sizes and settings
+// the host knows, and the most bodies whose sweep velocities fit in one
+// block's shared memory.
+struct WideShape {
+  int nb, nbins, broadphase, n_nocollide;
+  int pairs_cap, contacts_cap, rows_cap, bins_cap;
+  int smem_vel;  // the sweeps keep vlambda / wlambda in shared memory
+};
+int cpk_wide_smem_vel_max();
+// nsteps steps of the world whose device descriptor is dw (hw: its host
+// copy); each step is a sequence of grid-wide kernels on `stream`; the
+// world's step status and counts end up in its parameters as with
+// cpk_launch_step.  *launches grows by the kernels launched.
+cudaError_t cpk_launch_wide_steps(const DWorld* dw, const DWorld& hw, const WideShape& ws, double dt, double time_inc,
+                                  int nsteps, cudaStream_t stream, long long* launches);
+// the wide sweep kernel's first failed index check {code, index, bound, 0}
+// (code 0: none); clears it once read
+cudaError_t cpk_wide_check(const DWorld& hw, int out[4], cudaStream_t stream);
 // CP_PROFILE_SLOTS counters: per-phase cycles summed over blocks (prepare,
 // broadphase, narrowphase, rows+wake+solve prep, row assembly, levels, GS
 // sweeps, apply+integrate), then 16 per-resolver thread-cycle sums and 16

@@ -155,7 +155,7 @@ DI f3 sb_side(const DShape& sb, q4 qB, int idx) {
 // products (which are also the reference's d1, d2).
 // one out-of-line copy: the resolver is large and is reached from several
 // dispatch cases; inlining it at each bloats the step kernel's instruction footprint
-__device__ __noinline__ int sphere_box(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
+static __device__ __noinline__ int sphere_box(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
   const DWorld& W = *C.W;
   const DShape& sb = W.shapes[shB];
   const double R = W.shapes[shA].radius;
@@ -274,7 +274,7 @@ DI f3 hv(const DWorld& W, int i) { return ld3(W.hverts + 4 * i); }
 // narrow_phase.dart:1039-1257
 // one out-of-line copy: the resolver is large and is reached from several
 // dispatch cases; inlining it at each bloats the step kernel's instruction footprint
-__device__ __noinline__ int sphere_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
+static __device__ __noinline__ int sphere_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qB, int& start) {
   const DWorld& W = *C.W;
   const DHull H = W.hulls[W.shapes[shB].hull];
   double R = W.shapes[shA].radius;
@@ -345,7 +345,7 @@ __device__ __noinline__ int sphere_convex(const NarrowCtx& C, int bA, int bB, in
 // narrow_phase.dart:1847-1915 (planeBox forwards here with its own shapes)
 // one out-of-line copy: the resolver is large and is reached from several
 // dispatch cases; inlining it at each bloats the step kernel's instruction footprint
-__device__ __noinline__ int plane_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qA, q4 qB, int& start) {
+static __device__ __noinline__ int plane_convex(const NarrowCtx& C, int bA, int bB, int shA, int shB, int rsi, int rsj, f3 xA, f3 xB, q4 qA, q4 qB, int& start) {
   const DWorld& W = *C.W;
   const DHull H = W.hulls[W.shapes[shB].hull];
   f3 wn = vmult(qA, f3{0.f, 0.f, 1.f});

@@ -1,7 +1,7 @@
 // cp_types.h -- device-resident world layout shared by the host runtime
 // (cp_host.cpp) and the step kernels (cp_step.cu).
 //
-// One World is a set of arrays in device memory.  Bodies are 512-byte
+// One World is a set of arrays in device memory.  Bodies are 432-byte
 // records: every phase of a step touches a handful of fields of a body, and
 // pairs and solver rows gather bodies by index, so a record per body keeps
 // those gathers to a few cache lines.  Scratch (pairs, contacts, rows,
@@ -62,6 +62,8 @@ struct __align__(16) DBody {
   int mask, material, shape, pad0;
   float brad32;  // bounding_radius rounded to float (broadphase filter only)
   float pad1[3];
+  float interp_pos[4];   // Body.interpolatedPosition
+  float interp_quat[4];  // Body.interpolatedQuaternion
 };
 
 struct __align__(16) DShape {
@@ -155,6 +157,20 @@ struct __align__(16) DWorldParams {
   long long step_limit;  // the step kernels leave the world alone once stepnumber reaches this
 };
 
+// Counters of a step of one world spread over the whole GPU (the wide
+// kernels, cp_wide.cu): what the one-block kernels keep in shared memory.
+struct __align__(16) DWide {
+  int run;        // the step runs: status clear and below the step limit
+  int overflow;   // ST_* bits found during this step
+  int n_pairs, n_cand_pairs, n_contacts, n_fric;
+  int n_cand, n_rows, n_levels, iters;
+  int n_queued, n_queued2, nh_padded, cursor;
+  int check[4];   // first failed index check of the sweep kernel: code, index, bound
+  int kcnt[16], kpos[16];
+  int total, pad[3];
+};
+#define CP_WIDE_SCAN_BLOCKS 128
+
 struct DWorld {
   DWorldParams* P;
   DBody* bodies;
@@ -214,4 +230,8 @@ struct DWorld {
   int2* sw_b;
   int* sw_orig;
   int sw_cap;
+  DWide* wide;      // counters of a wide step
+  int* wpart;       // per-block partial sums of the wide scans (CP_WIDE_SCAN_BLOCKS + 1)
+  float* wvel;      // wide sweeps: vlambda, wlambda (6 floats per body) when they do not fit in shared memory
+  unsigned char* wflag;  // wide sweeps: solve flag per body
 };

@@ -38,6 +38,11 @@ def lib():
         L.cp_world_create.argtypes = [vp, vp, vp]
         L.cp_world_destroy.argtypes = [vp, i32]
         L.cp_world_step.argtypes = [vp, i32, f64, i32]
+        L.cp_world_internal_step.argtypes = [vp, i32, f64, i32]
+        L.cp_world_step_interpolated.argtypes = [vp, i32, f64, f64, i32, vp]
+        L.cp_world_set_time.argtypes = [vp, i32, f64, C.c_int64, f64]
+        L.cp_world_get_states.argtypes = [vp, i32, vp, i32]
+        L.cp_world_set_states.argtypes = [vp, i32, vp, i32]
         L.cp_world_get_bodies.argtypes = [vp, i32, vp, i32]
         L.cp_world_set_bodies.argtypes = [vp, i32, vp, i32]
         L.cp_world_get_pairs.argtypes = [vp, i32, vp, vp, i32, vp]
@@ -57,6 +62,7 @@ def lib():
         L.cp_autotune_info.argtypes = [vp, vp, vp, vp, i32]
         L.cp_set_variant.argtypes = [vp, i32]
         L.cp_set_group_bodies.argtypes = [vp, i32]
+        L.cp_set_wide_bodies.argtypes = [vp, i32]
         _lib = L
     return _lib
 
@@ -118,6 +124,11 @@ class Context:
     def resolver_profile(self, on=True):
         """Count per-resolver cycles and calls (off by default; per device)."""
         check(lib().cp_set_resolver_profile(self.h, int(bool(on))), "cp_set_resolver_profile")
+
+    def set_wide_bodies(self, n):
+        """Single-world steps of worlds with at least n bodies spread over the
+        whole GPU (0: never)."""
+        check(lib().cp_set_wide_bodies(self.h, n), "cp_set_wide_bodies")
 
     def set_group_bodies(self, n):
         check(lib().cp_set_group_bodies(self.h, n), "cp_set_group_bodies")
@@ -185,6 +196,29 @@ class GpuWorld:
 
     def step(self, dt=None, nsteps=1):
         check(lib().cp_world_step(self.ctx.h, self.id, self.scene.dt if dt is None else dt, nsteps), "cp_world_step")
+
+    def internal_step(self, dt=None, nsteps=1):
+        """World.internalStep: stepnumber advances, time does not."""
+        check(lib().cp_world_internal_step(self.ctx.h, self.id, self.scene.dt if dt is None else dt, nsteps), "internal_step")
+
+    def step_interpolated(self, dt, time_since_last_called, max_sub_steps=10):
+        """World.step(dt, timeSinceLastCalled, maxSubSteps); returns the sub-steps taken."""
+        n = C.c_int32()
+        check(lib().cp_world_step_interpolated(self.ctx.h, self.id, dt, time_since_last_called, max_sub_steps, C.byref(n)),
+              "step_interpolated")
+        return n.value
+
+    def set_time(self, time, stepnumber, accumulator=0.0):
+        check(lib().cp_world_set_time(self.ctx.h, self.id, time, stepnumber, accumulator), "set_time")
+
+    def states(self):
+        out = np.zeros(self.n, dtype=A.BODY_STATE_DTYPE)
+        check(lib().cp_world_get_states(self.ctx.h, self.id, out.ctypes.data, self.n), "get_states")
+        return out
+
+    def set_states(self, states):
+        states = np.ascontiguousarray(states, dtype=A.BODY_STATE_DTYPE)
+        check(lib().cp_world_set_states(self.ctx.h, self.id, states.ctypes.data, self.n), "set_states")
 
     def bodies(self):
         out = np.zeros(self.n, dtype=A.BODY_DTYPE)

@@ -5,11 +5,17 @@
 // Plane, ConvexPolyhedron, Cylinder, Material, ContactMaterial,
 // PointToPointConstraint, HingeConstraint, DistanceConstraint, GSSolver).
 // On the first step, and after markDirty(), the bodies, shapes, materials and
-// constraints are packed into a cp_world_desc and uploaded; every step after
-// that is one cp_world_step call followed by a write-back of the fields that
-// World.internalStep changes (lib/world/world_class.dart:433-701): position,
-// quaternion, velocity, angular velocity, previous pose, world inertia,
-// AABB, sleep state, time of the last sleepy state, forces (cleared).
+// constraints are packed into a cp_world_desc and uploaded.  Every
+// internalStep after that pushes World.time / stepnumber (cp_world_set_time)
+// and the per-step body fields an app may have changed (cp_world_set_states:
+// pose, velocities, forces, sleep state), runs one cp_world_internal_step,
+// and writes back the per-step fields World.internalStep changes
+// (lib/world/world_class.dart:433-701; cp_world_get_states).  World.step
+// (world_class.dart:392-430) is not overridden: it keeps the only clock,
+// adding dt (fixed mode) or timeSinceLastCalled (interpolating mode) after
+// the internal steps, and interpolates the written-back poses itself.
+// Fields outside cp_body_state (mass, damping, shapes, materials, factors,
+// the world inertia of a body the app rotated) travel only with markDirty().
 //
 // This file is written for a maintainer; it is not compiled in this
 // repository (no Dart or Flutter SDK is present).  The C side checks every
@@ -44,6 +50,8 @@ class GpuWorld extends World {
   bool _dirty = true;
   Pointer<CpBodyDesc> _bodyBuf = nullptr;
   int _bodyCap = 0;
+  Pointer<CpBodyState> _stateBuf = nullptr;
+  int _stateCap = 0;
 
   /// Call after adding or removing bodies, shapes, materials or constraints,
   /// or after changing a body field other than the ones a step writes.
@@ -77,21 +85,16 @@ class GpuWorld extends World {
   void internalStep(double dt) {
     final api = _lib;
     if (_dirty) _upload(api);
-    // Body fields the app may have changed between steps (forces, velocities,
-    // kinematic poses) travel with every step.
-    _packBodies();
-    _check(api.worldSetBodies(_ctx, _worldId, _bodyBuf, bodies.length));
-    _check(api.worldStep(_ctx, _worldId, dt, 1));
-    _check(api.worldGetBodies(_ctx, _worldId, _bodyBuf, bodies.length));
-    _unpackBodies();
-    final info = calloc<CpStepInfo>();
-    try {
-      _check(api.worldGetInfo(_ctx, _worldId, info));
-      stepnumber = info.ref.stepnumber;
-      time = info.ref.time;
-    } finally {
-      calloc.free(info);
-    }
+    // sleepTick inside the step reads World.time as World.step holds it
+    _check(api.worldSetTime(_ctx, _worldId, time, stepnumber, accumulator));
+    _packStates();
+    _check(api.worldSetStates(_ctx, _worldId, _stateBuf, bodies.length));
+    _check(api.worldInternalStep(_ctx, _worldId, dt, 1));
+    _check(api.worldGetStates(_ctx, _worldId, _stateBuf, bodies.length));
+    _unpackStates();
+    // World.internalStep's own counter (world_class.dart:680); time is left
+    // to World.step
+    stepnumber += 1;
     this.dt = dt;
   }
 
@@ -102,9 +105,11 @@ class GpuWorld extends World {
     if (_worldId >= 0) api.worldDestroy(_ctx, _worldId);
     if (_ctx != nullptr) api.destroy(_ctx);
     if (_bodyBuf != nullptr) calloc.free(_bodyBuf);
+    if (_stateBuf != nullptr) calloc.free(_stateBuf);
     _worldId = -1;
     _ctx = nullptr;
     _bodyBuf = nullptr;
+    _stateBuf = nullptr;
   }
 
   // ---------------------------------------------------------------- packing
@@ -406,10 +411,46 @@ class GpuWorld extends World {
     }
   }
 
-  void _unpackBodies() {
+  void _ensureStateBuf() {
+    if (_stateCap >= bodies.length) return;
+    if (_stateBuf != nullptr) calloc.free(_stateBuf);
+    _stateCap = bodies.length < 16 ? 16 : bodies.length;
+    _stateBuf = calloc<CpBodyState>(_stateCap);
+  }
+
+  static void _setQ(Array<Float> a, Quaternion q) {
+    a[0] = q.x;
+    a[1] = q.y;
+    a[2] = q.z;
+    a[3] = q.w;
+  }
+
+  void _packStates() {
+    _ensureStateBuf();
     for (var i = 0; i < bodies.length; i++) {
       final b = bodies[i];
-      final d = _bodyBuf[i];
+      final d = _stateBuf[i];
+      _set3(d.position, b.position);
+      _setQ(d.quaternion, b.quaternion);
+      _set3(d.velocity, b.velocity);
+      _set3(d.angularVelocity, b.angularVelocity);
+      _set3(d.force, b.force);
+      _set3(d.torque, b.torque);
+      _set3(d.previousPosition, b.previousPosition);
+      _setQ(d.previousQuaternion, b.previousQuaternion);
+      _set3(d.interpolatedPosition, b.interpolatedPosition);
+      _setQ(d.interpolatedQuaternion, b.interpolatedQuaternion);
+      d.sleepState = b.sleepState.index;
+      d.wakeUpAfterNarrowphase = b.wakeUpAfterNarrowphase ? 1 : 0;
+      d.aabbNeedsUpdate = b.aabbNeedsUpdate ? 1 : 0;
+      d.timeLastSleepy = b.timeLastSleepy.toDouble();
+    }
+  }
+
+  void _unpackStates() {
+    for (var i = 0; i < bodies.length; i++) {
+      final b = bodies[i];
+      final d = _stateBuf[i];
       b.position.setValues(d.position[0], d.position[1], d.position[2]);
       b.quaternion.setValues(d.quaternion[0], d.quaternion[1], d.quaternion[2], d.quaternion[3]);
       b.velocity.setValues(d.velocity[0], d.velocity[1], d.velocity[2]);
@@ -419,11 +460,6 @@ class GpuWorld extends World {
       b.previousPosition.setValues(d.previousPosition[0], d.previousPosition[1], d.previousPosition[2]);
       b.previousQuaternion.setValues(
           d.previousQuaternion[0], d.previousQuaternion[1], d.previousQuaternion[2], d.previousQuaternion[3]);
-      for (var k = 0; k < 9; k++) {
-        b.invInertiaWorld.storage[k] = d.invInertiaWorld[k];
-      }
-      b.aabb.lowerBound.setValues(d.aabbLower[0], d.aabbLower[1], d.aabbLower[2]);
-      b.aabb.upperBound.setValues(d.aabbUpper[0], d.aabbUpper[1], d.aabbUpper[2]);
       b.aabbNeedsUpdate = d.aabbNeedsUpdate != 0;
       b.sleepState = BodySleepStates.values[d.sleepState];
       b.timeLastSleepy = d.timeLastSleepy;

@@ -6,7 +6,7 @@
 // only during the call.
 import 'dart:ffi';
 
-const int cpAbiVersion = 1;
+const int cpAbiVersion = 2;
 
 const int cpOk = 0;
 const int cpErrArg = 1;
@@ -81,6 +81,27 @@ final class CpBodyDesc extends Struct {
   @Int32() external int shape;
   @Int32() external int fixedRotation;
   @Int32() external int aabbNeedsUpdate;
+  @Array(3) external Array<Float> interpolatedPosition;
+  @Array(4) external Array<Float> interpolatedQuaternion;
+  @Int32() external int pad0;
+}
+
+final class CpBodyState extends Struct {
+  @Array(3) external Array<Float> position;
+  @Array(4) external Array<Float> quaternion;
+  @Array(3) external Array<Float> velocity;
+  @Array(3) external Array<Float> angularVelocity;
+  @Array(3) external Array<Float> force;
+  @Array(3) external Array<Float> torque;
+  @Array(3) external Array<Float> previousPosition;
+  @Array(4) external Array<Float> previousQuaternion;
+  @Array(3) external Array<Float> interpolatedPosition;
+  @Array(4) external Array<Float> interpolatedQuaternion;
+  @Int32() external int sleepState;
+  @Int32() external int wakeUpAfterNarrowphase;
+  @Int32() external int aabbNeedsUpdate;
+  @Int32() external int pad0;
+  @Double() external double timeLastSleepy;
 }
 
 final class CpMaterial extends Struct {
@@ -161,7 +182,8 @@ final class CpStepInfo extends Struct {
   @Int32() external int status;
   @Int32() external int numBodies;
   @Int32() external int numLevels;
-  @Int32() external int pad;
+  @Int32() external int substeps;
+  @Double() external double accumulator;
 }
 
 final class CpConfig extends Struct {
@@ -197,6 +219,14 @@ class CannonGpu {
             int Function(Pointer<CpCtx>, int, Pointer<CpBodyDesc>, int)>('cp_world_set_bodies'),
         worldGetInfo = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Pointer<CpStepInfo>),
             int Function(Pointer<CpCtx>, int, Pointer<CpStepInfo>)>('cp_world_get_info'),
+        worldInternalStep = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Double, Int32),
+            int Function(Pointer<CpCtx>, int, double, int)>('cp_world_internal_step'),
+        worldSetTime = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Double, Int64, Double),
+            int Function(Pointer<CpCtx>, int, double, int, double)>('cp_world_set_time'),
+        worldGetStates = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Pointer<CpBodyState>, Int32),
+            int Function(Pointer<CpCtx>, int, Pointer<CpBodyState>, int)>('cp_world_get_states'),
+        worldSetStates = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Pointer<CpBodyState>, Int32),
+            int Function(Pointer<CpCtx>, int, Pointer<CpBodyState>, int)>('cp_world_set_states'),
         worldStepStatic = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Double, Int32),
             int Function(Pointer<CpCtx>, int, double, int)>('cp_world_step_static'),
         batchStep = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Pointer<Int32>, Int32, Double, Int32),
@@ -214,6 +244,16 @@ class CannonGpu {
   final int Function(Pointer<CpCtx>, int, Pointer<CpBodyDesc>, int) worldGetBodies;
   final int Function(Pointer<CpCtx>, int, Pointer<CpBodyDesc>, int) worldSetBodies;
   final int Function(Pointer<CpCtx>, int, Pointer<CpStepInfo>) worldGetInfo;
+
+  /// World.internalStep on the device: stepnumber advances, time does not.
+  final int Function(Pointer<CpCtx>, int, double, int) worldInternalStep;
+
+  /// World.time, World.stepnumber and World.accumulator of the device world.
+  final int Function(Pointer<CpCtx>, int, double, int, double) worldSetTime;
+
+  /// The per-step Body fields only (cp_body_state).
+  final int Function(Pointer<CpCtx>, int, Pointer<CpBodyState>, int) worldGetStates;
+  final int Function(Pointer<CpCtx>, int, Pointer<CpBodyState>, int) worldSetStates;
 
   /// `worldStep` without device allocation (fixed step scratch; a world too
   /// large for it, or a step that overflows a list, returns CP_ERR_CAPACITY).

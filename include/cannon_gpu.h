@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define CP_ABI_VERSION 1
+#define CP_ABI_VERSION 2
 
 /* status codes */
 #define CP_OK               0
@@ -119,7 +119,33 @@ typedef struct cp_body_desc {
   int32_t material;                 /* -1 = null */
   int32_t shape;                    /* index into cp_world_desc.shapes */
   int32_t fixed_rotation, aabb_needs_update;
+  /* Body.interpolatedPosition / interpolatedQuaternion (rigid_body.dart:135,190),
+   * written by cp_world_step_interpolated */
+  float interpolated_position[3];
+  float interpolated_quaternion[4];
+  int32_t pad0;
 } cp_body_desc;
+
+/* The Body fields one World.step changes or an app typically sets between
+ * steps (applyForce, a new velocity, a teleport, a wake-up), moved without
+ * the rest of the record: what a Dart GpuWorld exchanges every step. */
+typedef struct cp_body_state {
+  float position[3];
+  float quaternion[4];
+  float velocity[3];
+  float angular_velocity[3];
+  float force[3];
+  float torque[3];
+  float previous_position[3];
+  float previous_quaternion[4];
+  float interpolated_position[3];
+  float interpolated_quaternion[4];
+  int32_t sleep_state;
+  int32_t wake_up_after_narrowphase;
+  int32_t aabb_needs_update;
+  int32_t pad0;
+  double time_last_sleepy;
+} cp_body_state;
 
 /* Material (lib/material/material.dart): -1 means "not set". */
 typedef struct cp_material {
@@ -196,7 +222,8 @@ typedef struct cp_step_info {
   int32_t num_pairs, num_contacts, num_rows, iterations;
   int32_t status, num_bodies;
   int32_t num_levels;               /* dependency levels of the last solve (rows of a level share no dynamic body) */
-  int32_t pad;
+  int32_t substeps;                 /* internal steps taken by the last cp_world_step_interpolated */
+  double accumulator;               /* World.accumulator (world_class.dart:119) */
 } cp_step_info;
 
 typedef struct cp_config {
@@ -237,8 +264,39 @@ int cp_world_create(cp_ctx* ctx, const cp_world_desc* desc, int32_t* world_id);
 int cp_world_destroy(cp_ctx* ctx, int32_t world_id);
 
 /* World.step(dt) in fixed mode, nsteps times: internalStep then time += dt
- * (world_class.dart:392-399,433-701). */
+ * (world_class.dart:392-399,433-701).  The world keeps its own copy of
+ * World.time and World.stepnumber (set at cp_world_create and by
+ * cp_world_set_time); sleepTick reads that time, as the reference does. */
 int cp_world_step(cp_ctx* ctx, int32_t world_id, double dt, int32_t nsteps);
+
+/* World.internalStep(dt), nsteps times (world_class.dart:433-701): stepnumber
+ * advances by one per step, time does not; sleepTick reads the world's
+ * current time.  This is the call for a binding that overrides
+ * World.internalStep and lets World.step keep the clock: push World.time with
+ * cp_world_set_time before it, and World.step adds dt (fixed mode) or
+ * timeSinceLastCalled (interpolating mode) itself afterwards. */
+int cp_world_internal_step(cp_ctx* ctx, int32_t world_id, double dt, int32_t nsteps);
+
+/* World.step(dt, timeSinceLastCalled, maxSubSteps), the interpolating form
+ * (world_class.dart:400-430): the accumulator gains timeSinceLastCalled;
+ * internal steps run while it holds a whole dt (at most max_sub_steps, and
+ * none after the steps so far took longer than dt of wall-clock time, as the
+ * reference bails out); the remainder is kept modulo dt; every body's
+ * interpolated position (previousPosition.lerp) and quaternion
+ * (previousQuaternion.slerp, Quaternion.slerp quaternion.dart:118-168) are
+ * written for t = accumulator / dt and previousQuaternion is normalised;
+ * then time += timeSinceLastCalled.  *substeps (may be NULL) receives the
+ * number of internal steps taken.  The slerp's acos and sin are the device's
+ * (within 2 ulp of the C library's), so interpolated quaternions can differ
+ * from a host computation in the last binary32 bit; every other field is
+ * exact. */
+int cp_world_step_interpolated(cp_ctx* ctx, int32_t world_id, double dt, double time_since_last_called,
+                               int32_t max_sub_steps, int32_t* substeps);
+
+/* Overwrite World.time, World.stepnumber and World.accumulator
+ * (world_class.dart:74-80,119) of a device world, e.g. from the host
+ * World object before cp_world_internal_step. */
+int cp_world_set_time(cp_ctx* ctx, int32_t world_id, double time, int64_t stepnumber, double accumulator);
 
 /* cp_world_step without any allocation.  It has no counterpart in the
  * reference (Dart allocates as it pleases).
@@ -254,7 +312,10 @@ int cp_world_step(cp_ctx* ctx, int32_t world_id, double dt, int32_t nsteps);
  * What it does: it gives the same results as cp_world_step, bit for bit.
  * The per-step lists (pairs, contacts, rows, levels, solver scratch) live
  * in one file-scope device array of CP_STATIC_SCRATCH_BYTES (64 MiB), not
- * in the world's own scratch.
+ * in the world's own scratch.  At the end of the call the last step's
+ * pairs, contacts and rows are copied (device to device, on the context's
+ * stream) into the world's own lists, so cp_world_get_pairs / get_contacts
+ * / get_rows / get_info report them as they do after cp_world_step.
  *
  * Limits:
  *  - A world whose lists, at its current capacities, need more than that
@@ -262,9 +323,9 @@ int cp_world_step(cp_ctx* ctx, int32_t world_id, double dt, int32_t nsteps);
  *    roughly 11 KB per body: a 4096-body world fits, 10,000 bodies do not.
  *  - A step that overflows a capacity is not regrown.  The world's bodies
  *    are left as they were at the start of that step (only their cached
- *    AABBs may be refreshed), its status is cleared, and the call returns
- *    CP_ERR_CAPACITY.  cp_world_step can then take that step and grow the
- *    capacities.
+ *    AABBs may be refreshed), its status is cleared, its pair, contact and
+ *    row lists read back empty, and the call returns CP_ERR_CAPACITY.
+ *    cp_world_step can then take that step and grow the capacities.
  *
  * Set-up: the first call on a device takes the array's address with
  * cudaGetSymbolAddress, with that device current.  Make that first call
@@ -284,6 +345,13 @@ int cp_world_step_static(cp_ctx* ctx, int32_t world_id, double dt, int32_t nstep
 /* Read back / overwrite body state (Body fields). */
 int cp_world_get_bodies(cp_ctx* ctx, int32_t world_id, cp_body_desc* out, int32_t n);
 int cp_world_set_bodies(cp_ctx* ctx, int32_t world_id, const cp_body_desc* in, int32_t n);
+
+/* Read back / overwrite only the per-step fields of cp_body_state (about a
+ * third of a cp_body_desc).  set_states writes every field of the record
+ * (aabb_needs_update and wake_up_after_narrowphase set or clear the body's
+ * flags); other Body fields keep their device values. */
+int cp_world_get_states(cp_ctx* ctx, int32_t world_id, cp_body_state* out, int32_t n);
+int cp_world_set_states(cp_ctx* ctx, int32_t world_id, const cp_body_state* in, int32_t n);
 
 /* Last step's broadphase pairs (worldStepP1/P2, world_class.dart:481-499),
  * contacts (World.contacts) and solver rows (Solver.equations with B, 1/C,
@@ -359,6 +427,14 @@ int cp_set_resolver_profile(cp_ctx* ctx, int32_t on);
  * (similar-size) worlds holding up to `bodies` bodies (at most 8 worlds);
  * the solver sweeps of a group share barriers.  0 = one world per group. */
 int cp_set_group_bodies(cp_ctx* ctx, int32_t bodies);
+
+/* cp_world_step, cp_world_internal_step and cp_world_step_interpolated on a
+ * world of at least `bodies` bodies spread the world over the whole GPU: each
+ * phase runs as a grid-wide kernel over its bodies, pairs, contacts or rows,
+ * and only the dependency levels and the Gauss-Seidel sweeps stay on one
+ * block.  The results are the same bits as on one block.  Default 1024;
+ * 0 keeps every world on one block.  No counterpart in the reference. */
+int cp_set_wide_bodies(cp_ctx* ctx, int32_t bodies);
 
 /* Device time (CUDA events on the context stream) of the batched-step graph
  * launches since the previous call, and how many step launches they held. */

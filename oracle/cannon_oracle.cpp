@@ -16,6 +16,7 @@
 #include "cannon_oracle.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -174,6 +175,31 @@ static inline void qnormalizeFast(Q4& q) {
   else { q.x = (float)(q.x * f); q.y = (float)(q.y * f); q.z = (float)(q.z * f); q.w = (float)(q.w * f); }
 }
 static inline void conjugate(Q4& q) { q.z = -q.z; q.y = -q.y; q.x = -q.x; }
+// Quaternion.slerp (quaternion.dart:118-168): binary64 arithmetic, libm's
+// acos and sin, each target component stored to binary32
+static inline void slerp(const Q4& a, const Q4& to, double t, Q4& target) {
+  const double ax = a.x, ay = a.y, az = a.z, aw = a.w;
+  double bx = to.x, by = to.y, bz = to.z, bw = to.w;
+  double cosom = ax * bx + ay * by + az * bz + aw * bw;
+  if (cosom < 0.0) {
+    cosom = -cosom;
+    bx = -bx; by = -by; bz = -bz; bw = -bw;
+  }
+  double scale0, scale1;
+  if (1.0 - cosom > 0.000001) {
+    double omega = std::acos(cosom);
+    double sinom = std::sin(omega);
+    scale0 = std::sin((1.0 - t) * omega) / sinom;
+    scale1 = std::sin(t * omega) / sinom;
+  } else {
+    scale0 = 1.0 - t;
+    scale1 = t;
+  }
+  target.x = (float)(scale0 * ax + scale1 * bx);
+  target.y = (float)(scale0 * ay + scale1 * by);
+  target.z = (float)(scale0 * az + scale1 * bz);
+  target.w = (float)(scale0 * aw + scale1 * bw);
+}
 
 // lib/math/mat3.dart:9-108 (storage indexed e[3*row+col])
 static inline void mvmult(const M3& m, const V3& v, V3& t) {
@@ -459,6 +485,7 @@ struct Body {
   V3 aabbLo, aabbHi;
   V3 shapeOffset; Q4 shapeOrientation;
   V3 vlambda, wlambda;
+  V3 interpolatedPosition; Q4 interpolatedQuaternion;  // rigid_body.dart:135,190
   double mass = 0, invMass = 0, invMassSolve = 0;
   double linearDamping = 0.01, angularDamping = 0.01;
   double sleepSpeedLimit = 0.1, sleepTimeLimit = 1, timeLastSleepy = 0;
@@ -526,6 +553,7 @@ static void bodyFromDesc(const cp_body_desc& d, Body& b) {
   b.aabbLo = v3(d.aabb_lower); b.aabbHi = v3(d.aabb_upper);
   b.shapeOffset = v3(d.shape_offset); b.shapeOrientation = q4(d.shape_orientation);
   b.previousPosition = v3(d.previous_position); b.previousQuaternion = q4(d.previous_quaternion);
+  b.interpolatedPosition = v3(d.interpolated_position); b.interpolatedQuaternion = q4(d.interpolated_quaternion);
   b.mass = d.mass; b.invMass = d.inv_mass;
   b.linearDamping = d.linear_damping; b.angularDamping = d.angular_damping;
   b.sleepSpeedLimit = d.sleep_speed_limit; b.sleepTimeLimit = d.sleep_time_limit; b.timeLastSleepy = d.time_last_sleepy;
@@ -550,6 +578,7 @@ static void bodyToDesc(const Body& b, cp_body_desc& d) {
   v3(d.aabb_lower, b.aabbLo); v3(d.aabb_upper, b.aabbHi);
   v3(d.shape_offset, b.shapeOffset); q4(d.shape_orientation, b.shapeOrientation);
   v3(d.previous_position, b.previousPosition); q4(d.previous_quaternion, b.previousQuaternion);
+  v3(d.interpolated_position, b.interpolatedPosition); q4(d.interpolated_quaternion, b.interpolatedQuaternion);
   d.mass = b.mass; d.inv_mass = b.invMass;
   d.linear_damping = b.linearDamping; d.angular_damping = b.angularDamping;
   d.sleep_speed_limit = b.sleepSpeedLimit; d.sleep_time_limit = b.sleepTimeLimit; d.time_last_sleepy = b.timeLastSleepy;
@@ -1709,6 +1738,34 @@ struct World {
     internalStep(dtv);
     time += dtv;
   }
+  double accumulator = 0;  // world_class.dart:119
+  int lastSubsteps = 0;
+  // world_class.dart:400-430 (interpolated stepping)
+  void stepInterpolated(double dtv, double timeSinceLastCalled, int maxSubSteps) {
+    accumulator += timeSinceLastCalled;
+    const auto t0 = std::chrono::steady_clock::now();
+    int substeps = 0;
+    while (accumulator >= dtv && substeps < maxSubSteps) {
+      internalStep(dtv);
+      accumulator -= dtv;
+      substeps++;
+      const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      if (ms > dtv * 1000) break;
+    }
+    // Dart's double % is never negative
+    double r = std::fmod(accumulator, dtv);
+    if (r < 0) r += dtv;
+    if (r == 0) r = 0.0;
+    accumulator = r;
+    lastSubsteps = substeps;
+    const double t = accumulator / dtv;
+    for (Body& b : bodies) {
+      lerp(b.previousPosition, b.position, t, b.interpolatedPosition);
+      slerp(b.previousQuaternion, b.quaternion, t, b.interpolatedQuaternion);
+      qnormalize(b.previousQuaternion);
+    }
+    time += timeSinceLastCalled;
+  }
 };
 
 static int buildWorld(const cp_world_desc& d, World& w) {
@@ -1829,6 +1886,8 @@ int orc_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc
     bodyFromDesc(*d, b);
     b.previousPosition = b.position;
     b.previousQuaternion = b.quaternion;
+    b.interpolatedPosition = b.position;
+    b.interpolatedQuaternion = b.quaternion;
     b.invMass = b.mass > 0 ? 1.0 / b.mass : 0;
     if (d->type < 0) b.type = b.mass <= 0.0 ? CP_BODY_STATIC : CP_BODY_DYNAMIC;
     int shapeIdx = b.shape;
@@ -1863,6 +1922,42 @@ void orc_world_destroy(orc_world* w) { delete w; }
 int orc_world_step(orc_world* o, double dt, int32_t nsteps) {
   if (!o || nsteps < 0) return CP_ERR_ARG;
   for (int s = 0; s < nsteps; s++) o->w.step(dt);
+  return CP_OK;
+}
+
+int orc_world_internal_step(orc_world* o, double dt, int32_t nsteps) {
+  if (!o || nsteps < 0) return CP_ERR_ARG;
+  for (int s = 0; s < nsteps; s++) o->w.internalStep(dt);
+  return CP_OK;
+}
+
+int orc_world_step_interpolated(orc_world* o, double dt, double since, int32_t max_sub_steps, int32_t* substeps) {
+  if (!o || !(dt > 0) || max_sub_steps < 0) return CP_ERR_ARG;
+  o->w.stepInterpolated(dt, since, max_sub_steps);
+  if (substeps) *substeps = o->w.lastSubsteps;
+  return CP_OK;
+}
+
+int orc_world_set_bodies(orc_world* o, const cp_body_desc* in, int32_t n) {
+  if (!o || (!in && n > 0) || n != (int32_t)o->w.bodies.size()) return CP_ERR_ARG;
+  for (int i = 0; i < n; i++) {
+    if (in[i].shape >= (int32_t)o->w.shapes.size()) return CP_ERR_ARG;
+    bodyFromDesc(in[i], o->w.bodies[i]);
+  }
+  return CP_OK;
+}
+
+int orc_world_set_sap_order(orc_world* o, const int32_t* in, int32_t n) {
+  if (!o || (!in && n > 0) || n != (int32_t)o->w.axisList.size()) return CP_ERR_ARG;
+  for (int i = 0; i < n; i++) o->w.axisList[i] = in[i];
+  return CP_OK;
+}
+
+int orc_world_set_time(orc_world* o, double time, int64_t stepnumber, double accumulator) {
+  if (!o || stepnumber < 0) return CP_ERR_ARG;
+  o->w.time = time;
+  o->w.stepnumber = stepnumber;
+  o->w.accumulator = accumulator;
   return CP_OK;
 }
 
@@ -1918,6 +2013,8 @@ int orc_world_get_info(orc_world* o, cp_step_info* out) {
   std::memset(out, 0, sizeof(*out));
   out->stepnumber = o->w.stepnumber;
   out->time = o->w.time;
+  out->substeps = o->w.lastSubsteps;
+  out->accumulator = o->w.accumulator;
   out->num_pairs = (int)o->w.p1.size();
   out->num_contacts = (int)o->w.contacts.size();
   out->num_rows = (int)o->w.solverRows.size();

@@ -35,6 +35,13 @@ int orc_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc
 orc_world* orc_world_create(const cp_world_desc* desc);
 void orc_world_destroy(orc_world* w);
 int orc_world_step(orc_world* w, double dt, int32_t nsteps);
+int orc_world_internal_step(orc_world* w, double dt, int32_t nsteps);
+int orc_world_step_interpolated(orc_world* w, double dt, double time_since_last_called, int32_t max_sub_steps, int32_t* substeps);
+int orc_world_set_time(orc_world* w, double time, int64_t stepnumber, double accumulator);
+/* Overwrite the bodies / the persisted SAP order (e.g. with a GPU world's
+ * state, to time or check the oracle from the same step). */
+int orc_world_set_bodies(orc_world* w, const cp_body_desc* in, int32_t n);
+int orc_world_set_sap_order(orc_world* w, const int32_t* in, int32_t n);
 int orc_world_get_bodies(orc_world* w, cp_body_desc* out, int32_t n);
 int orc_world_get_pairs(orc_world* w, int32_t* p1, int32_t* p2, int32_t cap, int32_t* count);
 int orc_world_get_contacts(orc_world* w, cp_contact* out, int32_t cap, int32_t* count);

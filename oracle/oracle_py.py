@@ -27,6 +27,11 @@ def lib():
         L.orc_world_create.restype = vp
         L.orc_world_destroy.argtypes = [vp]
         L.orc_world_step.argtypes = [vp, f64, i32]
+        L.orc_world_internal_step.argtypes = [vp, f64, i32]
+        L.orc_world_step_interpolated.argtypes = [vp, f64, f64, i32, vp]
+        L.orc_world_set_time.argtypes = [vp, f64, C.c_int64, f64]
+        L.orc_world_set_bodies.argtypes = [vp, vp, i32]
+        L.orc_world_set_sap_order.argtypes = [vp, vp, i32]
         L.orc_world_get_bodies.argtypes = [vp, vp, i32]
         L.orc_world_get_pairs.argtypes = [vp, vp, vp, i32, vp]
         L.orc_world_get_contacts.argtypes = [vp, vp, i32, vp]
@@ -70,10 +75,38 @@ class OracleWorld:
     def step(self, dt=None, nsteps=1):
         _check(lib().orc_world_step(self.h, self.scene.dt if dt is None else dt, nsteps), "step")
 
+    def internal_step(self, dt=None, nsteps=1):
+        _check(lib().orc_world_internal_step(self.h, self.scene.dt if dt is None else dt, nsteps), "internal step")
+
+    def step_interpolated(self, dt, time_since_last_called, max_sub_steps=10):
+        n = C.c_int32()
+        _check(lib().orc_world_step_interpolated(self.h, dt, time_since_last_called, max_sub_steps, C.byref(n)),
+               "interpolated step")
+        return n.value
+
+    def set_time(self, time, stepnumber, accumulator=0.0):
+        _check(lib().orc_world_set_time(self.h, time, stepnumber, accumulator), "set time")
+
     def bodies(self):
         out = np.zeros(self.n, dtype=A.BODY_DTYPE)
         _check(lib().orc_world_get_bodies(self.h, out.ctypes.data, self.n), "get bodies")
         return out
+
+    def set_bodies(self, bodies):
+        bodies = np.ascontiguousarray(bodies, dtype=A.BODY_DTYPE)
+        _check(lib().orc_world_set_bodies(self.h, bodies.ctypes.data, self.n), "set bodies")
+
+    def set_sap_order(self, order):
+        order = np.ascontiguousarray(order, dtype=np.int32)
+        _check(lib().orc_world_set_sap_order(self.h, order.ctypes.data, self.n), "set sap order")
+
+    def load_state(self, gpu_world):
+        """Continue from a GPU world's state (bodies, SAP order, time, step
+        number): both then take the same next steps."""
+        inf = gpu_world.info()
+        self.set_bodies(gpu_world.bodies())
+        self.set_sap_order(gpu_world.sap_order())
+        self.set_time(inf.time, inf.stepnumber, inf.accumulator)
 
     def info(self):
         inf = A.StepInfo()

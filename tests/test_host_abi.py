@@ -34,7 +34,7 @@ def test_library_exports_every_header_entry_point(lib):
     assert len(names) >= 18
     for n in names:
         assert hasattr(lib, n), f"libcannon_gpu.so does not export {n}"
-    assert lib.cp_abi_version() == 1
+    assert lib.cp_abi_version() == 2
 
 
 def test_ctypes_layouts_match_the_c_header(tmp_path):
@@ -45,7 +45,7 @@ def test_ctypes_layouts_match_the_c_header(tmp_path):
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
-    structs = [("cp_body_desc", A.BodyDesc), ("cp_shape_desc", A.ShapeDesc), ("cp_world_desc", A.WorldDesc),
+    structs = [("cp_body_desc", A.BodyDesc), ("cp_body_state", A.BodyState), ("cp_shape_desc", A.ShapeDesc), ("cp_world_desc", A.WorldDesc),
                ("cp_contact", A.Contact), ("cp_row", A.Row), ("cp_constraint_desc", A.ConstraintDesc),
                ("cp_contact_material", A.ContactMaterial), ("cp_step_info", A.StepInfo), ("cp_config", A.Config),
                ("cp_serve_config", S.ServeConfig), ("cp_serve_stats", S.ServeStats)]

@@ -4,7 +4,8 @@ cp_world_step.
 Each scene is created twice; one copy is stepped with cp_world_step, the
 other with cp_world_step_static, over two calls in a row.  After each call
 the body records must be byte-identical, the tolerance every parity test
-here uses.  The file runs last so that it also covers a process in which
+here uses, and so must the last step's pairs, contacts, solver rows and step
+info that the getters return.  The file runs last so that it also covers a process in which
 the other tests have already used the library; it creates its own context,
 so it passes alone in a fresh process too.
 """
@@ -14,6 +15,8 @@ import pytest
 
 from cannon_physics_gb300 import _abi as A
 from cannon_physics_gb300 import engine, scenes
+
+from tests.parity import CONTACT_FIELDS, ROW_FIELDS, diff_records
 
 pytestmark = pytest.mark.gpu
 
@@ -32,24 +35,46 @@ def ctx():
 
 
 SCENES = [
-    ("spheres_on_plane", lambda: scenes.spheres_on_plane()),
-    ("box_pile", lambda: scenes.box_pile(6, 6, 3)),
-    ("mixed_column", lambda: scenes.column_world(300, 11, "mixed")),
+    ("spheres_on_plane", lambda: scenes.spheres_on_plane(), 0),
+    ("box_pile", lambda: scenes.box_pile(6, 6, 3), 0),
+    ("mixed_column", lambda: scenes.column_world(300, 11, "mixed"), 0),
+    # a GridBroadphase world with constraints and sleeping; both copies first
+    # take 12 steps through cp_world_step, which grows the capacities its
+    # first steps overflow (the static step never grows them)
+    ("grid_chains", lambda: scenes.mixed_chains(8, 8, 4, seed=5, chains=4, chain_len=8), 12),
 ]
 
 
-@pytest.mark.parametrize("name,make", SCENES, ids=[n for n, _ in SCENES])
-def test_static_step_matches_world_step(ctx, name, make):
+def _same_lists(ref, sta, what):
+    errs = []
+    rp, sp = ref.pairs(), sta.pairs()
+    if not (len(rp[0]) == len(sp[0]) and (rp[0] == sp[0]).all() and (rp[1] == sp[1]).all()):
+        errs.append(f"pairs differ: {len(rp[0])} vs {len(sp[0])}")
+    errs += diff_records(ref.contacts(), sta.contacts(), CONTACT_FIELDS, "contacts")
+    errs += diff_records(ref.rows(), sta.rows(), ROW_FIELDS, "rows")
+    ri, si = ref.info(), sta.info()
+    for f in ("stepnumber", "time", "num_pairs", "num_contacts", "num_rows", "iterations", "status", "num_levels"):
+        if getattr(ri, f) != getattr(si, f):
+            errs.append(f"info.{f}: {getattr(ri, f)} vs {getattr(si, f)}")
+    assert not errs, f"{what}:\n" + "\n".join(errs[:10])
+
+
+@pytest.mark.parametrize("name,make,grow", SCENES, ids=[n for n, _, _ in SCENES])
+def test_static_step_matches_world_step(ctx, name, make, grow):
     sc = engine.setup_scene(make())
     ref = ctx.world(sc)
     sta = ctx.world(sc)
+    if grow:
+        ref.step(sc.dt, grow)
+        sta.step(sc.dt, grow)
     L = _lib()
     for call in range(2):
         ref.step(sc.dt, 6)
         st = L.cp_world_step_static(ctx.h, sta.id, sc.dt, 6)
         assert st == A.CP_OK, L.cp_last_error().decode()
-        assert ref.info().stepnumber == sta.info().stepnumber
         assert ref.bodies().tobytes() == sta.bodies().tobytes(), f"{name}: call {call}"
+        _same_lists(ref, sta, f"{name}: call {call}")
+        assert sta.info().num_pairs > 0
     ref.destroy()
     sta.destroy()
 
@@ -74,6 +99,9 @@ def test_static_step_reports_overflow(ctx):
     assert [after[f].tobytes() for f in dynamic] == before
     assert sta.info().stepnumber == 0
     assert sta.info().status == 0
+    # the failed step's partial lists are not reported
+    assert (sta.info().num_pairs, sta.info().num_contacts, sta.info().num_rows) == (0, 0, 0)
+    assert len(sta.pairs()[0]) == 0 and len(sta.contacts()) == 0 and len(sta.rows()) == 0
     ref.step(sc.dt, 6)
     sta.step(sc.dt, 6)
     assert ref.bodies().tobytes() == sta.bodies().tobytes()
