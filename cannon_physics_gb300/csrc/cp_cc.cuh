@@ -159,57 +159,6 @@ DI int dclip_face_against_plane(const d3* in, int nin, d3* out, d3 n, double c) 
   return nout;
 }
 
-// binary32 projection radius of a hull about its center along unit axis a
-DI float proj_radius32(const DWorld& W, const DHull& H, q4 q, const f3* ax, f3 a) {
-  if (H.is_box) {
-    return fabsf(dot32(a, ax[0])) * (float)H.he[0] + fabsf(dot32(a, ax[1])) * (float)H.he[1] +
-           fabsf(dot32(a, ax[2])) * (float)H.he[2];
-  }
-  f3 la = rot32(q4{-q.x, -q.y, -q.z, q.w}, a);
-  float m = 0.f;
-  for (int i = 0; i < H.nv; i++) {
-    const float* v = W.hverts + 4 * (H.v0 + i);
-    m = fmaxf(m, fabsf(la.x * v[0] + la.y * v[1] + la.z * v[2]));
-  }
-  return m;
-}
-
-// true when one of the axes findSeparatingAxis tests (canonical face
-// normals, edge crosses that are not almost zero) separates the hulls by a
-// clear margin in binary32: then the reference's SAT reports separation too.
-DI bool hulls_apart32(const DWorld& W, const DHull& A, const DHull& B, f3 xA, f3 xB, q4 qA, q4 qB, float rsum) {
-  f3 axA[3] = {rot32(qA, f3{1.f, 0.f, 0.f}), rot32(qA, f3{0.f, 1.f, 0.f}), rot32(qA, f3{0.f, 0.f, 1.f})};
-  f3 axB[3] = {rot32(qB, f3{1.f, 0.f, 0.f}), rot32(qB, f3{0.f, 1.f, 0.f}), rot32(qB, f3{0.f, 0.f, 1.f})};
-  f3 d = f3{xB.x - xA.x, xB.y - xA.y, xB.z - xA.z};
-  const float margin = 1e-4f * (rsum + fabsf(d.x) + fabsf(d.y) + fabsf(d.z)) + 1e-6f;
-  for (int side = 0; side < 2; side++) {
-    const DHull& H = side ? B : A;
-    if (!H.has_axes) continue;
-    q4 q = side ? qB : qA;
-    for (int k = 0; k < H.ncf; k++) {
-      const float* n = W.faces[H.f0 + W.hcanon[H.cf0 + k]].normal;
-      f3 a = rot32(q, f3{n[0], n[1], n[2]});
-      float dist = fabsf(dot32(a, d));
-      if (dist > proj_radius32(W, A, qA, axA, a) + proj_radius32(W, B, qB, axB, a) + margin) return true;
-    }
-  }
-  for (int k0 = 0; k0 < A.nce; k0++) {
-    const float* e0 = W.hedges + 4 * (A.e0 + W.hcanon[A.ce0 + k0]);
-    f3 we0 = rot32(qA, f3{e0[0], e0[1], e0[2]});
-    for (int k1 = 0; k1 < B.nce; k1++) {
-      const float* e1 = W.hedges + 4 * (B.e0 + W.hcanon[B.ce0 + k1]);
-      f3 we1 = rot32(qB, f3{e1[0], e1[1], e1[2]});
-      f3 cr = f3{we0.y * we1.z - we0.z * we1.y, we0.z * we1.x - we0.x * we1.z, we0.x * we1.y - we0.y * we1.x};
-      if (fmaxf(fabsf(cr.x), fmaxf(fabsf(cr.y), fabsf(cr.z))) < 1e-4f) continue;  // near the almostZero skip
-      float l = len32(cr);
-      f3 a = f3{cr.x / l, cr.y / l, cr.z / l};
-      float dist = fabsf(dot32(a, d));
-      if (dist > proj_radius32(W, A, qA, axA, a) + proj_radius32(W, B, qB, axB, a) + margin) return true;
-    }
-  }
-  return false;
-}
-
 // ---------------------------------------------------------------------------
 // findSeparatingAxis with a binary32 filter.
 //
@@ -440,6 +389,51 @@ DI bool cc_stage1(const DWorld& W, int shA, int shB, f3 xAf, f3 xBf, q4 qAf, q4 
   return cc_setup32(W, shA, shB, xAf, xBf, qAf, qBf, S32) && sat32_bound(S32, U);
 }
 
+// ---------------------------------------------------------------------------
+// Filter check (a test switch, off by default).  With g_filter_check set,
+// every decision a binary32 filter takes for a hull pair is compared with the
+// reference's unfiltered binary64 walk (dfind_separating_axis: every axis in
+// the reference's order): the separation verdict and, for touching hulls,
+// the chosen axis bit for bit.  g_filter_count: {pairs checked, pairs that
+// disagree}.  Per translation unit (the one-block and the wide kernels each
+// keep their own).
+static __device__ int g_filter_check;
+static __device__ unsigned long long g_filter_count[2];
+static __device__ int g_filter_sink[2];  // cursor and overflow flag of a count-only resolver context
+
+DI bool same_bits(d3 a, d3 b) {
+  return __double_as_longlong(a.x) == __double_as_longlong(b.x) && __double_as_longlong(a.y) == __double_as_longlong(b.y) &&
+         __double_as_longlong(a.z) == __double_as_longlong(b.z);
+}
+
+// touch / sep: what the filtered path decided for the pair (sep: the axis
+// after the flip toward A, when touching)
+static __device__ __noinline__ void cc_filter_check(const DWorld& W, int shA, int shB, f3 xAf, f3 xBf, q4 qAf, q4 qBf,
+                                                    bool touch, d3 sep) {
+  const DShape& SA = W.shapes[shA];
+  const DShape& SB = W.shapes[shB];
+  DHullPose A, B;
+  A.H = W.hulls[SA.hull]; A.x = d3of(xAf); A.q = d4of(qAf);
+  B.H = W.hulls[SB.hull]; B.x = d3of(xBf); B.q = d4of(qBf);
+  if (A.H.nf > CP_MAX_HULL_VERTS || B.H.nf > CP_MAX_HULL_VERTS || B.H.nce > CP_MAX_HULL_VERTS) return;
+  A.origin = dvmult(d4{-A.q.x, -A.q.y, -A.q.z, A.q.w}, dsub(d3{0.0, 0.0, 0.0}, A.x));
+  B.origin = dvmult(d4{-B.q.x, -B.q.y, -B.q.z, B.q.w}, dsub(d3{0.0, 0.0, 0.0}, B.x));
+  d3 wnA[CP_MAX_HULL_VERTS], wnB[CP_MAX_HULL_VERTS];
+  for (int k = 0; k < A.H.ncf; k++) {
+    int f = W.hcanon[A.H.cf0 + k];
+    wnA[f] = dvmult(A.q, ldd3(W.faces[A.H.f0 + f].dnormal));
+  }
+  for (int k = 0; k < B.H.ncf; k++) {
+    int f = W.hcanon[B.H.cf0 + k];
+    wnB[f] = dvmult(B.q, ldd3(W.faces[B.H.f0 + f].dnormal));
+  }
+  d3 t = d3{0.0, 0.0, 0.0};
+  const bool ref = dfind_separating_axis(W, A, B, wnA, wnB, t);
+  const bool same = ref == touch && (!ref || same_bits(t, sep));
+  atomicAdd(&g_filter_count[0], 1ull);
+  if (!same) atomicAdd(&g_filter_count[1], 1ull);
+}
+
 // Narrowphase.convexConvex (narrow_phase.dart:1981-2043).  Lanes leave at
 // data-dependent points (the stage-1 test, the binary64 separating-axis
 // walk); a ballot over the lanes that entered together at each such point
@@ -459,7 +453,13 @@ static __device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int
   float U = U1;
   const bool near = U1 == U1 ? cc_setup32(W, shA, shB, xAf, xBf, qAf, qBf, S32) : cc_stage1(W, shA, shB, xAf, xBf, qAf, qBf, S32, U);
   lanes = __ballot_sync(lanes, near);
-  if (!near) return 0;
+  if (!near) {
+    // a binary32 separation certificate (not the bounding spheres, which are
+    // the reference's own test) is checked against the full walk
+    if (*(volatile int*)&g_filter_check && !(distance_to(xAf, xBf) > SA.bsr + SB.bsr))
+      cc_filter_check(W, shA, shB, xAf, xBf, qAf, qBf, false, d3{0.0, 0.0, 0.0});
+    return 0;
+  }
   DHullPose A, B;
   A.H = W.hulls[SA.hull]; A.x = d3of(xAf); A.q = d4of(qAf);
   B.H = W.hulls[SB.hull]; B.x = d3of(xBf); B.q = d4of(qBf);
@@ -480,6 +480,7 @@ static __device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int
       wnB[f] = dvmult(B.q, ldd3(W.faces[B.H.f0 + f].dnormal));
     }
     touch = sat64_compact(W, A, B, wnA, wnB, S32, U, sep);
+    if (*(volatile int*)&g_filter_check) cc_filter_check(W, shA, shB, xAf, xBf, qAf, qBf, touch, sep);
   }
   lanes = __ballot_sync(lanes, touch);
   if (!touch) return 0;

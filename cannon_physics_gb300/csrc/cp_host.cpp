@@ -19,6 +19,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <iterator>
 #include <map>
 #include <mutex>
 #include <string>
@@ -314,6 +315,7 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   size_t o_pb = L.take(sizeof(int) * (pc + 1));
   size_t o_pc = L.take(sizeof(int) * (pc + 1));
   size_t o_pt = L.take(sizeof(int) * (pc + 1));
+  size_t o_pf = L.take(sizeof(int) * (pc + 1));
   size_t o_hv = L.take(sizeof(int) * (pc + 1));
   size_t o_hv2 = L.take(sizeof(int) * (pc + 16 * 32 + 1));
   size_t o_ct = L.take(sizeof(DContact) * (cc + 1));
@@ -350,6 +352,7 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   d.pair_b = (int*)(base + o_pb);
   d.pair_cnt = (int*)(base + o_pc);
   d.pair_tstart = (int*)(base + o_pt);
+  d.pair_flag = (int*)(base + o_pf);
   d.heavy = (int*)(base + o_hv);
   d.heavy2 = (int*)(base + o_hv2);
   d.ctmp = (DContact*)(base + o_ct);
@@ -535,6 +538,9 @@ int grow(cp_ctx* c, int id, int status) {
   if (status & ST_ROWS_OVERFLOW) w.rows_cap *= 2;
   if (status & ST_BINS_OVERFLOW) w.bins_cap *= 2;
   if (w.pairs_cap > (1 << 28) || w.contacts_cap > (1 << 28) || w.rows_cap > (1 << 28)) return fail(CP_ERR_CAPACITY, "capacity limit");
+  const long long lim = c->list_cap_limit;
+  if (lim > 0 && (w.pairs_cap > lim || w.contacts_cap > lim || w.rows_cap > lim || w.bins_cap > lim))
+    return fail(CP_ERR_CAPACITY, "world %d: its pair, contact or row list would grow beyond %lld entries", id, lim);
   int st = alloc_scratch(c, w);
   if (st) return st;
   DWorldParams p;
@@ -784,7 +790,6 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
   if ((d->num_bodies && !d->bodies) || (d->num_shapes && !d->shapes) || (d->num_materials && !d->materials) ||
       (d->num_contact_materials && !d->contact_materials) || (d->num_constraints && !d->constraints))
     return fail(CP_ERR_ARG, "null array");
-  if (d->enable_friction_reduction) return fail(CP_ERR_UNSUPPORTED, "Narrowphase.enableFrictionReduction is not supported");
   if (d->broadphase < CP_BROAD_NAIVE || d->broadphase > CP_BROAD_GRID) return fail(CP_ERR_ARG, "unknown broadphase %d", d->broadphase);
   if (d->solver_iterations < 0) return fail(CP_ERR_ARG, "negative solver iterations");
   const int nb = d->num_bodies, ns = d->num_shapes, nm = d->num_materials;
@@ -942,11 +947,12 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
   WorldRec w;
   w.nb = nb; w.nshapes = ns; w.nmat = nm; w.ncm = (int)cms.size(); w.ncons = d->num_constraints; w.ncon_rows = con_rows;
   w.broadphase = d->broadphase;
-  w.lin_damp.resize(nb); w.ang_damp.resize(nb);
+  w.lin_damp.resize(nb); w.ang_damp.resize(nb); w.body_shape.resize(nb);
   for (int i = 0; i < nb; i++) {
     body_to_device(d->bodies[i], bodies[i]);
     w.lin_damp[i] = d->bodies[i].linear_damping;
     w.ang_damp[i] = d->bodies[i].angular_damping;
+    w.body_shape[i] = d->bodies[i].shape;
   }
   w.cms = cms;
   // params
@@ -964,6 +970,7 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
   P.qn_fast = d->quat_normalize_fast != 0; P.has_fgrav = d->has_friction_gravity != 0;
   P.grid_nx = d->grid_n[0]; P.grid_ny = d->grid_n[1]; P.grid_nz = d->grid_n[2];
   P.n_nocollide = (int)nocollide.size() / 2;
+  P.fric_reduction = d->enable_friction_reduction != 0;
   w.n_nocollide = P.n_nocollide;
   if (d->sap_axis < 0 || d->sap_axis > 2) return fail(CP_ERR_ARG, "sap_axis %d", d->sap_axis);
   if (d->broadphase == CP_BROAD_GRID) {
@@ -1162,13 +1169,136 @@ int cp_world_destroy(cp_ctx* c, int32_t id) {
   return destroy_world(c, id);
 }
 
+}  // extern "C"
+
+namespace {
+
+unsigned long long overlap_key(int a, int b) {
+  const unsigned lo = (unsigned)std::min(a, b), hi = (unsigned)std::max(a, b);
+  return ((unsigned long long)lo << 32) | hi;
+}
+
+// The events of the step just taken (World.internalStep's collide loop,
+// world_class.dart:593-608, and emitContactEvents, :703-770): collide per
+// contact in contact order, then the overlap keepers' diffs in key order.
+int collect_events(cp_ctx* c, int id) {
+  WorldRec& w = c->worlds[id];
+  DWorldParams p;
+  int st = read_params(c, w, p);
+  if (st) return st;
+  std::vector<DContact> ct(p.num_contacts);
+  std::vector<int> pa(p.num_pairs), pb(p.num_pairs), pf(p.num_pairs);
+  if (p.num_contacts)
+    CUDA_TRY(cudaMemcpyAsync(ct.data(), w.dw.contacts, sizeof(DContact) * ct.size(), cudaMemcpyDeviceToHost, c->stream));
+  if (p.num_pairs) {
+    CUDA_TRY(cudaMemcpyAsync(pa.data(), w.dw.pair_a, sizeof(int) * pa.size(), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(pb.data(), w.dw.pair_b, sizeof(int) * pb.size(), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(pf.data(), w.dw.pair_flag, sizeof(int) * pf.size(), cudaMemcpyDeviceToHost, c->stream));
+  }
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  const auto bid = [&](int i) { return w.body_ids.empty() ? i : w.body_ids[i]; };
+  const auto sid = [&](int i) { return w.shape_ids.empty() ? i : w.shape_ids[i]; };
+  std::vector<unsigned long long> bk, sk;
+  for (size_t k = 0; k < ct.size(); k++) {
+    w.event_queue.push_back(cp_event{CP_EV_COLLIDE, ct[k].bi, ct[k].bj, (int32_t)k, p.stepnumber});
+    bk.push_back(overlap_key(bid(ct[k].bi), bid(ct[k].bj)));
+    sk.push_back(overlap_key(sid(ct[k].si), sid(ct[k].sj)));
+  }
+  for (size_t k = 0; k < pf.size(); k++)
+    if (pf[k]) {  // a justTest pair whose shapes overlap
+      bk.push_back(overlap_key(bid(pa[k]), bid(pb[k])));
+      sk.push_back(overlap_key(sid(w.body_shape[pa[k]]), sid(w.body_shape[pb[k]])));
+    }
+  // the index whose id is `v` (ids are unique)
+  const auto index_of = [](const std::vector<int>& ids, unsigned v) {
+    if (ids.empty()) return (int)v;
+    for (size_t i = 0; i < ids.size(); i++)
+      if ((unsigned)ids[i] == v) return (int)i;
+    return -1;
+  };
+  const auto diff = [&](std::vector<unsigned long long>& now, std::vector<unsigned long long>& prev, int ev_add, int ev_rem,
+                        const std::vector<int>& ids) {
+    std::sort(now.begin(), now.end());
+    now.erase(std::unique(now.begin(), now.end()), now.end());
+    std::vector<unsigned long long> add, rem;
+    std::set_difference(now.begin(), now.end(), prev.begin(), prev.end(), std::back_inserter(add));
+    std::set_difference(prev.begin(), prev.end(), now.begin(), now.end(), std::back_inserter(rem));
+    for (unsigned long long key : add)
+      w.event_queue.push_back(cp_event{ev_add, index_of(ids, (unsigned)(key >> 32)), index_of(ids, (unsigned)key), -1, p.stepnumber});
+    for (unsigned long long key : rem)
+      w.event_queue.push_back(cp_event{ev_rem, index_of(ids, (unsigned)(key >> 32)), index_of(ids, (unsigned)key), -1, p.stepnumber});
+    prev.swap(now);
+  };
+  // emitContactEvents: body pairs (begin, then end), then shape pairs
+  diff(bk, w.body_keys, CP_EV_BEGIN_CONTACT, CP_EV_END_CONTACT, w.body_ids);
+  diff(sk, w.shape_keys, CP_EV_BEGIN_SHAPE_CONTACT, CP_EV_END_SHAPE_CONTACT, w.shape_ids);
+  return CP_OK;
+}
+
+// plain_steps, with the event feed collected after every step when it is on
+int world_steps(cp_ctx* c, int id, double dt, int nsteps, double time_inc) {
+  if (!c->worlds[id].events) return plain_steps(c, id, dt, nsteps, time_inc);
+  for (int s = 0; s < nsteps; s++) {
+    int st = plain_steps(c, id, dt, 1, time_inc);
+    if (!st) st = collect_events(c, id);
+    if (st) return st;
+  }
+  return CP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cp_world_set_events(cp_ctx* c, int32_t id, int32_t on, const int32_t* body_ids, const int32_t* shape_ids) {
+  int st = check_world(c, id);
+  if (st) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  WorldRec& w = c->worlds[id];
+  const auto check_ids = [](const int32_t* ids, int n) {
+    std::vector<int> v(ids, ids + n);
+    std::sort(v.begin(), v.end());
+    for (int i = 0; i < n; i++)
+      if (v[i] < 0 || v[i] > 0xffff || (i && v[i] == v[i - 1])) return false;
+    return true;
+  };
+  if (on && body_ids && !check_ids(body_ids, w.nb)) return fail(CP_ERR_ARG, "body ids must be distinct and in [0, 65535]");
+  if (on && shape_ids && !check_ids(shape_ids, w.nshapes)) return fail(CP_ERR_ARG, "shape ids must be distinct and in [0, 65535]");
+  if (on && !body_ids && w.nb > 0x10000) return fail(CP_ERR_ARG, "more than 65536 bodies need explicit ids");
+  w.events = on != 0;
+  w.body_ids.assign(on && body_ids ? body_ids : nullptr, on && body_ids ? body_ids + w.nb : nullptr);
+  w.shape_ids.assign(on && shape_ids ? shape_ids : nullptr, on && shape_ids ? shape_ids + w.nshapes : nullptr);
+  w.body_keys.clear();
+  w.shape_keys.clear();
+  w.event_queue.clear();
+  const int flag = w.events ? 1 : 0;
+  CUDA_TRY(cudaMemcpyAsync(&w.dw.P->events, &flag, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return CP_OK;
+}
+
+int cp_world_get_events(cp_ctx* c, int32_t id, cp_event* out, int32_t cap, int32_t* count) {
+  int st = check_world(c, id);
+  if (st) return st;
+  if (!count) return fail(CP_ERR_ARG, "null count");
+  std::lock_guard<std::mutex> lock(c->mu);
+  WorldRec& w = c->worlds[id];
+  *count = (int32_t)w.event_queue.size();
+  if ((int)w.event_queue.size() > cap || (!out && !w.event_queue.empty()))
+    return fail(CP_ERR_CAPACITY, "need room for %zu events", w.event_queue.size());
+  std::copy(w.event_queue.begin(), w.event_queue.end(), out);
+  w.event_queue.clear();
+  return CP_OK;
+}
+
 int cp_world_step(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
   int st = check_world(c, id);
   if (st) return st;
   if (nsteps < 0 || !(dt > 0)) return fail(CP_ERR_ARG, "need dt > 0 and nsteps >= 0");
   std::lock_guard<std::mutex> lock(c->mu);
   cudaSetDevice(c->device);
-  return plain_steps(c, id, dt, nsteps, dt);
+  return world_steps(c, id, dt, nsteps, dt);
 }
 
 int cp_world_internal_step(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
@@ -1177,7 +1307,7 @@ int cp_world_internal_step(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
   if (nsteps < 0 || !(dt > 0)) return fail(CP_ERR_ARG, "need dt > 0 and nsteps >= 0");
   std::lock_guard<std::mutex> lock(c->mu);
   cudaSetDevice(c->device);
-  return plain_steps(c, id, dt, nsteps, 0.0);
+  return world_steps(c, id, dt, nsteps, 0.0);
 }
 
 int cp_world_set_time(cp_ctx* c, int32_t id, double time, int64_t stepnumber, double accumulator) {
@@ -1209,7 +1339,7 @@ int cp_world_step_interpolated(cp_ctx* c, int32_t id, double dt, double since, i
   const auto t0 = std::chrono::steady_clock::now();
   int n = 0;
   while (w.accumulator >= dt && n < max_sub_steps) {
-    st = plain_steps(c, id, dt, 1, 0.0);  // returns with the stream synchronised
+    st = world_steps(c, id, dt, 1, 0.0);  // returns with the stream synchronised
     if (st) return st;
     w.accumulator -= dt;
     n++;
@@ -1363,6 +1493,7 @@ int cp_world_set_bodies(cp_ctx* c, int32_t id, const cp_body_desc* in, int32_t n
     body_to_device(in[i], b[i]);
     w.lin_damp[i] = in[i].linear_damping;
     w.ang_damp[i] = in[i].angular_damping;
+    w.body_shape[i] = in[i].shape;
   }
   CUDA_TRY(cudaMemcpyAsync(w.dw.bodies, b.data(), sizeof(DBody) * w.nb, cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1509,7 +1640,7 @@ int cp_world_get_sap_order(cp_ctx* c, int32_t id, int32_t* out, int32_t n) {
 
 namespace cpi {
 
-int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool use_graph) {
+int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool use_graph, std::vector<int>* failed) {
   for (int i = 0; i < n; i++) {
     if (ids[i] < 0 || ids[i] >= (int)c->worlds.size() || !c->worlds[ids[i]].live) return fail(CP_ERR_ARG, "no world %d", ids[i]);
     int st = ensure_dt(c, c->worlds[ids[i]], dt);
@@ -1660,9 +1791,11 @@ int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool us
       const long long limit = c->worlds[id].step_limit;
       long long left = std::min(before[4 * i + 1] + nsteps, limit) - after[4 * i + 1];
       st = grow(c, id, (int)after[4 * i]);
-      if (st) return st;
-      st = plain_steps(c, id, dt, (int)left, dt);
-      if (st) return st;
+      if (!st) st = plain_steps(c, id, dt, (int)left, dt);
+      if (st) {
+        if (!failed) return st;
+        failed->push_back(id);  // this world fails alone; the others go on
+      }
     }
   }
   return CP_OK;
@@ -1776,6 +1909,29 @@ int cp_set_resolver_profile(cp_ctx* c, int32_t on) {
   cudaSetDevice(c->device);
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   CUDA_TRY(cpk_set_resolver_profile(on));
+  return CP_OK;
+}
+
+int cp_set_filter_check(cp_ctx* c, int32_t on) {
+  if (!c) return fail(CP_ERR_ARG, "null context");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  CUDA_TRY(cpk_filter_check(on ? 1 : 0));
+  CUDA_TRY(cpk_wide_filter_check(on ? 1 : 0));
+  return CP_OK;
+}
+
+int cp_filter_check_counts(cp_ctx* c, int64_t* checked, int64_t* disagreed, int32_t reset) {
+  if (!c || !checked || !disagreed) return fail(CP_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  unsigned long long a[2], b[2];
+  CUDA_TRY(cpk_filter_counts(a, reset != 0));
+  CUDA_TRY(cpk_wide_filter_counts(b, reset != 0));
+  *checked = (int64_t)(a[0] + b[0]);
+  *disagreed = (int64_t)(a[1] + b[1]);
   return CP_OK;
 }
 

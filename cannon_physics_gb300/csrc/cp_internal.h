@@ -43,6 +43,12 @@ struct WorldRec {
   double accumulator = 0.0;  // World.accumulator of the interpolating World.step
   int last_substeps = 0;     // internal steps of the last interpolating step
   std::vector<double> lin_damp, ang_damp;
+  std::vector<int> body_shape;  // each body's shape index (justTest overlaps of the event feed)
+  // event feed
+  bool events = false;
+  std::vector<int> body_ids, shape_ids;                // the ids overlap keys sort by
+  std::vector<unsigned long long> body_keys, shape_keys;  // overlaps of the last step, sorted
+  std::vector<cp_event> event_queue;
   std::vector<DContactMaterial> cms;  // host copy for SPOOK updates
 };
 
@@ -88,6 +94,9 @@ struct cp_ctx {
   // cp_world_step on a world of at least this many bodies runs the wide
   // kernels (the world spread over the whole GPU); 0: never
   int wide_bodies = CP_WIDE_BODIES_DEFAULT;
+  // a world whose pair, contact, row or bin list would grow beyond this many
+  // entries fails with CP_ERR_CAPACITY instead (0: no limit)
+  long long list_cap_limit = 0;
   long long* d_status = nullptr;  // 4 per world after a batched call, then 4 per world before it
   int d_status_cap = 0;
   std::vector<int> dev_order, dev_gstart;  // what d_ids and d_gstart hold
@@ -134,7 +143,10 @@ int destroy_world(cp_ctx* c, int id);
 // Steps a world set `nsteps` times; worlds stop at their step limit.  With
 // `use_graph` the launch sequence is captured and replayed while the set, dt
 // and step count repeat; without it the kernels are launched directly.
-int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool use_graph);
+// With `failed`, a world that cannot complete its steps (a capacity beyond
+// its limit, a failed regrowth) is listed there and the others complete;
+// without it the first such world's error is returned.
+int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool use_graph, std::vector<int>* failed = nullptr);
 int read_bodies(cp_ctx* c, int id, cp_body_desc* out);
 int read_info(cp_ctx* c, int id, cp_step_info* out);
 // Creates the context's memory pool (release threshold: never) if absent.

@@ -63,6 +63,13 @@ cudaError_t cpk_launch_wide_steps(const DWorld* dw, const DWorld& hw, const Wide
 // the wide sweep kernel's first failed index check {code, index, bound, 0}
 // (code 0: none); clears it once read
 cudaError_t cpk_wide_check(const DWorld& hw, int out[4], cudaStream_t stream);
+// Filter check switch and counters {pairs checked, disagreements} of the
+// one-block kernels (cp_step.cu) and of the wide kernels (cp_wide.cu); the
+// device must be current
+cudaError_t cpk_filter_check(int on);
+cudaError_t cpk_filter_counts(unsigned long long out[2], bool reset);
+cudaError_t cpk_wide_filter_check(int on);
+cudaError_t cpk_wide_filter_counts(unsigned long long out[2], bool reset);
 // CP_PROFILE_SLOTS counters: per-phase cycles summed over blocks (prepare,
 // broadphase, narrowphase, rows+wake+solve prep, row assembly, levels, GS
 // sweeps, apply+integrate), then 16 per-resolver thread-cycle sums and 16

@@ -67,8 +67,11 @@ DI void fill_contact(const NarrowCtx& C, DContact& c, int bA, int bB, int shA, i
   put_contact(c, contact_head(C, bA, bB, shA, shB, rsi, rsj), g);
 }
 
+// cap == 0: a context that only counts contacts (the filter check), never
+// writes them
 DI int reserve(const NarrowCtx& C, int n) {
   if (n == 0) return 0;
+  if (C.cap <= 0) return -1;
   int s = atomicAdd(C.cursor, n);
   if (s + n > C.cap) { atomicOr(C.overflow, ST_CONTACTS_OVERFLOW); return -1; }
   return s;

@@ -674,6 +674,10 @@ struct PairJob {
   float U1;  // hull pairs: stage 1's bound U, or NaN
 };
 
+struct PairJob;
+DI void certificate_check(Smem& S, int k, int rk, PairJob& X);
+DI void just_test_overlap(Smem& S, int k, int rk, PairJob& X);
+
 // Resolver kind of pair k and its job; RK_NONE when the pair makes no
 // contact for a reason that needs no resolver (no shape, a kinematic/static
 // pair, no resolver for the shape types, the collision filter, the bounding
@@ -685,11 +689,14 @@ DI int pair_job(Smem& S, int k, PairJob& X, bool tests) {
   const int i = W.pair_a[k], j = W.pair_b[k];
   const DBody& bi = W.bodies[i];
   const DBody& bj = W.bodies[j];
+  bool just_test = false;
   if (tests) {
-    const bool just_test = (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_STATIC) ||
-                           (bi.type == CP_BODY_STATIC && bj.type == CP_BODY_KINEMATIC) ||
-                           (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_KINEMATIC);
-    if (bi.shape < 0 || bj.shape < 0 || just_test) return RK_NONE;
+    just_test = (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_STATIC) ||
+                (bi.type == CP_BODY_STATIC && bj.type == CP_BODY_KINEMATIC) ||
+                (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_KINEMATIC);
+    if (P.events) W.pair_flag[k] = 0;
+    // a justTest pair only registers an overlap for the event feed
+    if (bi.shape < 0 || bj.shape < 0 || (just_test && !P.events)) return RK_NONE;
   }
   const DShape& si = W.shapes[bi.shape];
   const DShape& sj = W.shapes[bj.shape];
@@ -706,6 +713,10 @@ DI int pair_job(Smem& S, int k, PairJob& X, bool tests) {
   X.qB = swap ? qi : qj;
   X.shA = swap ? bj.shape : bi.shape;
   X.shB = swap ? bi.shape : bj.shape;
+  if (tests && just_test) {
+    just_test_overlap(S, k, rk, X);
+    return RK_NONE;
+  }
   if (tests) {
     // binary32 no-contact certificates (see cp_narrow.cuh)
     const long long t_res = S.rprof ? clock64() : 0;
@@ -716,6 +727,7 @@ DI int pair_job(Smem& S, int k, PairJob& X, bool tests) {
         atomicAdd(&S.r_cyc[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], (unsigned long long)(clock64() - t_res));
         atomicAdd(&S.r_cnt[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], 1u);
       }
+      if (*(volatile int*)&g_filter_check) certificate_check(S, k, rk, X);
       return RK_NONE;
     }
   }
@@ -731,9 +743,45 @@ DI int pair_job(Smem& S, int k, PairJob& X, bool tests) {
   return rk;
 }
 
-DI int run_resolver(Smem& S, int rk, const PairJob& X, int& start) {
+DI int run_resolver(Smem& S, int rk, const PairJob& X, int& start, bool prof);
+
+// The resolver of pair k run into nothing: its contact count (it counts the
+// contacts it finds and writes none)
+DI int count_contacts(Smem& S, int k, int rk, PairJob& X) {
+  const DWorld& W = S.W;
+  const DBody& bi = W.bodies[W.pair_a[k]];
+  const DBody& bj = W.bodies[W.pair_b[k]];
+  const bool swap = !(W.shapes[bi.shape].type < W.shapes[bj.shape].type);
+  X.C.W = &W; X.C.cursor = &g_filter_sink[0]; X.C.cap = 0; X.C.overflow = &g_filter_sink[1]; X.C.cm = 0; X.C.pair = k;
+  X.rsi = bi.shape;
+  X.rsj = bj.shape;
+  X.bA = swap ? W.pair_b[k] : W.pair_a[k];
+  X.bB = swap ? W.pair_a[k] : W.pair_b[k];
+  X.U1 = __int_as_float(0x7fc00000);
+  int start = 0;
+  return run_resolver(S, rk, X, start, false);
+}
+
+// getContacts' justTest call (narrow_phase.dart:665-716): a kinematic /
+// static pair makes no contact, but when its shapes overlap (the resolver
+// would find a contact) the pair enters the overlap keepers that feed the
+// begin / end contact events
+DI void just_test_overlap(Smem& S, int k, int rk, PairJob& X) {
+  S.W.pair_flag[k] = count_contacts(S, k, rk, X) > 0;
+}
+
+// Filter check of a binary32 no-contact certificate: the resolver runs with
+// room for no contact (it counts them and writes none); a nonzero count
+// means the reference would have found a contact.
+DI void certificate_check(Smem& S, int k, int rk, PairJob& X) {
+  const int n = count_contacts(S, k, rk, X);
+  atomicAdd(&g_filter_count[0], 1ull);
+  if (n != 0) atomicAdd(&g_filter_count[1], 1ull);
+}
+
+DI int run_resolver(Smem& S, int rk, const PairJob& X, int& start, bool prof) {
   const NarrowCtx& C = X.C;
-  const long long t_res = S.rprof ? clock64() : 0;
+  const long long t_res = prof ? clock64() : 0;
   int cnt;
   switch (rk) {
     case RK_SS: cnt = sphere_sphere(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, start); break;
@@ -746,7 +794,7 @@ DI int run_resolver(Smem& S, int rk, const PairJob& X, int& start) {
     case RK_BC: cnt = convex_convex(C, X.bA, X.bB, X.shA, X.shB, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, start, X.U1); break;
     default: cnt = convex_convex(C, X.bA, X.bB, X.shA, X.shB, X.rsi, X.rsj, X.xA, X.xB, X.qA, X.qB, start, X.U1); break;
   }
-  if (S.rprof) {
+  if (prof) {
     atomicAdd(&S.r_cyc[rk], (unsigned long long)(clock64() - t_res));
     atomicAdd(&S.r_cnt[rk], 1u);
   }
@@ -779,7 +827,7 @@ DI void narrow_queued(Smem& S, int k, int rk, float U1) {
   pair_job(S, k, X, false);
   X.U1 = U1;
   int start = 0;
-  const int cnt = run_resolver(S, rk, X, start);
+  const int cnt = run_resolver(S, rk, X, start, S.rprof != 0);
   W.pair_cnt[k] = cnt;
   W.pair_tstart[k] = start;
 }
@@ -801,6 +849,9 @@ DI void narrow_stage1(Smem& S, int h, int* nq2) {
       W.pair_tstart[k] = __float_as_int(U);  // until the binary64 stage sets it
       W.heavy[atomicAdd(nq2, 1)] = (int)e;
     } else {
+      if (*(volatile int*)&g_filter_check &&
+          !(distance_to(X.xA, X.xB) > W.shapes[X.shA].bsr + W.shapes[X.shB].bsr))
+        cc_filter_check(W, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, false, d3{0.0, 0.0, 0.0});
       W.pair_cnt[k] = 0;
       W.pair_tstart[k] = 0;
     }
@@ -900,9 +951,27 @@ DI bool row_kept(const DWorld& W, int bi, int bj, bool enabled) {  // Solver.add
 //   [0, nF)          friction rows, two per contact with friction > 0
 //   [nF, nF+nC)      contact rows
 //   [nF+nC, ...)     constraint rows (constraint order, equation order)
+// Narrowphase.enableFrictionReduction (narrow_phase.dart:114): planeConvex
+// and convexConvex (:1904-1911, :2033-2038) create no friction equations per
+// contact but one pair of them per shape pair, from its last contact, with
+// the pair's contacts averaged (createFrictionFromAverage, :589-627).  The
+// other resolvers create theirs per contact as always.
+DI bool fric_reduced(const DWorld& W, const DWorldParams& P, const DContact& ct) {
+  if (!P.fric_reduction) return false;
+  const int ta = W.shapes[ct.si].type, tb = W.shapes[ct.sj].type;
+  return resolver_kind(min(ta, tb), max(ta, tb)) >= RK_PB;
+}
+
 // friction rows of contact c (cscr[c] = 2 or 0) and its slip force
 DI void contact_fric_count(const DWorld& W, const DWorldParams& P, int c) {
   DContact& ct = W.contacts[c];
+  // with friction reduction only the last contact of a plane-hull or
+  // hull-hull shape pair carries friction rows (the pair's contacts are
+  // W.contacts[heavy[k] .. heavy[k] + pair_cnt[k]))
+  if (fric_reduced(W, P, ct) && c != W.heavy[ct.pair] + W.pair_cnt[ct.pair] - 1) {
+    W.cscr[c] = 0;
+    return;
+  }
   double fr = contact_friction(W, ct);
   W.cscr[c] = fr > 0 ? 2 : 0;
   if (fr > 0) {
@@ -1148,8 +1217,32 @@ DI void assemble_row(const DWorld& W, const RowGeom& G, DRow& R, double h) {
   R.kind = G.kind;
 }
 
+// createFrictionFromAverage (narrow_phase.dart:589-627): the friction rows
+// of the last contact `last` of a shape pair with n >= 2 contacts take the
+// pair's averaged contact points and the tangents of its averaged normal
+DI void fric_average(const DWorld& W, int last, int n, f3& ri, f3& rj, f3& t1, f3& t2) {
+  f3 avgN{0.f, 0.f, 0.f}, avgA{0.f, 0.f, 0.f}, avgB{0.f, 0.f, 0.f};
+  const int bodyA = W.contacts[last].bi;
+  for (int i = 0; i != n; i++) {
+    const DContact& c = W.contacts[last - i];
+    if (c.bi != bodyA) {
+      avgN = add(avgN, ld3(c.ni));
+      avgA = add(avgA, ld3(c.ri));
+      avgB = add(avgB, ld3(c.rj));
+    } else {
+      avgN = sub(avgN, ld3(c.ni));
+      avgA = add(avgA, ld3(c.rj));
+      avgB = add(avgB, ld3(c.ri));
+    }
+  }
+  const double inv = 1.0 / n;
+  ri = scale(avgA, inv);
+  rj = scale(avgB, inv);
+  tangents(normalized(avgN), t1, t2);
+}
+
 // the friction and contact rows of contact c
-DI void assemble_contact_rows(const DWorld& W, int c, int nF, int ncand, int nrows, double h) {
+DI void assemble_contact_rows(const DWorld& W, const DWorldParams& P, int c, int nF, int ncand, int nrows, double h) {
   const DContact& ct = W.contacts[c];
   const DContactMaterial& cm = W.cms[ct.cm];
   RowGeom G;
@@ -1158,7 +1251,9 @@ DI void assemble_contact_rows(const DWorld& W, int c, int nF, int ncand, int nro
   f3 ni = ld3(ct.ni);
   if (ct.frow >= 0) {
     f3 t1, t2;
-    tangents(ni, t1, t2);
+    const int np = fric_reduced(W, P, ct) ? W.pair_cnt[ct.pair] : 1;
+    if (np > 1) fric_average(W, c, np, G.ri, G.rj, t1, t2);
+    else tangents(ni, t1, t2);
     G.kind = CP_ROW_FRICTION;
     G.a = cm.fa; G.b = cm.fb; G.eps = cm.feps;
     G.minF = -ct.slip; G.maxF = ct.slip;
@@ -1175,6 +1270,7 @@ DI void assemble_contact_rows(const DWorld& W, int c, int nF, int ncand, int nro
   int cd = nF + c;
   if (cand_kept(W, cd, ncand, nrows)) {
     G.kind = CP_ROW_CONTACT;
+    G.ri = ld3(ct.ri); G.rj = ld3(ct.rj);
     G.n = ni;
     G.restitution = ct.restitution;
     G.a = cm.ca; G.b = cm.cb; G.eps = cm.ceps;
@@ -1225,7 +1321,7 @@ DI void assemble_constraint_rows(const DWorld& W, int k, int base0, int ncand, i
 DI void ph_rows_assemble(Smem& S, double h) {
   const DWorld& W = S.W;
   const int nc = S.n_contacts, nF = S.n_fric, ncand = S.n_cand, nrows = S.n_rows;
-  for (int c = threadIdx.x; c < nc; c += BT) assemble_contact_rows(W, c, nF, ncand, nrows, h);
+  for (int c = threadIdx.x; c < nc; c += BT) assemble_contact_rows(W, S.P, c, nF, ncand, nrows, h);
   for (int k = threadIdx.x; k < S.P.ncons; k += BT) assemble_constraint_rows(W, k, nF + nc, ncand, nrows, h);
   __syncthreads();
 }

@@ -187,19 +187,23 @@ struct cp_server {
       for (Request* r : act)
         if (r->remaining > 0 && !r->cancel) by_dt[r->dt].push_back(r->world);
       int st = CP_OK;
+      std::vector<int> failed;
+      std::string fail_msg;
       const double t0 = now_s();
       {
         std::lock_guard<std::mutex> lc(ctx->mu);
         cudaSetDevice(ctx->device);
         for (auto& kv : by_dt) {
-          st = step_worlds(ctx, kv.second.data(), (int)kv.second.size(), kv.first, m, false);
+          const size_t before = failed.size();
+          st = step_worlds(ctx, kv.second.data(), (int)kv.second.size(), kv.first, m, false, &failed);
+          if (failed.size() > before && fail_msg.empty()) fail_msg = last_error();
           if (st) break;
         }
       }
       device_s += now_s() - t0;
       if (st) {
-        // a step that cannot complete (a capacity beyond its limit, a CUDA
-        // error) fails every world of the tick; their memory is released
+        // an error no single world explains (a CUDA error, bad arguments)
+        // fails every world of the tick; their memory is released
         std::string msg = last_error();
         {
           std::lock_guard<std::mutex> lc(ctx->mu);
@@ -207,6 +211,24 @@ struct cp_server {
         }
         fail_all_active(st, msg);
         continue;
+      }
+      if (!failed.empty()) {
+        // a world that cannot complete its steps (a capacity beyond its limit)
+        // fails alone: its request ends with the error, the others go on
+        std::lock_guard<std::mutex> lc(ctx->mu);
+        std::lock_guard<std::mutex> lk(mu);
+        for (int id : failed) {
+          auto it = std::find_if(act.begin(), act.end(), [&](Request* r) { return r->world == id; });
+          if (it == act.end()) continue;
+          Request* r = *it;
+          destroy_world(ctx, r->world);
+          r->status = CP_ERR_CAPACITY;
+          r->error = fail_msg;
+          finish(r, REQ_FAILED);
+          active.erase(std::find(active.begin(), active.end(), r));
+          act.erase(it);
+        }
+        cv_done.notify_all();
       }
       // retire finished and cancelled worlds
       std::vector<Request*> done;
@@ -246,7 +268,7 @@ extern "C" {
 int cp_serve_start(const cp_serve_config* cfg, cp_server** out) {
   if (!cfg || !out) return fail(CP_ERR_ARG, "null argument");
   *out = nullptr;
-  if (cfg->hbm_budget_bytes <= 0 || cfg->steps_per_tick < 0 || cfg->max_active_bodies < 0)
+  if (cfg->hbm_budget_bytes <= 0 || cfg->steps_per_tick < 0 || cfg->max_active_bodies < 0 || cfg->max_list_entries < 0)
     return fail(CP_ERR_ARG, "bad server configuration");
   cp_config cc{};
   cc.device = cfg->device;
@@ -261,6 +283,7 @@ int cp_serve_start(const cp_serve_config* cfg, cp_server** out) {
       ctx->forced = cfg->variant;
     }
     if (cfg->group_bodies > 0) ctx->group_bodies = cfg->group_bodies;
+    ctx->list_cap_limit = cfg->max_list_entries;
   }
   if (st) {
     cp_destroy(ctx);

@@ -826,6 +826,17 @@ cudaError_t cpk_phase_cycles(unsigned long long* out, bool reset) {
   return e;
 }
 
+cudaError_t cpk_filter_check(int on) { return cudaMemcpyToSymbol(g_filter_check, &on, sizeof(int)); }
+
+cudaError_t cpk_filter_counts(unsigned long long out[2], bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_filter_count, 2 * sizeof(unsigned long long));
+  if (e == cudaSuccess && reset) {
+    const unsigned long long z[2] = {0, 0};
+    e = cudaMemcpyToSymbol(g_filter_count, z, sizeof(z));
+  }
+  return e;
+}
+
 cudaError_t cpk_set_resolver_profile(int on) {
   const int v = on ? 1 : 0;
   return cudaMemcpyToSymbol(g_res_profile, &v, sizeof(v));

@@ -152,7 +152,7 @@ struct __align__(16) DWorldParams {
   int grid_nz, nbins, status, last_iterations;
   int num_pairs, num_contacts, num_rows, num_levels;
   int pairs_cap, contacts_cap, rows_cap, bins_cap;
-  int grid_plane_done, n_nocollide, pad[2];
+  int grid_plane_done, n_nocollide, fric_reduction, events;
   float grid_plane_n[4];
   long long step_limit;  // the step kernels leave the world alone once stepnumber reaches this
 };
@@ -199,6 +199,7 @@ struct DWorld {
   int* pair_b;
   int* pair_cnt;
   int* pair_tstart;
+  int* pair_flag;   // event feed: 1 for a kinematic/static pair whose shapes overlap (the reference's justTest)
   int* heavy;       // pairs queued for a resolver, (kind << 28) | pair; later scan scratch
   int* heavy2;      // queued pairs sorted by resolver kind (pairs + 16 * 32 slots)
   DContact* ctmp;

@@ -252,7 +252,7 @@ __global__ void k_w_naive(const DWorld* dw, int pass) {
 }
 
 // scan of the naive per-block counts (one block)
-__global__ void k_w_naive_scan(const DWorld* dw, int nblocks) {
+__global__ void __launch_bounds__(1024) k_w_naive_scan(const DWorld* dw, int nblocks) {
   __shared__ Smem S;
   if (!wide_enter(S, dw)) return;
   const int total = block_scan_array(S, S.W.wpart, nblocks);
@@ -278,7 +278,7 @@ __global__ void k_w_grid_bin(const DWorld* dw, int pass) {
   WIDE_LOOP(i, S.P.nb) grid_bin_body(S.W, S.P, c, i, pass);
 }
 
-__global__ void k_w_grid_planes(const DWorld* dw, int pass) {
+__global__ void __launch_bounds__(1024) k_w_grid_planes(const DWorld* dw, int pass) {
   __shared__ Smem S;
   if (!wide_enter(S, dw)) return;
   double c[10];
@@ -481,7 +481,7 @@ __global__ void k_w_assemble(const DWorld* dw, double h) {
   const DWide* x = W.wide;
   const int nc = x->n_contacts, nF = x->n_fric, ncand = x->n_cand, nrows = x->n_rows;
   WIDE_LOOP(t, nc + S.P.ncons) {
-    if (t < nc) assemble_contact_rows(W, t, nF, ncand, nrows, h);
+    if (t < nc) assemble_contact_rows(W, S.P, t, nF, ncand, nrows, h);
     else assemble_constraint_rows(W, t - nc, nF + nc, ncand, nrows, h);
   }
 }
@@ -875,6 +875,17 @@ cudaError_t cpk_launch_wide_steps(const DWorld* dw, const DWorld& hw, const Wide
   }
   if (launches) *launches += n;
   return cudaSuccess;
+}
+
+cudaError_t cpk_wide_filter_check(int on) { return cudaMemcpyToSymbol(g_filter_check, &on, sizeof(int)); }
+
+cudaError_t cpk_wide_filter_counts(unsigned long long out[2], bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, g_filter_count, 2 * sizeof(unsigned long long));
+  if (e == cudaSuccess && reset) {
+    const unsigned long long z[2] = {0, 0};
+    e = cudaMemcpyToSymbol(g_filter_count, z, sizeof(z));
+  }
+  return e;
 }
 
 cudaError_t cpk_wide_check(const DWorld& hw, int out[4], cudaStream_t st) {

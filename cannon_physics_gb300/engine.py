@@ -63,6 +63,8 @@ def lib():
         L.cp_set_variant.argtypes = [vp, i32]
         L.cp_set_group_bodies.argtypes = [vp, i32]
         L.cp_set_wide_bodies.argtypes = [vp, i32]
+        L.cp_set_filter_check.argtypes = [vp, i32]
+        L.cp_filter_check_counts.argtypes = [vp, vp, vp, i32]
         _lib = L
     return _lib
 
@@ -124,6 +126,17 @@ class Context:
     def resolver_profile(self, on=True):
         """Count per-resolver cycles and calls (off by default; per device)."""
         check(lib().cp_set_resolver_profile(self.h, int(bool(on))), "cp_set_resolver_profile")
+
+    def set_filter_check(self, on=True):
+        """Check every binary32 filter decision against the unfiltered binary64
+        computation (slow; for tests and audits)."""
+        check(lib().cp_set_filter_check(self.h, int(bool(on))), "cp_set_filter_check")
+
+    def filter_check_counts(self, reset=False):
+        """(pairs checked, disagreements) since the last reset."""
+        a, b = C.c_int64(), C.c_int64()
+        check(lib().cp_filter_check_counts(self.h, C.byref(a), C.byref(b), int(bool(reset))), "cp_filter_check_counts")
+        return a.value, b.value
 
     def set_wide_bodies(self, n):
         """Single-world steps of worlds with at least n bodies spread over the

@@ -25,6 +25,7 @@ class ServeConfig(C.Structure):
         ("max_active_bodies", C.c_int64),
         ("variant", C.c_int32),
         ("group_bodies", C.c_int32),
+        ("max_list_entries", C.c_int64),
     ]
 
 
@@ -59,9 +60,11 @@ class Server:
     advances per launch sequence; max_active_bodies: optional cap on the
     bodies stepping at once (0: only the budget limits admission)."""
 
-    def __init__(self, device=0, hbm_budget=150e9, steps_per_tick=2, max_active_bodies=0, variant=-1, group_bodies=0):
+    def __init__(self, device=0, hbm_budget=150e9, steps_per_tick=2, max_active_bodies=0, variant=-1, group_bodies=0,
+                 max_list_entries=0):
         L = _bind(lib())
-        cfg = ServeConfig(device, steps_per_tick, int(hbm_budget), int(max_active_bodies), variant, group_bodies)
+        cfg = ServeConfig(device, steps_per_tick, int(hbm_budget), int(max_active_bodies), variant, group_bodies,
+                          int(max_list_entries))
         h = C.c_void_p()
         check(L.cp_serve_start(C.byref(cfg), C.byref(h)), "cp_serve_start")
         self.h = h

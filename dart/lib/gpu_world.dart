@@ -143,9 +143,6 @@ class GpuWorld extends World {
       _check(api.worldDestroy(_ctx, _worldId));
       _worldId = -1;
     }
-    if (narrowphase.enableFrictionReduction) {
-      throw UnsupportedError('GpuWorld: enableFrictionReduction is not on the GPU path');
-    }
     final arena = Arena();
     try {
       // materials: every Material reachable from shapes, bodies and contact
@@ -261,6 +258,7 @@ class GpuWorld extends World {
       r.solverIterations = solver.iterations;
       r.solverTolerance = solver is GSSolver ? (solver as GSSolver).tolerance : 1e-7;
       r.useBoundingBoxes = broadphase.useBoundingBoxes ? 1 : 0;
+      r.enableFrictionReduction = narrowphase.enableFrictionReduction ? 1 : 0;
       final bp = broadphase;
       if (bp is SAPBroadphase) {
         r.broadphase = cpBroadSap;

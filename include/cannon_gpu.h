@@ -342,6 +342,41 @@ int cp_world_set_time(cp_ctx* ctx, int32_t world_id, double time, int64_t stepnu
 #define CP_STATIC_SCRATCH_BYTES (64u * 1024u * 1024u)
 int cp_world_step_static(cp_ctx* ctx, int32_t world_id, double dt, int32_t nsteps);
 
+/* ---- event feed (World events, lib/world/world_class.dart:593-610,703-770) --
+ *
+ * The reference dispatches, inside World.internalStep, a `collide` event to
+ * both bodies of every contact (its collision matrices alias, so every
+ * contact counts as a first contact), and then beginContact / endContact /
+ * beginShapeContact / endShapeContact for the body and shape pairs whose
+ * overlap started or ended since the previous step (OverlapKeeper,
+ * lib/collision/overlap_keeper.dart; kinematic / static pairs whose shapes
+ * overlap count too, through getContacts' justTest call).  With the feed on,
+ * every step of the world records those events in that order; the O(N^3)
+ * collision matrix and the O(K^2) insertion sorts are replaced by sorted
+ * key sets built from the step's contact and pair lists on the host. */
+enum cp_event_type {
+  CP_EV_COLLIDE = 0,             /* a = contact.bi, b = contact.bj, contact = its index in the step's contacts */
+  CP_EV_BEGIN_CONTACT = 1,       /* a, b: bodies (the lower id first, as OverlapKeeper unpacks its keys) */
+  CP_EV_END_CONTACT = 2,
+  CP_EV_BEGIN_SHAPE_CONTACT = 3, /* a, b: shapes (lower id first) */
+  CP_EV_END_SHAPE_CONTACT = 4
+};
+typedef struct cp_event {
+  int32_t type, a, b, contact;
+  int64_t stepnumber;               /* World.stepnumber after the step that raised it */
+} cp_event;
+
+/* Turn a world's event feed on or off (off by default: it costs a
+ * device-to-host copy of the step's lists and a synchronisation per step).
+ * body_ids / shape_ids (may be NULL: the indices) give the Body.id and
+ * Shape.id values the overlap keys sort by, so events of one step come in
+ * the reference's order; ids must be below 65536 (the reference packs two
+ * into one key).  Turning the feed on starts with empty overlap sets. */
+int cp_world_set_events(cp_ctx* ctx, int32_t world_id, int32_t on, const int32_t* body_ids, const int32_t* shape_ids);
+/* Drains the world's recorded events (oldest first).  CP_ERR_CAPACITY with
+ * *count set when more than cap are waiting (nothing is drained then). */
+int cp_world_get_events(cp_ctx* ctx, int32_t world_id, cp_event* out, int32_t cap, int32_t* count);
+
 /* Read back / overwrite body state (Body fields). */
 int cp_world_get_bodies(cp_ctx* ctx, int32_t world_id, cp_body_desc* out, int32_t n);
 int cp_world_set_bodies(cp_ctx* ctx, int32_t world_id, const cp_body_desc* in, int32_t n);
@@ -436,6 +471,19 @@ int cp_set_group_bodies(cp_ctx* ctx, int32_t bodies);
  * 0 keeps every world on one block.  No counterpart in the reference. */
 int cp_set_wide_bodies(cp_ctx* ctx, int32_t bodies);
 
+/* Filter check, a test switch with no counterpart in the reference (off by
+ * default; per device).  Where a binary32 filter settles a pair without the
+ * reference's binary64 arithmetic (the no-contact certificates of
+ * sphere-plane, sphere-box and plane-hull pairs; the separating-axis bound
+ * and the candidate axes of hull pairs), the step also runs the unfiltered
+ * binary64 computation and compares: the resolver's contact count for a
+ * certificate, and the separation verdict and the chosen axis (bit for bit)
+ * for findSeparatingAxis.  Steps run several times slower while it is on.
+ * cp_filter_check_counts reads the pairs checked and the disagreements since
+ * the last reset. */
+int cp_set_filter_check(cp_ctx* ctx, int32_t on);
+int cp_filter_check_counts(cp_ctx* ctx, int64_t* checked, int64_t* disagreed, int32_t reset);
+
 /* Device time (CUDA events on the context stream) of the batched-step graph
  * launches since the previous call, and how many step launches they held. */
 int cp_batch_profile(cp_ctx* ctx, double* graph_ms, int64_t* step_launches);
@@ -463,6 +511,11 @@ typedef struct cp_serve_config {
   int64_t max_active_bodies;        /* 0 = no cap; else admission also stops at this many bodies stepping */
   int32_t variant;                  /* kernel variant pair, -1 = default */
   int32_t group_bodies;             /* world grouping of the solve kernel, 0 = default */
+  /* a world whose pair, contact or row list would have to grow beyond this
+   * many entries (its step scratch beyond what admission counted on) fails
+   * alone with CP_ERR_CAPACITY; the other requests of its ticks go on.
+   * 0 = no limit */
+  int64_t max_list_entries;
 } cp_serve_config;
 
 /* request states */

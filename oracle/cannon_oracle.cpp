@@ -632,6 +632,45 @@ struct Constraint {
   std::vector<Eq> eqs;  // p2p: x,y,z; hinge: x,y,z,rot1,rot2,motor; distance: one contact
 };
 
+// OverlapKeeper (lib/collision/overlap_keeper.dart): a sorted list of pair
+// keys built by insertion, swapped out every step, and a merge-style diff
+struct OverlapKeeper {
+  std::vector<long long> current, previous;
+  static long long getKey(long long i, long long j) {
+    if (j < i) std::swap(i, j);
+    return (i << 16) | j;
+  }
+  void set(int i, int j) {  // overlap_keeper.dart:22-38
+    const long long key = getKey(i, j);
+    size_t index = 0;
+    while (index < current.size() && key > current[index]) index++;
+    if (index < current.size() && key == current[index]) return;
+    current.insert(current.begin() + index, key);
+  }
+  void tick() {  // :41-46
+    std::swap(current, previous);
+    current.clear();
+  }
+  void getDiff(std::vector<int>& additions, std::vector<int>& removals) const {  // :49-85
+    const std::vector<long long>& a = current;
+    const std::vector<long long>& b = previous;
+    size_t j = 0;
+    for (size_t i = 0; i < a.size(); i++) {
+      const long long keyA = a[i];
+      while (j < b.size() && keyA > b[j]) j++;
+      const bool found = j < b.size() && keyA == b[j];
+      if (!found) { additions.push_back((int)((keyA & 0xffff0000LL) >> 16)); additions.push_back((int)(keyA & 0xffff)); }
+    }
+    j = 0;
+    for (size_t i = 0; i < b.size(); i++) {
+      const long long keyB = b[i];
+      while (j < a.size() && keyB > a[j]) j++;
+      const bool found = j < a.size() && a[j] == keyB;
+      if (!found) { removals.push_back((int)((keyB & 0xffff0000LL) >> 16)); removals.push_back((int)(keyB & 0xffff)); }
+    }
+  }
+};
+
 struct World {
   std::vector<Body> bodies;
   std::vector<Shape> shapes;
@@ -656,6 +695,23 @@ struct World {
   std::vector<char> planeNormalDone;
   std::vector<V3> planeWorldNormal;
   bool enableFrictionReduction = false;
+  // events (world_class.dart:213-221,593-610,703-770), when recorded
+  bool events = false;
+  std::vector<int> bodyIds, shapeIds;
+  OverlapKeeper bodyOverlapKeeper, shapeOverlapKeeper;
+  std::vector<cp_event> eventQueue;
+  int bodyId(int i) const { return bodyIds.empty() ? i : bodyIds[i]; }
+  int shapeId(int i) const { return shapeIds.empty() ? i : shapeIds[i]; }
+  int bodyIndex(int id) const {
+    if (bodyIds.empty()) return id;
+    for (size_t i = 0; i < bodyIds.size(); i++) if (bodyIds[i] == id) return (int)i;
+    return -1;
+  }
+  int shapeIndex(int id) const {
+    if (shapeIds.empty()) return id;
+    for (size_t i = 0; i < shapeIds.size(); i++) if (shapeIds[i] == id) return (int)i;
+    return -1;
+  }
   double time = 0;
   long long stepnumber = 0;
   double dt = -1;
@@ -1396,7 +1452,23 @@ struct World {
       const ContactMat* shapeCM = nullptr;
       if (si.material >= 0 && sj.material >= 0) shapeCM = getCM(si.material, sj.material);
       current = shapeCM ? *shapeCM : (bodyCM ? *bodyCM : defaultCM);
-      if (justTest) continue;  // justTest resolvers add no contacts
+      if (justTest) {
+        // a justTest resolver adds no contacts; where it would find one it
+        // registers the overlap (narrow_phase.dart:712-715)
+        if (events) {
+          const size_t nc = contacts.size(), nf = frictionEqs.size();
+          curPair = k;
+          if (si.type < sj.type) dispatch(si, sj, xi, xj, qi, qj, ibi, ibj, bi.shape, bj.shape);
+          else dispatch(sj, si, xj, xi, qj, qi, ibj, ibi, bi.shape, bj.shape);
+          if (contacts.size() > nc) {
+            shapeOverlapKeeper.set(shapeId(bi.shape), shapeId(bj.shape));
+            bodyOverlapKeeper.set(bodyId(ibi), bodyId(ibj));
+          }
+          contacts.resize(nc);
+          frictionEqs.resize(nf);
+        }
+        continue;
+      }
       curPair = k;
       if (si.type < sj.type) dispatch(si, sj, xi, xj, qi, qj, ibi, ibj, bi.shape, bj.shape);
       else dispatch(sj, si, xj, xi, qj, qi, ibj, ibi, bi.shape, bj.shape);
@@ -1638,6 +1710,10 @@ struct World {
         }
       }
     }
+    if (events) {  // collisionMatrixTick (world_class.dart:213-221)
+      bodyOverlapKeeper.tick();
+      shapeOverlapKeeper.tick();
+    }
     getContacts();
     std::vector<Eq*> eqs;
     for (auto& f : frictionEqs) addEquation(eqs, f);
@@ -1659,7 +1735,15 @@ struct World {
         double l2 = bi.sleepSpeedLimit * bi.sleepSpeedLimit;
         if (s2 >= l2 * 2) bj.wakeUpAfterNarrowphase = true;
       }
+      if (events) {
+        // the collision matrices alias, so every contact is a "first" one
+        // and dispatches collide to both bodies (world_class.dart:593-604)
+        eventQueue.push_back(cp_event{CP_EV_COLLIDE, c.bi, c.bj, (int32_t)(&c - &contacts[0]), stepnumber + 1});
+        bodyOverlapKeeper.set(bodyId(c.bi), bodyId(c.bj));
+        shapeOverlapKeeper.set(shapeId(c.si), shapeId(c.sj));
+      }
     }
+    if (events) emitContactEvents();
     for (int i = 0; i != N; i++) {
       Body& b = bodies[i];
       if (b.wakeUpAfterNarrowphase) { wakeUp(b); b.wakeUpAfterNarrowphase = false; }
@@ -1686,6 +1770,24 @@ struct World {
     dirty = true;
     stepnumber += 1;
     if (allowSleep) for (int i = 0; i != N; i++) sleepTick(bodies[i], time);
+  }
+  // world_class.dart:703-770
+  void emitContactEvents() {
+    std::vector<int> additions, removals;
+    bodyOverlapKeeper.getDiff(additions, removals);
+    for (size_t i = 0; i < additions.size(); i += 2)
+      eventQueue.push_back(cp_event{CP_EV_BEGIN_CONTACT, bodyIndex(additions[i]), bodyIndex(additions[i + 1]), -1, stepnumber + 1});
+    for (size_t i = 0; i < removals.size(); i += 2)
+      eventQueue.push_back(cp_event{CP_EV_END_CONTACT, bodyIndex(removals[i]), bodyIndex(removals[i + 1]), -1, stepnumber + 1});
+    additions.clear();
+    removals.clear();
+    shapeOverlapKeeper.getDiff(additions, removals);
+    for (size_t i = 0; i < additions.size(); i += 2)
+      eventQueue.push_back(
+          cp_event{CP_EV_BEGIN_SHAPE_CONTACT, shapeIndex(additions[i]), shapeIndex(additions[i + 1]), -1, stepnumber + 1});
+    for (size_t i = 0; i < removals.size(); i += 2)
+      eventQueue.push_back(
+          cp_event{CP_EV_END_SHAPE_CONTACT, shapeIndex(removals[i]), shapeIndex(removals[i + 1]), -1, stepnumber + 1});
   }
   // solver.dart:30-34
   void addEquation(std::vector<Eq*>& eqs, Eq& e) {
@@ -1935,6 +2037,28 @@ int orc_world_step_interpolated(orc_world* o, double dt, double since, int32_t m
   if (!o || !(dt > 0) || max_sub_steps < 0) return CP_ERR_ARG;
   o->w.stepInterpolated(dt, since, max_sub_steps);
   if (substeps) *substeps = o->w.lastSubsteps;
+  return CP_OK;
+}
+
+int orc_world_set_events(orc_world* o, int32_t on, const int32_t* body_ids, const int32_t* shape_ids) {
+  if (!o) return CP_ERR_ARG;
+  World& w = o->w;
+  w.events = on != 0;
+  w.bodyIds.assign(on && body_ids ? body_ids : nullptr, on && body_ids ? body_ids + w.bodies.size() : nullptr);
+  w.shapeIds.assign(on && shape_ids ? shape_ids : nullptr, on && shape_ids ? shape_ids + w.shapes.size() : nullptr);
+  w.bodyOverlapKeeper = OverlapKeeper();
+  w.shapeOverlapKeeper = OverlapKeeper();
+  w.eventQueue.clear();
+  return CP_OK;
+}
+
+int orc_world_get_events(orc_world* o, cp_event* out, int32_t cap, int32_t* count) {
+  if (!o || !count) return CP_ERR_ARG;
+  World& w = o->w;
+  *count = (int32_t)w.eventQueue.size();
+  if ((int)w.eventQueue.size() > cap || (!out && !w.eventQueue.empty())) return CP_ERR_CAPACITY;
+  std::copy(w.eventQueue.begin(), w.eventQueue.end(), out);
+  w.eventQueue.clear();
   return CP_OK;
 }
 

@@ -41,6 +41,11 @@ int orc_world_set_time(orc_world* w, double time, int64_t stepnumber, double acc
 /* Overwrite the bodies / the persisted SAP order (e.g. with a GPU world's
  * state, to time or check the oracle from the same step). */
 int orc_world_set_bodies(orc_world* w, const cp_body_desc* in, int32_t n);
+/* Record World's events (collide, begin / end contact, begin / end shape
+ * contact) in dispatch order, restating the reference's collision matrix
+ * and OverlapKeeper; ids as in cp_world_set_events. */
+int orc_world_set_events(orc_world* w, int32_t on, const int32_t* body_ids, const int32_t* shape_ids);
+int orc_world_get_events(orc_world* w, cp_event* out, int32_t cap, int32_t* count);
 int orc_world_set_sap_order(orc_world* w, const int32_t* in, int32_t n);
 int orc_world_get_bodies(orc_world* w, cp_body_desc* out, int32_t n);
 int orc_world_get_pairs(orc_world* w, int32_t* p1, int32_t* p2, int32_t cap, int32_t* count);

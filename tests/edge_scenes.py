@@ -12,7 +12,7 @@ from cannon_physics_gb300 import scenes
 
 EDGE_NAMES = ["materials", "filters", "kinematic_trigger", "sleep_wake", "motor", "nocollide", "quat_modes",
               "bbox_naive", "friction_gravity", "shape_offsets", "convex_hulls", "empty", "single", "all_static",
-              "sap_y_axis", "grid_spheres"]
+              "sap_y_axis", "grid_spheres", "friction_reduction"]
 
 
 def _mix(n, seed, spacing=1.1, side=4, kinds=(A.SHAPE_SPHERE, A.SHAPE_BOX, A.SHAPE_CYLINDER)):
@@ -181,6 +181,18 @@ def edge_scene(name):
         shapes, bodies = _mix(40, 19, side=5, kinds=(A.SHAPE_SPHERE,))
         sc = scenes.Scene(name, shapes, bodies, broadphase=A.BROAD_GRID, grid_n=(7, 9, 6), grid_min=(-4.0, -1.0, -4.0),
                           grid_max=(4.0, 6.0, 4.0))
+    elif name == "friction_reduction":
+        # Narrowphase.enableFrictionReduction: plane-hull and hull-hull pairs
+        # take one averaged friction pair per shape pair; materials put the
+        # friction of some pairs at zero
+        shapes, bodies = _mix(30, 20, spacing=0.95, side=4)
+        keep = _tetra_shapes(shapes, [4, 13], with_axes=True)
+        mats = np.zeros(2, dtype=A.MATERIAL_DTYPE)
+        mats[0] = (0.0, -1.0)
+        mats[1] = (0.5, -1.0)
+        bodies["material"][1:] = np.where(np.arange(30) % 7 == 0, 0, 1)
+        bodies["material"][0] = 1
+        sc = scenes.Scene(name, shapes, bodies, materials=mats, enable_friction_reduction=True)
     else:
         raise KeyError(name)
     sc._keep = keep

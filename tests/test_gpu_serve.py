@@ -130,3 +130,60 @@ def test_cancel_pending_and_active_requests():
     st = srv.stats()
     assert st["cancelled"] == 2 and st["completed"] == 2
     srv.close()
+
+
+def _dense_cluster(seed=99, n=300):
+    """300 spheres in a 1.2 m cube: far more pairs than a world of 301 bodies
+    starts with room for (4 * 301 + 64), so its lists must grow."""
+    sc = scenes.spheres_on_plane(n)
+    rng = scenes.SplitMix64(seed)
+    sc.bodies["position"][1:] = rng.uniform(3 * n).reshape(n, 3) * 1.2 + (-0.6, 0.6, -0.6)
+    return engine.setup_scene(sc)
+
+
+def test_a_world_that_cannot_grow_fails_alone(ctx):
+    """With max_list_entries below what a dense cluster needs, that request
+    fails with CP_ERR_CAPACITY; the requests stepped in the same ticks
+    complete and equal their plain results."""
+    reqs = _requests(10, seed=51, lo=16, hi=200, max_horizon=12)
+    bad = _dense_cluster()
+    srv = S.Server(hbm_budget=8e9, steps_per_tick=2, max_list_entries=2048)
+    tickets = [srv.submit(sc, sc.dt, r.horizon) for r, sc in reqs[:5]]
+    tb = srv.submit(bad, bad.dt, 6)
+    tickets += [srv.submit(sc, sc.dt, r.horizon) for r, sc in reqs[5:]]
+    assert srv.wait(tb, 120.0) == S.FAILED
+    for t, (r, sc) in zip(tickets, reqs):
+        assert srv.wait(t, 120.0) == S.DONE
+        out, inf = srv.result(t)
+        assert inf.stepnumber == r.horizon
+        assert _plain(ctx, sc, r.horizon).tobytes() == out.tobytes(), sc.name
+    st = srv.stats()
+    assert st["failed"] == 1 and st["completed"] == len(reqs)
+    srv.close()
+
+
+def test_served_requests_of_the_full_size_range_match_the_oracle():
+    """Requests drawn from the served workload's own distribution (16 to 4096
+    bodies in the 40/40/20 sphere/box/cylinder mix), including worlds above
+    the solve kernel's shared-memory group limit (640 bodies per 128 threads)
+    next to small ones, each checked against the oracle at its horizon."""
+    from oracle import oracle_py as O
+    reqs = scenes.serve_requests(rate=2000.0, window=1.0, seed=77)
+    big = [r for r in reqs if r.n_bodies > 2000][:2]
+    mid = [r for r in reqs if 640 < r.n_bodies <= 2000][:3]
+    small = [r for r in reqs if r.n_bodies <= 200][:6]
+    chosen = big + mid + small
+    assert len(big) == 2 and len(mid) == 3
+    built = []
+    for r in chosen:
+        r.horizon = min(r.horizon, 24)  # keeps the oracle's share of the test short
+        built.append((r, engine.setup_scene(scenes.request_world(r))))
+    srv = S.Server(hbm_budget=20e9, steps_per_tick=4)
+    tickets = [srv.submit(sc, sc.dt, r.horizon) for r, sc in built]
+    for t, (r, sc) in zip(tickets, built):
+        assert srv.wait(t, 600.0) == S.DONE
+        out, inf = srv.result(t)
+        ow = O.OracleWorld(O.setup_scene(scenes.request_world(r)))
+        ow.step(sc.dt, r.horizon)
+        assert out.tobytes() == ow.bodies().tobytes(), f"{sc.name} ({sc.num_bodies} bodies)"
+    srv.close()
