@@ -269,7 +269,14 @@ def np_dtype(struct_cls):
     return np.dtype({"names": names, "formats": formats, "offsets": offsets, "itemsize": C.sizeof(struct_cls)})
 
 
+class Event(C.Structure):
+    _fields_ = [("type", C.c_int32), ("a", C.c_int32), ("b", C.c_int32), ("contact", C.c_int32), ("stepnumber", C.c_int64)]
+
+
+EV_COLLIDE, EV_BEGIN_CONTACT, EV_END_CONTACT, EV_BEGIN_SHAPE_CONTACT, EV_END_SHAPE_CONTACT = 0, 1, 2, 3, 4
+
 SHAPE_DTYPE = np_dtype(ShapeDesc)
+EVENT_DTYPE = np_dtype(Event)
 BODY_DTYPE = np_dtype(BodyDesc)
 BODY_STATE_DTYPE = np_dtype(BodyState)
 MATERIAL_DTYPE = np_dtype(Material)

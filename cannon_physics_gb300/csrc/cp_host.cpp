@@ -1101,6 +1101,8 @@ int destroy_world(cp_ctx* c, int id) {
   return CP_OK;
 }
 
+
+
 int read_bodies(cp_ctx* c, int id, cp_body_desc* out) {
   WorldRec& w = c->worlds[id];
   if (w.nb == 0) return CP_OK;
@@ -1247,6 +1249,10 @@ int world_steps(cp_ctx* c, int id, double dt, int nsteps, double time_inc) {
 }
 
 }  // namespace
+
+namespace cpi {
+int world_step_plain(cp_ctx* c, int id, double dt, int nsteps) { return world_steps(c, id, dt, nsteps, dt); }
+}  // namespace cpi
 
 extern "C" {
 

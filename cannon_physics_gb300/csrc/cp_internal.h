@@ -147,6 +147,10 @@ int destroy_world(cp_ctx* c, int id);
 // its limit, a failed regrowth) is listed there and the others complete;
 // without it the first such world's error is returned.
 int step_worlds(cp_ctx* c, const int* ids, int n, double dt, int nsteps, bool use_graph, std::vector<int>* failed = nullptr);
+// World.step(dt) nsteps times on one world (cp_world_step without the
+// argument checks): the wide kernels for a world of at least wide_bodies
+// bodies, the one-block kernels otherwise; capacities grow as needed.
+int world_step_plain(cp_ctx* c, int id, double dt, int nsteps);
 int read_bodies(cp_ctx* c, int id, cp_body_desc* out);
 int read_info(cp_ctx* c, int id, cp_step_info* out);
 // Creates the context's memory pool (release threshold: never) if absent.

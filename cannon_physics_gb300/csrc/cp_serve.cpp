@@ -19,6 +19,15 @@
 // and new requests overlaps on the device.  A world's result does not depend
 // on which other worlds share its ticks: every world is stepped by the same
 // kernels on its own data, so results match stepping it alone bit for bit.
+//
+// Large worlds (at least `wide_bodies` bodies) do not join the ticks: each of
+// `wide_lanes` lane threads takes one at a time, on a context (a CUDA stream)
+// of its own, and steps it to its horizon through the wide kernels (the world
+// spread over the whole GPU), in chunks of a few steps so that a
+// cancellation takes effect.  The lanes' work overlaps with the ticks of the
+// small worlds on the device, so a small request never waits for the serial
+// solver levels of a large one in its tick, and the large ones take the
+// faster path.  Both classes share the HBM budget.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -78,9 +87,15 @@ struct cp_server {
   std::thread thread;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  bool stop = false;
+  std::atomic<bool> stop{false};
   std::deque<Request*> pending;
   std::vector<Request*> active;  // modified by the server thread only, under mu
+  // large worlds: queued for, and stepped by, the wide lanes
+  std::deque<Request*> pending_wide;
+  std::vector<cp_ctx*> lane_ctx;
+  std::vector<std::thread> lanes;
+  std::vector<Request*> lane_req;  // the request each lane is stepping, or null
+  int wide_bodies = 0;
   std::map<int64_t, std::unique_ptr<Request>> requests;
   int64_t next_ticket = 1;
   size_t bytes_in_use = 0, bytes_peak = 0;
@@ -118,6 +133,91 @@ struct cp_server {
     }
     active.clear();
     cv_done.notify_all();
+  }
+
+  bool is_wide(const Request* r) const { return wide_bodies > 0 && !lane_ctx.empty() && r->nb >= wide_bodies; }
+
+  // One wide lane: a large world at a time, stepped to its horizon on the
+  // lane's own context.
+  void run_lane(int lane) {
+    cp_ctx* c = lane_ctx[lane];
+    for (;;) {
+      Request* r = nullptr;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        for (;;) {
+          if (stop) return;
+          while (!pending_wide.empty() && pending_wide.front()->cancel) {
+            Request* q = pending_wide.front();
+            pending_wide.pop_front();
+            q->state = REQ_CANCELLED;
+            cancelled++;
+            cv_done.notify_all();
+          }
+          if (!pending_wide.empty() && bytes_in_use + pending_wide.front()->bytes <= (size_t)cfg.hbm_budget_bytes) break;
+          cv_work.wait(lk);
+        }
+        r = pending_wide.front();
+        pending_wide.pop_front();
+        bytes_in_use += r->bytes;
+        bytes_peak = std::max(bytes_peak, bytes_in_use);
+        active_bodies += r->nb;
+        lane_req[lane] = r;
+      }
+      int st;
+      int id = -1;
+      {
+        std::lock_guard<std::mutex> lc(c->mu);
+        cudaSetDevice(c->device);
+        DWorldParams* P = (DWorldParams*)&r->prep.host[r->prep.off.P];
+        P->step_limit = P->stepnumber + r->nsteps;
+        r->prep.w.step_limit = P->step_limit;
+        st = commit_world(c, r->prep, &id);
+      }
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!st) {
+          r->world = id;
+          r->state = REQ_ACTIVE;
+          r->t_admit = now_s();
+          r->remaining = r->nsteps;
+          admitted++;
+        }
+      }
+      std::string msg;
+      while (!st && r->remaining > 0 && !r->cancel && !stop) {
+        const int chunk = (int)std::min<long long>(r->remaining, 16);
+        std::lock_guard<std::mutex> lc(c->mu);
+        cudaSetDevice(c->device);
+        st = world_step_plain(c, id, r->dt, chunk);
+        if (!st) r->remaining -= chunk;
+      }
+      if (stop && !st && r->remaining > 0) {
+        std::lock_guard<std::mutex> lc(c->mu);
+        destroy_world(c, id);
+        return;
+      }
+      if (!st && !r->cancel) {
+        std::lock_guard<std::mutex> lc(c->mu);
+        r->result.resize(r->nb);
+        st = read_bodies(c, id, r->result.data());
+        if (!st) st = read_info(c, id, &r->info);
+      }
+      if (st) msg = last_error();
+      if (id >= 0) {
+        std::lock_guard<std::mutex> lc(c->mu);
+        destroy_world(c, id);
+      }
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        r->status = st;
+        r->error = msg;
+        lane_req[lane] = nullptr;
+        finish(r, r->cancel ? REQ_CANCELLED : (st ? REQ_FAILED : REQ_DONE));
+        cv_done.notify_all();
+      }
+      cv_work.notify_all();  // budget freed: a queued request may fit now
+    }
   }
 
   void run() {
@@ -293,7 +393,29 @@ int cp_serve_start(const cp_serve_config* cfg, cp_server** out) {
   s->ctx = ctx;
   s->cfg = *cfg;
   if (s->cfg.steps_per_tick == 0) s->cfg.steps_per_tick = 2;
+  const int nlanes = cfg->wide_lanes > 0 ? cfg->wide_lanes : (cfg->wide_lanes == 0 ? 4 : 0);
+  s->wide_bodies = cfg->wide_bodies > 0 ? cfg->wide_bodies : CP_WIDE_BODIES_DEFAULT;
+  for (int l = 0; l < nlanes; l++) {
+    cp_ctx* lc = nullptr;
+    st = cp_create(&cc, &lc);
+    if (!st) {
+      std::lock_guard<std::mutex> g(lc->mu);
+      st = enable_pool(lc);
+      lc->wide_bodies = s->wide_bodies;
+      lc->list_cap_limit = cfg->max_list_entries;
+    }
+    if (st) {
+      if (lc) cp_destroy(lc);
+      for (cp_ctx* x : s->lane_ctx) cp_destroy(x);
+      cp_destroy(ctx);
+      delete s;
+      return st;
+    }
+    s->lane_ctx.push_back(lc);
+  }
+  s->lane_req.assign(s->lane_ctx.size(), nullptr);
   s->thread = std::thread([s] { s->run(); });
+  for (int l = 0; l < (int)s->lane_ctx.size(); l++) s->lanes.emplace_back([s, l] { s->run_lane(l); });
   *out = s;
   return CP_OK;
 }
@@ -306,10 +428,13 @@ int cp_serve_stop(cp_server* s) {
   }
   s->cv_work.notify_all();
   if (s->thread.joinable()) s->thread.join();
+  for (auto& t : s->lanes)
+    if (t.joinable()) t.join();
   {
     std::lock_guard<std::mutex> lc(s->ctx->mu);
     for (Request* r : s->active) destroy_world(s->ctx, r->world);
   }
+  for (cp_ctx* x : s->lane_ctx) cp_destroy(x);
   cp_destroy(s->ctx);
   delete s;
   return CP_OK;
@@ -335,10 +460,10 @@ int cp_serve_submit(cp_server* s, const cp_world_desc* desc, double dt, int32_t 
     *ticket = r->ticket;
     s->submitted++;
     if (s->t_first < 0) s->t_first = r->t_submit;
-    s->pending.push_back(r.get());
+    (s->is_wide(r.get()) ? s->pending_wide : s->pending).push_back(r.get());
     s->requests[r->ticket] = std::move(r);
   }
-  s->cv_work.notify_one();
+  s->cv_work.notify_all();
   return CP_OK;
 }
 
@@ -398,14 +523,17 @@ int cp_serve_cancel(cp_server* s, int64_t ticket) {
     if (r->state >= REQ_DONE) return CP_OK;
     r->cancel = true;
     if (r->state == REQ_PENDING) {  // never admitted: drop it now
-      s->pending.erase(std::find(s->pending.begin(), s->pending.end(), r));
+      auto& q = s->is_wide(r) ? s->pending_wide : s->pending;
+      auto qi = std::find(q.begin(), q.end(), r);
+      if (qi == q.end()) return CP_OK;  // a lane has just taken it; it ends at its next chunk
+      q.erase(qi);
       r->state = REQ_CANCELLED;
       s->cancelled++;
       s->cv_done.notify_all();
       return CP_OK;
     }
   }
-  s->cv_work.notify_one();
+  s->cv_work.notify_all();
   return CP_OK;
 }
 
@@ -418,8 +546,9 @@ int cp_serve_get_stats(cp_server* s, cp_serve_stats* out, int32_t reset) {
   out->completed = s->completed;
   out->failed = s->failed;
   out->cancelled = s->cancelled;
-  out->pending = (int64_t)s->pending.size();
+  out->pending = (int64_t)(s->pending.size() + s->pending_wide.size());
   out->active = (int64_t)s->active.size();
+  for (Request* r : s->lane_req) out->active += r != nullptr;
   out->ticks = s->ticks;
   out->bytes_in_use = (int64_t)s->bytes_in_use;
   out->bytes_peak = (int64_t)s->bytes_peak;

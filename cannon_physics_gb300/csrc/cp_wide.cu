@@ -188,13 +188,50 @@ __global__ void k_w_sap_copy(const DWorld* dw) {
   WIDE_LOOP(p, S.P.nb) S.W.sap_order[p] = S.W.sap_tmp[p];
 }
 
+// SAPBroadphase.collisionPairs' scan from list position i (sap_broadphase.dart:
+// 149-165) by one warp, 32 list positions at a time: `continue` on a pair
+// the filter rejects, `break` at the first remaining pair whose bounds are
+// apart (the lowest such lane), a pair for every earlier lane that
+// intersects.  Counts the pairs, or writes them from pair_cnt[i] on.  A
+// plane (infinite bounds, it sorts first and pairs with every body) scans
+// the whole list 32 times faster than a thread alone would.
+DI int sap_scan_warp(const DWorld& W, const DWorldParams& P, int i, bool write) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int nb = P.nb, axis = P.sap_axis;
+  const int ai = W.sap_order[i];
+  const DBody& bi = W.bodies[ai];
+  const int out = write ? W.pair_cnt[i] : 0;
+  int count = 0;
+  for (int j0 = i + 1; j0 < nb; j0 += 32) {
+    const int j = j0 + lane;
+    const int aj = j < nb ? W.sap_order[j] : 0;
+    const DBody& bj = W.bodies[aj];
+    const bool np = j < nb && need_pair(bi, bj);
+    const bool brk = np && !check_bounds(bi, bj, axis);
+    const unsigned bm = __ballot_sync(FULL, brk);
+    const int first = bm ? __ffs(bm) - 1 : 32;
+    const bool hit = np && lane < first && intersection_test(P, bi, bj);
+    const unsigned hm = __ballot_sync(FULL, hit);
+    if (write && hit) {
+      const int o = out + count + __popc(hm & ((1u << lane) - 1u));
+      W.pair_a[o] = ai;
+      W.pair_b[o] = aj;
+    }
+    count += __popc(hm);
+    if (bm) break;
+  }
+  return count;
+}
+
 __global__ void k_w_sap_pairs(const DWorld* dw, int write) {
   __shared__ Smem S;
   if (!wide_enter(S, dw)) return;
   if (write && S.W.wide->n_cand_pairs > S.P.pairs_cap) return;
-  WIDE_LOOP(i, S.P.nb) {
-    const int c = sap_scan(S.W, S.P, i, write != 0);
-    if (!write) S.W.pair_cnt[i] = c;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < S.P.nb; i += nwarps) {
+    const int c = sap_scan_warp(S.W, S.P, i, write != 0);
+    if (!write && (threadIdx.x & 31) == 0) S.W.pair_cnt[i] = c;
   }
 }
 
@@ -502,11 +539,11 @@ __global__ void __launch_bounds__(1024) k_w_levels(const DWorld* dw, int last_ca
 // GSSolver sweeps (gs_solver.dart:122-155) of one world on one block.
 //
 // Thread t takes, in every sweep, the same rows: offset t of each level, or
-// with a level of at most half a block, one body's half of row t % half
-// (side 0: bi on threads [0, half), side 1: bj on [half, BT); the halves of
-// G*Wlambda meet in shared memory).  Its first row record of the next level
-// is loaded during the current one, so the level's path holds the binary64
-// arithmetic, the shared-memory vlambda / wlambda and one barrier.
+// with a level of at most half a block, one body's half of a row (side 0:
+// bi, side 1: bj, in neighbouring warps; the halves of G*Wlambda meet in
+// shared memory).  Its first row record of the next level is loaded during
+// the current one, so the level's path holds the binary64 arithmetic, the
+// shared-memory vlambda / wlambda and the barriers.
 
 // vlambda (x, y, z), wlambda (x, y, z) of body i at vel[6 i]; the solve
 // flag at flg[i]
@@ -537,7 +574,7 @@ DI bool wide_ok(DWide* x, int code, int idx, int bound) {
   return false;
 }
 
-#define WS_THREADS 512
+#define WS_THREADS 256  // 186 registers a thread, no spills
 #define WS_LEVELS_SMEM 4096  // level bounds kept in shared memory up to this many levels
 
 // dynamic shared memory: level bounds (WS_LEVELS_SMEM + 1 ints), then, when
@@ -567,13 +604,20 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve(const DWorld* dw, int
   __syncthreads();
   const int half = BT >> 1;
   const int cap = W.sw_cap;
+  // a level of at most `half` rows is split: the two sides of a row are in
+  // neighbouring warps (side = warp & 1), which the scheduler places on
+  // different sub-partitions, so their binary64 instructions issue in
+  // parallel; the partner of thread t is t ^ 32
+  const int split_side = (threadIdx.x >> 5) & 1;
+  const int split_off = (((int)threadIdx.x >> 6) << 5) | ((int)threadIdx.x & 31);
+  const int partner = threadIdx.x ^ 32;
   int iters = S.P.iterations;
   for (int sweep = 0; sweep < S.P.iterations; sweep++) {
     double acc = 0.0;
-    // this thread's first row of level 0, loaded ahead
+    // this thread's first row of level l
     auto first_row = [&](int l, int& p) {
       const int b = ls[l], cnt = ls[l + 1] - b;
-      const int off = cnt <= half ? (int)threadIdx.x % half : (int)threadIdx.x;
+      const int off = cnt <= half ? split_off : (int)threadIdx.x;
       p = off < cnt ? b + off : -1;
     };
     int pn;
@@ -601,8 +645,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve(const DWorld* dw, int
         }
       }
       if (cnt <= half) {
-        const int side = threadIdx.x >= half;
-        const int partner = side ? threadIdx.x - half : threadIdx.x + half;
+        const int side = split_side;
         const bool mine = pc >= 0 && wide_ok(x, 2, bbc.x, nb) && wide_ok(x, 2, bbc.y, nb);
         const int me = side ? bbc.y : bbc.x;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f), w = v;
@@ -790,9 +833,10 @@ static cudaError_t wide_step(const DWorld* dw, const DWorld& hw, const WideShape
     WIDE_LAUNCH(k_w_sap_key, gb, WT, 0, dw);
     WIDE_LAUNCH(k_w_sap_rank, gb, WT, 0, dw);
     WIDE_LAUNCH(k_w_sap_copy, gb, WT, 0, dw);
-    WIDE_LAUNCH(k_w_sap_pairs, gb, WT, 0, dw, 0);
+    const int gw = std::max(1, std::min(G, (nb * 32 + WT - 1) / WT));  // one warp per list position
+    WIDE_LAUNCH(k_w_sap_pairs, gw, WT, 0, dw, 0);
     WIDE_SCAN(hw.pair_cnt, &P->nb, &x->n_cand_pairs, &x->n_pairs, ws.pairs_cap, ST_PAIRS_OVERFLOW);
-    WIDE_LAUNCH(k_w_sap_pairs, gb, WT, 0, dw, 1);
+    WIDE_LAUNCH(k_w_sap_pairs, gw, WT, 0, dw, 1);
   } else if (ws.broadphase == CP_BROAD_GRID) {
     const int gbin = std::max(1, std::min(G, (ws.nbins + WT - 1) / WT));
     WIDE_LAUNCH(k_w_grid_zero, gbin, WT, 0, dw);

@@ -42,6 +42,8 @@ def lib():
         L.cp_world_step_interpolated.argtypes = [vp, i32, f64, f64, i32, vp]
         L.cp_world_set_time.argtypes = [vp, i32, f64, C.c_int64, f64]
         L.cp_world_get_states.argtypes = [vp, i32, vp, i32]
+        L.cp_world_set_events.argtypes = [vp, i32, i32, vp, vp]
+        L.cp_world_get_events.argtypes = [vp, i32, vp, i32, vp]
         L.cp_world_set_states.argtypes = [vp, i32, vp, i32]
         L.cp_world_get_bodies.argtypes = [vp, i32, vp, i32]
         L.cp_world_set_bodies.argtypes = [vp, i32, vp, i32]
@@ -223,6 +225,25 @@ class GpuWorld:
 
     def set_time(self, time, stepnumber, accumulator=0.0):
         check(lib().cp_world_set_time(self.ctx.h, self.id, time, stepnumber, accumulator), "set_time")
+
+    def set_events(self, on=True, body_ids=None, shape_ids=None):
+        """Record World's events (collide, begin/end contact, begin/end shape
+        contact) every step; ids: the Body.id / Shape.id values (default: the
+        indices)."""
+        self._ids = (None if body_ids is None else np.ascontiguousarray(body_ids, np.int32),
+                     None if shape_ids is None else np.ascontiguousarray(shape_ids, np.int32))
+        bi, si = self._ids
+        check(lib().cp_world_set_events(self.ctx.h, self.id, int(bool(on)), None if bi is None else bi.ctypes.data,
+                                        None if si is None else si.ctypes.data), "set_events")
+
+    def events(self):
+        """The recorded events since the last call, oldest first."""
+        cnt = C.c_int32()
+        if lib().cp_world_get_events(self.ctx.h, self.id, None, 0, C.byref(cnt)) == A.CP_OK:
+            return np.zeros(0, dtype=A.EVENT_DTYPE)
+        out = np.zeros(cnt.value, dtype=A.EVENT_DTYPE)
+        check(lib().cp_world_get_events(self.ctx.h, self.id, out.ctypes.data, len(out), C.byref(cnt)), "get_events")
+        return out[:cnt.value]
 
     def states(self):
         out = np.zeros(self.n, dtype=A.BODY_STATE_DTYPE)

@@ -26,6 +26,8 @@ class ServeConfig(C.Structure):
         ("variant", C.c_int32),
         ("group_bodies", C.c_int32),
         ("max_list_entries", C.c_int64),
+        ("wide_bodies", C.c_int32),
+        ("wide_lanes", C.c_int32),
     ]
 
 
@@ -61,10 +63,10 @@ class Server:
     bodies stepping at once (0: only the budget limits admission)."""
 
     def __init__(self, device=0, hbm_budget=150e9, steps_per_tick=2, max_active_bodies=0, variant=-1, group_bodies=0,
-                 max_list_entries=0):
+                 max_list_entries=0, wide_bodies=0, wide_lanes=0):
         L = _bind(lib())
         cfg = ServeConfig(device, steps_per_tick, int(hbm_budget), int(max_active_bodies), variant, group_bodies,
-                          int(max_list_entries))
+                          int(max_list_entries), int(wide_bodies), int(wide_lanes))
         h = C.c_void_p()
         check(L.cp_serve_start(C.byref(cfg), C.byref(h)), "cp_serve_start")
         self.h = h

@@ -31,6 +31,8 @@ def lib():
         L.orc_world_step_interpolated.argtypes = [vp, f64, f64, i32, vp]
         L.orc_world_set_time.argtypes = [vp, f64, C.c_int64, f64]
         L.orc_world_set_bodies.argtypes = [vp, vp, i32]
+        L.orc_world_set_events.argtypes = [vp, i32, vp, vp]
+        L.orc_world_get_events.argtypes = [vp, vp, i32, vp]
         L.orc_world_set_sap_order.argtypes = [vp, vp, i32]
         L.orc_world_get_bodies.argtypes = [vp, vp, i32]
         L.orc_world_get_pairs.argtypes = [vp, vp, vp, i32, vp]
@@ -91,6 +93,21 @@ class OracleWorld:
         out = np.zeros(self.n, dtype=A.BODY_DTYPE)
         _check(lib().orc_world_get_bodies(self.h, out.ctypes.data, self.n), "get bodies")
         return out
+
+    def set_events(self, on=True, body_ids=None, shape_ids=None):
+        self._ids = (None if body_ids is None else np.ascontiguousarray(body_ids, np.int32),
+                     None if shape_ids is None else np.ascontiguousarray(shape_ids, np.int32))
+        bi, si = self._ids
+        _check(lib().orc_world_set_events(self.h, int(bool(on)), None if bi is None else bi.ctypes.data,
+                                          None if si is None else si.ctypes.data), "set events")
+
+    def events(self):
+        cnt = C.c_int32()
+        if lib().orc_world_get_events(self.h, None, 0, C.byref(cnt)) == A.CP_OK:
+            return np.zeros(0, dtype=A.EVENT_DTYPE)
+        out = np.zeros(cnt.value, dtype=A.EVENT_DTYPE)
+        _check(lib().orc_world_get_events(self.h, out.ctypes.data, len(out), C.byref(cnt)), "events")
+        return out[:cnt.value]
 
     def set_bodies(self, bodies):
         bodies = np.ascontiguousarray(bodies, dtype=A.BODY_DTYPE)
