@@ -94,8 +94,13 @@ class BodyDesc(C.Structure):
         ("aabb_needs_update", C.c_int32),
         ("interpolated_position", f3),
         ("interpolated_quaternion", f4),
-        ("pad0", C.c_int32),
+        ("extra_shapes_first", C.c_int32),
+        ("extra_shapes_count", C.c_int32),
     ]
+
+
+class BodyShape(C.Structure):
+    _fields_ = [("shape", C.c_int32), ("offset", f3), ("orientation", f4)]
 
 
 class BodyState(C.Structure):
@@ -188,6 +193,9 @@ class WorldDesc(C.Structure):
         ("constraints", C.c_void_p),
         ("sap_axis_list", C.c_void_p),
         ("default_contact_material", ContactMaterial),
+        ("body_shapes", C.c_void_p),
+        ("num_body_shapes", C.c_int32),
+        ("pad0", C.c_int32),
     ]
 
 
@@ -279,6 +287,15 @@ SHAPE_DTYPE = np_dtype(ShapeDesc)
 EVENT_DTYPE = np_dtype(Event)
 BODY_DTYPE = np_dtype(BodyDesc)
 BODY_STATE_DTYPE = np_dtype(BodyState)
+BODY_SHAPE_DTYPE = np_dtype(BodyShape)
+
+
+def body_shapes(n):
+    """Extra-shape entries (Body.addShape beyond the first) with identity
+    orientations."""
+    t = np.zeros(n, dtype=BODY_SHAPE_DTYPE)
+    t["orientation"][:, 3] = 1.0
+    return t
 MATERIAL_DTYPE = np_dtype(Material)
 CONTACT_MATERIAL_DTYPE = np_dtype(ContactMaterial)
 CONSTRAINT_DTYPE = np_dtype(ConstraintDesc)

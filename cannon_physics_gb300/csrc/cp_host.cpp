@@ -234,6 +234,35 @@ double shape_bsr(const cp_shape_desc& d, const Hull* h) {
 }
 
 // Shape.calculateWorldAABB
+// dart:math min / max on doubles: NaN wins, and -0.0 is below 0.0
+double dart_min(double a, double b) {
+  if (a > b) return b;
+  if (a < b) return a;
+  if (std::isnan(a) || std::isnan(b)) return NAN;
+  return (std::signbit(a) || std::signbit(b)) ? -0.0 : a;
+}
+double dart_max(double a, double b) {
+  if (a < b) return b;
+  if (a > b) return a;
+  if (std::isnan(a) || std::isnan(b)) return NAN;
+  return (std::signbit(a) && std::signbit(b)) ? -0.0 : (a == 0 ? 0.0 : a);
+}
+
+// a body's extra shapes lie inside the table and name existing shapes, only
+// a body with a first shape has any, and a body has at most CP_MAX_BODY_SHAPES
+// shapes
+bool extras_valid(const cp_body_desc& d, int num_shapes, const cp_body_shape* table, int ntable) {
+  if (d.extra_shapes_count == 0) return true;
+  if (d.extra_shapes_count < 0 || d.extra_shapes_count >= CP_MAX_BODY_SHAPES || d.shape < 0 || !table || d.extra_shapes_first < 0 ||
+      (long long)d.extra_shapes_first + d.extra_shapes_count > ntable)
+    return false;
+  for (int k = 0; k < d.extra_shapes_count; k++) {
+    const int sh = table[d.extra_shapes_first + k].shape;
+    if (sh < 0 || sh >= num_shapes) return false;
+  }
+  return true;
+}
+
 void shape_aabb(const cp_shape_desc& d, const Hull* h, const h3& pos, const hq& q, h3& mn, h3& mx) {
   if (d.type == CP_SHAPE_SPHERE) {
     double r = d.radius;
@@ -305,14 +334,17 @@ int pow2_at_least(int v) {
 // and, when `base` is given, points the scratch arrays of `d` into it.
 size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   const int nb = w.nb, cc = w.contacts_cap, rc = w.rows_cap;
-  const int pc = std::max(w.pairs_cap, nb);  // SAP also keeps one count per list position in the pair arrays
+  const int pc0 = std::max(w.pairs_cap, nb);  // SAP also keeps one count per list position in the pair arrays
+  const int pc = std::max(pc0, w.jobs_cap);   // arrays indexed by narrowphase job
   const int cand_cap = 3 * cc + w.ncon_rows + 1;
-  const int hash_cap = w.broadphase == CP_BROAD_GRID ? pow2_at_least(2 * pc + 2) : 2;
+  const int hash_cap = w.broadphase == CP_BROAD_GRID ? pow2_at_least(2 * pc0 + 2) : 2;
   Layout L;
   size_t o_bscr = L.take(sizeof(DBodyScr) * (nb + 1));
   size_t o_tmp = L.take(sizeof(int) * (nb + 1));
-  size_t o_pa = L.take(sizeof(int) * (pc + 1));
-  size_t o_pb = L.take(sizeof(int) * (pc + 1));
+  size_t o_pa = L.take(sizeof(int) * (pc0 + 1));
+  size_t o_pb = L.take(sizeof(int) * (pc0 + 1));
+  size_t o_jp = L.take(sizeof(int) * (w.jobs_cap + 1));
+  size_t o_js = L.take(sizeof(int) * (w.jobs_cap + 1));
   size_t o_pc = L.take(sizeof(int) * (pc + 1));
   size_t o_pt = L.take(sizeof(int) * (pc + 1));
   size_t o_pf = L.take(sizeof(int) * (pc + 1));
@@ -350,6 +382,8 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   d.sap_tmp = (int*)(base + o_tmp);
   d.pair_a = (int*)(base + o_pa);
   d.pair_b = (int*)(base + o_pb);
+  d.job_pair = (int*)(base + o_jp);
+  d.job_sh = (int*)(base + o_js);
   d.pair_cnt = (int*)(base + o_pc);
   d.pair_tstart = (int*)(base + o_pt);
   d.pair_flag = (int*)(base + o_pf);
@@ -452,6 +486,8 @@ void body_to_device(const cp_body_desc& s, DBody& b) {
   b.group = s.collision_filter_group; b.mask = s.collision_filter_mask;
   b.material = s.material; b.shape = s.shape;
   b.brad32 = (float)s.bounding_radius;
+  b.xs0 = s.extra_shapes_first;
+  b.nxs = s.extra_shapes_count;
 }
 
 void body_from_device(const DBody& b, cp_body_desc& s) {
@@ -487,6 +523,8 @@ void body_from_device(const DBody& b, cp_body_desc& s) {
   s.aabb_needs_update = (b.flags & BF_AABB_DIRTY) != 0;
   s.collision_filter_group = b.group; s.collision_filter_mask = b.mask;
   s.material = b.material; s.shape = b.shape;
+  s.extra_shapes_first = b.xs0;
+  s.extra_shapes_count = b.nxs;
 }
 
 // Equation.setSpookParams (equation_class.dart:53-60)
@@ -537,7 +575,9 @@ int grow(cp_ctx* c, int id, int status) {
   if (status & ST_CONTACTS_OVERFLOW) w.contacts_cap *= 2;
   if (status & ST_ROWS_OVERFLOW) w.rows_cap *= 2;
   if (status & ST_BINS_OVERFLOW) w.bins_cap *= 2;
-  if (w.pairs_cap > (1 << 28) || w.contacts_cap > (1 << 28) || w.rows_cap > (1 << 28)) return fail(CP_ERR_CAPACITY, "capacity limit");
+  if (status & ST_JOBS_OVERFLOW) w.jobs_cap *= 2;
+  if (w.pairs_cap > (1 << 28) || w.contacts_cap > (1 << 28) || w.rows_cap > (1 << 28) || w.jobs_cap > (1 << 28))
+    return fail(CP_ERR_CAPACITY, "capacity limit");
   const long long lim = c->list_cap_limit;
   if (lim > 0 && (w.pairs_cap > lim || w.contacts_cap > lim || w.rows_cap > lim || w.bins_cap > lim))
     return fail(CP_ERR_CAPACITY, "world %d: its pair, contact or row list would grow beyond %lld entries", id, lim);
@@ -551,6 +591,7 @@ int grow(cp_ctx* c, int id, int status) {
   p.contacts_cap = w.contacts_cap;
   p.rows_cap = w.rows_cap;
   p.bins_cap = w.bins_cap;
+  p.jobs_cap = w.jobs_cap;
   CUDA_TRY(cudaMemcpy(w.dw.P, &p, sizeof(p), cudaMemcpyHostToDevice));
   return upload_world_entry(c, id);
 }
@@ -596,6 +637,8 @@ WideShape wide_shape(const WorldRec& w) {
   s.rows_cap = w.rows_cap;
   s.bins_cap = w.bins_cap;
   s.smem_vel = w.nb <= cpk_wide_smem_vel_max();
+  s.compound = w.compound;
+  s.jobs_cap = w.jobs_cap;
   return s;
 }
 
@@ -665,13 +708,18 @@ int cp_shape_setup(cp_shape_desc* s) {
   return CP_OK;
 }
 
-int cp_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc* bodies, int32_t num_bodies) {
-  if ((!bodies && num_bodies > 0) || num_bodies < 0 || num_shapes < 0 || (num_shapes > 0 && !shapes)) return fail(CP_ERR_ARG, "bad arguments");
+int cp_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, const cp_body_shape* body_shapes, int32_t num_body_shapes,
+                  cp_body_desc* bodies, int32_t num_bodies) {
+  if ((!bodies && num_bodies > 0) || num_bodies < 0 || num_shapes < 0 || (num_shapes > 0 && !shapes) || num_body_shapes < 0)
+    return fail(CP_ERR_ARG, "bad arguments");
   std::vector<Hull> hulls(num_shapes);
   std::vector<char> has_hull(num_shapes, 0);
   for (int k = 0; k < num_bodies; k++) {
     cp_body_desc& b = bodies[k];
     if (b.shape >= num_shapes) return fail(CP_ERR_ARG, "body %d: shape %d out of range", k, b.shape);
+    if (!extras_valid(b, num_shapes, body_shapes, num_body_shapes))
+      return fail(CP_ERR_ARG, "body %d: extra shapes [%d, %d) outside the table of %d, or naming a missing shape", k,
+                  b.extra_shapes_first, b.extra_shapes_first + b.extra_shapes_count, num_body_shapes);
     std::memcpy(b.previous_position, b.position, 12);
     std::memcpy(b.previous_quaternion, b.quaternion, 16);
     std::memcpy(b.interpolated_position, b.position, 12);
@@ -681,25 +729,42 @@ int cp_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc*
     h3 he = mk3(0, 0, 0);
     hq q; q.x = b.quaternion[0]; q.y = b.quaternion[1]; q.z = b.quaternion[2]; q.w = b.quaternion[3];
     h3 mn = mk3(0, 0, 0), mx = mk3(0, 0, 0);
-    b.bounding_radius = 0;
-    if (b.shape >= 0) {
-      const cp_shape_desc& sd = shapes[b.shape];
-      if (sd.type != CP_SHAPE_SPHERE && sd.type != CP_SHAPE_PLANE && !has_hull[b.shape]) {
-        int st = build_hull(sd, hulls[b.shape]);
+    // addShape for each shape in Body.shapes order; the last
+    // updateMassProperties (AABB of all shapes, the first copied and the
+    // others extended in, rigid_body.dart:415-447) and updateBoundingRadius
+    // see them all
+    const int nsh = b.shape >= 0 ? 1 + b.extra_shapes_count : 0;
+    double radius = 0;
+    for (int sl = 0; sl < nsh; sl++) {
+      const int si = sl == 0 ? b.shape : body_shapes[b.extra_shapes_first + sl - 1].shape;
+      const float* offp = sl == 0 ? b.shape_offset : body_shapes[b.extra_shapes_first + sl - 1].offset;
+      const float* orp = sl == 0 ? b.shape_orientation : body_shapes[b.extra_shapes_first + sl - 1].orientation;
+      const cp_shape_desc& sd = shapes[si];
+      if (sd.type != CP_SHAPE_SPHERE && sd.type != CP_SHAPE_PLANE && !has_hull[si]) {
+        int st = build_hull(sd, hulls[si]);
         if (st) return st;
-        has_hull[b.shape] = 1;
+        has_hull[si] = 1;
       }
-      h3 off = mk3(b.shape_offset[0], b.shape_offset[1], b.shape_offset[2]);
+      h3 off = mk3(offp[0], offp[1], offp[2]);
       h3 pos = mk3(b.position[0], b.position[1], b.position[2]);
-      hq so; so.x = b.shape_orientation[0]; so.y = b.shape_orientation[1]; so.z = b.shape_orientation[2]; so.w = b.shape_orientation[3];
+      hq so; so.x = orp[0]; so.y = orp[1]; so.z = orp[2]; so.w = orp[3];
       h3 wpos = add3(qrot(q, off), pos);
       hq wq = qmul(q, so);
-      shape_aabb(sd, &hulls[b.shape], wpos, wq, mn, mx);
-      he = mk3(((double)mx.x - mn.x) / 2, ((double)mx.y - mn.y) / 2, ((double)mx.z - mn.z) / 2);
-      double r = shape_bsr(sd, &hulls[b.shape]);
+      h3 smn, smx;
+      shape_aabb(sd, &hulls[si], wpos, wq, smn, smx);
+      if (sl == 0) {
+        mn = smn;
+        mx = smx;
+      } else {  // AABB.extend (aabb.dart:121-128)
+        mn = mk3(dart_min(mn.x, smn.x), dart_min(mn.y, smn.y), dart_min(mn.z, smn.z));
+        mx = mk3(dart_max(mx.x, smx.x), dart_max(mx.y, smx.y), dart_max(mx.z, smx.z));
+      }
+      double r = shape_bsr(sd, &hulls[si]);
       double o = len3(off);
-      if (o + r > 0) b.bounding_radius = o + r;
+      if (o + r > radius) radius = o + r;
     }
+    if (nsh) he = mk3(((double)mx.x - mn.x) / 2, ((double)mx.y - mn.y) / 2, ((double)mx.z - mn.z) / 2);
+    b.bounding_radius = radius;
     b.aabb_lower[0] = mn.x; b.aabb_lower[1] = mn.y; b.aabb_lower[2] = mn.z;
     b.aabb_upper[0] = mx.x; b.aabb_upper[1] = mx.y; b.aabb_upper[2] = mx.z;
     // Box.calculateInertia (box.dart:88-94)
@@ -798,7 +863,10 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
     if (b.shape < -1 || b.shape >= ns) return fail(CP_ERR_ARG, "body %d: shape %d out of range", i, b.shape);
     if (b.material < -1 || b.material >= nm) return fail(CP_ERR_ARG, "body %d: material out of range", i);
     if (b.type < 0 || b.type > 2) return fail(CP_ERR_ARG, "body %d: type %d (run cp_body_setup first)", i, b.type);
+    if (!extras_valid(b, ns, d->body_shapes, d->num_body_shapes))
+      return fail(CP_ERR_ARG, "body %d: extra shapes outside the body_shapes table or naming a missing shape", i);
   }
+  if (d->num_body_shapes < 0 || (d->num_body_shapes > 0 && !d->body_shapes)) return fail(CP_ERR_ARG, "bad body_shapes table");
   // shapes and hulls
   std::vector<DShape> shapes(ns);
   std::vector<DHull> hulls;
@@ -947,12 +1015,22 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
   WorldRec w;
   w.nb = nb; w.nshapes = ns; w.nmat = nm; w.ncm = (int)cms.size(); w.ncons = d->num_constraints; w.ncon_rows = con_rows;
   w.broadphase = d->broadphase;
-  w.lin_damp.resize(nb); w.ang_damp.resize(nb); w.body_shape.resize(nb);
+  w.lin_damp.resize(nb); w.ang_damp.resize(nb); w.body_shape.resize(nb); w.body_xs0.resize(nb);
   for (int i = 0; i < nb; i++) {
     body_to_device(d->bodies[i], bodies[i]);
     w.lin_damp[i] = d->bodies[i].linear_damping;
     w.ang_damp[i] = d->bodies[i].angular_damping;
     w.body_shape[i] = d->bodies[i].shape;
+    w.body_xs0[i] = d->bodies[i].extra_shapes_first;
+    w.compound = w.compound || d->bodies[i].extra_shapes_count > 0;
+  }
+  w.body_shapes.assign(d->body_shapes, d->body_shapes ? d->body_shapes + d->num_body_shapes : d->body_shapes);
+  std::vector<DBodyShape> bshapes(w.body_shapes.size());
+  for (size_t k = 0; k < bshapes.size(); k++) {
+    std::memset(&bshapes[k], 0, sizeof(DBodyShape));
+    bshapes[k].shape = w.body_shapes[k].shape;
+    std::memcpy(bshapes[k].off, w.body_shapes[k].offset, 12);
+    std::memcpy(bshapes[k].quat, w.body_shapes[k].orientation, 16);
   }
   w.cms = cms;
   // params
@@ -986,7 +1064,10 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
   w.contacts_cap = 2 * w.pairs_cap + 64;
   w.rows_cap = 3 * w.contacts_cap + con_rows + 64;
   w.bins_cap = 4 * nb + (d->broadphase == CP_BROAD_GRID ? w.nbins : 0) + 64;
+  w.jobs_cap = w.compound ? 4 * w.pairs_cap : 0;
   P.pairs_cap = w.pairs_cap; P.contacts_cap = w.contacts_cap; P.rows_cap = w.rows_cap; P.bins_cap = w.bins_cap;
+  P.compound = w.compound;
+  P.jobs_cap = w.jobs_cap;
   // state allocation
   Layout L;
   size_t o_P = L.take(sizeof(DWorldParams));
@@ -1008,6 +1089,7 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
   size_t o_nc = L.take(sizeof(int) * (nocollide.size() + 2));
   size_t o_dp = L.take(sizeof(double) * (2 * nb + 2));
   size_t o_so = L.take(sizeof(int) * (nb + 1));
+  size_t o_bsh = L.take(sizeof(DBodyShape) * (bshapes.size() + 1));
   std::vector<char> host(L.off, 0);
   std::memcpy(&host[o_P], &P, sizeof(P));
   if (nb) std::memcpy(&host[o_b], bodies.data(), sizeof(DBody) * nb);
@@ -1032,10 +1114,11 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
     if (order[i] < 0 || order[i] >= nb) return fail(CP_ERR_ARG, "sap_axis_list[%d] out of range", i);
   }
   if (nb) std::memcpy(&host[o_so], order.data(), sizeof(int) * nb);
+  if (!bshapes.empty()) std::memcpy(&host[o_bsh], bshapes.data(), sizeof(DBodyShape) * bshapes.size());
   w.state_bytes = L.off;
   w.scratch_bytes = scratch_layout(w, nullptr);
   out.off = StateOffsets{o_P, o_b, o_s, o_h, o_f, o_hv, o_he, o_hfi, o_hvd, o_hed, o_hcn, o_hc,
-                         o_m, o_ct, o_cm, o_cn, o_nc, o_dp, o_so};
+                         o_m, o_ct, o_cm, o_cn, o_nc, o_dp, o_so, o_bsh};
   out.w = std::move(w);
   out.host = std::move(host);
   return CP_OK;
@@ -1076,6 +1159,7 @@ int commit_world(cp_ctx* c, PreparedWorld& p, int* world_id) {
   dw.nocollide = (int*)(base + o.nocollide);
   dw.dpow = (double*)(base + o.dpow);
   dw.sap_order = (int*)(base + o.sap_order);
+  dw.bshapes = (DBodyShape*)(base + o.bshapes);
   st = alloc_scratch(c, w);
   if (st) { dev_free(c, w.state, w.pooled); w.state = nullptr; return st; }
   w.live = true;
@@ -1189,13 +1273,18 @@ int collect_events(cp_ctx* c, int id) {
   int st = read_params(c, w, p);
   if (st) return st;
   std::vector<DContact> ct(p.num_contacts);
-  std::vector<int> pa(p.num_pairs), pb(p.num_pairs), pf(p.num_pairs);
+  std::vector<int> pa(p.num_pairs), pb(p.num_pairs), pf(p.num_jobs);
+  std::vector<int> jp(w.compound ? p.num_jobs : 0), js(jp.size());
   if (p.num_contacts)
     CUDA_TRY(cudaMemcpyAsync(ct.data(), w.dw.contacts, sizeof(DContact) * ct.size(), cudaMemcpyDeviceToHost, c->stream));
   if (p.num_pairs) {
     CUDA_TRY(cudaMemcpyAsync(pa.data(), w.dw.pair_a, sizeof(int) * pa.size(), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(cudaMemcpyAsync(pb.data(), w.dw.pair_b, sizeof(int) * pb.size(), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(cudaMemcpyAsync(pf.data(), w.dw.pair_flag, sizeof(int) * pf.size(), cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (p.num_jobs) CUDA_TRY(cudaMemcpyAsync(pf.data(), w.dw.pair_flag, sizeof(int) * pf.size(), cudaMemcpyDeviceToHost, c->stream));
+  if (!jp.empty()) {
+    CUDA_TRY(cudaMemcpyAsync(jp.data(), w.dw.job_pair, sizeof(int) * jp.size(), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(js.data(), w.dw.job_sh, sizeof(int) * js.size(), cudaMemcpyDeviceToHost, c->stream));
   }
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   const auto bid = [&](int i) { return w.body_ids.empty() ? i : w.body_ids[i]; };
@@ -1206,10 +1295,16 @@ int collect_events(cp_ctx* c, int id) {
     bk.push_back(overlap_key(bid(ct[k].bi), bid(ct[k].bj)));
     sk.push_back(overlap_key(sid(ct[k].si), sid(ct[k].sj)));
   }
+  // shape `slot` of body i (slot 0: its first shape)
+  const auto slot_shape = [&](int i, int slot) {
+    return slot == 0 ? w.body_shape[i] : w.body_shapes[w.body_xs0[i] + slot - 1].shape;
+  };
   for (size_t k = 0; k < pf.size(); k++)
-    if (pf[k]) {  // a justTest pair whose shapes overlap
-      bk.push_back(overlap_key(bid(pa[k]), bid(pb[k])));
-      sk.push_back(overlap_key(sid(w.body_shape[pa[k]]), sid(w.body_shape[pb[k]])));
+    if (pf[k]) {  // a justTest job whose shapes overlap
+      const int q = w.compound ? jp[k] : (int)k;
+      const int sa = w.compound ? js[k] >> 16 : 0, sb = w.compound ? js[k] & 0xffff : 0;
+      bk.push_back(overlap_key(bid(pa[q]), bid(pb[q])));
+      sk.push_back(overlap_key(sid(slot_shape(pa[q], sa)), sid(slot_shape(pb[q], sb))));
     }
   // the index whose id is `v` (ids are unique)
   const auto index_of = [](const std::vector<int>& ids, unsigned v) {
@@ -1455,6 +1550,7 @@ int cp_world_step_static(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
     static_assert(offsetof(DWorldParams, num_levels) == offsetof(DWorldParams, num_pairs) + 3 * sizeof(int), "layout");
     CUDA_TRY(cudaMemsetAsync(&w.dw.P->status, 0, sizeof(int), c->stream));
     CUDA_TRY(cudaMemsetAsync(&w.dw.P->num_pairs, 0, 4 * sizeof(int), c->stream));
+    CUDA_TRY(cudaMemsetAsync(&w.dw.P->num_jobs, 0, sizeof(int), c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     return fail(CP_ERR_CAPACITY, "world %d: step %lld overflowed a capacity (status %d); the world is left before that step",
                 id, p.stepnumber + 1, p.status);
@@ -1470,6 +1566,10 @@ int cp_world_step_static(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
     }
     if (p.num_contacts > 0)
       CUDA_TRY(cudaMemcpyAsync(w.dw.contacts, dw.contacts, sizeof(DContact) * p.num_contacts, cudaMemcpyDeviceToDevice, c->stream));
+    if (w.compound && p.num_jobs > 0) {  // contacts name their job; the job list maps them to pairs
+      CUDA_TRY(cudaMemcpyAsync(w.dw.job_pair, dw.job_pair, sizeof(int) * p.num_jobs, cudaMemcpyDeviceToDevice, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(w.dw.job_sh, dw.job_sh, sizeof(int) * p.num_jobs, cudaMemcpyDeviceToDevice, c->stream));
+    }
     if (p.num_rows > 0)
       CUDA_TRY(cudaMemcpyAsync(w.dw.rows, dw.rows, sizeof(DRow) * p.num_rows, cudaMemcpyDeviceToDevice, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1496,10 +1596,15 @@ int cp_world_set_bodies(cp_ctx* c, int32_t id, const cp_body_desc* in, int32_t n
   std::vector<DBody> b(w.nb);
   for (int i = 0; i < w.nb; i++) {
     if (in[i].shape < -1 || in[i].shape >= w.nshapes) return fail(CP_ERR_ARG, "body %d: shape out of range", i);
+    if (!extras_valid(in[i], w.nshapes, w.body_shapes.data(), (int)w.body_shapes.size()))
+      return fail(CP_ERR_ARG, "body %d: extra shapes outside the world's body_shapes table", i);
+    if (in[i].extra_shapes_count > 0 && !w.compound)
+      return fail(CP_ERR_ARG, "body %d: a world created without compound bodies cannot take one (create it again)", i);
     body_to_device(in[i], b[i]);
     w.lin_damp[i] = in[i].linear_damping;
     w.ang_damp[i] = in[i].angular_damping;
     w.body_shape[i] = in[i].shape;
+    w.body_xs0[i] = in[i].extra_shapes_first;
   }
   CUDA_TRY(cudaMemcpyAsync(w.dw.bodies, b.data(), sizeof(DBody) * w.nb, cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1601,11 +1706,16 @@ int cp_world_get_contacts(cp_ctx* c, int32_t id, cp_contact* out, int32_t cap, i
   if (p.num_contacts > cap || (p.num_contacts && !out)) return fail(CP_ERR_CAPACITY, "need room for %d contacts", p.num_contacts);
   std::vector<DContact> v(p.num_contacts);
   if (p.num_contacts) CUDA_TRY(cudaMemcpy(v.data(), w.dw.contacts, sizeof(DContact) * v.size(), cudaMemcpyDeviceToHost));
+  // a contact records its narrowphase job; in a compound world the job's
+  // broadphase pair is job_pair[job]
+  std::vector<int> jp(w.compound ? p.num_jobs : 0);
+  if (!jp.empty()) CUDA_TRY(cudaMemcpy(jp.data(), w.dw.job_pair, sizeof(int) * jp.size(), cudaMemcpyDeviceToHost));
   for (int i = 0; i < p.num_contacts; i++) {
     cp_contact& o = out[i];
     o.bi = v[i].bi; o.bj = v[i].bj; o.si = v[i].si; o.sj = v[i].sj;
     std::memcpy(o.ni, v[i].ni, 12); std::memcpy(o.ri, v[i].ri, 12); std::memcpy(o.rj, v[i].rj, 12);
-    o.enabled = v[i].enabled; o.pair = v[i].pair; o.restitution = v[i].restitution;
+    o.enabled = v[i].enabled; o.restitution = v[i].restitution;
+    o.pair = w.compound ? jp[v[i].pair] : v[i].pair;
   }
   return CP_OK;
 }

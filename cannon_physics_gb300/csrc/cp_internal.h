@@ -38,12 +38,16 @@ struct WorldRec {
   int n_nocollide = 0;
   int broadphase = 0, nbins = 0;
   int pairs_cap = 0, contacts_cap = 0, rows_cap = 0, bins_cap = 0;
+  int jobs_cap = 0;   // shape-pair jobs (compound worlds only)
+  bool compound = false;
+  std::vector<cp_body_shape> body_shapes;  // the world's extra-shape table
   long long step_limit = LLONG_MAX;  // the kernels leave the world alone at this step number
   double dt_cached = -1.0;
   double accumulator = 0.0;  // World.accumulator of the interpolating World.step
   int last_substeps = 0;     // internal steps of the last interpolating step
   std::vector<double> lin_damp, ang_damp;
   std::vector<int> body_shape;  // each body's shape index (justTest overlaps of the event feed)
+  std::vector<int> body_xs0;    // each body's first entry in body_shapes (its extra shapes)
   // event feed
   bool events = false;
   std::vector<int> body_ids, shape_ids;                // the ids overlap keys sort by
@@ -55,7 +59,7 @@ struct WorldRec {
 // Offsets of the state sub-arrays inside a world's state allocation.
 struct StateOffsets {
   size_t P, bodies, shapes, hulls, faces, hverts, hedges, hfi, hvd, hed, hcanon, hconn;
-  size_t mats, cm_table, cms, cons, nocollide, dpow, sap_order;
+  size_t mats, cm_table, cms, cons, nocollide, dpow, sap_order, bshapes;
 };
 
 // A world checked and laid out on the host, ready to be copied to the device:

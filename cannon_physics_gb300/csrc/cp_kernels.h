@@ -52,6 +52,7 @@ struct WideShape {
   int nb, nbins, broadphase, n_nocollide;
   int pairs_cap, contacts_cap, rows_cap, bins_cap;
   int smem_vel;  // the sweeps keep vlambda / wlambda in shared memory
+  int compound, jobs_cap;  // shape-pair jobs of compound bodies, their capacity
 };
 int cpk_wide_smem_vel_max();
 // nsteps steps of the world whose device descriptor is dw (hw: its host

@@ -40,7 +40,7 @@ struct __align__(16) Smem {
   int rprof;  // g_res_profile at kernel start
   int n_pairs, n_contacts, n_queued, n_rows;
   int n_fric, n_cand, n_levels, cursor;
-  int overflow, converged, wi, pad;
+  int overflow, converged, wi, n_jobs;  // n_jobs: narrowphase jobs (shape pairs)
   int kcnt[16], kpos[16];  // narrowphase: heavy pairs per resolver kind, segment cursors
   int cursor2, pad2[3];
   // where the narrowphase's contact cursor and overflow flag live: this
@@ -174,6 +174,21 @@ DI void shape_world_aabb(const DWorld& W, const DShape& s, f3 pos, q4 q, f3& mn,
 
 // shape world transform of body i and, where the broadphase reads it, its
 // world AABB
+// dart:math min / max of two doubles, here of binary32 values: a NaN
+// operand wins, and -0.0 is below 0.0
+DI float dart_min(float a, float b) {
+  if (a > b) return b;
+  if (a < b) return a;
+  if (a != a || b != b) return __int_as_float(0x7fc00000);
+  return (signbit(a) || signbit(b)) ? -0.0f : a;
+}
+DI float dart_max(float a, float b) {
+  if (a < b) return b;
+  if (a > b) return a;
+  if (a != a || b != b) return __int_as_float(0x7fc00000);
+  return (signbit(a) && signbit(b)) ? -0.0f : (a == 0.0f ? 0.0f : a);
+}
+
 DI void prepare_body(const DWorld& W, const DWorldParams& P, int i) {
   const int bp = P.broadphase;
   const bool aabb_all = bp == CP_BROAD_SAP || (bp == CP_BROAD_NAIVE && P.use_bb);
@@ -190,6 +205,15 @@ DI void prepare_body(const DWorld& W, const DWorldParams& P, int i) {
     if (aabb_all || (aabb_grid && s.type != CP_SHAPE_SPHERE && s.type != CP_SHAPE_PLANE)) {
       f3 mn, mx;
       shape_world_aabb(W, s, xs, qs, mn, mx);
+      // a compound body's AABB extends over each further shape's
+      // (rigid_body.dart:415-447, AABB.extend in aabb.dart:121-128)
+      for (int e = 0; e < B.nxs; e++) {
+        const DBodyShape& X = W.bshapes[B.xs0 + e];
+        f3 lo, hi;
+        shape_world_aabb(W, W.shapes[X.shape], add(vmult(q, ld3(X.off)), p), qmul(q, ld4q(X.quat)), lo, hi);
+        mn = f3{dart_min(mn.x, lo.x), dart_min(mn.y, lo.y), dart_min(mn.z, lo.z)};
+        mx = f3{dart_max(mx.x, hi.x), dart_max(mx.y, hi.y), dart_max(mx.z, hi.z)};
+      }
       st3(B.aabb_lo, mn);
       st3(B.aabb_hi, mx);
       B.flags &= ~BF_AABB_DIRTY;
@@ -683,9 +707,42 @@ DI void just_test_overlap(Smem& S, int k, int rk, PairJob& X);
 // pair, no resolver for the shape types, the collision filter, the bounding
 // spheres, or a binary32 no-contact certificate).  With tests == false the
 // pair is known to have passed them and only the job is filled.
-DI int pair_job(Smem& S, int k, PairJob& X, bool tests) {
+// Narrowphase job `job` of a world: its broadphase pair k and the shape
+// slots of the pair's two bodies (slot 0: a body's first shape); in a world
+// without compound bodies the job is pair k with both first shapes.
+DI void job_slots(const DWorld& W, const DWorldParams& P, int job, int& k, int& sa, int& sb) {
+  if (!P.compound) {
+    k = job; sa = 0; sb = 0;
+    return;
+  }
+  k = W.job_pair[job];
+  const int sh = W.job_sh[job];
+  sa = sh >> 16;
+  sb = sh & 0xffff;
+}
+
+// Shape `slot` of body i: its index and world pose (getContacts,
+// narrow_phase.dart:671-680; slot 0's pose is the one prepare stored)
+DI void slot_pose(const DWorld& W, int i, int slot, int& shape, f3& xs, q4& qs) {
+  const DBody& B = W.bodies[i];
+  if (slot == 0) {
+    shape = B.shape;
+    xs = ld3(W.bscr[i].xs);
+    qs = ld4q(W.bscr[i].qs);
+    return;
+  }
+  const DBodyShape& e = W.bshapes[B.xs0 + slot - 1];
+  const q4 q = ld4q(B.quat);
+  shape = e.shape;
+  xs = add(vmult(q, ld3(e.off)), ld3(B.pos));
+  qs = qmul(q, ld4q(e.quat));
+}
+
+DI int pair_job(Smem& S, int job, PairJob& X, bool tests) {
   const DWorld& W = S.W;
   const DWorldParams& P = S.P;
+  int k, sa, sb;
+  job_slots(W, P, job, k, sa, sb);
   const int i = W.pair_a[k], j = W.pair_b[k];
   const DBody& bi = W.bodies[i];
   const DBody& bj = W.bodies[j];
@@ -694,27 +751,34 @@ DI int pair_job(Smem& S, int k, PairJob& X, bool tests) {
     just_test = (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_STATIC) ||
                 (bi.type == CP_BODY_STATIC && bj.type == CP_BODY_KINEMATIC) ||
                 (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_KINEMATIC);
-    if (P.events) W.pair_flag[k] = 0;
+    if (P.events) W.pair_flag[job] = 0;
     // a justTest pair only registers an overlap for the event feed
     if (bi.shape < 0 || bj.shape < 0 || (just_test && !P.events)) return RK_NONE;
   }
-  const DShape& si = W.shapes[bi.shape];
-  const DShape& sj = W.shapes[bj.shape];
+  int shi, shj;
+  f3 xi, xj;
+  q4 qi, qj;
+  slot_pose(W, i, sa, shi, xi, qi);
+  slot_pose(W, j, sb, shj, xj, qj);
+  const DShape& si = W.shapes[shi];
+  const DShape& sj = W.shapes[shj];
   const bool swap = !(si.type < sj.type);
   const int rk = swap ? resolver_kind(sj.type, si.type) : resolver_kind(si.type, sj.type);
   if (tests && rk == RK_NONE) return RK_NONE;
   if (tests && !((si.mask & sj.group) != 0 && (sj.mask & si.group) != 0)) return RK_NONE;
-  const f3 xi = ld3(W.bscr[i].xs), xj = ld3(W.bscr[j].xs);
   if (tests && distance_to(xi, xj) > si.bsr + sj.bsr) return RK_NONE;
-  const q4 qi = ld4q(W.bscr[i].qs), qj = ld4q(W.bscr[j].qs);
   X.xA = swap ? xj : xi;
   X.xB = swap ? xi : xj;
   X.qA = swap ? qj : qi;
   X.qB = swap ? qi : qj;
-  X.shA = swap ? bj.shape : bi.shape;
-  X.shB = swap ? bi.shape : bj.shape;
+  X.shA = swap ? shj : shi;
+  X.shB = swap ? shi : shj;
+  X.rsi = shi;
+  X.rsj = shj;
+  X.bA = swap ? j : i;
+  X.bB = swap ? i : j;
   if (tests && just_test) {
-    just_test_overlap(S, k, rk, X);
+    just_test_overlap(S, job, rk, X);
     return RK_NONE;
   }
   if (tests) {
@@ -727,18 +791,14 @@ DI int pair_job(Smem& S, int k, PairJob& X, bool tests) {
         atomicAdd(&S.r_cyc[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], (unsigned long long)(clock64() - t_res));
         atomicAdd(&S.r_cnt[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], 1u);
       }
-      if (*(volatile int*)&g_filter_check) certificate_check(S, k, rk, X);
+      if (*(volatile int*)&g_filter_check) certificate_check(S, job, rk, X);
       return RK_NONE;
     }
   }
   int cm = contact_material(W, P, si.material, sj.material);
   if (cm < 0) cm = contact_material(W, P, bi.material, bj.material);
   if (cm < 0) cm = 0;
-  X.C.W = &W; X.C.cursor = S.cursor_p; X.C.cap = P.contacts_cap; X.C.overflow = S.overflow_p; X.C.cm = cm; X.C.pair = k;
-  X.rsi = bi.shape;
-  X.rsj = bj.shape;
-  X.bA = swap ? j : i;
-  X.bB = swap ? i : j;
+  X.C.W = &W; X.C.cursor = S.cursor_p; X.C.cap = P.contacts_cap; X.C.overflow = S.overflow_p; X.C.cm = cm; X.C.pair = job;
   X.U1 = __int_as_float(0x7fc00000);
   return rk;
 }
@@ -749,14 +809,7 @@ DI int run_resolver(Smem& S, int rk, const PairJob& X, int& start, bool prof);
 // contacts it finds and writes none)
 DI int count_contacts(Smem& S, int k, int rk, PairJob& X) {
   const DWorld& W = S.W;
-  const DBody& bi = W.bodies[W.pair_a[k]];
-  const DBody& bj = W.bodies[W.pair_b[k]];
-  const bool swap = !(W.shapes[bi.shape].type < W.shapes[bj.shape].type);
   X.C.W = &W; X.C.cursor = &g_filter_sink[0]; X.C.cap = 0; X.C.overflow = &g_filter_sink[1]; X.C.cm = 0; X.C.pair = k;
-  X.rsi = bi.shape;
-  X.rsj = bj.shape;
-  X.bA = swap ? W.pair_b[k] : W.pair_a[k];
-  X.bB = swap ? W.pair_a[k] : W.pair_b[k];
   X.U1 = __int_as_float(0x7fc00000);
   int start = 0;
   return run_resolver(S, rk, X, start, false);
@@ -875,10 +928,50 @@ DI void narrow_place(const DWorld& W, int k) {
   for (int m = 0; m < c; m++) W.contacts[o + m] = W.ctmp[t + m];
 }
 
-DI void ph_narrow(Smem& S) {
+// shape slots of a body (0 for a body without shapes)
+DI int body_slots(const DBody& B) { return B.shape < 0 ? 0 : 1 + B.nxs; }
+
+// jobs of broadphase pair k: one per shape of its first body times one per
+// shape of its second (getContacts' two shape loops, narrow_phase.dart:654-676)
+DI int pair_jobs(const DWorld& W, int k) {
+  return body_slots(W.bodies[W.pair_a[k]]) * body_slots(W.bodies[W.pair_b[k]]);
+}
+
+// pair k's jobs from job o on, pair-major, first body's slot outer
+DI void pair_jobs_fill(const DWorld& W, int k, int o) {
+  const int na = body_slots(W.bodies[W.pair_a[k]]), nb = body_slots(W.bodies[W.pair_b[k]]);
+  for (int a = 0; a < na; a++)
+    for (int b = 0; b < nb; b++, o++) {
+      W.job_pair[o] = k;
+      W.job_sh[o] = (a << 16) | b;
+    }
+}
+
+// The narrowphase's jobs: the broadphase pairs themselves, or in a world
+// with compound bodies their shape pairs (job_pair / job_sh).  Returns the
+// job count; sets ST_JOBS_OVERFLOW when they outgrow the job list.
+DI int ph_jobs(Smem& S) {
   const DWorld& W = S.W;
   const int np = S.n_pairs;
-  if (threadIdx.x == 0) { S.n_queued = 0; S.cursor = 0; }
+  if (!S.P.compound) return np;
+  for (int k = threadIdx.x; k < np; k += BT) W.pair_cnt[k] = pair_jobs(W, k);
+  __syncthreads();
+  const int total = block_scan_array(S, W.pair_cnt, np);
+  if (total > S.P.jobs_cap) {
+    if (threadIdx.x == 0) S.overflow |= ST_JOBS_OVERFLOW;
+    __syncthreads();
+    return 0;
+  }
+  for (int k = threadIdx.x; k < np; k += BT) pair_jobs_fill(W, k, W.pair_cnt[k]);
+  __syncthreads();
+  return total;
+}
+
+DI void ph_narrow(Smem& S) {
+  const DWorld& W = S.W;
+  const int np = ph_jobs(S);
+  if (S.overflow) return;
+  if (threadIdx.x == 0) { S.n_queued = 0; S.cursor = 0; S.n_jobs = np; }
   __syncthreads();
   for (int k = threadIdx.x; k < np; k += BT) narrow_first(S, k, &S.n_queued);
   __syncthreads();
@@ -1636,7 +1729,7 @@ DI bool step_pre(Smem& S, int* s_last, int last_cap, int2* s_pairs, double dt) {
   if (threadIdx.x == 0) {
     S.overflow = 0;
     S.n_pairs = S.n_contacts = S.n_rows = S.n_levels = 0;
-    S.n_fric = S.n_cand = 0;
+    S.n_fric = S.n_cand = S.n_jobs = 0;
     S.t_last = clock64();
   }
   __syncthreads();

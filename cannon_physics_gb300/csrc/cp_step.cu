@@ -317,6 +317,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step_pre(const DWorld* __rest
       if (threadIdx.x == 0) {
         DWorldParams* gp = S.W.P;
         gp->num_pairs = S.n_pairs;
+        gp->num_jobs = S.n_jobs;
         gp->num_contacts = S.n_contacts;
         gp->num_rows = ok ? S.n_rows : 0;
         gp->num_levels = ok ? S.n_levels : 0;

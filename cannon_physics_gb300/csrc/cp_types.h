@@ -38,6 +38,7 @@
 #define ST_BINS_OVERFLOW 32
 #define ST_NONFINITE 64
 #define ST_TIMEOUT 128
+#define ST_JOBS_OVERFLOW 256  // shape-pair jobs of compound bodies
 
 struct __align__(16) DBody {
   float pos[4];     // Body.position
@@ -61,7 +62,8 @@ struct __align__(16) DBody {
   int type, sleep_state, flags, group;
   int mask, material, shape, pad0;
   float brad32;  // bounding_radius rounded to float (broadphase filter only)
-  float pad1[3];
+  int xs0, nxs;   // a compound body's further shapes: bshapes[xs0 .. xs0 + nxs)
+  int pad1;
   float interp_pos[4];   // Body.interpolatedPosition
   float interp_quat[4];  // Body.interpolatedQuaternion
 };
@@ -155,6 +157,16 @@ struct __align__(16) DWorldParams {
   int grid_plane_done, n_nocollide, fric_reduction, events;
   float grid_plane_n[4];
   long long step_limit;  // the step kernels leave the world alone once stepnumber reaches this
+  int compound, jobs_cap;  // some body has several shapes; capacity of the shape-pair job list
+  int num_jobs, pad3;  // narrowphase jobs of the last step (shape pairs; the pairs without compound bodies)
+};
+
+// A compound body's second, third, ... shape (Body.shapes[1..] with its
+// offset and orientation)
+struct __align__(16) DBodyShape {
+  int shape, pad[3];
+  float off[4];
+  float quat[4];
 };
 
 // Counters of a step of one world spread over the whole GPU (the wide
@@ -167,7 +179,7 @@ struct __align__(16) DWide {
   int n_queued, n_queued2, nh_padded, cursor;
   int check[4];   // first failed index check of the sweep kernel: code, index, bound
   int kcnt[16], kpos[16];
-  int total, pad[3];
+  int total, n_jobs, pad[2];  // n_jobs: narrowphase jobs of a compound world
 };
 #define CP_WIDE_SCAN_BLOCKS 128
 
@@ -191,6 +203,7 @@ struct DWorld {
   DConstraint* cons;
   int* nocollide;  // body pairs (a, b) of constraints with collideConnected == false
   double* dpow;    // per body: pow(1 - linearDamping, dt), pow(1 - angularDamping, dt) for the cached dt
+  DBodyShape* bshapes;  // compound bodies' further shapes
   // scratch
   DBodyScr* bscr;
   int* sap_order;
@@ -199,7 +212,15 @@ struct DWorld {
   int* pair_b;
   int* pair_cnt;
   int* pair_tstart;
-  int* pair_flag;   // event feed: 1 for a kinematic/static pair whose shapes overlap (the reference's justTest)
+  int* pair_flag;   // event feed: 1 for a kinematic/static job whose shapes overlap (the reference's justTest)
+  // Narrowphase jobs of a compound world: one per shape pair of a body pair,
+  // pair-major (getContacts' loops, narrow_phase.dart:654-676); job j is
+  // shape slot job_sh >> 16 of pair job_pair[j]'s first body against slot
+  // job_sh & 0xffff of its second (slot 0: the body's first shape).  In a
+  // world without compound bodies a job is a pair.  pair_cnt, pair_tstart,
+  // pair_flag and the queues are indexed by job.
+  int* job_pair;
+  int* job_sh;
   int* heavy;       // pairs queued for a resolver, (kind << 28) | pair; later scan scratch
   int* heavy2;      // queued pairs sorted by resolver kind (pairs + 16 * 32 slots)
   DContact* ctmp;

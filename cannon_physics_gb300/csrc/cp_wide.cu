@@ -30,6 +30,9 @@
 
 // The block's copy of the world descriptor and parameters; false when the
 // step does not run (status set, step limit reached) or has overflowed.
+// the narrowphase's job count: the pairs, or a compound world's shape pairs
+DI int wide_jobs(const DWorld& W) { return W.P->compound ? W.wide->n_jobs : W.wide->n_pairs; }
+
 DI bool wide_enter(Smem& S, const DWorld* dw) {
   if (threadIdx.x == 0) {
     S.W = *dw;
@@ -103,7 +106,7 @@ __global__ void k_w_begin(const DWorld* dw) {
     x->n_pairs = x->n_cand_pairs = x->n_contacts = x->n_fric = 0;
     x->n_cand = x->n_rows = x->n_levels = x->iters = 0;
     x->n_queued = x->n_queued2 = x->nh_padded = x->cursor = 0;
-    x->total = 0;
+    x->total = x->n_jobs = 0;
   }
   if (threadIdx.x < 16) { x->kcnt[threadIdx.x] = 0; x->kpos[threadIdx.x] = 0; }
 }
@@ -117,6 +120,7 @@ __global__ void k_w_mid(const DWorld* dw) {
   if (!x->run) return;
   DWorldParams* P = W.P;
   P->num_pairs = x->n_pairs;
+  P->num_jobs = wide_jobs(W);
   P->num_contacts = x->n_contacts;
   if (x->overflow) {
     P->num_rows = 0;
@@ -399,10 +403,21 @@ __global__ void k_w_nocollide(const DWorld* dw) {
 // ---------------------------------------------------------------------------
 // narrowphase
 
+// a compound world's jobs: count per pair, then (after a scan) the list
+__global__ void k_w_jobs(const DWorld* dw, int fill) {
+  __shared__ Smem S;
+  if (!wide_enter(S, dw)) return;
+  if (fill) {
+    WIDE_LOOP(k, S.W.wide->n_pairs) pair_jobs_fill(S.W, k, S.W.pair_cnt[k]);
+  } else {
+    WIDE_LOOP(k, S.W.wide->n_pairs) S.W.pair_cnt[k] = pair_jobs(S.W, k);
+  }
+}
+
 __global__ void k_w_narrow_first(const DWorld* dw) {
   __shared__ Smem S;
   if (!wide_enter(S, dw)) return;
-  WIDE_LOOP(k, S.W.wide->n_pairs) narrow_first(S, k, &S.W.wide->n_queued);
+  WIDE_LOOP(k, wide_jobs(S.W)) narrow_first(S, k, &S.W.wide->n_queued);
 }
 
 __global__ void k_w_kind_count(const DWorld* dw) {
@@ -464,13 +479,13 @@ __global__ void __launch_bounds__(THREADS) k_w_stage2(const DWorld* dw) {
 __global__ void k_w_contact_counts(const DWorld* dw) {
   __shared__ Smem S;
   if (!wide_enter(S, dw)) return;
-  WIDE_LOOP(k, S.W.wide->n_pairs) S.W.heavy[k] = S.W.pair_cnt[k];
+  WIDE_LOOP(k, wide_jobs(S.W)) S.W.heavy[k] = S.W.pair_cnt[k];
 }
 
 __global__ void k_w_contact_place(const DWorld* dw) {
   __shared__ Smem S;
   if (!wide_enter(S, dw)) return;
-  WIDE_LOOP(k, S.W.wide->n_pairs) narrow_place(S.W, k);
+  WIDE_LOOP(k, wide_jobs(S.W)) narrow_place(S.W, k);
 }
 
 // ---------------------------------------------------------------------------
@@ -866,7 +881,13 @@ static cudaError_t wide_step(const DWorld* dw, const DWorld& hw, const WideShape
     WIDE_SCAN(hw.pair_cnt, &x->n_cand_pairs, &x->n_pairs, nullptr, -1, 0);
     WIDE_LAUNCH(k_w_compact, G, WT, 0, dw);
   }
-  // narrowphase: contacts in pair order
+  // narrowphase: contacts in job order (pair order; shape pairs within a
+  // pair for compound bodies)
+  if (ws.compound) {
+    WIDE_LAUNCH(k_w_jobs, G, WT, 0, dw, 0);
+    WIDE_SCAN(hw.pair_cnt, &x->n_pairs, &x->n_jobs, nullptr, ws.jobs_cap, ST_JOBS_OVERFLOW);
+    WIDE_LAUNCH(k_w_jobs, G, WT, 0, dw, 1);
+  }
   WIDE_LAUNCH(k_w_narrow_first, G, WT, 0, dw);
   WIDE_LAUNCH(k_w_kind_count, G, WT, 0, dw);
   WIDE_LAUNCH(k_w_kind_pos, 1, 1, 0, dw);
@@ -875,7 +896,8 @@ static cudaError_t wide_step(const DWorld* dw, const DWorld& hw, const WideShape
   WIDE_LAUNCH(k_w_stage1<WT>, G, WT, 0, dw);
   WIDE_LAUNCH(k_w_stage2<WT>, G, WT, 0, dw);
   WIDE_LAUNCH(k_w_contact_counts, G, WT, 0, dw);
-  WIDE_SCAN(hw.heavy, &x->n_pairs, &x->n_contacts, nullptr, ws.contacts_cap, ST_CONTACTS_OVERFLOW);
+  WIDE_SCAN(hw.heavy, ws.compound ? &x->n_jobs : &x->n_pairs, &x->n_contacts, nullptr, ws.contacts_cap,
+            ST_CONTACTS_OVERFLOW);
   WIDE_LAUNCH(k_w_contact_place, G, WT, 0, dw);
   // solver rows: friction, contact, constraint candidates and the kept rows
   WIDE_LAUNCH(k_w_fric, G, WT, 0, dw);

@@ -32,7 +32,7 @@ def lib():
         L.cp_last_error.restype = C.c_char_p
         L.cp_abi_version.restype = C.c_int
         L.cp_shape_setup.argtypes = [vp]
-        L.cp_body_setup.argtypes = [vp, i32, vp, i32]
+        L.cp_body_setup.argtypes = [vp, i32, vp, i32, vp, i32]
         L.cp_create.argtypes = [vp, vp]
         L.cp_destroy.argtypes = [vp]
         L.cp_world_create.argtypes = [vp, vp, vp]
@@ -82,7 +82,8 @@ def setup_scene(scene):
     L = lib()
     for i in range(len(scene.shapes)):
         check(L.cp_shape_setup(scene.shapes[i:i + 1].ctypes.data), "cp_shape_setup")
-    check(L.cp_body_setup(A.ptr(scene.shapes), len(scene.shapes), A.ptr(scene.bodies), len(scene.bodies)), "cp_body_setup")
+    check(L.cp_body_setup(A.ptr(scene.shapes), len(scene.shapes), A.ptr(scene.body_shapes), len(scene.body_shapes),
+                          A.ptr(scene.bodies), len(scene.bodies)), "cp_body_setup")
     return scene
 
 

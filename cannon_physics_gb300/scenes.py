@@ -94,6 +94,8 @@ class Scene:
     time: float = 0.0
     stepnumber: int = 0
     friction_gravity: tuple = None
+    # the extra shapes of compound bodies (bodies' extra_shapes_first / _count index it)
+    body_shapes: np.ndarray = field(default_factory=lambda: np.zeros(0, dtype=A.BODY_SHAPE_DTYPE))
     _keep: list = field(default_factory=list)
 
     @property
@@ -126,8 +128,10 @@ class Scene:
         d.gravity[:] = list(self.gravity)
         d.grid_aabb_min[:] = list(self.grid_min)
         d.grid_aabb_max[:] = list(self.grid_max)
-        for arr in (self.bodies, self.shapes, self.materials, self.contact_materials, self.constraints):
+        for arr in (self.bodies, self.shapes, self.materials, self.contact_materials, self.constraints, self.body_shapes):
             assert arr.flags["C_CONTIGUOUS"]
+        d.body_shapes = A.ptr(self.body_shapes)
+        d.num_body_shapes = len(self.body_shapes)
         d.bodies = A.ptr(self.bodies)
         d.shapes = A.ptr(self.shapes)
         d.materials = A.ptr(self.materials)
@@ -321,6 +325,112 @@ def column_world(n, seed, mix="sphere_box", footprint=None, pitch=1.2, name="wor
     bodies["shape"][1:] = np.arange(1, n + 1)
     return Scene(name, shapes, bodies, friction=0.3, restitution=0.0, iterations=10, broadphase=A.BROAD_NAIVE,
                  dt=1 / 60, steps=120)
+
+
+def compound_pile(n=40, seed=31, broadphase=A.BROAD_NAIVE, kinematic=True, pitch=1.9, per_row=5, kinds=(0, 1, 2, 3, 4)):
+    """Compound bodies (Body.addShape with offsets and orientations) dropped
+    in a pile on a Plane, with single-shape bodies between them: dumbbells
+    (a box bar and two spheres), L pieces (two boxes, the second turned
+    90 degrees about z), tables (a box top on four box legs), and a cylinder
+    with a sphere cap.  With `kinematic`, a kinematic dumbbell sweeps through
+    the pile and a static L piece stands in it, so kinematic / static shape
+    pairs take the justTest path.  Body i is of kind kinds[i % len(kinds)]
+    (0 dumbbell, 1 L piece, 2 table, 3 capped cylinder, 4 single shape)."""
+    rng = SplitMix64(seed)
+    shapes, entries, bodies_l = [], [], []  # shape rows, extra-shape rows, (first shape, extras, mass, pos, quat)
+
+    def shape(kind, **f):
+        shapes.append((kind, f))
+        return len(shapes) - 1
+
+    def body(parts, mass, pos, quat, **extra):
+        # parts: (shape index, offset, orientation); the first is the body's shape
+        first = len(entries)
+        for sh, off, q in parts[1:]:
+            entries.append((sh, off, q))
+        bodies_l.append(dict(first=parts[0], extra_first=first, extra_count=len(parts) - 1, mass=mass, pos=pos,
+                             quat=quat, **extra))
+
+    ident = (0.0, 0.0, 0.0, 1.0)
+    zq = euler_xyz(0.0, 0.0, math.pi / 2)
+    plane = shape(A.SHAPE_PLANE)
+    body([(plane, (0.0, 0.0, 0.0), ident)], 0.0, (0.0, 0.0, 0.0), euler_xyz(-math.pi / 2, 0.0, 0.0))
+    u = rng.uniform(8 * n).reshape(n, 8)
+    for i in range(n):
+        kind = kinds[i % len(kinds)]
+        pos = ((i % per_row - (per_row - 1) / 2) * pitch + 0.2 * u[i, 0], 1.0 + 1.2 * (i // per_row),
+               ((i // per_row) % 3 - 1) * 0.6 + 0.2 * u[i, 1])
+        q = tuple(shoemake(u[i:i + 1, 2], u[i:i + 1, 3], u[i:i + 1, 4])[0])
+        if kind == 0:  # dumbbell
+            bar = shape(A.SHAPE_BOX, half_extents=(0.4, 0.08, 0.08))
+            s1 = shape(A.SHAPE_SPHERE, radius=0.18 + 0.05 * u[i, 5])
+            s2 = shape(A.SHAPE_SPHERE, radius=0.18)
+            body([(bar, (0.0, 0.0, 0.0), ident), (s1, (-0.45, 0.0, 0.0), ident), (s2, (0.45, 0.0, 0.0), ident)],
+                 1.2, pos, q)
+        elif kind == 1:  # L piece
+            a = shape(A.SHAPE_BOX, half_extents=(0.35, 0.1, 0.15))
+            b = shape(A.SHAPE_BOX, half_extents=(0.25, 0.1, 0.15))
+            body([(a, (0.1, 0.0, 0.0), ident), (b, (-0.15, 0.3, 0.0), zq)], 0.9, pos, q)
+        elif kind == 2:  # table: top and four legs, the top offset from the centre of mass
+            top = shape(A.SHAPE_BOX, half_extents=(0.45, 0.05, 0.3))
+            legs = [shape(A.SHAPE_BOX, half_extents=(0.04, 0.2, 0.04)) for _ in range(4)]
+            parts = [(top, (0.0, 0.2, 0.0), ident)]
+            for k, (sx, sz) in enumerate(((1, 1), (1, -1), (-1, 1), (-1, -1))):
+                parts.append((legs[k], (0.4 * sx, -0.05, 0.25 * sz), ident))
+            body(parts, 1.5, pos, q)
+        elif kind == 3:  # cylinder with a sphere cap
+            cyl = shape(A.SHAPE_CYLINDER, radius_top=0.2, radius_bottom=0.2, height=0.6, num_segments=8)
+            cap = shape(A.SHAPE_SPHERE, radius=0.22)
+            body([(cyl, (0.0, 0.0, 0.0), ident), (cap, (0.0, 0.35, 0.0), ident)], 1.0, pos, q)
+        else:  # a single box or sphere between the compounds
+            if u[i, 6] < 0.5:
+                body([(shape(A.SHAPE_BOX, half_extents=(0.25, 0.2, 0.3)), (0.0, 0.0, 0.0), ident)], 0.6, pos, q)
+            else:
+                body([(shape(A.SHAPE_SPHERE, radius=0.3), (0.05, 0.0, 0.0), ident)], 0.5, pos, ident)
+    if kinematic:
+        bar = shape(A.SHAPE_BOX, half_extents=(0.6, 0.1, 0.1))
+        s1 = shape(A.SHAPE_SPHERE, radius=0.25)
+        s2 = shape(A.SHAPE_BOX, half_extents=(0.2, 0.2, 0.2))
+        body([(bar, (0.0, 0.0, 0.0), ident), (s1, (-0.7, 0.0, 0.0), ident), (s2, (0.7, 0.0, 0.0), euler_xyz(0.3, 0.2, 0.1))],
+             0.0, (-6.0, 0.6, 0.0), ident, type=A.BODY_KINEMATIC, velocity=(2.0, 0.0, 0.0), angular_velocity=(0.0, 1.0, 0.0))
+        a = shape(A.SHAPE_BOX, half_extents=(0.5, 0.1, 0.5))
+        b = shape(A.SHAPE_BOX, half_extents=(0.1, 0.5, 0.1))
+        body([(a, (0.0, 1.0, 0.0), ident), (b, (0.0, 0.4, 0.0), ident)], 0.0, (3.0, 0.0, 1.5), ident)
+    S = A.default_shapes(len(shapes))
+    for k, (kind, f) in enumerate(shapes):
+        S[k]["type"] = kind
+        for name, v in f.items():
+            S[k][name] = v
+    E = A.body_shapes(len(entries))
+    for k, (sh, off, q) in enumerate(entries):
+        E[k]["shape"] = sh
+        E[k]["offset"] = off
+        E[k]["orientation"] = q
+    B = A.default_bodies(len(bodies_l))
+    for k, d in enumerate(bodies_l):
+        sh, off, q = d["first"]
+        B[k]["shape"] = sh
+        B[k]["shape_offset"] = off
+        B[k]["shape_orientation"] = q
+        B[k]["extra_shapes_first"] = d["extra_first"] if d["extra_count"] else 0
+        B[k]["extra_shapes_count"] = d["extra_count"]
+        B[k]["mass"] = d["mass"]
+        B[k]["position"] = d["pos"]
+        B[k]["quaternion"] = d["quat"]
+        if "type" in d:
+            B[k]["type"] = d["type"]
+        for f in ("velocity", "angular_velocity"):
+            if f in d:
+                B[k][f] = d[f]
+    sc = Scene("compound_pile", S, B, friction=0.4, restitution=0.1, iterations=12, broadphase=broadphase, dt=1 / 60,
+               steps=150, body_shapes=E)
+    if broadphase == A.BROAD_SAP:
+        sc.sap_axis = 0
+    elif broadphase == A.BROAD_GRID:
+        sc.grid_n = (8, 4, 4)
+        sc.grid_min = (-6.0, -1.0, -3.0)
+        sc.grid_max = (6.0, 8.0, 3.0)
+    return sc
 
 
 def batch_sizes(n_worlds=4096, seed=1000, lo=8, hi=512):

@@ -4,7 +4,9 @@
 // The scene is built with the reference's own API (World, Body, Sphere, Box,
 // Plane, ConvexPolyhedron, Cylinder, Material, ContactMaterial,
 // PointToPointConstraint, HingeConstraint, DistanceConstraint, GSSolver).
-// On the first step, and after markDirty(), the bodies, shapes, materials and
+// A body with several shapes (Body.addShape) sends its first shape as the
+// body's shape and the others, with their offsets and orientations, through
+// cp_world_desc.body_shapes.  On the first step, and after markDirty(), the bodies, shapes, materials and
 // constraints are packed into a cp_world_desc and uploaded.  Every
 // internalStep after that pushes World.time / stepnumber (cp_world_set_time)
 // and the per-step body fields an app may have changed (cp_world_set_states:
@@ -50,6 +52,10 @@ class GpuWorld extends World {
   bool _dirty = true;
   Pointer<CpBodyDesc> _bodyBuf = nullptr;
   int _bodyCap = 0;
+  // each body's first shape and its first entry in the extra-shape table,
+  // as last uploaded
+  List<int> _firstShape = const [];
+  List<int> _extraFirst = const [];
   Pointer<CpBodyState> _stateBuf = nullptr;
   int _stateCap = 0;
 
@@ -156,15 +162,39 @@ class GpuWorld extends World {
         return mats.length - 1;
       }
 
-      final shapes = arena<CpShapeDesc>(bodies.isEmpty ? 1 : bodies.length);
+      // every body's shapes in Body.shapes order: the first is the body's
+      // `shape`, the others (a compound body) go to the extra-shape table
+      _firstShape = List<int>.filled(bodies.length, -1);
+      _extraFirst = List<int>.filled(bodies.length, 0);
+      var numShapes = 0, numExtra = 0;
+      for (var i = 0; i < bodies.length; i++) {
+        final n = bodies[i].shapes.length;
+        if (n > 0) {
+          _firstShape[i] = numShapes;
+          _extraFirst[i] = numExtra;
+          numShapes += n;
+          numExtra += n - 1;
+        }
+      }
+      final shapes = arena<CpShapeDesc>(numShapes == 0 ? 1 : numShapes);
+      final bodyShapes = arena<CpBodyShape>(numExtra == 0 ? 1 : numExtra);
       final vertexBuffers = <Pointer<Float>>[];
       _ensureBodyBuf();
+      final shapeList = <Shape>[];
       for (var i = 0; i < bodies.length; i++) {
         final b = bodies[i];
-        if (b.shapes.length != 1) {
-          throw UnsupportedError('GpuWorld: body $i has ${b.shapes.length} shapes; the GPU path takes one');
+        for (var k = 0; k < b.shapes.length; k++) {
+          shapeList.add(b.shapes[k]);
+          if (k == 0) continue;
+          final e = bodyShapes[_extraFirst[i] + k - 1];
+          e.shape = _firstShape[i] + k;
+          _set3(e.offset, b.shapeOffsets[k]);
+          _setQ(e.orientation, b.shapeOrientations[k]);
         }
-        final s = b.shapes[0];
+        matIndex(b.material);
+      }
+      for (var i = 0; i < shapeList.length; i++) {
+        final s = shapeList[i];
         final d = shapes[i];
         d.type = _shapeType(s);
         d.collisionFilterGroup = s.collisionFilterGroup;
@@ -225,7 +255,6 @@ class GpuWorld extends World {
           vertexBuffers.add(verts);
         }
         _check(api.shapeSetup(d));
-        matIndex(b.material);
       }
       _packBodies(materialIndex: matIndex);
 
@@ -248,7 +277,7 @@ class GpuWorld extends World {
       final w = arena<CpWorldDesc>();
       final r = w.ref;
       r.numBodies = bodies.length;
-      r.numShapes = bodies.length;
+      r.numShapes = numShapes;
       r.numMaterials = mats.length;
       r.numContactMaterials = contactmaterials.length;
       r.numConstraints = constraints.length;
@@ -295,6 +324,8 @@ class GpuWorld extends World {
       r.contactMaterials = cmats;
       r.constraints = cons;
       r.sapAxisList = nullptr;
+      r.bodyShapes = bodyShapes;
+      r.numBodyShapes = numExtra;
       _fillContactMaterial(r.defaultContactMaterial, defaultContactMaterial, -1, -1);
 
       final id = arena<Int32>();
@@ -375,12 +406,13 @@ class GpuWorld extends World {
       }
       _set3(d.aabbLower, b.aabb.lowerBound);
       _set3(d.aabbUpper, b.aabb.upperBound);
-      _set3(d.shapeOffset, b.shapeOffsets[0]);
-      final so = b.shapeOrientations[0];
-      d.shapeOrientation[0] = so.x;
-      d.shapeOrientation[1] = so.y;
-      d.shapeOrientation[2] = so.z;
-      d.shapeOrientation[3] = so.w;
+      if (b.shapes.isNotEmpty) {
+        _set3(d.shapeOffset, b.shapeOffsets[0]);
+        _setQ(d.shapeOrientation, b.shapeOrientations[0]);
+      } else {
+        _set3(d.shapeOffset, Vector3.zero());
+        _setQ(d.shapeOrientation, Quaternion(0, 0, 0, 1));
+      }
       _set3(d.previousPosition, b.previousPosition);
       d.previousQuaternion[0] = b.previousQuaternion.x;
       d.previousQuaternion[1] = b.previousQuaternion.y;
@@ -403,7 +435,9 @@ class GpuWorld extends World {
       d.collisionResponse = b.collisionResponse ? 1 : 0;
       d.isTrigger = b.isTrigger ? 1 : 0;
       if (materialIndex != null) d.material = materialIndex(b.material);
-      d.shape = i;
+      d.shape = _firstShape[i];
+      d.extraShapesFirst = _extraFirst[i];
+      d.extraShapesCount = b.shapes.isEmpty ? 0 : b.shapes.length - 1;
       d.fixedRotation = b.fixedRotation ? 1 : 0;
       d.aabbNeedsUpdate = b.aabbNeedsUpdate ? 1 : 0;
     }

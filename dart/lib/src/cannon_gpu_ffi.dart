@@ -6,7 +6,7 @@
 // only during the call.
 import 'dart:ffi';
 
-const int cpAbiVersion = 2;
+const int cpAbiVersion = 3;
 
 const int cpOk = 0;
 const int cpErrArg = 1;
@@ -83,7 +83,15 @@ final class CpBodyDesc extends Struct {
   @Int32() external int aabbNeedsUpdate;
   @Array(3) external Array<Float> interpolatedPosition;
   @Array(4) external Array<Float> interpolatedQuaternion;
-  @Int32() external int pad0;
+  @Int32() external int extraShapesFirst;
+  @Int32() external int extraShapesCount;
+}
+
+/// cp_body_shape: a compound body's second, third, ... shape.
+final class CpBodyShape extends Struct {
+  @Int32() external int shape;
+  @Array(3) external Array<Float> offset;
+  @Array(4) external Array<Float> orientation;
 }
 
 final class CpBodyState extends Struct {
@@ -170,6 +178,9 @@ final class CpWorldDesc extends Struct {
   external Pointer<CpConstraintDesc> constraints;
   external Pointer<Int32> sapAxisList;
   external CpContactMaterial defaultContactMaterial;
+  external Pointer<CpBodyShape> bodyShapes;
+  @Int32() external int numBodyShapes;
+  @Int32() external int pad0;
 }
 
 final class CpStepInfo extends Struct {
@@ -202,8 +213,8 @@ class CannonGpu {
         shapeSetup = lib.lookupFunction<Int32 Function(Pointer<CpShapeDesc>), int Function(Pointer<CpShapeDesc>)>(
             'cp_shape_setup'),
         bodySetup = lib.lookupFunction<
-            Int32 Function(Pointer<CpShapeDesc>, Int32, Pointer<CpBodyDesc>, Int32),
-            int Function(Pointer<CpShapeDesc>, int, Pointer<CpBodyDesc>, int)>('cp_body_setup'),
+            Int32 Function(Pointer<CpShapeDesc>, Int32, Pointer<CpBodyShape>, Int32, Pointer<CpBodyDesc>, Int32),
+            int Function(Pointer<CpShapeDesc>, int, Pointer<CpBodyShape>, int, Pointer<CpBodyDesc>, int)>('cp_body_setup'),
         create = lib.lookupFunction<Int32 Function(Pointer<CpConfig>, Pointer<Pointer<CpCtx>>),
             int Function(Pointer<CpConfig>, Pointer<Pointer<CpCtx>>)>('cp_create'),
         destroy = lib.lookupFunction<Int32 Function(Pointer<CpCtx>), int Function(Pointer<CpCtx>)>('cp_destroy'),
@@ -235,7 +246,7 @@ class CannonGpu {
   final int Function() abiVersion;
   final Pointer<Uint8> Function() lastError;
   final int Function(Pointer<CpShapeDesc>) shapeSetup;
-  final int Function(Pointer<CpShapeDesc>, int, Pointer<CpBodyDesc>, int) bodySetup;
+  final int Function(Pointer<CpShapeDesc>, int, Pointer<CpBodyShape>, int, Pointer<CpBodyDesc>, int) bodySetup;
   final int Function(Pointer<CpConfig>, Pointer<Pointer<CpCtx>>) create;
   final int Function(Pointer<CpCtx>) destroy;
   final int Function(Pointer<CpCtx>, Pointer<CpWorldDesc>, Pointer<Int32>) worldCreate;

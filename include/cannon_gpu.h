@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define CP_ABI_VERSION 2
+#define CP_ABI_VERSION 3
 
 /* status codes */
 #define CP_OK               0
@@ -91,8 +91,22 @@ typedef struct cp_shape_desc {
   double bounding_sphere_radius;    /* output of cp_shape_setup */
 } cp_shape_desc;
 
-/* Body state (lib/objects/rigid_body.dart:27-260).  One shape per body, at
- * `shape_offset` / `shape_orientation` in the body frame. */
+/* A body's second, third, ... shape (Body.addShape(shape, offset,
+ * orientation), lib/objects/rigid_body.dart:348-369): an entry of
+ * cp_world_desc.body_shapes.  A body has at most CP_MAX_BODY_SHAPES shapes,
+ * its first included. */
+#define CP_MAX_BODY_SHAPES 65535
+typedef struct cp_body_shape {
+  int32_t shape;                    /* index into cp_world_desc.shapes */
+  float offset[3];
+  float orientation[4];
+} cp_body_shape;
+
+/* Body state (lib/objects/rigid_body.dart:27-260).  Its first shape is
+ * `shape` at `shape_offset` / `shape_orientation` in the body frame; the
+ * shapes added after it (a compound body) are body_shapes[
+ * extra_shapes_first .. extra_shapes_first + extra_shapes_count) of the
+ * world (or of the table given to cp_body_setup), in Body.shapes order. */
 typedef struct cp_body_desc {
   float position[3];
   float quaternion[4];              /* x, y, z, w */
@@ -123,7 +137,7 @@ typedef struct cp_body_desc {
    * written by cp_world_step_interpolated */
   float interpolated_position[3];
   float interpolated_quaternion[4];
-  int32_t pad0;
+  int32_t extra_shapes_first, extra_shapes_count;
 } cp_body_desc;
 
 /* The Body fields one World.step changes or an app typically sets between
@@ -199,6 +213,9 @@ typedef struct cp_world_desc {
   const cp_constraint_desc* constraints;
   const int32_t* sap_axis_list;     /* optional persisted SAP order, NULL = body order */
   cp_contact_material default_contact_material;
+  const cp_body_shape* body_shapes; /* shapes after each body's first (compound bodies) */
+  int32_t num_body_shapes;
+  int32_t pad0;
 } cp_world_desc;
 
 /* One narrowphase contact, in the order the reference appends them. */
@@ -243,14 +260,17 @@ typedef struct cp_ctx cp_ctx;
 int cp_shape_setup(cp_shape_desc* shape);
 
 /* Body(mass, position, quaternion) followed by addShape(shape, offset,
- * orientation), for each of `num_bodies` bodies: updateMassProperties
- * (rigid_body.dart:587-609, inertia from the body AABB) and
- * updateBoundingRadius (:395-412).  Reads mass, position, quaternion, shape,
- * shape_offset, shape_orientation, fixed_rotation and type (-1 = derive from
- * mass); writes inv_mass, type, inertia-derived fields, aabb,
- * bounding_radius, previous_* and aabb_needs_update.  Other fields are left
- * as given (callers start from the Body constructor defaults). */
-int cp_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc* bodies, int32_t num_bodies);
+ * orientation) for each of its shapes, for each of `num_bodies` bodies:
+ * updateMassProperties (rigid_body.dart:587-609, inertia from the AABB of
+ * all the body's shapes) and updateBoundingRadius (:395-412).  Reads mass,
+ * position, quaternion, shape, shape_offset, shape_orientation, the extra
+ * shapes (body_shapes, may be NULL when no body has any), fixed_rotation and
+ * type (-1 = derive from mass); writes inv_mass, type, inertia-derived
+ * fields, aabb, bounding_radius, previous_* and aabb_needs_update.  Other
+ * fields are left as given (callers start from the Body constructor
+ * defaults). */
+int cp_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, const cp_body_shape* body_shapes, int32_t num_body_shapes,
+                  cp_body_desc* bodies, int32_t num_bodies);
 
 /* ---- context and worlds ------------------------------------------------- */
 

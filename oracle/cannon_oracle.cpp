@@ -495,17 +495,49 @@ struct Body {
   int group = 1, mask = -1;
   bool response = true, isTrigger = false, fixedRotation = false, aabbNeedsUpdate = true;
   int material = -1;
-  int shape = -1;
+  int shape = -1;  // Body.shapes[0] (at shapeOffset / shapeOrientation)
+  // Body.shapes[1..] of a compound body, with their offsets and orientations
+  struct Extra { int shape; V3 offset; Q4 orientation; };
+  std::vector<Extra> extra;
+  int extraFirst = 0;  // where they came from in the world's body_shapes table
+  int numShapes() const { return shape < 0 ? 0 : 1 + (int)extra.size(); }
+  int shapeAt(int k) const { return k == 0 ? shape : extra[k - 1].shape; }
+  const V3& offsetAt(int k) const { return k == 0 ? shapeOffset : extra[k - 1].offset; }
+  const Q4& orientationAt(int k) const { return k == 0 ? shapeOrientation : extra[k - 1].orientation; }
 };
 
-// rigid_body.dart:415-447 (one shape)
+// dart:math min / max on doubles: NaN wins, and -0.0 is below 0.0
+static inline double dartMin(double a, double b) {
+  if (a > b) return b;
+  if (a < b) return a;
+  if (std::isnan(a) || std::isnan(b)) return std::numeric_limits<double>::quiet_NaN();
+  return (std::signbit(a) || std::signbit(b)) ? -0.0 : a;
+}
+static inline double dartMax(double a, double b) {
+  if (a < b) return b;
+  if (a > b) return a;
+  if (std::isnan(a) || std::isnan(b)) return std::numeric_limits<double>::quiet_NaN();
+  return (std::signbit(a) && std::signbit(b)) ? -0.0 : (a == 0 ? 0.0 : a);
+}
+
+// rigid_body.dart:415-447: each shape's world AABB, the first copied, the
+// others extended in (AABB.extend, aabb.dart:121-128)
 static void updateAABB(Body& b, const std::vector<Shape>& shapes) {
-  if (b.shape < 0) { b.aabbNeedsUpdate = false; return; }
-  V3 offset; Q4 orientation;
-  vmult(b.quaternion, b.shapeOffset, offset);
-  add2(offset, b.position, offset);
-  qmultiply2(b.quaternion, b.shapeOrientation, orientation);
-  shapeWorldAABB(shapes[b.shape], offset, orientation, b.aabbLo, b.aabbHi);
+  const int N = b.numShapes();
+  for (int i = 0; i != N; i++) {
+    V3 offset, lo, hi; Q4 orientation;
+    vmult(b.quaternion, b.offsetAt(i), offset);
+    add2(offset, b.position, offset);
+    qmultiply2(b.quaternion, b.orientationAt(i), orientation);
+    shapeWorldAABB(shapes[b.shapeAt(i)], offset, orientation, lo, hi);
+    if (i == 0) {
+      b.aabbLo = lo; b.aabbHi = hi;
+    } else {
+      b.aabbLo.x = (float)dartMin(b.aabbLo.x, lo.x); b.aabbHi.x = (float)dartMax(b.aabbHi.x, hi.x);
+      b.aabbLo.y = (float)dartMin(b.aabbLo.y, lo.y); b.aabbHi.y = (float)dartMax(b.aabbHi.y, hi.y);
+      b.aabbLo.z = (float)dartMin(b.aabbLo.z, lo.z); b.aabbHi.z = (float)dartMax(b.aabbHi.z, hi.z);
+    }
+  }
   b.aabbNeedsUpdate = false;
 }
 
@@ -541,7 +573,22 @@ static void updateMassProperties(Body& b, const std::vector<Shape>& shapes) {
   updateInertiaWorld(b, true);
 }
 
-static void bodyFromDesc(const cp_body_desc& d, Body& b) {
+// a body's extra shapes lie inside the table and name existing shapes, only
+// a body with a first shape has any, and a body has at most
+// CP_MAX_BODY_SHAPES shapes (the ABI's limit)
+static bool extrasValid(const cp_body_desc& d, int num_shapes, const cp_body_shape* table, int ntable) {
+  if (d.extra_shapes_count == 0) return true;
+  if (d.extra_shapes_count < 0 || d.extra_shapes_count >= CP_MAX_BODY_SHAPES || d.shape < 0 || !table ||
+      d.extra_shapes_first < 0 || (long long)d.extra_shapes_first + d.extra_shapes_count > ntable)
+    return false;
+  for (int k = 0; k < d.extra_shapes_count; k++) {
+    const int sh = table[d.extra_shapes_first + k].shape;
+    if (sh < 0 || sh >= num_shapes) return false;
+  }
+  return true;
+}
+
+static void bodyFromDesc(const cp_body_desc& d, Body& b, const cp_body_shape* table) {
   auto v3 = [](const float* f) { V3 v; v.x = f[0]; v.y = f[1]; v.z = f[2]; return v; };
   auto q4 = [](const float* f) { Q4 q; q.x = f[0]; q.y = f[1]; q.z = f[2]; q.w = f[3]; return q; };
   b.position = v3(d.position); b.quaternion = q4(d.quaternion);
@@ -564,6 +611,12 @@ static void bodyFromDesc(const cp_body_desc& d, Body& b) {
   b.response = d.collision_response != 0; b.isTrigger = d.is_trigger != 0;
   b.material = d.material; b.shape = d.shape;
   b.fixedRotation = d.fixed_rotation != 0; b.aabbNeedsUpdate = d.aabb_needs_update != 0;
+  b.extra.clear();
+  b.extraFirst = d.extra_shapes_first;
+  for (int k = 0; k < d.extra_shapes_count; k++) {
+    const cp_body_shape& e = table[d.extra_shapes_first + k];
+    b.extra.push_back(Body::Extra{e.shape, v3(e.offset), q4(e.orientation)});
+  }
 }
 
 static void bodyToDesc(const Body& b, cp_body_desc& d) {
@@ -589,6 +642,8 @@ static void bodyToDesc(const Body& b, cp_body_desc& d) {
   d.collision_response = b.response; d.is_trigger = b.isTrigger;
   d.material = b.material; d.shape = b.shape;
   d.fixed_rotation = b.fixedRotation; d.aabb_needs_update = b.aabbNeedsUpdate;
+  d.extra_shapes_first = b.extraFirst;
+  d.extra_shapes_count = (int32_t)b.extra.size();
 }
 
 // ---------------------------------------------------------------------------
@@ -695,6 +750,7 @@ struct World {
   std::vector<char> planeNormalDone;
   std::vector<V3> planeWorldNormal;
   bool enableFrictionReduction = false;
+  std::vector<cp_body_shape> bodyShapeTable;  // the compound bodies' extra shapes
   // events (world_class.dart:213-221,593-610,703-770), when recorded
   bool events = false;
   std::vector<int> bodyIds, shapeIds;
@@ -1424,7 +1480,7 @@ struct World {
   }
 
   // narrow_phase.dart:634-721
-  void getContacts() {
+  void getContacts() {  // narrow_phase.dart:634-721
     contacts.clear();
     frictionEqs.clear();
     const int NP = (int)p1.size();
@@ -1437,48 +1493,54 @@ struct World {
       bool justTest = (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_STATIC) ||
                       (bi.type == CP_BODY_STATIC && bj.type == CP_BODY_KINEMATIC) ||
                       (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_KINEMATIC);
-      if (bi.shape < 0 || bj.shape < 0) continue;
-      Q4 qi, qj; V3 xi, xj;
-      qmultiply2(bi.quaternion, bi.shapeOrientation, qi);
-      vmult(bi.quaternion, bi.shapeOffset, xi);
-      add2(xi, bi.position, xi);
-      qmultiply2(bj.quaternion, bj.shapeOrientation, qj);
-      vmult(bj.quaternion, bj.shapeOffset, xj);
-      add2(xj, bj.position, xj);
-      const Shape& si = shapes[bi.shape];
-      const Shape& sj = shapes[bj.shape];
-      if (!((si.mask & sj.group) != 0 && (sj.mask & si.group) != 0)) continue;
-      if (distanceTo(xi, xj) > si.bsr + sj.bsr) continue;
-      const ContactMat* shapeCM = nullptr;
-      if (si.material >= 0 && sj.material >= 0) shapeCM = getCM(si.material, sj.material);
-      current = shapeCM ? *shapeCM : (bodyCM ? *bodyCM : defaultCM);
-      if (justTest) {
-        // a justTest resolver adds no contacts; where it would find one it
-        // registers the overlap (narrow_phase.dart:712-715)
-        if (events) {
-          const size_t nc = contacts.size(), nf = frictionEqs.size();
+      for (int a = 0; a < bi.numShapes(); a++) {
+        Q4 qi; V3 xi;
+        qmultiply2(bi.quaternion, bi.orientationAt(a), qi);
+        vmult(bi.quaternion, bi.offsetAt(a), xi);
+        add2(xi, bi.position, xi);
+        const int isi = bi.shapeAt(a);
+        const Shape& si = shapes[isi];
+        for (int b = 0; b < bj.numShapes(); b++) {
+          Q4 qj; V3 xj;
+          qmultiply2(bj.quaternion, bj.orientationAt(b), qj);
+          vmult(bj.quaternion, bj.offsetAt(b), xj);
+          add2(xj, bj.position, xj);
+          const int isj = bj.shapeAt(b);
+          const Shape& sj = shapes[isj];
+          if (!((si.mask & sj.group) != 0 && (sj.mask & si.group) != 0)) continue;
+          if (distanceTo(xi, xj) > si.bsr + sj.bsr) continue;
+          const ContactMat* shapeCM = nullptr;
+          if (si.material >= 0 && sj.material >= 0) shapeCM = getCM(si.material, sj.material);
+          current = shapeCM ? *shapeCM : (bodyCM ? *bodyCM : defaultCM);
           curPair = k;
-          if (si.type < sj.type) dispatch(si, sj, xi, xj, qi, qj, ibi, ibj, bi.shape, bj.shape);
-          else dispatch(sj, si, xj, xi, qj, qi, ibj, ibi, bi.shape, bj.shape);
-          if (contacts.size() > nc) {
-            shapeOverlapKeeper.set(shapeId(bi.shape), shapeId(bj.shape));
-            bodyOverlapKeeper.set(bodyId(ibi), bodyId(ibj));
+          if (justTest) {
+            // a justTest resolver adds no contacts; where it would find one it
+            // registers the overlap (narrow_phase.dart:712-715)
+            if (events) {
+              const size_t nc = contacts.size(), nf = frictionEqs.size();
+              if (si.type < sj.type) dispatch(si, sj, xi, xj, qi, qj, ibi, ibj, isi, isj, isi, isj);
+              else dispatch(sj, si, xj, xi, qj, qi, ibj, ibi, isj, isi, isi, isj);
+              if (contacts.size() > nc) {
+                shapeOverlapKeeper.set(shapeId(isi), shapeId(isj));
+                bodyOverlapKeeper.set(bodyId(ibi), bodyId(ibj));
+              }
+              contacts.resize(nc);
+              frictionEqs.resize(nf);
+            }
+            continue;
           }
-          contacts.resize(nc);
-          frictionEqs.resize(nf);
+          if (si.type < sj.type) dispatch(si, sj, xi, xj, qi, qj, ibi, ibj, isi, isj, isi, isj);
+          else dispatch(sj, si, xj, xi, qj, qi, ibj, ibi, isj, isi, isi, isj);
         }
-        continue;
       }
-      curPair = k;
-      if (si.type < sj.type) dispatch(si, sj, xi, xj, qi, qj, ibi, ibj, bi.shape, bj.shape);
-      else dispatch(sj, si, xj, xi, qj, qi, ibj, ibi, bi.shape, bj.shape);
     }
   }
   // narrow_phase.dart:116-238 (resolver table); rsi/rsj are the shapes in
   // getContacts order, passed through unchanged as in :707-709.
-  void dispatch(const Shape& a, const Shape& b, const V3& xa, const V3& xb, const Q4& qa, const Q4& qb, int ba, int bb, int rsi, int rsj) {
+  // shA / shB: the indices of shapes a / b (type order)
+  void dispatch(const Shape& a, const Shape& b, const V3& xa, const V3& xb, const Q4& qa, const Q4& qb, int ba, int bb, int shA,
+                int shB, int rsi, int rsj) {
     int ta = a.type, tb = b.type;
-    int shA = bodies[ba].shape, shB = bodies[bb].shape;
     if (ta == CP_SHAPE_SPHERE && tb == CP_SHAPE_SPHERE) sphereSphere(a, b, xa, xb, ba, bb, rsi, rsj);
     else if (ta == CP_SHAPE_SPHERE && tb == CP_SHAPE_PLANE) spherePlane(a, b, xa, xb, qb, ba, bb, rsi, rsj);
     else if (ta == CP_SHAPE_SPHERE && tb == CP_SHAPE_BOX) sphereBox(a, b, xa, xb, qb, ba, bb, rsi, rsj);
@@ -1880,8 +1942,10 @@ static int buildWorld(const cp_world_desc& d, World& w) {
   w.planeNormalDone.assign(d.num_shapes, 0);
   w.planeWorldNormal.assign(d.num_shapes, V3());
   w.bodies.resize(d.num_bodies);
+  w.bodyShapeTable.assign(d.body_shapes, d.body_shapes ? d.body_shapes + d.num_body_shapes : d.body_shapes);
   for (int i = 0; i < d.num_bodies; i++) {
-    bodyFromDesc(d.bodies[i], w.bodies[i]);
+    if (!extrasValid(d.bodies[i], d.num_shapes, d.body_shapes, d.num_body_shapes)) return CP_ERR_ARG;
+    bodyFromDesc(d.bodies[i], w.bodies[i], d.body_shapes);
     if (w.bodies[i].shape >= d.num_shapes) return CP_ERR_ARG;
   }
   w.materials.resize(d.num_materials);
@@ -1977,15 +2041,16 @@ int orc_shape_setup(cp_shape_desc* shape) {
 }
 
 // rigid_body.dart:27-86 (constructor) then addShape :348-369
-int orc_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc* bodies, int32_t num_bodies) {
-  if ((!bodies && num_bodies > 0) || num_bodies < 0 || num_shapes < 0) return CP_ERR_ARG;
+int orc_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, const cp_body_shape* body_shapes, int32_t num_body_shapes,
+                   cp_body_desc* bodies, int32_t num_bodies) {
+  if ((!bodies && num_bodies > 0) || num_bodies < 0 || num_shapes < 0 || num_body_shapes < 0) return CP_ERR_ARG;
   std::vector<Shape> sh(num_shapes);
   for (int i = 0; i < num_shapes; i++) { int st = buildShape(shapes[i], sh[i]); if (st) return st; }
   for (int k = 0; k < num_bodies; k++) {
     cp_body_desc* d = &bodies[k];
-    if (d->shape >= num_shapes) return CP_ERR_ARG;
+    if (d->shape >= num_shapes || !extrasValid(*d, num_shapes, body_shapes, num_body_shapes)) return CP_ERR_ARG;
     Body b;
-    bodyFromDesc(*d, b);
+    bodyFromDesc(*d, b, body_shapes);
     b.previousPosition = b.position;
     b.previousQuaternion = b.quaternion;
     b.interpolatedPosition = b.position;
@@ -1993,17 +2058,24 @@ int orc_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc
     b.invMass = b.mass > 0 ? 1.0 / b.mass : 0;
     if (d->type < 0) b.type = b.mass <= 0.0 ? CP_BODY_STATIC : CP_BODY_DYNAMIC;
     int shapeIdx = b.shape;
+    std::vector<Body::Extra> extra;
+    extra.swap(b.extra);
     b.shape = -1;
     setValues(b.aabbLo, 0, 0, 0); setValues(b.aabbHi, 0, 0, 0);
     updateMassProperties(b, sh);  // constructor, before the shape is added
     b.boundingRadius = 0;
     if (shapeIdx >= 0) {
+      // addShape for the first shape, then for each further one: the last
+      // updateMassProperties / updateBoundingRadius see them all
       b.shape = shapeIdx;
+      b.extra.swap(extra);
       updateMassProperties(b, sh);
-      double radius = 0;  // updateBoundingRadius
-      double offset = length(b.shapeOffset);
-      double r = sh[shapeIdx].bsr;
-      if (offset + r > radius) radius = offset + r;
+      double radius = 0;  // updateBoundingRadius (rigid_body.dart:395-412)
+      for (int i = 0; i != b.numShapes(); i++) {
+        double offset = length(b.offsetAt(i));
+        double r = sh[b.shapeAt(i)].bsr;
+        if (offset + r > radius) radius = offset + r;
+      }
       b.boundingRadius = radius;
     }
     b.aabbNeedsUpdate = true;
@@ -2065,8 +2137,11 @@ int orc_world_get_events(orc_world* o, cp_event* out, int32_t cap, int32_t* coun
 int orc_world_set_bodies(orc_world* o, const cp_body_desc* in, int32_t n) {
   if (!o || (!in && n > 0) || n != (int32_t)o->w.bodies.size()) return CP_ERR_ARG;
   for (int i = 0; i < n; i++) {
-    if (in[i].shape >= (int32_t)o->w.shapes.size()) return CP_ERR_ARG;
-    bodyFromDesc(in[i], o->w.bodies[i]);
+    const World& w = o->w;
+    if (in[i].shape >= (int32_t)w.shapes.size() ||
+        !extrasValid(in[i], (int)w.shapes.size(), w.bodyShapeTable.data(), (int)w.bodyShapeTable.size()))
+      return CP_ERR_ARG;
+    bodyFromDesc(in[i], o->w.bodies[i], w.bodyShapeTable.data());
   }
   return CP_OK;
 }

@@ -30,7 +30,8 @@ extern "C" {
 typedef struct orc_world orc_world;
 
 int orc_shape_setup(cp_shape_desc* shape);
-int orc_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, cp_body_desc* bodies, int32_t num_bodies);
+int orc_body_setup(const cp_shape_desc* shapes, int32_t num_shapes, const cp_body_shape* body_shapes, int32_t num_body_shapes,
+                   cp_body_desc* bodies, int32_t num_bodies);
 
 orc_world* orc_world_create(const cp_world_desc* desc);
 void orc_world_destroy(orc_world* w);

@@ -22,7 +22,7 @@ def lib():
         L = C.CDLL(path)
         vp, i32, f64 = C.c_void_p, C.c_int32, C.c_double
         L.orc_shape_setup.argtypes = [vp]
-        L.orc_body_setup.argtypes = [vp, i32, vp, i32]
+        L.orc_body_setup.argtypes = [vp, i32, vp, i32, vp, i32]
         L.orc_world_create.argtypes = [vp]
         L.orc_world_create.restype = vp
         L.orc_world_destroy.argtypes = [vp]
@@ -56,7 +56,8 @@ def setup_scene(scene):
     L = lib()
     for i in range(len(scene.shapes)):
         _check(L.orc_shape_setup(scene.shapes[i:i + 1].ctypes.data), "shape setup")
-    _check(L.orc_body_setup(A.ptr(scene.shapes), len(scene.shapes), A.ptr(scene.bodies), len(scene.bodies)), "body setup")
+    _check(L.orc_body_setup(A.ptr(scene.shapes), len(scene.shapes), A.ptr(scene.body_shapes), len(scene.body_shapes),
+                            A.ptr(scene.bodies), len(scene.bodies)), "body setup")
     return scene
 
 

@@ -8,7 +8,9 @@ scene stepped by the oracle; after every step the counters (pairs, contacts,
 rows, solver iterations) are recorded, and after the last step the body
 state, the pair list, the contacts and the solver rows.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [case ...]
+(with case names, only those cases are written again; the others' files and
+manifest entries stay as they are)
 """
 import json
 import os
@@ -32,6 +34,7 @@ CASES = [
     ("mixed_grid_chains_sleep", lambda: scenes.mixed_chains(8, 4, 4, seed=3, chains=4, chain_len=8), 60),
     ("column_sphere_box", lambda: scenes.column_world(120, 1234, "sphere_box"), 50),
     ("column_mixed", lambda: scenes.column_world(80, 4321, "mixed"), 50),
+    ("compound_naive", lambda: scenes.compound_pile(20, seed=12), 60),
 ]
 
 BODY_FIELDS = ["position", "quaternion", "velocity", "angular_velocity", "inv_inertia_world", "sleep_state"]
@@ -57,10 +60,16 @@ def run_case(make, steps):
     return out
 
 
-def main():
+def main(only=()):
     OB.build()
+    path = os.path.join(HERE, "manifest.json")
     manifest = {}
+    if only and os.path.exists(path):
+        with open(path) as f:
+            manifest = json.load(f)["cases"]
     for name, make, steps in CASES:
+        if only and name not in only:
+            continue
         data = run_case(make, steps)
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **data)
         manifest[name] = {"steps": steps, "bodies": int(len(data["body_position"])),
@@ -75,4 +84,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

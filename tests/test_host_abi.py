@@ -34,7 +34,7 @@ def test_library_exports_every_header_entry_point(lib):
     assert len(names) >= 18
     for n in names:
         assert hasattr(lib, n), f"libcannon_gpu.so does not export {n}"
-    assert lib.cp_abi_version() == 2
+    assert lib.cp_abi_version() == 3
 
 
 def test_ctypes_layouts_match_the_c_header(tmp_path):
@@ -45,7 +45,7 @@ def test_ctypes_layouts_match_the_c_header(tmp_path):
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
-    structs = [("cp_body_desc", A.BodyDesc), ("cp_body_state", A.BodyState), ("cp_shape_desc", A.ShapeDesc), ("cp_world_desc", A.WorldDesc),
+    structs = [("cp_body_desc", A.BodyDesc), ("cp_body_state", A.BodyState), ("cp_body_shape", A.BodyShape), ("cp_shape_desc", A.ShapeDesc), ("cp_world_desc", A.WorldDesc),
                ("cp_contact", A.Contact), ("cp_row", A.Row), ("cp_constraint_desc", A.ConstraintDesc),
                ("cp_contact_material", A.ContactMaterial), ("cp_step_info", A.StepInfo), ("cp_config", A.Config),
                ("cp_serve_config", S.ServeConfig), ("cp_serve_stats", S.ServeStats)]
@@ -73,7 +73,7 @@ def _bytes(arr):
 
 @pytest.mark.parametrize("make", [scenes.spheres_on_plane, lambda: scenes.box_pile(8, 8, 4),
                                   lambda: scenes.mixed_chains(8, 8, 4, chains=4, chain_len=8),
-                                  lambda: scenes.column_world(300, 9, "mixed")])
+                                  lambda: scenes.column_world(300, 9, "mixed"), scenes.compound_pile])
 def test_body_setup_matches_oracle_bitwise(lib, make):
     a, b = make(), make()
     O.setup_scene(a)
@@ -95,4 +95,34 @@ def test_invalid_inputs_are_rejected(lib):
     assert lib.cp_shape_setup(s.ctypes.data) == A.CP_ERR_UNSUPPORTED
     b = A.default_bodies(1)
     b[0]["shape"] = 3
-    assert lib.cp_body_setup(s.ctypes.data, 1, b.ctypes.data, 1) == A.CP_ERR_ARG
+    assert lib.cp_body_setup(s.ctypes.data, 1, None, 0, b.ctypes.data, 1) == A.CP_ERR_ARG
+
+
+def test_compound_bodies_are_checked(lib):
+    """Extra shapes must lie inside the table, name existing shapes and
+    belong to a body with a first shape; the oracle takes the same view."""
+    from oracle import oracle_py as Op
+    s = A.default_shapes(2)
+    s["type"] = A.SHAPE_SPHERE
+    s["radius"] = 0.5
+    t = A.body_shapes(2)
+    t["shape"] = (1, 0)
+    OL = Op.lib()
+    cases = [(0, 3, 0), (1, 2, 0), (-1, 1, 0), (0, 1, -1), (0, 2, 5), (0, 65535, 0)]
+    for first, count, shape in cases:
+        b = A.default_bodies(1)
+        b[0]["shape"] = shape
+        b[0]["mass"] = 1.0
+        b[0]["extra_shapes_first"] = first
+        b[0]["extra_shapes_count"] = count
+        t2 = t.copy()
+        if (first, count, shape) == (0, 2, 5):
+            b[0]["shape"] = 0
+            t2["shape"][1] = 5
+        assert lib.cp_body_setup(s.ctypes.data, 2, t2.ctypes.data, 2, b.ctypes.data, 1) == A.CP_ERR_ARG, (first, count, shape)
+        assert OL.orc_body_setup(s.ctypes.data, 2, t2.ctypes.data, 2, b.ctypes.data, 1) == A.CP_ERR_ARG, (first, count, shape)
+    b = A.default_bodies(1)
+    b[0]["shape"] = 0
+    b[0]["mass"] = 1.0
+    b[0]["extra_shapes_count"] = 2
+    assert lib.cp_body_setup(s.ctypes.data, 2, t.ctypes.data, 2, b.ctypes.data, 1) == A.CP_OK
