@@ -17,10 +17,11 @@ CP_ERR_CUDA = 6
 CP_ERR_UNSUPPORTED = 7
 
 SHAPE_SPHERE, SHAPE_PLANE, SHAPE_BOX, SHAPE_CONVEX, SHAPE_CYLINDER = 0, 1, 2, 3, 4
+SHAPE_CAPSULE, SHAPE_CONE, SHAPE_SIZED_PLANE = 5, 6, 7
 BODY_DYNAMIC, BODY_STATIC, BODY_KINEMATIC = 0, 1, 2
 AWAKE, SLEEPY, SLEEPING = 0, 1, 2
 BROAD_NAIVE, BROAD_SAP, BROAD_GRID = 0, 1, 2
-CON_P2P, CON_HINGE, CON_DISTANCE = 0, 1, 2
+CON_P2P, CON_HINGE, CON_DISTANCE, CON_LOCK, CON_CONE_TWIST, CON_SPRING = 0, 1, 2, 3, 4, 5
 ROW_CONTACT, ROW_FRICTION, ROW_ROTATIONAL, ROW_MOTOR = 0, 1, 2, 3
 
 f3 = C.c_float * 3
@@ -159,6 +160,9 @@ class ConstraintDesc(C.Structure):
         ("spook_stiffness", C.c_double),
         ("spook_relaxation", C.c_double),
         ("spook_time_step", C.c_double),
+        ("lock_axes", (C.c_float * 3) * 6),
+        ("angle", C.c_double),
+        ("twist_angle", C.c_double),
     ]
 
 
@@ -268,6 +272,8 @@ def np_dtype(struct_cls):
         offsets.append(field.offset)
         if ctype in _SCALARS:
             formats.append(_SCALARS[ctype])
+        elif issubclass(ctype, C.Array) and issubclass(ctype._type_, C.Array):  # two-dimensional
+            formats.append((_SCALARS[ctype._type_._type_], (ctype._length_, ctype._type_._length_)))
         elif issubclass(ctype, C.Array):
             formats.append((_SCALARS[ctype._type_], (ctype._length_,)))
         elif issubclass(ctype, C.Structure):
@@ -288,14 +294,6 @@ EVENT_DTYPE = np_dtype(Event)
 BODY_DTYPE = np_dtype(BodyDesc)
 BODY_STATE_DTYPE = np_dtype(BodyState)
 BODY_SHAPE_DTYPE = np_dtype(BodyShape)
-
-
-def body_shapes(n):
-    """Extra-shape entries (Body.addShape beyond the first) with identity
-    orientations."""
-    t = np.zeros(n, dtype=BODY_SHAPE_DTYPE)
-    t["orientation"][:, 3] = 1.0
-    return t
 MATERIAL_DTYPE = np_dtype(Material)
 CONTACT_MATERIAL_DTYPE = np_dtype(ContactMaterial)
 CONSTRAINT_DTYPE = np_dtype(ConstraintDesc)
@@ -334,6 +332,14 @@ def default_bodies(n):
     b["shape"] = -1
     b["aabb_needs_update"] = 1
     return b
+
+
+def body_shapes(n):
+    """Extra-shape entries (Body.addShape beyond the first) with identity
+    orientations."""
+    t = np.zeros(n, dtype=BODY_SHAPE_DTYPE)
+    t["orientation"][:, 3] = 1.0
+    return t
 
 
 def default_shapes(n):

@@ -192,9 +192,11 @@ int build_hull(const cp_shape_desc& d, Hull& h) {
     std::vector<int> rev(top.rbegin(), top.rend());
     h.faces.push_back(rev);
     h.has_axes = true;
-  } else if (d.type == CP_SHAPE_CONVEX) {
-    if (d.num_vertices < 4 || d.num_faces < 4 || !d.vertices || !d.face_sizes || !d.face_indices)
-      return fail(CP_ERR_ARG, "convex shape needs >= 4 vertices and faces");
+  } else if (d.type == CP_SHAPE_CONVEX || d.type == CP_SHAPE_CAPSULE || d.type == CP_SHAPE_CONE || d.type == CP_SHAPE_SIZED_PLANE) {
+    // Capsule, Cone and SizedPlane: hulls as their constructors built them
+    const bool conv = d.type == CP_SHAPE_CONVEX;
+    if (d.num_vertices < (conv ? 4 : 3) || d.num_faces < (conv ? 4 : 1) || !d.vertices || !d.face_sizes || !d.face_indices)
+      return fail(CP_ERR_ARG, conv ? "convex shape needs >= 4 vertices and faces" : "hull shape needs >= 3 vertices and a face");
     for (int i = 0; i < d.num_vertices; i++) h.verts.push_back(mk3(d.vertices[3 * i], d.vertices[3 * i + 1], d.vertices[3 * i + 2]));
     int off = 0;
     for (int f = 0; f < d.num_faces; f++) {
@@ -889,8 +891,7 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
       o.bsr = shape_bsr(sd, nullptr);
       continue;
     }
-    if (sd.type != CP_SHAPE_BOX && sd.type != CP_SHAPE_CONVEX && sd.type != CP_SHAPE_CYLINDER)
-      return fail(CP_ERR_UNSUPPORTED, "shape type %d", sd.type);
+    if (sd.type < CP_SHAPE_BOX || sd.type > CP_SHAPE_SIZED_PLANE) return fail(CP_ERR_UNSUPPORTED, "shape type %d", sd.type);
     int st = build_hull(sd, h);
     if (st) return st;
     o.bsr = shape_bsr(sd, &h);
@@ -980,12 +981,13 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
   for (int k = 0; k < d->num_constraints; k++) {
     const cp_constraint_desc& cd = d->constraints[k];
     if (cd.body_a < 0 || cd.body_a >= nb || cd.body_b < 0 || cd.body_b >= nb) return fail(CP_ERR_ARG, "constraint %d: bad bodies", k);
-    if (cd.type < CP_CON_POINT_TO_POINT || cd.type > CP_CON_DISTANCE) return fail(CP_ERR_ARG, "constraint %d: type", k);
+    if (cd.type < CP_CON_POINT_TO_POINT || cd.type > CP_CON_SPRING) return fail(CP_ERR_ARG, "constraint %d: type", k);
     DConstraint& o = cons[k];
     std::memset(&o, 0, sizeof(o));
     o.type = cd.type; o.a = cd.body_a; o.b = cd.body_b; o.collide = cd.collide_connected != 0;
     o.row0 = con_rows;
-    o.nrows = cd.type == CP_CON_DISTANCE ? 1 : (cd.type == CP_CON_HINGE ? 6 : 3);
+    static const int kRows[] = {3, 6, 1, 6, 5, 1};  // equations per constraint type
+    o.nrows = kRows[cd.type];
     o.motor = cd.motor_enabled != 0;
     con_rows += o.nrows;
     h3 pa = mk3(cd.pivot_a[0], cd.pivot_a[1], cd.pivot_a[2]), pb = mk3(cd.pivot_b[0], cd.pivot_b[1], cd.pivot_b[2]);
@@ -996,7 +998,13 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
       o.axis_a[0] = aa.x; o.axis_a[1] = aa.y; o.axis_a[2] = aa.z;
       o.axis_b[0] = ab.x; o.axis_b[1] = ab.y; o.axis_b[2] = ab.z;
     }
-    if (cd.type == CP_CON_DISTANCE) {
+    if (cd.type == CP_CON_CONE_TWIST) {  // the axes are cloned as given (cone_twist_constraint.dart:44-45)
+      for (int e = 0; e < 3; e++) { o.axis_a[e] = cd.axis_a[e]; o.axis_b[e] = cd.axis_b[e]; }
+    }
+    if (cd.type == CP_CON_LOCK)
+      for (int v = 0; v < 6; v++)
+        for (int e = 0; e < 3; e++) o.loc[v][e] = cd.lock_axes[v][e];
+    if (cd.type == CP_CON_DISTANCE || cd.type == CP_CON_SPRING) {
       const float* A = d->bodies[cd.body_a].position;
       const float* B = d->bodies[cd.body_b].position;
       double px = B[0], py = B[1], pz = B[2];
@@ -1007,7 +1015,10 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
     o.motor_target = cd.motor_target_velocity;
     o.motor_max_force = cd.motor_max_force > 0 ? cd.motor_max_force : cd.max_force;
     spook(cd.spook_stiffness, cd.spook_relaxation, cd.spook_time_step, o.sa, o.sb, o.seps);
-    o.cos_max = cos_max;
+    // RotationalEquation / ConeEquation: cos(maxAngle) (rotational_equation.dart:51,
+    // cone_equation.dart:46); a cone-twist's cone and twist rows take its angles
+    o.cos_rot[0] = cd.type == CP_CON_CONE_TWIST ? std::cos(cd.angle) : cos_max;
+    o.cos_rot[1] = cd.type == CP_CON_CONE_TWIST ? std::cos(cd.twist_angle) : cos_max;
     if (!o.collide) { nocollide.push_back(cd.body_a); nocollide.push_back(cd.body_b); }
   }
   // bodies

@@ -424,5 +424,9 @@ DI int resolver_kind(int ta, int tb) {  // ta <= tb
     return RK_PC;
   }
   if (ta == 2) return tb == 2 ? RK_BB : RK_BC;
+  // convex + sizedPlane: the reference finds no resolver (its table key is
+  // spelled "convexSizedPlane" but looked up lower-cased,
+  // narrow_phase.dart:444,476-479)
+  if (ta == CP_SHAPE_CONVEX && tb == CP_SHAPE_SIZED_PLANE) return RK_NONE;
   return RK_CC;
 }

@@ -1161,28 +1161,45 @@ DI void constraint_geom(const DWorld& W, int k) {
   DConstraint& cn = W.cons[k];
   const DBody& A = W.bodies[cn.a];
   const DBody& B = W.bodies[cn.b];
-  if (cn.type == CP_CON_DISTANCE) {  // distance_constraint.dart:269-280
+  if (cn.type == CP_CON_DISTANCE || cn.type == CP_CON_SPRING) {
+    // distance_constraint.dart:269-280, spring_constraint.dart:45-57
     double half = cn.distance * 0.5;
     f3 n = normalized(sub(ld3(B.pos), ld3(A.pos)));
     st3(cn.n, n);
     st3(cn.ri, scale(n, half));
     st3(cn.rj, scale(n, -half));
-  } else {  // point_to_point_constraint.dart:122-137, hinge_constraint.dart:217-242
+  } else {  // point_to_point_constraint.dart:122-137 and the subclasses' update()
     q4 qa = ld4q(A.quat), qb = ld4q(B.quat);
     st3(cn.ri, vmult(qa, ld3(cn.piv_a)));
     st3(cn.rj, vmult(qb, ld3(cn.piv_b)));
-    if (cn.type == CP_CON_HINGE) {
+    if (cn.type == CP_CON_HINGE) {  // hinge_constraint.dart:217-242
       f3 wa = vmult(qa, ld3(cn.axis_a));
       f3 wb = vmult(qb, ld3(cn.axis_b));
       f3 t1, t2;
       tangents(wa, t1, t2);
-      st3(cn.r1a, t1);
-      st3(cn.r2a, t2);
-      st3(cn.wb, wb);
+      st3(cn.rot_a[0], t1);
+      st3(cn.rot_a[1], t2);
+      st3(cn.rot_b[0], wb);
+      st3(cn.rot_b[1], wb);
       if (cn.motor) {
         st3(cn.ma, vmult(qa, ld3(cn.axis_a)));
         st3(cn.mb, vmult(qb, ld3(cn.axis_b)));
       }
+    } else if (cn.type == CP_CON_LOCK) {  // lock_constraint.dart:86-103: (xA, yB), (yA, zB), (zA, xB)
+#pragma unroll
+      for (int r = 0; r < 3; r++) {
+        st3(cn.rot_a[r], vmult(qa, ld3(cn.loc[2 * r])));
+        st3(cn.rot_b[r], vmult(qb, ld3(cn.loc[(2 * r + 3) % 6])));
+      }
+    } else if (cn.type == CP_CON_CONE_TWIST) {  // cone_twist_constraint.dart:77-96
+      st3(cn.rot_a[0], vmult(qa, ld3(cn.axis_a)));
+      st3(cn.rot_b[0], vmult(qb, ld3(cn.axis_b)));
+      // axis.tangents(t, t) leaves the second tangent in t
+      f3 t1, t2a, t2b;
+      tangents(ld3(cn.axis_a), t1, t2a);
+      tangents(ld3(cn.axis_b), t1, t2b);
+      st3(cn.rot_a[1], vmult(qa, t2a));
+      st3(cn.rot_b[1], vmult(qb, t2b));
     }
   }
 }
@@ -1381,29 +1398,33 @@ DI void assemble_constraint_rows(const DWorld& W, int k, int base0, int ncand, i
   RowGeom G;
   G.bi = cn.a; G.bj = cn.b;
   G.a = cn.sa; G.b = cn.sb; G.eps = cn.seps;
-  G.minF = -cn.max_force; G.maxF = cn.max_force;
   G.restitution = 0.0;
-  G.cos_max = cn.cos_max;
   G.target = cn.motor_target;
   for (int r = 0; r < cn.nrows; r++) {
     int cd = base + r;
     if (!cand_kept(W, cd, ncand, nrows)) continue;
-    if (cn.type == CP_CON_DISTANCE) {
+    G.minF = -cn.max_force; G.maxF = cn.max_force;
+    G.cos_max = cn.cos_rot[0];
+    if (cn.type == CP_CON_DISTANCE || cn.type == CP_CON_SPRING) {
       G.kind = CP_ROW_CONTACT;
       G.ri = ld3(cn.ri); G.rj = ld3(cn.rj); G.n = ld3(cn.n);
     } else if (r < 3) {
       G.kind = CP_ROW_CONTACT;
       G.ri = ld3(cn.ri); G.rj = ld3(cn.rj);
       G.n = r == 0 ? f3{1.f, 0.f, 0.f} : (r == 1 ? f3{0.f, 1.f, 0.f} : f3{0.f, 0.f, 1.f});
-    } else if (r < 5) {
-      G.kind = CP_ROW_ROTATIONAL;
-      G.axA = ld3(r == 3 ? cn.r1a : cn.r2a);
-      G.axB = ld3(cn.wb);
-    } else {
+    } else if (cn.type == CP_CON_HINGE && r == 5) {
       G.kind = CP_ROW_MOTOR;
       G.axA = ld3(cn.ma);
       G.axB = ld3(cn.mb);
       G.minF = -cn.motor_max_force; G.maxF = cn.motor_max_force;
+    } else {
+      G.kind = CP_ROW_ROTATIONAL;
+      G.axA = ld3(cn.rot_a[r - 3]);
+      G.axB = ld3(cn.rot_b[r - 3]);
+      if (cn.type == CP_CON_CONE_TWIST) {  // both rows push one way: [-maxForce, 0]
+        G.maxF = 0.0;
+        if (r == 4) G.cos_max = cn.cos_rot[1];
+      }
     }
     DRow& R = W.rows[W.cand[cd]];
     assemble_row(W, G, R, h);

@@ -105,11 +105,17 @@ struct __align__(16) DConstraint {
   int type, a, b, collide;
   int row0, nrows, motor, pad;
   float piv_a[4], piv_b[4], axis_a[4], axis_b[4];
+  float loc[6][4];  // LockConstraint local axes xA, xB, yA, yB, zA, zB
   double distance, max_force, motor_target, motor_max_force;
-  double sa, sb, seps, cos_max;  // SPOOK params of the constraint rows; cos(maxAngle) from libm
+  double sa, sb, seps;  // SPOOK params of the constraint rows
+  // cos(maxAngle) of the rotational rows, from libm: rows 0-2 take cos_rot[0]
+  // (a cone-twist's twist row takes cos_rot[1])
+  double cos_rot[2];
+  double pad2;
   // per-step geometry
   float ri[4], rj[4], n[4];
-  float r1a[4], r2a[4], wb[4], ma[4], mb[4];
+  float rot_a[3][4], rot_b[3][4];  // world axes (axisA, axisB) of the rotational rows
+  float ma[4], mb[4];              // motor axes
 };
 
 struct __align__(16) DContact {

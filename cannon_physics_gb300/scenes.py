@@ -433,6 +433,266 @@ def compound_pile(n=40, seed=31, broadphase=A.BROAD_NAIVE, kinematic=True, pitch
     return sc
 
 
+# ---------------------------------------------------------------------------
+# hulls of the ConvexPolyhedron subclasses with their own ShapeType, built as
+# their constructors build them (vertices in binary32, faces, uniqueAxes)
+
+
+def cone_hull(radius=1.0, height=1.0, num_segments=8):
+    """Cone (lib/rigid_body_shapes/cone.dart:15-64): apex, base ring, side
+    triangles and the base face; uniqueAxes [(0, 1, 0)]."""
+    n = num_segments
+    verts = [(0.0, height * 0.5, 0.0), (-radius * math.sin(0), -height * 0.5, radius * math.cos(0))]
+    faces, bottom = [], [1]
+    for i in range(n):
+        theta = ((2 * math.pi) / n) * (i + 1)
+        if i < n - 1:
+            verts.append((-radius * math.sin(theta), -height * 0.5, radius * math.cos(theta)))
+            bottom.append(i + 2)
+            faces.append([0, i + 2, i + 1])
+        else:
+            faces.append([0, 1, i + 1])
+    faces.append(bottom)
+    return np.array(verts, np.float32), faces, np.array([(0.0, 1.0, 0.0)], np.float32)
+
+
+def sized_plane_hull(width=1.0, height=1.0):
+    """SizedPlane (lib/rigid_body_shapes/sized_plane.dart:19-37): one face at y = 0."""
+    sx, sy, sz = width / 2, 0.0, height / 2
+    verts = [(-sx, sy, -sz), (sx, sy, -sz), (sx, sy, sz), (-sx, sy, sz)]
+    return np.array(verts, np.float32), [[3, 2, 1, 0]], None
+
+
+def capsule_hull(radius_top=1.0, radius_bottom=1.0, height=1.0, num_segments=8, num_height_segments=4):
+    """Capsule (lib/rigid_body_shapes/capsule.dart:27-170): the cylinder's
+    side walls, then two hemisphere grids, both drawn with radiusTop as the
+    constructor draws them; no uniqueAxes."""
+    rt, rb, h = radius_top, radius_bottom, height
+    ns, nh = num_segments, num_height_segments
+    verts = [(-rb * math.sin(0), -h * 0.5, rb * math.cos(0)), (-rt * math.sin(0), h * 0.5, rt * math.cos(0))]
+    faces, top, bottom, grid = [], [], [], []
+    index = 0
+    phi_start, phi_length, theta_start, theta_length = math.pi, 2 * math.pi, math.pi / 2, math.pi / 2
+    for iy in range(nh + 1):
+        row = []
+        v = iy / nh
+        for ix in range(ns + 1):
+            ub = ix / ns
+            ut = (ns - ix) / ns
+            if iy == 0 and ix < ns:
+                theta = ((2 * math.pi) / ns) * (ix + 1)
+                if ix < ns - 1:
+                    verts.append((-rb * math.sin(theta), -h * 0.5, rb * math.cos(theta)))
+                    verts.append((-rt * math.sin(theta), h * 0.5, rt * math.cos(theta)))
+                    faces.append([2 * ix, 2 * ix + 1, 2 * ix + 3, 2 * ix + 2])
+                else:
+                    faces.append([2 * ix, 2 * ix + 1, 1, 0])
+            st = math.sin(theta_start + v * theta_length)
+            ct = math.cos(theta_start + v * theta_length)
+            top.append((-rt * math.cos(phi_start + ut * phi_length) * st, h * 0.5 - rt * ct,
+                        rt * math.sin(phi_start + ut * phi_length) * st))
+            bottom.append((-rt * math.cos(phi_start + ub * phi_length) * st, -h * 0.5 + rt * ct,
+                           rt * math.sin(phi_start + ub * phi_length) * st))
+            row.append(index)
+            index += 1
+        grid.append(row)
+    s1 = len(verts)
+    s2 = s1 + len(top)
+    for iy in range(nh):
+        for ix in range(ns):
+            for s in (s1, s2):
+                a, b = grid[iy][ix + 1] + s, grid[iy][ix] + s
+                c, d = grid[iy + 1][ix] + s, grid[iy + 1][ix + 1] + s
+                faces.append([a, b, d])
+                faces.append([b, c, d])
+    verts += top + bottom
+    return np.array(verts, np.float32), faces, None
+
+
+def set_hull(shape, kind, hull, keep):
+    """Point shape record `shape` at hull (vertices, faces, axes or None) as a
+    shape of type `kind`; the arrays are appended to `keep`."""
+    v, faces, axes = hull
+    sizes = np.array([len(f) for f in faces], np.int32)
+    flat = np.array([k for f in faces for k in f], np.int32)
+    v = np.ascontiguousarray(v, np.float32)
+    keep += [v, sizes, flat]
+    shape["type"] = kind
+    shape["num_vertices"] = len(v)
+    shape["num_faces"] = len(faces)
+    shape["vertices"] = v.ctypes.data
+    shape["face_sizes"] = sizes.ctypes.data
+    shape["face_indices"] = flat.ctypes.data
+    if axes is not None:
+        axes = np.ascontiguousarray(axes, np.float32)
+        keep.append(axes)
+        shape["has_axes"] = 1
+        shape["num_axes"] = len(axes)
+        shape["axes"] = axes.ctypes.data
+    else:
+        shape["has_axes"] = 0
+        shape["num_axes"] = 0
+
+
+# ---------------------------------------------------------------------------
+# constraint records as the reference's constructors leave them
+
+
+def _f32(x):
+    return float(np.float32(x))
+
+
+def _vmult(q, v):
+    """Quaternion.vmult (lib/math/quaternion.dart:21-44): binary64 arithmetic,
+    binary32 result."""
+    x, y, z = (float(c) for c in v)
+    qx, qy, qz, qw = (float(c) for c in q)
+    ix = qw * x + qy * z - qz * y
+    iy = qw * y + qz * x - qx * z
+    iz = qw * z + qx * y - qy * x
+    iw = -qx * x - qy * y - qz * z
+    return (_f32(ix * qw + iw * -qx + iy * -qz - iz * -qy), _f32(iy * qw + iw * -qy + iz * -qx - ix * -qz),
+            _f32(iz * qw + iw * -qz + ix * -qy - iy * -qx))
+
+
+def _conj(q):
+    return (-float(q[0]), -float(q[1]), -float(q[2]), float(q[3]))
+
+
+def lock_frames(pos_a, quat_a, pos_b, quat_b):
+    """LockConstraint's constructor (lib/constraints/lock_constraint.dart:26-76):
+    returns pivot_a, pivot_b and (xA, xB, yA, yB, zA, zB).  Body.pointToLocalFrame
+    and vectorToLocalFrame (rigid_body.dart:317-329) conjugate the body's own
+    quaternion in place before rotating, so successive calls alternate between
+    the conjugate and the quaternion itself: the pivots and yA, yB use the
+    conjugates, xA, xB, zA, zB the quaternions (each body ends as it began)."""
+    half = tuple(_f32(_f32(float(a) + float(b)) * 0.5) for a, b in zip(pos_a, pos_b))
+    rel_b = tuple(_f32(h - float(p)) for h, p in zip(half, pos_b))
+    rel_a = tuple(_f32(h - float(p)) for h, p in zip(half, pos_a))
+    qa, qb = _conj(quat_a), _conj(quat_b)
+    pivot_b = _vmult(qb, rel_b)
+    pivot_a = _vmult(qa, rel_a)
+    ex, ey, ez = (1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 1.0)
+    axes = []
+    for e in (ex, ey, ez):
+        qa, qb = _conj(qa), _conj(qb)
+        axes.append(_vmult(qa, e))
+        axes.append(_vmult(qb, e))
+    return pivot_a, pivot_b, axes
+
+
+def _con(rec, kind, a, b, max_force=1e6, collide=1):
+    rec["type"] = kind
+    rec["body_a"] = a
+    rec["body_b"] = b
+    rec["collide_connected"] = collide
+    rec["distance"] = -1.0
+    rec["max_force"] = max_force
+    rec["spook_stiffness"] = 1e7
+    rec["spook_relaxation"] = 4.0
+    rec["spook_time_step"] = 1.0 / 60.0
+
+
+def joints_and_hulls(n_chains=4, seed=41, broadphase=A.BROAD_NAIVE):
+    """Chains of boxes, cones and capsules joined by LockConstraints,
+    ConeTwistConstraints and SpringConstraints in turn, hanging from static
+    anchors above a Plane and SizedPlane tiles, and loose spheres, boxes,
+    cones, capsules and ConvexPolyhedron pyramids dropped onto the tiles (a
+    pyramid finds no resolver against a SizedPlane and falls through to the
+    plane); the chains swing into each other and onto the tiles."""
+    rng = SplitMix64(seed)
+    keep = []
+    per = 5
+    loose = 10
+    n = 1 + 4 + n_chains * (per + 1) + loose
+    shapes = A.default_shapes(n)
+    bodies = A.default_bodies(n)
+    _plane_body(bodies, shapes, 0, 0)
+    i = 1
+    for t in range(4):  # SizedPlane tiles: static, tilted a little
+        set_hull(shapes[i], A.SHAPE_SIZED_PLANE, sized_plane_hull(2.4, 1.6), keep)
+        bodies[i]["mass"] = 0.0
+        bodies[i]["position"] = ((t - 1.5) * 2.6, 0.3 + 0.1 * t, 0.4)
+        bodies[i]["quaternion"] = euler_xyz(0.15 * (t - 1.5), 0.0, 0.1)
+        bodies[i]["shape"] = i
+        i += 1
+    cons = np.zeros(n_chains * per, dtype=A.CONSTRAINT_DTYPE)
+    c = 0
+    u = rng.uniform(4 * n).reshape(n, 4)
+    for ch in range(n_chains):
+        x0 = (ch - (n_chains - 1) / 2) * 1.7
+        anchor = i
+        shapes[i]["type"] = A.SHAPE_SPHERE
+        shapes[i]["radius"] = 0.1
+        bodies[i]["mass"] = 0.0
+        bodies[i]["position"] = (x0, 2.2, 0.0)
+        bodies[i]["shape"] = i
+        i += 1
+        for k in range(per):
+            kind = (ch + k) % 3
+            if kind == 0:
+                shapes[i]["type"] = A.SHAPE_BOX
+                shapes[i]["half_extents"] = (0.2, 0.25, 0.15)
+            elif kind == 1:
+                set_hull(shapes[i], A.SHAPE_CONE, cone_hull(0.25, 0.5, 6 + ch % 3), keep)
+            else:
+                set_hull(shapes[i], A.SHAPE_CAPSULE, capsule_hull(0.15, 0.15, 0.3, 3, 1), keep)
+            bodies[i]["mass"] = 0.5 + 0.5 * u[i, 0]
+            bodies[i]["position"] = (x0 + 0.3 * (k + 1) + 0.05 * u[i, 1], 2.2 - 0.1 * (k + 1), 0.05 * u[i, 2])
+            bodies[i]["quaternion"] = euler_xyz(0.2 * u[i, 3], 0.1 * k, 0.0)
+            bodies[i]["shape"] = i
+            prev = anchor if k == 0 else i - 1
+            rec = cons[c]
+            jt = (ch + k) % 3
+            if jt == 0:
+                _con(rec, A.CON_LOCK, prev, i, max_force=1e6)
+                pa, pb, axes = lock_frames(bodies[prev]["position"], bodies[prev]["quaternion"], bodies[i]["position"],
+                                           bodies[i]["quaternion"])
+                rec["pivot_a"], rec["pivot_b"] = pa, pb
+                rec["lock_axes"] = axes
+            elif jt == 1:
+                _con(rec, A.CON_CONE_TWIST, prev, i, max_force=1e6)
+                rec["pivot_a"] = (0.15, -0.05, 0.0)
+                rec["pivot_b"] = (-0.15, 0.05, 0.0)
+                rec["axis_a"] = (1.0, 0.0, 0.0)
+                rec["axis_b"] = (1.0, 0.0, 0.0)
+                rec["angle"] = 0.3 + 0.2 * (ch % 2)
+                rec["twist_angle"] = 0.2 + 0.1 * k
+            else:
+                _con(rec, A.CON_SPRING, prev, i, max_force=30.0 + 10.0 * k)
+            c += 1
+            i += 1
+    pyramid = (np.array([(-0.2, 0.0, -0.2), (0.2, 0.0, -0.2), (0.2, 0.0, 0.2), (-0.2, 0.0, 0.2), (0.0, 0.3, 0.0)],
+                        np.float32), [[3, 2, 1, 0], [0, 1, 4], [1, 2, 4], [2, 3, 4], [3, 0, 4]], None)
+    for k in range(loose):
+        kind = k % 5
+        if kind == 0:
+            shapes[i]["type"] = A.SHAPE_SPHERE
+            shapes[i]["radius"] = 0.2
+        elif kind == 1:
+            shapes[i]["type"] = A.SHAPE_BOX
+            shapes[i]["half_extents"] = (0.2, 0.15, 0.25)
+        elif kind == 2:
+            set_hull(shapes[i], A.SHAPE_CONE, cone_hull(0.2, 0.4, 8), keep)
+        elif kind == 3:
+            set_hull(shapes[i], A.SHAPE_CAPSULE, capsule_hull(0.12, 0.12, 0.3, 3, 1), keep)
+        else:
+            set_hull(shapes[i], A.SHAPE_CONVEX, pyramid, keep)
+        bodies[i]["mass"] = 0.4 + 0.4 * u[i, 0]
+        bodies[i]["position"] = ((k % 4 - 1.5) * 2.6 + 0.4 * u[i, 1], 0.9 + 0.5 * (k // 4), 0.4 + 0.3 * u[i, 2])
+        bodies[i]["quaternion"] = shoemake(u[i:i + 1, 3], u[i:i + 1, 1], u[i:i + 1, 2])[0]
+        bodies[i]["shape"] = i
+        i += 1
+    sc = Scene("joints_and_hulls", shapes, bodies, constraints=cons[:c], friction=0.3, restitution=0.0, iterations=12,
+               broadphase=broadphase, dt=1 / 60, steps=200)
+    sc._keep = keep
+    if broadphase == A.BROAD_GRID:
+        sc.grid_n = (6, 3, 2)
+        sc.grid_min = (-5.0, -1.0, -2.0)
+        sc.grid_max = (5.0, 5.0, 2.0)
+    return sc
+
+
 def batch_sizes(n_worlds=4096, seed=1000, lo=8, hi=512):
     """Body counts floor(exp(U[ln lo, ln hi])) of the batched workload, one
     SplitMix64 stream per world (seed+w)."""

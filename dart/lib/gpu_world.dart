@@ -132,6 +132,12 @@ class GpuWorld extends World {
         return cpShapeConvex;
       case ShapeType.cylinder:
         return cpShapeCylinder;
+      case ShapeType.capsule:
+        return cpShapeCapsule;
+      case ShapeType.cone:
+        return cpShapeCone;
+      case ShapeType.sizedPlane:
+        return cpShapeSizedPlane;
       default:
         throw UnsupportedError('GpuWorld: shape type ${s.type} is not on the GPU path');
     }
@@ -357,7 +363,33 @@ class GpuWorld extends World {
     d.spookRelaxation = eq.relaxation;
     d.spookTimeStep = 1 / 60;
     d.maxForce = eq.maxForce;
-    if (c is HingeConstraint) {
+    if (c is LockConstraint) {
+      // the local frames the constructor stored (lock_constraint.dart:26-76)
+      d.type = cpConLock;
+      _set3(d.pivotA, c.pivotA);
+      _set3(d.pivotB, c.pivotB);
+      final axes = [c.xA, c.xB, c.yA, c.yB, c.zA, c.zB];
+      for (var v = 0; v < 6; v++) {
+        d.lockAxes[v][0] = axes[v].x;
+        d.lockAxes[v][1] = axes[v].y;
+        d.lockAxes[v][2] = axes[v].z;
+      }
+    } else if (c is ConeTwistConstraint) {
+      d.type = cpConConeTwist;
+      _set3(d.pivotA, c.pivotA);
+      _set3(d.pivotB, c.pivotB);
+      _set3(d.axisA, c.axisA);
+      _set3(d.axisB, c.axisB);
+      d.angle = c.angle;
+      d.twistAngle = c.twistAngle;
+    } else if (c is SpringConstraint) {
+      // rest length: the bodies' distance when the world is uploaded (the
+      // constructor's value is private to the reference library); the row's
+      // force bound is the stiffness
+      d.type = cpConSpring;
+      d.distance = -1;
+      d.maxForce = c.stiffness;
+    } else if (c is HingeConstraint) {
       d.type = cpConHinge;
       _set3(d.pivotA, c.pivotA);
       _set3(d.pivotB, c.pivotB);

@@ -6,7 +6,7 @@
 // only during the call.
 import 'dart:ffi';
 
-const int cpAbiVersion = 3;
+const int cpAbiVersion = 4;
 
 const int cpOk = 0;
 const int cpErrArg = 1;
@@ -18,8 +18,10 @@ const int cpErrCuda = 6;
 const int cpErrUnsupported = 7;
 
 const int cpShapeSphere = 0, cpShapePlane = 1, cpShapeBox = 2, cpShapeConvex = 3, cpShapeCylinder = 4;
+const int cpShapeCapsule = 5, cpShapeCone = 6, cpShapeSizedPlane = 7;
 const int cpBroadNaive = 0, cpBroadSap = 1, cpBroadGrid = 2;
 const int cpConPointToPoint = 0, cpConHinge = 1, cpConDistance = 2;
+const int cpConLock = 3, cpConConeTwist = 4, cpConSpring = 5;
 
 final class CpShapeDesc extends Struct {
   @Int32() external int type;
@@ -146,6 +148,9 @@ final class CpConstraintDesc extends Struct {
   @Double() external double spookStiffness;
   @Double() external double spookRelaxation;
   @Double() external double spookTimeStep;
+  @Array(6, 3) external Array<Array<Float>> lockAxes;
+  @Double() external double angle;
+  @Double() external double twistAngle;
 }
 
 final class CpWorldDesc extends Struct {

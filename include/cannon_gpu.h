@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define CP_ABI_VERSION 3
+#define CP_ABI_VERSION 4
 
 /* status codes */
 #define CP_OK               0
@@ -50,7 +50,10 @@ enum cp_shape_type {
   CP_SHAPE_PLANE = 1,
   CP_SHAPE_BOX = 2,
   CP_SHAPE_CONVEX = 3,
-  CP_SHAPE_CYLINDER = 4
+  CP_SHAPE_CYLINDER = 4,
+  CP_SHAPE_CAPSULE = 5,             /* Capsule, Cone and SizedPlane are ConvexPolyhedrons with */
+  CP_SHAPE_CONE = 6,                /* their own ShapeType: their hulls are given as for CONVEX */
+  CP_SHAPE_SIZED_PLANE = 7
 };
 
 /* BodyTypes / BodySleepStates, lib/objects/rigid_body.dart:15-16 */
@@ -64,15 +67,24 @@ enum cp_sleep_state { CP_AWAKE = 0, CP_SLEEPY = 1, CP_SLEEPING = 2 };
 enum cp_broadphase_kind { CP_BROAD_NAIVE = 0, CP_BROAD_SAP = 1, CP_BROAD_GRID = 2 };
 
 /* Constraint classes, lib/constraints/*.dart */
-enum cp_constraint_type { CP_CON_POINT_TO_POINT = 0, CP_CON_HINGE = 1, CP_CON_DISTANCE = 2 };
+enum cp_constraint_type {
+  CP_CON_POINT_TO_POINT = 0,
+  CP_CON_HINGE = 1,
+  CP_CON_DISTANCE = 2,
+  CP_CON_LOCK = 3,                  /* lock_constraint.dart */
+  CP_CON_CONE_TWIST = 4,            /* cone_twist_constraint.dart */
+  CP_CON_SPRING = 5                 /* spring_constraint.dart */
+};
 
 /* Equation classes appearing as solver rows, lib/equations/*.dart */
 enum cp_row_kind { CP_ROW_CONTACT = 0, CP_ROW_FRICTION = 1, CP_ROW_ROTATIONAL = 2, CP_ROW_MOTOR = 3 };
 
-/* Shape (lib/rigid_body_shapes/{sphere,plane,box,convex_polyhedron,cylinder}.dart).
- * A CONVEX shape lists its hull: `vertices` (3 floats each), `face_sizes`
- * (vertex count per face) and `face_indices` (concatenated faces); `axes`
- * (3 floats each) is the optional `uniqueAxes` list (has_axes=0 means null). */
+/* Shape (lib/rigid_body_shapes/{sphere,plane,box,convex_polyhedron,cylinder,
+ * capsule,cone,sized_plane}.dart).  A CONVEX, CAPSULE, CONE or SIZED_PLANE
+ * shape lists its hull as the reference's constructor built it: `vertices`
+ * (3 floats each), `face_sizes` (vertex count per face) and `face_indices`
+ * (concatenated faces); `axes` (3 floats each) is the optional `uniqueAxes`
+ * list (has_axes=0 means null).  A Lathe is a CONVEX shape. */
 typedef struct cp_shape_desc {
   int32_t type;
   int32_t collision_filter_group;   /* Shape default -1 */
@@ -174,10 +186,21 @@ typedef struct cp_contact_material {
   double friction_stiffness, friction_relaxation;
 } cp_contact_material;
 
-/* PointToPoint / Hinge / Distance constraint (lib/constraints/*.dart).
- * spook_* are the Equation SPOOK parameters of the constraint rows; the
- * reference constructor uses (1e7, 4, 1/60) whatever the step size
- * (lib/equations/equation_class.dart:38). */
+/* Constraint (lib/constraints/*.dart).  spook_* are the Equation SPOOK
+ * parameters of the constraint rows; the reference constructor uses
+ * (1e7, 4, 1/60) whatever the step size (lib/equations/equation_class.dart:38).
+ * The local vectors are those the reference's constructor stored:
+ *   POINT_TO_POINT  pivot_a, pivot_b; rows x, y, z
+ *   HINGE           + axis_a, axis_b (normalised here); rows x, y, z, two
+ *                   rotational, motor
+ *   DISTANCE        distance (<0: the bodies' current distance); one row
+ *   LOCK            pivot_a, pivot_b and lock_axes = xA, xB, yA, yB, zA, zB;
+ *                   rows x, y, z, rotational (xA, yB), (yA, zB), (zA, xB)
+ *   CONE_TWIST      pivot_a, pivot_b, axis_a, axis_b, angle, twist_angle;
+ *                   rows x, y, z, cone, twist
+ *   SPRING          distance = the rest length, max_force = the stiffness
+ *                   (the row's force bound); one row
+ */
 typedef struct cp_constraint_desc {
   int32_t type, body_a, body_b, collide_connected;
   int32_t motor_enabled, pad0;
@@ -187,6 +210,8 @@ typedef struct cp_constraint_desc {
   double max_force;
   double motor_target_velocity, motor_max_force;
   double spook_stiffness, spook_relaxation, spook_time_step;
+  float lock_axes[6][3];            /* LockConstraint xA, xB, yA, yB, zA, zB */
+  double angle, twist_angle;        /* ConeTwistConstraint */
 } cp_constraint_desc;
 
 /* World (lib/world/world_class.dart:135-162) plus solver/broadphase settings. */

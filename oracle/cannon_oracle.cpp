@@ -377,8 +377,13 @@ static int buildShape(const cp_shape_desc& d, Shape& s) {
       s.bsr = std::sqrt(max2);
       break;
     }
-    case CP_SHAPE_CONVEX: {
-      if (d.num_vertices < 4 || d.num_faces < 4 || !d.vertices || !d.face_sizes || !d.face_indices) return CP_ERR_ARG;
+    case CP_SHAPE_CONVEX:
+    case CP_SHAPE_CAPSULE:       // capsule.dart, cone.dart, sized_plane.dart: their
+    case CP_SHAPE_CONE:          // constructors build the vertices and faces, then
+    case CP_SHAPE_SIZED_PLANE: {  // ConvexPolyhedron.init as for any hull
+      const bool conv = d.type == CP_SHAPE_CONVEX;
+      if (d.num_vertices < (conv ? 4 : 3) || d.num_faces < (conv ? 4 : 1) || !d.vertices || !d.face_sizes || !d.face_indices)
+        return CP_ERR_ARG;
       for (int i = 0; i < d.num_vertices; i++) h.vertices.push_back(mk(d.vertices[3 * i], d.vertices[3 * i + 1], d.vertices[3 * i + 2]));
       int off = 0;
       for (int f = 0; f < d.num_faces; f++) {
@@ -683,8 +688,11 @@ struct Constraint {
   int bodyA = 0, bodyB = 0;
   bool collideConnected = true;
   V3 pivotA, pivotB, axisA, axisB;
+  V3 xA, xB, yA, yB, zA, zB;  // LockConstraint's local axes (lock_constraint.dart:41-46)
   double distance = 0;
-  std::vector<Eq> eqs;  // p2p: x,y,z; hinge: x,y,z,rot1,rot2,motor; distance: one contact
+  // p2p: x,y,z; hinge: x,y,z,rot1,rot2,motor; lock: x,y,z,rot1,rot2,rot3;
+  // cone-twist: x,y,z,cone,twist; distance / spring: one contact
+  std::vector<Eq> eqs;
 };
 
 // OverlapKeeper (lib/collision/overlap_keeper.dart): a sorted list of pair
@@ -1535,6 +1543,9 @@ struct World {
       }
     }
   }
+  // a ConvexPolyhedron with a resolver row of its own type: Convex, Cylinder,
+  // Capsule, Cone, SizedPlane (narrow_phase.dart:130-168)
+  static bool isHull(int t) { return t >= CP_SHAPE_CONVEX && t <= CP_SHAPE_SIZED_PLANE; }
   // narrow_phase.dart:116-238 (resolver table); rsi/rsj are the shapes in
   // getContacts order, passed through unchanged as in :707-709.
   // shA / shB: the indices of shapes a / b (type order)
@@ -1544,13 +1555,16 @@ struct World {
     if (ta == CP_SHAPE_SPHERE && tb == CP_SHAPE_SPHERE) sphereSphere(a, b, xa, xb, ba, bb, rsi, rsj);
     else if (ta == CP_SHAPE_SPHERE && tb == CP_SHAPE_PLANE) spherePlane(a, b, xa, xb, qb, ba, bb, rsi, rsj);
     else if (ta == CP_SHAPE_SPHERE && tb == CP_SHAPE_BOX) sphereBox(a, b, xa, xb, qb, ba, bb, rsi, rsj);
-    else if (ta == CP_SHAPE_SPHERE && (tb == CP_SHAPE_CONVEX || tb == CP_SHAPE_CYLINDER)) sphereConvex(a, b, xa, xb, qb, ba, bb, rsi, rsj);
+    else if (ta == CP_SHAPE_SPHERE && isHull(tb)) sphereConvex(a, b, xa, xb, qb, ba, bb, rsi, rsj);
     // planeBox / boxBox / boxConvex pass their own (type-ordered) shapes on
     else if (ta == CP_SHAPE_PLANE && tb == CP_SHAPE_BOX) planeConvex(a, b, xa, xb, qa, qb, ba, bb, shA, shB);
-    else if (ta == CP_SHAPE_PLANE && (tb == CP_SHAPE_CONVEX || tb == CP_SHAPE_CYLINDER)) planeConvex(a, b, xa, xb, qa, qb, ba, bb, rsi, rsj);
+    else if (ta == CP_SHAPE_PLANE && isHull(tb)) planeConvex(a, b, xa, xb, qa, qb, ba, bb, rsi, rsj);
     else if (ta == CP_SHAPE_BOX && tb == CP_SHAPE_BOX) convexConvex(a, b, xa, xb, qa, qb, ba, bb, shA, shB);
-    else if (ta == CP_SHAPE_BOX && (tb == CP_SHAPE_CONVEX || tb == CP_SHAPE_CYLINDER)) convexConvex(a, b, xa, xb, qa, qb, ba, bb, shA, shB);
-    else if ((ta == CP_SHAPE_CONVEX || ta == CP_SHAPE_CYLINDER) && (tb == CP_SHAPE_CONVEX || tb == CP_SHAPE_CYLINDER)) convexConvex(a, b, xa, xb, qa, qb, ba, bb, rsi, rsj);
+    else if (ta == CP_SHAPE_BOX && isHull(tb)) convexConvex(a, b, xa, xb, qa, qb, ba, bb, shA, shB);
+    // convex + sizedPlane finds no resolver: its table key is spelled
+    // "convexSizedPlane" but looked up lower-cased (narrow_phase.dart:444,476-479)
+    else if (isHull(ta) && isHull(tb) && !(ta == CP_SHAPE_CONVEX && tb == CP_SHAPE_SIZED_PLANE))
+      convexConvex(a, b, xa, xb, qa, qb, ba, bb, rsi, rsj);
     // plane-plane: no resolver
   }
 
@@ -1715,7 +1729,7 @@ struct World {
   void updateConstraint(Constraint& c) {
     Body& A = bodies[c.bodyA];
     Body& B = bodies[c.bodyB];
-    if (c.type == CP_CON_DISTANCE) {
+    if (c.type == CP_CON_DISTANCE || c.type == CP_CON_SPRING) {  // spring_constraint.dart:45-57 is the same
       Eq& eq = c.eqs[0];
       double halfDist = c.distance * 0.5;
       sub2(B.position, A.position, eq.ni);
@@ -1739,6 +1753,24 @@ struct World {
         vmult(A.quaternion, c.axisA, motor.axisA);
         vmult(B.quaternion, c.axisB, motor.axisB);
       }
+    } else if (c.type == CP_CON_LOCK) {  // lock_constraint.dart:86-103
+      Eq &r1 = c.eqs[3], &r2 = c.eqs[4], &r3 = c.eqs[5];
+      vmult(A.quaternion, c.xA, r1.axisA);
+      vmult(B.quaternion, c.yB, r1.axisB);
+      vmult(A.quaternion, c.yA, r2.axisA);
+      vmult(B.quaternion, c.zB, r2.axisB);
+      vmult(A.quaternion, c.zA, r3.axisA);
+      vmult(B.quaternion, c.xB, r3.axisB);
+    } else if (c.type == CP_CON_CONE_TWIST) {  // cone_twist_constraint.dart:77-96
+      Eq &cone = c.eqs[3], &twist = c.eqs[4];
+      vmult(A.quaternion, c.axisA, cone.axisA);
+      vmult(B.quaternion, c.axisB, cone.axisB);
+      // axisA.tangents(twist.axisA, twist.axisA): both tangents land in one
+      // vector, the second (cross2 reads its argument before writing)
+      tangents(c.axisA, twist.axisA, twist.axisA);
+      vmult(A.quaternion, twist.axisA, twist.axisA);
+      tangents(c.axisB, twist.axisB, twist.axisB);
+      vmult(B.quaternion, twist.axisB, twist.axisB);
     }
   }
 
@@ -1998,7 +2030,11 @@ static int buildWorld(const cp_world_desc& d, World& w) {
       return e;
     };
     double mf = cd.max_force;
-    if (cd.type == CP_CON_DISTANCE) {
+    if (cd.type < CP_CON_POINT_TO_POINT || cd.type > CP_CON_SPRING) return CP_ERR_ARG;
+    if (cd.type == CP_CON_DISTANCE || cd.type == CP_CON_SPRING) {
+      // DistanceConstraint (distance_constraint.dart); SpringConstraint
+      // (spring_constraint.dart:26-42): rest length, one ContactEquation
+      // bounded by +-stiffness
       V3 pa = w.bodies[cd.body_a].position, pb = w.bodies[cd.body_b].position;
       c.distance = cd.distance >= 0 ? cd.distance : distanceTo(pa, pb);
       c.eqs.push_back(newEq(CP_ROW_CONTACT, -mf, mf));
@@ -2016,6 +2052,24 @@ static int buildWorld(const cp_world_desc& d, World& w) {
         motor.targetVelocity = cd.motor_target_velocity;
         if (cd.motor_max_force > 0) { motor.maxForce = cd.motor_max_force; motor.minForce = -cd.motor_max_force; }
         c.eqs.push_back(r1); c.eqs.push_back(r2); c.eqs.push_back(motor);
+      } else if (cd.type == CP_CON_LOCK) {  // lock_constraint.dart:26-76
+        V3* loc[6] = {&c.xA, &c.xB, &c.yA, &c.yB, &c.zA, &c.zB};
+        for (int v = 0; v < 6; v++) *loc[v] = mk(cd.lock_axes[v][0], cd.lock_axes[v][1], cd.lock_axes[v][2]);
+        for (int r = 0; r < 3; r++) {
+          Eq e = newEq(CP_ROW_ROTATIONAL, -mf, mf);
+          e.cosMaxAngle = cosHalfPi;
+          c.eqs.push_back(e);
+        }
+      } else if (cd.type == CP_CON_CONE_TWIST) {  // cone_twist_constraint.dart:26-73
+        c.axisA = mk(cd.axis_a[0], cd.axis_a[1], cd.axis_a[2]);
+        c.axisB = mk(cd.axis_b[0], cd.axis_b[1], cd.axis_b[2]);
+        // ConeEquation / RotationalEquation built with maxForce 0 (bounds
+        // [-0, 0]), then minForce = -maxForce
+        Eq cone = newEq(CP_ROW_ROTATIONAL, -mf, 0.0);
+        cone.cosMaxAngle = std::cos(cd.angle);
+        Eq twist = newEq(CP_ROW_ROTATIONAL, -mf, 0.0);
+        twist.cosMaxAngle = std::cos(cd.twist_angle);
+        c.eqs.push_back(cone); c.eqs.push_back(twist);
       }
     }
     w.constraints.push_back(c);

@@ -34,7 +34,7 @@ def test_library_exports_every_header_entry_point(lib):
     assert len(names) >= 18
     for n in names:
         assert hasattr(lib, n), f"libcannon_gpu.so does not export {n}"
-    assert lib.cp_abi_version() == 3
+    assert lib.cp_abi_version() == 4
 
 
 def test_ctypes_layouts_match_the_c_header(tmp_path):
@@ -73,7 +73,8 @@ def _bytes(arr):
 
 @pytest.mark.parametrize("make", [scenes.spheres_on_plane, lambda: scenes.box_pile(8, 8, 4),
                                   lambda: scenes.mixed_chains(8, 8, 4, chains=4, chain_len=8),
-                                  lambda: scenes.column_world(300, 9, "mixed"), scenes.compound_pile])
+                                  lambda: scenes.column_world(300, 9, "mixed"), scenes.compound_pile,
+                                  scenes.joints_and_hulls])
 def test_body_setup_matches_oracle_bitwise(lib, make):
     a, b = make(), make()
     O.setup_scene(a)
