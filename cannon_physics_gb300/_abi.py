@@ -289,8 +289,23 @@ class Event(C.Structure):
 
 EV_COLLIDE, EV_BEGIN_CONTACT, EV_END_CONTACT, EV_BEGIN_SHAPE_CONTACT, EV_END_SHAPE_CONTACT = 0, 1, 2, 3, 4
 
+
+class Ray(C.Structure):
+    _fields_ = [("from_", f3), ("to", f3), ("collision_filter_group", C.c_int32), ("collision_filter_mask", C.c_int32),
+                ("skip_backfaces", C.c_int32), ("check_collision_response", C.c_int32)]
+
+
+class RayHit(C.Structure):
+    _fields_ = [("has_hit", C.c_int32), ("body", C.c_int32), ("shape", C.c_int32), ("hit_face_index", C.c_int32),
+                ("hit_point", f3), ("hit_normal", f3), ("distance", C.c_double)]
+
+
+RAY_CLOSEST, RAY_ANY, RAY_ALL = 0, 1, 2
+
 SHAPE_DTYPE = np_dtype(ShapeDesc)
 EVENT_DTYPE = np_dtype(Event)
+RAY_DTYPE = np_dtype(Ray)
+RAY_HIT_DTYPE = np_dtype(RayHit)
 BODY_DTYPE = np_dtype(BodyDesc)
 BODY_STATE_DTYPE = np_dtype(BodyState)
 BODY_SHAPE_DTYPE = np_dtype(BodyShape)
@@ -332,6 +347,20 @@ def default_bodies(n):
     b["shape"] = -1
     b["aabb_needs_update"] = 1
     return b
+
+
+def rays(from_, to, group=-1, mask=-1, skip_backfaces=True, check_collision_response=True):
+    """Ray records (RayOptions defaults of Ray.intersectWorld) from (n, 3)
+    start and end points."""
+    from_ = np.asarray(from_, np.float32).reshape(-1, 3)
+    r = np.zeros(len(from_), dtype=RAY_DTYPE)
+    r["from_"] = from_
+    r["to"] = np.asarray(to, np.float32).reshape(-1, 3)
+    r["collision_filter_group"] = group
+    r["collision_filter_mask"] = mask
+    r["skip_backfaces"] = int(skip_backfaces)
+    r["check_collision_response"] = int(check_collision_response)
+    return r
 
 
 def body_shapes(n):

@@ -21,7 +21,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 DEVICE_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-ftz=false", "-prec-div=true", "-prec-sqrt=true",
                 "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-I" + os.path.join(ROOT, "include")]
 
-UNITS = ["cp_step.cu", "cp_wide.cu", "cp_host.cpp", "cp_serve.cpp"]
+UNITS = ["cp_step.cu", "cp_wide.cu", "cp_ray.cu", "cp_host.cpp", "cp_serve.cpp"]
 
 
 def _sources():

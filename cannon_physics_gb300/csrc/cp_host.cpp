@@ -839,6 +839,7 @@ int cp_destroy(cp_ctx* c) {
   if (c->d_io_first) cudaFree(c->d_io_first);
   if (c->d_io) cudaFree(c->d_io);
   if (c->d_states) cudaFree(c->d_states);
+  if (c->d_rays) cudaFree(c->d_rays);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -1641,6 +1642,41 @@ int ensure_states(cp_ctx* c, int n) {
 }  // namespace
 
 extern "C" {
+
+int cp_world_raycast(cp_ctx* c, int32_t id, const cp_ray* rays, int32_t n, int32_t mode, cp_ray_hit* hits, int32_t max_hits,
+                     int32_t* counts) {
+  int st = check_world(c, id);
+  if (st) return st;
+  if (n < 0 || (n > 0 && (!rays || !hits)) || mode < CP_RAY_CLOSEST || mode > CP_RAY_ALL)
+    return fail(CP_ERR_ARG, "bad raycast arguments");
+  if (mode == CP_RAY_ALL && (max_hits < 0 || (n > 0 && !counts))) return fail(CP_ERR_ARG, "RAY_ALL needs max_hits >= 0 and counts");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaSetDevice(c->device);
+  const size_t per = mode == CP_RAY_ALL ? (size_t)max_hits : 1;
+  Layout L;
+  const size_t o_r = L.take(sizeof(cp_ray) * (size_t)n);
+  const size_t o_h = L.take(sizeof(cp_ray_hit) * per * (size_t)n);
+  const size_t o_c = L.take(sizeof(int32_t) * (size_t)n);
+  if (L.off > c->rays_bytes) {
+    const size_t cap = std::max(L.off, 2 * c->rays_bytes);
+    if (c->d_rays) cudaFree(c->d_rays);
+    c->d_rays = nullptr;
+    c->rays_bytes = 0;
+    CUDA_TRY(cudaMalloc(&c->d_rays, cap));
+    c->rays_bytes = cap;
+  }
+  char* base = (char*)c->d_rays;
+  if (n > 0) CUDA_TRY(cudaMemcpyAsync(base + o_r, rays, sizeof(cp_ray) * n, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cpk_raycast(c->d_worlds + id, (const cp_ray*)(base + o_r), n, mode, (cp_ray_hit*)(base + o_h), (int)per,
+                       (int*)(base + o_c), c->stream));
+  c->launches += n > 0 ? 2 : 1;
+  if (n > 0) {
+    CUDA_TRY(cudaMemcpyAsync(hits, base + o_h, sizeof(cp_ray_hit) * per * n, cudaMemcpyDeviceToHost, c->stream));
+    if (mode == CP_RAY_ALL) CUDA_TRY(cudaMemcpyAsync(counts, base + o_c, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return kernel_check();
+}
 
 int cp_world_get_states(cp_ctx* c, int32_t id, cp_body_state* out, int32_t n) {
   int st = check_world(c, id);

@@ -127,6 +127,8 @@ struct cp_ctx {
   // staging of cp_world_get_states / set_states
   cp_body_state* d_states = nullptr;
   int states_cap = 0;
+  void* d_rays = nullptr;  // raycast scratch: rays, then hits, then counts
+  size_t rays_bytes = 0;
   double graph_ms = 0.0;
   long long graph_step_launches = 0;
   // batched-step graph cache

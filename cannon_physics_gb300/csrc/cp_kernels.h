@@ -85,3 +85,7 @@ cudaError_t cpk_static_scratch(int device, void** ptr, size_t* bytes);
 // First failed index check of the solve kernel since the last read, as
 // {code, world id, index, bound} (code 0: none); clears it once read.
 cudaError_t cpk_read_check(int out[4]);
+// World.raycastClosest / Any / All over one world (cp_ray.cu): refresh the
+// AABBs that need it (and re-sort a SAP axis list), then one ray per thread
+cudaError_t cpk_raycast(const DWorld* d_world, const cp_ray* d_rays, int n, int mode, cp_ray_hit* d_hits, int max_hits,
+                        int* d_counts, cudaStream_t stream);

@@ -52,6 +52,7 @@ def lib():
         L.cp_world_get_rows.argtypes = [vp, i32, vp, i32, vp]
         L.cp_world_get_info.argtypes = [vp, i32, vp]
         L.cp_world_get_sap_order.argtypes = [vp, i32, vp, i32]
+        L.cp_world_raycast.argtypes = [vp, i32, vp, i32, i32, vp, i32, vp]
         L.cp_batch_step.argtypes = [vp, vp, i32, f64, i32]
         L.cp_batch_set_forces.argtypes = [vp, vp, i32, vp, C.c_int64]
         L.cp_batch_get_poses.argtypes = [vp, vp, i32, vp, C.c_int64]
@@ -245,6 +246,21 @@ class GpuWorld:
         out = np.zeros(cnt.value, dtype=A.EVENT_DTYPE)
         check(lib().cp_world_get_events(self.ctx.h, self.id, out.ctypes.data, len(out), C.byref(cnt)), "get_events")
         return out[:cnt.value]
+
+    def raycast(self, rays, mode=A.RAY_CLOSEST, max_hits=16):
+        """World.raycastClosest / Any (one RaycastResult per ray) or
+        raycastAll (mode RAY_ALL: (hits of shape (n, max_hits), counts))."""
+        rays = np.ascontiguousarray(rays, dtype=A.RAY_DTYPE)
+        n = len(rays)
+        if mode == A.RAY_ALL:
+            hits = np.zeros(max(1, n * max_hits), dtype=A.RAY_HIT_DTYPE)
+            counts = np.zeros(max(1, n), dtype=np.int32)
+            check(lib().cp_world_raycast(self.ctx.h, self.id, rays.ctypes.data, n, mode, hits.ctypes.data, max_hits,
+                                         counts.ctypes.data), "raycast")
+            return hits[:n * max_hits].reshape(n, max_hits), counts[:n]
+        hits = np.zeros(max(1, n), dtype=A.RAY_HIT_DTYPE)
+        check(lib().cp_world_raycast(self.ctx.h, self.id, rays.ctypes.data, n, mode, hits.ctypes.data, 1, None), "raycast")
+        return hits[:n]
 
     def states(self):
         out = np.zeros(self.n, dtype=A.BODY_STATE_DTYPE)

@@ -56,6 +56,7 @@ class GpuWorld extends World {
   // as last uploaded
   List<int> _firstShape = const [];
   List<int> _extraFirst = const [];
+  List<Shape> _shapeList = const [];  // shape index -> Shape, as uploaded
   Pointer<CpBodyState> _stateBuf = nullptr;
   int _stateCap = 0;
 
@@ -102,6 +103,82 @@ class GpuWorld extends World {
     // to World.step
     stepnumber += 1;
     this.dt = dt;
+  }
+
+  // ---------------------------------------------------------------- raycasts
+  // World.raycastClosest / Any / All (world_class.dart:248-278) answered by
+  // cp_world_raycast on the device copy of the world.  The bodies' per-step
+  // fields are pushed first, as before a step.
+
+  /// Hits of RAY_ALL beyond this many per ray are dropped.
+  int raycastAllMaxHits = 64;
+
+  List<CpRayHit> _cast(Vector3 from, Vector3 to, RayOptions? options, int mode, Arena arena, Pointer<Int32> count) {
+    final api = _lib;
+    if (_dirty) _upload(api);
+    _packStates();
+    _check(api.worldSetStates(_ctx, _worldId, _stateBuf, bodies.length));
+    final ray = arena<CpRay>();
+    _set3(ray.ref.from, from);
+    _set3(ray.ref.to, to);
+    ray.ref.collisionFilterGroup = options?.collisionFilterGroup ?? -1;
+    ray.ref.collisionFilterMask = options?.collisionFilterMask ?? -1;
+    ray.ref.skipBackfaces = (options?.skipBackfaces ?? true) ? 1 : 0;
+    ray.ref.checkCollisionResponse = (options?.checkCollisionResponse ?? true) ? 1 : 0;
+    final maxHits = mode == cpRayAll ? raycastAllMaxHits : 1;
+    final hits = arena<CpRayHit>(maxHits);
+    _check(api.worldRaycast(_ctx, _worldId, ray, 1, mode, hits, maxHits, count));
+    final n = mode == cpRayAll ? (count.value < maxHits ? count.value : maxHits) : 1;
+    return [for (var k = 0; k < n; k++) hits[k]];
+  }
+
+  void _fill(RaycastResult r, CpRayHit h, Vector3 from, Vector3 to) {
+    r.reset();
+    r.hitFaceIndex = h.hitFaceIndex;
+    if (h.hasHit == 0) return;
+    r.set(from, to, Vector3(h.hitNormal[0], h.hitNormal[1], h.hitNormal[2]),
+        Vector3(h.hitPoint[0], h.hitPoint[1], h.hitPoint[2]), _shapeList[h.shape], bodies[h.body], h.distance);
+    r.hasHit = true;
+  }
+
+  @override
+  bool raycastClosest([Vector3? from, Vector3? to, RayOptions? options, RaycastResult? result]) =>
+      _castOne(from, to, options, result, cpRayClosest);
+
+  @override
+  bool raycastAny([Vector3? from, Vector3? to, RayOptions? options, RaycastResult? result]) =>
+      _castOne(from, to, options, result, cpRayAny);
+
+  bool _castOne(Vector3? from, Vector3? to, RayOptions? options, RaycastResult? result, int mode) {
+    final f = from ?? options?.from ?? Vector3.zero();
+    final t = to ?? options?.to ?? Vector3.zero();
+    final arena = Arena();
+    try {
+      final h = _cast(f, t, options, mode, arena, arena<Int32>())[0];
+      if (result != null) _fill(result, h, f, t);
+      return h.hasHit != 0;
+    } finally {
+      arena.releaseAll();
+    }
+  }
+
+  @override
+  bool raycastAll([Vector3? from, Vector3? to, RayOptions? options, RaycastCallback? callback]) {
+    final f = from ?? options?.from ?? Vector3.zero();
+    final t = to ?? options?.to ?? Vector3.zero();
+    final arena = Arena();
+    try {
+      final count = arena<Int32>();
+      final hits = _cast(f, t, options, cpRayAll, arena, count);
+      final r = RaycastResult();
+      for (final h in hits) {
+        _fill(r, h, f, t);
+        callback?.call(r);
+      }
+      return count.value > 0;
+    } finally {
+      arena.releaseAll();
+    }
   }
 
   /// Releases the device world and the context.
@@ -199,6 +276,7 @@ class GpuWorld extends World {
         }
         matIndex(b.material);
       }
+      _shapeList = shapeList;
       for (var i = 0; i < shapeList.length; i++) {
         final s = shapeList[i];
         final d = shapes[i];

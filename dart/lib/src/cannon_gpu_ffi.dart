@@ -188,6 +188,29 @@ final class CpWorldDesc extends Struct {
   @Int32() external int pad0;
 }
 
+/// cp_ray: one ray of World.raycastClosest / Any / All.
+final class CpRay extends Struct {
+  @Array(3) external Array<Float> from;
+  @Array(3) external Array<Float> to;
+  @Int32() external int collisionFilterGroup;
+  @Int32() external int collisionFilterMask;
+  @Int32() external int skipBackfaces;
+  @Int32() external int checkCollisionResponse;
+}
+
+/// cp_ray_hit: a RaycastResult.
+final class CpRayHit extends Struct {
+  @Int32() external int hasHit;
+  @Int32() external int body;
+  @Int32() external int shape;
+  @Int32() external int hitFaceIndex;
+  @Array(3) external Array<Float> hitPoint;
+  @Array(3) external Array<Float> hitNormal;
+  @Double() external double distance;
+}
+
+const int cpRayClosest = 0, cpRayAny = 1, cpRayAll = 2;
+
 final class CpStepInfo extends Struct {
   @Int64() external int stepnumber;
   @Double() external double time;
@@ -246,7 +269,11 @@ class CannonGpu {
         worldStepStatic = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Int32, Double, Int32),
             int Function(Pointer<CpCtx>, int, double, int)>('cp_world_step_static'),
         batchStep = lib.lookupFunction<Int32 Function(Pointer<CpCtx>, Pointer<Int32>, Int32, Double, Int32),
-            int Function(Pointer<CpCtx>, Pointer<Int32>, int, double, int)>('cp_batch_step');
+            int Function(Pointer<CpCtx>, Pointer<Int32>, int, double, int)>('cp_batch_step'),
+        worldRaycast = lib.lookupFunction<
+            Int32 Function(Pointer<CpCtx>, Int32, Pointer<CpRay>, Int32, Int32, Pointer<CpRayHit>, Int32, Pointer<Int32>),
+            int Function(Pointer<CpCtx>, int, Pointer<CpRay>, int, int, Pointer<CpRayHit>, int, Pointer<Int32>)>(
+            'cp_world_raycast');
 
   final int Function() abiVersion;
   final Pointer<Uint8> Function() lastError;
@@ -277,6 +304,10 @@ class CannonGpu {
 
   /// Many independent worlds stepped together: ids, count, dt, steps.
   final int Function(Pointer<CpCtx>, Pointer<Int32>, int, double, int) batchStep;
+
+  /// Rays against a world's resident state: ctx, world, rays, n, mode, hits,
+  /// max hits per ray (RAY_ALL), counts (RAY_ALL).
+  final int Function(Pointer<CpCtx>, int, Pointer<CpRay>, int, int, Pointer<CpRayHit>, int, Pointer<Int32>) worldRaycast;
 
   /// The thread-local message of the last failing call.
   String errorText() {

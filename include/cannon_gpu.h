@@ -422,6 +422,42 @@ int cp_world_set_events(cp_ctx* ctx, int32_t world_id, int32_t on, const int32_t
  * *count set when more than cap are waiting (nothing is drained then). */
 int cp_world_get_events(cp_ctx* ctx, int32_t world_id, cp_event* out, int32_t cap, int32_t* count);
 
+/* ---- raycasts over the resident state -------------------------------------
+ * World.raycastClosest / raycastAny / raycastAll (lib/world/world_class.dart:
+ * 248-278) through Ray.intersectWorld (lib/collision/ray_class.dart:163-199),
+ * one ray per record, all against the world as it stands.  Like the
+ * reference, a raycast refreshes the AABBs of the bodies that need it (and
+ * re-sorts a SAPBroadphase's axis list), and a GridBroadphase world answers
+ * no hits (GridBroadphase has no aabbQuery).  Capsule, Cone and SizedPlane
+ * shapes have no ray intersector in the reference and are never hit. */
+typedef struct cp_ray {
+  float from[3], to[3];
+  int32_t collision_filter_group;   /* RayOptions: default -1 */
+  int32_t collision_filter_mask;    /* default -1 */
+  int32_t skip_backfaces;           /* intersectWorld default 1 */
+  int32_t check_collision_response; /* default 1 */
+} cp_ray;
+
+enum cp_ray_mode { CP_RAY_CLOSEST = 0, CP_RAY_ANY = 1, CP_RAY_ALL = 2 };
+
+/* RaycastResult (lib/collision/raycast_result.dart); after reset() a miss
+ * reads has_hit 0, body / shape -1, hit_face_index -1, distance -1.  As in
+ * the reference, hit_face_index of a CLOSEST result is that of the last hit
+ * reported, kept or not. */
+typedef struct cp_ray_hit {
+  int32_t has_hit, body, shape, hit_face_index;
+  float hit_point[3];
+  float hit_normal[3];
+  double distance;
+} cp_ray_hit;
+
+/* Casts n rays.  CLOSEST / ANY: hits[r] is ray r's result (max_hits and counts
+ * are not used).  ALL: the hits of ray r in report order go to
+ * hits[r * max_hits ..] (at most max_hits of them) and counts[r] is their
+ * number (it may exceed max_hits: the rest are dropped). */
+int cp_world_raycast(cp_ctx* ctx, int32_t world_id, const cp_ray* rays, int32_t n, int32_t mode, cp_ray_hit* hits,
+                     int32_t max_hits, int32_t* counts);
+
 /* Read back / overwrite body state (Body fields). */
 int cp_world_get_bodies(cp_ctx* ctx, int32_t world_id, cp_body_desc* out, int32_t n);
 int cp_world_set_bodies(cp_ctx* ctx, int32_t world_id, const cp_body_desc* in, int32_t n);

@@ -845,19 +845,23 @@ struct World {
     return boundB1 < boundA2;
   }
   // sap_broadphase.dart:66-111,138-189
+  // sortList (sap_broadphase.dart:168-189) with the insertion sorts (:66-111)
+  void sapSort() {
+    for (int bi : axisList) if (bodies[bi].aabbNeedsUpdate) updateAABB(bodies[bi], shapes);
+    for (size_t i = 1, l = axisList.size(); i < l; i++) {
+      int v = axisList[i];
+      double vk = axisComp(bodies[v].aabbLo, sapAxis);
+      long j;
+      for (j = (long)i - 1; j >= 0; j--) {
+        if (axisComp(bodies[axisList[j]].aabbLo, sapAxis) <= vk) break;
+        axisList[j + 1] = axisList[j];
+      }
+      axisList[j + 1] = v;
+    }
+  }
   void sapPairs() {
     if (dirty) {
-      for (int bi : axisList) if (bodies[bi].aabbNeedsUpdate) updateAABB(bodies[bi], shapes);
-      for (size_t i = 1, l = axisList.size(); i < l; i++) {
-        int v = axisList[i];
-        double vk = axisComp(bodies[v].aabbLo, sapAxis);
-        long j;
-        for (j = (long)i - 1; j >= 0; j--) {
-          if (axisComp(bodies[axisList[j]].aabbLo, sapAxis) <= vk) break;
-          axisList[j + 1] = axisList[j];
-        }
-        axisList[j + 1] = v;
-      }
+      sapSort();
       dirty = false;
     }
     int N = (int)axisList.size();
@@ -1723,6 +1727,238 @@ struct World {
     return iter;
   }
 
+  // ---------------------------------------------------------------- raycast
+  // Ray (lib/collision/ray_class.dart) as World.raycastClosest / Any / All
+  // drive it (world_class.dart:248-278): one ray's state and result.
+  struct RayRun {
+    V3 from, to, direction;
+    int mode = CP_RAY_ANY;
+    bool skipBackfaces = true, checkResponse = true;
+    int group = -1, mask = -1;
+    cp_ray_hit result;
+    bool shouldStop = false;
+    cp_ray_hit* all = nullptr;  // RayMode.all: every hit, in report order
+    int cap = 0, count = 0;
+  };
+  // raycast_result.dart:38-50
+  static void rayReset(cp_ray_hit& r) {
+    std::memset(&r, 0, sizeof(r));
+    r.body = r.shape = r.hit_face_index = -1;
+    r.distance = -1;
+  }
+  // ray_class.dart:669-678
+  static bool pointInTriangle(const V3& p, const V3& a, const V3& b, const V3& c) {
+    V3 v0, v1, v2;
+    sub2(c, a, v0);
+    sub2(b, a, v1);
+    sub2(p, a, v2);
+    double dot00 = dot(v0, v0), dot01 = dot(v0, v1), dot02 = dot(v0, v2), dot11 = dot(v1, v1), dot12 = dot(v1, v2);
+    double u = dot11 * dot02 - dot01 * dot12;
+    double v = dot00 * dot12 - dot01 * dot02;
+    return u >= 0 && v >= 0 && (u + v) < (dot00 * dot11 - dot01 * dot01);
+  }
+  // ray_class.dart:679-691
+  static double distanceFromIntersection(const V3& from, const V3& direction, const V3& position) {
+    V3 v0, is;
+    sub2(position, from, v0);
+    double d = dot(v0, direction);
+    scale2(direction, d, is);
+    add2(is, from, is);
+    return distanceTo(position, is);
+  }
+  // ray_class.dart:617-664 (_reportIntersection; the face index is stored
+  // before the mode decides whether the hit is kept)
+  void rayReport(RayRun& R, const V3& normal, const V3& hit, int shape, int body, int faceIndex) {
+    const double distance = distanceTo(R.from, hit);
+    if (R.skipBackfaces && dot(normal, R.direction) > 0) return;
+    R.result.hit_face_index = faceIndex;
+    auto set = [&]() {
+      R.result.hit_point[0] = hit.x; R.result.hit_point[1] = hit.y; R.result.hit_point[2] = hit.z;
+      R.result.hit_normal[0] = normal.x; R.result.hit_normal[1] = normal.y; R.result.hit_normal[2] = normal.z;
+      R.result.shape = shape;
+      R.result.body = body;
+      R.result.distance = distance;
+    };
+    if (R.mode == CP_RAY_ALL) {
+      set();
+      R.result.has_hit = 1;
+      if (R.count < R.cap) R.all[R.count] = R.result;
+      R.count++;
+    } else if (R.mode == CP_RAY_CLOSEST) {
+      if (distance < R.result.distance || !R.result.has_hit) {
+        R.result.has_hit = 1;
+        set();
+      }
+    } else {
+      R.result.has_hit = 1;
+      set();
+      R.shouldStop = true;
+    }
+  }
+  // ray_class.dart:387-438 (the pow(x, 2) terms as x * x)
+  void raySphere(RayRun& R, double r, const V3& position, int shape, int body) {
+    const V3 &from = R.from, &to = R.to;
+    double dx = (double)to.x - from.x, dy = (double)to.y - from.y, dz = (double)to.z - from.z;
+    double fx = (double)from.x - position.x, fy = (double)from.y - position.y, fz = (double)from.z - position.z;
+    double a = dx * dx + dy * dy + dz * dz;
+    double b = 2 * (dx * fx + dy * fy + dz * fz);
+    double c = fx * fx + fy * fy + fz * fz - r * r;
+    double delta = b * b - 4 * a * c;
+    V3 ip, normal;
+    if (delta < 0) return;
+    if (delta == 0) {
+      lerp(from, to, delta, ip);
+      sub2(ip, position, normal);
+      normalize(normal);
+      rayReport(R, normal, ip, shape, body, -1);
+      return;
+    }
+    double d1 = (-b - std::sqrt(delta)) / (2 * a);
+    double d2 = (-b + std::sqrt(delta)) / (2 * a);
+    if (d1 >= 0 && d1 <= 1) {
+      lerp(from, to, d1, ip);
+      sub2(ip, position, normal);
+      normalize(normal);
+      rayReport(R, normal, ip, shape, body, -1);
+    }
+    if (R.shouldStop) return;
+    if (d2 >= 0 && d2 <= 1) {
+      lerp(from, to, d2, ip);
+      sub2(ip, position, normal);
+      normalize(normal);
+      rayReport(R, normal, ip, shape, body, -1);
+    }
+  }
+  // ray_class.dart:290-334
+  void rayPlane(RayRun& R, const Q4& quat, const V3& position, int shape, int body) {
+    const V3 &from = R.from, &to = R.to;
+    V3 n = mk(0, 0, 1), len;
+    vmult(quat, n, n);
+    sub2(from, position, len);
+    double planeToFrom = dot(len, n);
+    sub2(to, position, len);
+    double planeToTo = dot(len, n);
+    if (planeToFrom * planeToTo > 0) return;
+    if (distanceTo(from, to) < planeToFrom) return;
+    double nDotDir = dot(n, R.direction);
+    if (std::fabs(nDotDir) < 0.0001) return;
+    V3 pp, ds, hit;
+    sub2(from, position, pp);
+    double t = -dot(n, pp) / nDotDir;
+    scale2(R.direction, t, ds);
+    add2(from, ds, hit);
+    rayReport(R, n, hit, shape, body, -1);
+  }
+  // ray_class.dart:440-530
+  void rayConvex(RayRun& R, const Hull& h, const Q4& q, const V3& x, int shape, int body) {
+    const V3 &from = R.from, &to = R.to;
+    const double fromToDistance = distanceTo(from, to);
+    for (size_t j = 0; !R.shouldStop && j < h.faces.size(); j++) {
+      const std::vector<int>& face = h.faces[j];
+      V3 vector, normal;
+      vmult(q, h.vertices[face[0]], vector);
+      add2(vector, x, vector);
+      sub2(vector, from, vector);
+      vmult(q, h.faceNormals[j], normal);
+      double d = dot(R.direction, normal);
+      double scalar = dot(normal, vector) / d;
+      if (scalar < 0) continue;
+      V3 ip, a;
+      scale2(R.direction, scalar, ip);
+      add2(ip, from, ip);
+      vmult(q, h.vertices[face[0]], a);
+      add2(x, a, a);
+      for (size_t i = 1; !R.shouldStop && i + 1 < face.size(); i++) {
+        V3 b, c;
+        vmult(q, h.vertices[face[i]], b);
+        vmult(q, h.vertices[face[i + 1]], c);
+        add2(x, b, b);
+        add2(x, c, c);
+        double distance = distanceTo(ip, from);
+        if (!(pointInTriangle(ip, a, b, c) || pointInTriangle(ip, b, a, c)) || distance > fromToDistance) continue;
+        rayReport(R, normal, ip, shape, body, (int)j);
+      }
+    }
+  }
+  // ray_class.dart:270-288 (the type table of :104-127 has no entry for
+  // Capsule, Cone or SizedPlane)
+  void rayShape(RayRun& R, int shapeIndex, const Q4& q, const V3& x, int body) {
+    const Shape& s = shapes[shapeIndex];
+    if (distanceFromIntersection(R.from, R.direction, x) > s.bsr) return;
+    if (s.type == CP_SHAPE_SPHERE) raySphere(R, s.radius, x, shapeIndex, body);
+    else if (s.type == CP_SHAPE_PLANE) rayPlane(R, q, x, shapeIndex, body);
+    else if (s.type == CP_SHAPE_BOX || s.type == CP_SHAPE_CONVEX || s.type == CP_SHAPE_CYLINDER)
+      rayConvex(R, s.hull, q, x, shapeIndex, body);
+  }
+  // ray_class.dart:201-244
+  void rayBody(RayRun& R, int i) {
+    const Body& b = bodies[i];
+    if (R.checkResponse && !b.response) return;
+    if ((R.group & b.mask) == 0 || (b.group & R.mask) == 0) return;
+    for (int k = 0; k < b.numShapes(); k++) {
+      const int si = b.shapeAt(k);
+      if (R.checkResponse && !shapes[si].response) continue;
+      Q4 qi;
+      V3 xi;
+      qmultiply2(b.quaternion, b.orientationAt(k), qi);
+      vmult(b.quaternion, b.offsetAt(k), xi);
+      add2(xi, b.position, xi);
+      rayShape(R, si, qi, xi, i);
+      if (R.shouldStop) break;
+    }
+  }
+  // Broadphase.aabbQuery: naive_broadphase.dart:39-56, sap_broadphase.dart:
+  // 240-261 (sorting first when the list is dirty, as after every step);
+  // GridBroadphase has none (broadphase.dart:151-154: no bodies)
+  void aabbQuery(const V3& lo, const V3& hi, std::vector<int>& out) {
+    out.clear();
+    auto overlapsQuery = [&](const Body& b) {
+      bool ox = (lo.x <= b.aabbHi.x && b.aabbHi.x <= hi.x) || (b.aabbLo.x <= hi.x && hi.x <= b.aabbHi.x);
+      bool oy = (lo.y <= b.aabbHi.y && b.aabbHi.y <= hi.y) || (b.aabbLo.y <= hi.y && hi.y <= b.aabbHi.y);
+      bool oz = (lo.z <= b.aabbHi.z && b.aabbHi.z <= hi.z) || (b.aabbLo.z <= hi.z && hi.z <= b.aabbHi.z);
+      return ox && oy && oz;
+    };
+    if (broadphase == CP_BROAD_NAIVE) {
+      for (int i = 0; i < (int)bodies.size(); i++) {
+        if (bodies[i].aabbNeedsUpdate) updateAABB(bodies[i], shapes);
+        if (overlapsQuery(bodies[i])) out.push_back(i);
+      }
+    } else if (broadphase == CP_BROAD_SAP) {
+      if (dirty) {
+        sapSort();
+        dirty = false;
+      }
+      for (int i : axisList) {
+        if (bodies[i].aabbNeedsUpdate) updateAABB(bodies[i], shapes);
+        if (overlapsQuery(bodies[i])) out.push_back(i);
+      }
+    }
+  }
+  // ray_class.dart:163-199
+  void raycast(const cp_ray& ray, int mode, cp_ray_hit& result, cp_ray_hit* all, int cap, int& count) {
+    RayRun R;
+    R.mode = mode;
+    R.skipBackfaces = ray.skip_backfaces != 0;
+    R.group = ray.collision_filter_group;
+    R.mask = ray.collision_filter_mask;
+    R.checkResponse = ray.check_collision_response != 0;
+    R.from = mk(ray.from[0], ray.from[1], ray.from[2]);
+    R.to = mk(ray.to[0], ray.to[1], ray.to[2]);
+    R.all = all;
+    R.cap = cap;
+    rayReset(R.result);
+    sub2(R.to, R.from, R.direction);
+    normalize(R.direction);
+    V3 lo, hi;  // Ray.getAABB (:337-349)
+    lo.x = (float)dartMin(R.to.x, R.from.x); lo.y = (float)dartMin(R.to.y, R.from.y); lo.z = (float)dartMin(R.to.z, R.from.z);
+    hi.x = (float)dartMax(R.to.x, R.from.x); hi.y = (float)dartMax(R.to.y, R.from.y); hi.z = (float)dartMax(R.to.z, R.from.z);
+    std::vector<int> cand;
+    aabbQuery(lo, hi, cand);
+    for (size_t k = 0; !R.shouldStop && k < cand.size(); k++) rayBody(R, cand[k]);
+    result = R.result;
+    count = R.count;
+  }
+
   // ---------------------------------------------------------------- constraints
   // point_to_point_constraint.dart:122-137, hinge_constraint.dart:217-242,
   // distance_constraint.dart:269-280
@@ -2273,6 +2509,24 @@ int orc_world_get_info(orc_world* o, cp_step_info* out) {
   out->num_rows = (int)o->w.solverRows.size();
   out->iterations = o->w.lastIterations;
   out->num_bodies = (int)o->w.bodies.size();
+  return CP_OK;
+}
+
+int orc_world_raycast(orc_world* o, const cp_ray* rays, int32_t n, int32_t mode, cp_ray_hit* hits, int32_t max_hits,
+                      int32_t* counts) {
+  if (!o || n < 0 || (n > 0 && (!rays || !hits)) || mode < CP_RAY_CLOSEST || mode > CP_RAY_ALL) return CP_ERR_ARG;
+  if (mode == CP_RAY_ALL && (max_hits < 0 || (n > 0 && !counts))) return CP_ERR_ARG;
+  for (int r = 0; r < n; r++) {
+    cp_ray_hit res;
+    int count = 0;
+    if (mode == CP_RAY_ALL) {
+      o->w.raycast(rays[r], mode, res, hits + (size_t)r * max_hits, max_hits, count);
+      counts[r] = count;
+    } else {
+      o->w.raycast(rays[r], mode, res, nullptr, 0, count);
+      hits[r] = res;
+    }
+  }
   return CP_OK;
 }
 

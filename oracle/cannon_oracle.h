@@ -54,6 +54,8 @@ int orc_world_get_contacts(orc_world* w, cp_contact* out, int32_t cap, int32_t* 
 int orc_world_get_rows(orc_world* w, cp_row* out, int32_t cap, int32_t* count);
 int orc_world_get_info(orc_world* w, cp_step_info* out);
 int orc_world_get_sap_order(orc_world* w, int32_t* out, int32_t n);
+int orc_world_raycast(orc_world* w, const cp_ray* rays, int32_t n, int32_t mode, cp_ray_hit* hits, int32_t max_hits,
+                      int32_t* counts);
 
 /* Step many independent worlds on `threads` host threads (one world per
  * thread at a time); used for the CPU baseline of the batched form. */

@@ -40,6 +40,7 @@ def lib():
         L.orc_world_get_rows.argtypes = [vp, vp, i32, vp]
         L.orc_world_get_info.argtypes = [vp, vp]
         L.orc_world_get_sap_order.argtypes = [vp, vp, i32]
+        L.orc_world_raycast.argtypes = [vp, vp, i32, i32, vp, i32, vp]
         L.orc_worlds_step_parallel.argtypes = [vp, i32, f64, i32, i32]
         L.orc_shape_hull.argtypes = [vp, vp, i32, vp, vp, i32, vp, vp, i32, vp]
         _lib = L
@@ -109,6 +110,19 @@ class OracleWorld:
         out = np.zeros(cnt.value, dtype=A.EVENT_DTYPE)
         _check(lib().orc_world_get_events(self.h, out.ctypes.data, len(out), C.byref(cnt)), "events")
         return out[:cnt.value]
+
+    def raycast(self, rays, mode=A.RAY_CLOSEST, max_hits=16):
+        rays = np.ascontiguousarray(rays, dtype=A.RAY_DTYPE)
+        n = len(rays)
+        if mode == A.RAY_ALL:
+            hits = np.zeros(max(1, n * max_hits), dtype=A.RAY_HIT_DTYPE)
+            counts = np.zeros(max(1, n), dtype=np.int32)
+            _check(lib().orc_world_raycast(self.h, rays.ctypes.data, n, mode, hits.ctypes.data, max_hits,
+                                           counts.ctypes.data), "raycast")
+            return hits[:n * max_hits].reshape(n, max_hits), counts[:n]
+        hits = np.zeros(max(1, n), dtype=A.RAY_HIT_DTYPE)
+        _check(lib().orc_world_raycast(self.h, rays.ctypes.data, n, mode, hits.ctypes.data, 1, None), "raycast")
+        return hits[:n]
 
     def set_bodies(self, bodies):
         bodies = np.ascontiguousarray(bodies, dtype=A.BODY_DTYPE)

@@ -45,7 +45,7 @@ def test_ctypes_layouts_match_the_c_header(tmp_path):
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
-    structs = [("cp_body_desc", A.BodyDesc), ("cp_body_state", A.BodyState), ("cp_body_shape", A.BodyShape), ("cp_shape_desc", A.ShapeDesc), ("cp_world_desc", A.WorldDesc),
+    structs = [("cp_body_desc", A.BodyDesc), ("cp_body_state", A.BodyState), ("cp_body_shape", A.BodyShape), ("cp_ray", A.Ray), ("cp_ray_hit", A.RayHit), ("cp_shape_desc", A.ShapeDesc), ("cp_world_desc", A.WorldDesc),
                ("cp_contact", A.Contact), ("cp_row", A.Row), ("cp_constraint_desc", A.ConstraintDesc),
                ("cp_contact_material", A.ContactMaterial), ("cp_step_info", A.StepInfo), ("cp_config", A.Config),
                ("cp_serve_config", S.ServeConfig), ("cp_serve_stats", S.ServeStats)]
@@ -55,7 +55,7 @@ def test_ctypes_layouts_match_the_c_header(tmp_path):
         lines.append(f'printf("%zu\\n", sizeof({cname}));')
         expect.append(C.sizeof(py))
         for fname, _ in py._fields_:
-            cf = "lambda" if fname == "lambda_" else fname
+            cf = {"lambda_": "lambda", "from_": "from"}.get(fname, fname)
             lines.append(f'printf("%zu\\n", offsetof({cname}, {cf}));')
             expect.append(getattr(py, fname).offset)
     lines.append("return 0; }")
