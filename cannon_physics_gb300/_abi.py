@@ -22,6 +22,7 @@ BODY_DYNAMIC, BODY_STATIC, BODY_KINEMATIC = 0, 1, 2
 AWAKE, SLEEPY, SLEEPING = 0, 1, 2
 BROAD_NAIVE, BROAD_SAP, BROAD_GRID = 0, 1, 2
 CON_P2P, CON_HINGE, CON_DISTANCE, CON_LOCK, CON_CONE_TWIST, CON_SPRING = 0, 1, 2, 3, 4, 5
+SOLVER_GS, SOLVER_SPLIT = 0, 1
 ROW_CONTACT, ROW_FRICTION, ROW_ROTATIONAL, ROW_MOTOR = 0, 1, 2, 3
 
 f3 = C.c_float * 3
@@ -163,6 +164,7 @@ class ConstraintDesc(C.Structure):
         ("lock_axes", (C.c_float * 3) * 6),
         ("angle", C.c_double),
         ("twist_angle", C.c_double),
+        ("first_equation_id", C.c_int64),
     ]
 
 
@@ -199,7 +201,8 @@ class WorldDesc(C.Structure):
         ("default_contact_material", ContactMaterial),
         ("body_shapes", C.c_void_p),
         ("num_body_shapes", C.c_int32),
-        ("pad0", C.c_int32),
+        ("solver", C.c_int32),
+        ("equation_id_counter", C.c_int64),
     ]
 
 
@@ -231,6 +234,7 @@ class Row(C.Structure):
         ("min_force", C.c_double),
         ("max_force", C.c_double),
         ("eps", C.c_double),
+        ("id", C.c_int64),
     ]
 
 

@@ -375,6 +375,21 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   size_t o_ba = L.take(sizeof(float) * (w.broadphase == CP_BROAD_GRID ? 3 * 4096 : 1));
   size_t o_hk = L.take(sizeof(long long) * hash_cap);
   size_t o_hw = L.take(sizeof(int) * hash_cap);
+  // SplitSolver arrays (one element each without it)
+  const bool sp = w.split;
+  const int sort_n = sp ? pow2_at_least(rc + 1) : 1;
+  size_t o_sct = L.take(sizeof(long long) * (sp ? cc + 1 : 1));
+  size_t o_sfr = L.take(sizeof(long long) * (sp ? 2 * (size_t)cc + 1 : 1));
+  size_t o_srw = L.take(sizeof(long long) * (sp ? rc + 1 : 1));
+  size_t o_skey = L.take(sizeof(long long) * sort_n);
+  size_t o_sval = L.take(sizeof(int) * sort_n);
+  size_t o_ipar = L.take(sizeof(int) * (sp ? nb + 1 : 1));
+  size_t o_irow = L.take(sizeof(int) * (sp ? nb + 1 : 1));
+  size_t o_iit = L.take(sizeof(int) * (sp ? nb + 1 : 1));
+  size_t o_isum = L.take(sizeof(double) * (sp ? nb + 1 : 1));
+  size_t o_risl = L.take(sizeof(int) * (sp ? rc + 1 : 1));
+  size_t o_jatt = L.take(sizeof(int) * (sp ? pc + 1 : 1));
+  size_t o_jbase = L.take(sizeof(int) * (sp ? pc + 1 : 1));
   size_t o_wd = L.take(sizeof(DWide));
   size_t o_wp = L.take(sizeof(int) * (CP_WIDE_SCAN_BLOCKS + 1));
   size_t o_wv = L.take(sizeof(float) * 6 * (size_t)(nb + 1));
@@ -385,6 +400,19 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   d.pair_a = (int*)(base + o_pa);
   d.pair_b = (int*)(base + o_pb);
   d.job_pair = (int*)(base + o_jp);
+  d.ct_id = (long long*)(base + o_sct);
+  d.fr_id = (long long*)(base + o_sfr);
+  d.row_id = (long long*)(base + o_srw);
+  d.sort_key = (long long*)(base + o_skey);
+  d.sort_val = (int*)(base + o_sval);
+  d.sort_n = sort_n;
+  d.isl_par = (int*)(base + o_ipar);
+  d.isl_rows = (int*)(base + o_irow);
+  d.isl_iter = (int*)(base + o_iit);
+  d.isl_sum = (double*)(base + o_isum);
+  d.row_isl = (int*)(base + o_risl);
+  d.job_att = (int*)(base + o_jatt);
+  d.job_base = (int*)(base + o_jbase);
   d.job_sh = (int*)(base + o_js);
   d.pair_cnt = (int*)(base + o_pc);
   d.pair_tstart = (int*)(base + o_pt);
@@ -453,6 +481,25 @@ int alloc_scratch(cp_ctx* c, WorldRec& w) {
   scratch_layout(w, base);
   // the wide path's index-check record must start clear
   CUDA_TRY(cudaMemsetAsync(w.dw.wide, 0, sizeof(DWide), c->stream));
+  // SplitSolver: the equation pools outlive the scratch; they hold at most
+  // the most contacts (friction objects: twice that) of any step, so they
+  // grow with the contact list, keeping what they hold
+  if (w.split && w.pool_cap < w.contacts_cap) {
+    const int cap = w.contacts_cap;
+    long long* np = nullptr;
+    CUDA_TRY(cudaMalloc(&np, sizeof(long long) * 3 * ((size_t)cap + 1)));
+    if (w.pool) {
+      const int old = w.pool_cap;
+      CUDA_TRY(cudaMemcpyAsync(np, w.pool, sizeof(long long) * old, cudaMemcpyDeviceToDevice, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(np + cap + 1, w.pool + old + 1, sizeof(long long) * 2 * old, cudaMemcpyDeviceToDevice, c->stream));
+      CUDA_TRY(cudaStreamSynchronize(c->stream));
+      cudaFree(w.pool);
+    }
+    w.pool = np;
+    w.pool_cap = cap;
+  }
+  w.dw.pool_c = w.pool;
+  w.dw.pool_f = w.pool ? w.pool + w.pool_cap + 1 : nullptr;
   return CP_OK;
 }
 
@@ -626,7 +673,8 @@ int kernel_check() {
   return CP_OK;
 }
 
-bool is_wide(const cp_ctx* c, const WorldRec& w) { return c->wide_bodies > 0 && w.nb >= c->wide_bodies; }
+// a SplitSolver world steps on the one-block path, whatever its size
+bool is_wide(const cp_ctx* c, const WorldRec& w) { return !w.split && c->wide_bodies > 0 && w.nb >= c->wide_bodies; }
 
 WideShape wide_shape(const WorldRec& w) {
   WideShape s;
@@ -825,6 +873,7 @@ int cp_destroy(cp_ctx* c) {
   for (auto& w : c->worlds) {
     if (w.state) dev_free(c, w.state, w.pooled);
     if (w.scratch) dev_free(c, w.scratch, w.pooled);
+    if (w.pool) cudaFree(w.pool);
   }
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->pool) cudaMemPoolDestroy(c->pool);
@@ -1020,6 +1069,12 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
     // cone_equation.dart:46); a cone-twist's cone and twist rows take its angles
     o.cos_rot[0] = cd.type == CP_CON_CONE_TWIST ? std::cos(cd.angle) : cos_max;
     o.cos_rot[1] = cd.type == CP_CON_CONE_TWIST ? std::cos(cd.twist_angle) : cos_max;
+    o.first_id = cd.first_equation_id;
+    // SplitSolver: the equations of a constraint between two static bodies
+    // belong to no island; the reference never solves them and leaves their
+    // rows as they were, which this library does not keep
+    if (d->solver == CP_SOLVER_SPLIT && d->bodies[cd.body_a].type == CP_BODY_STATIC && d->bodies[cd.body_b].type == CP_BODY_STATIC)
+      return fail(CP_ERR_UNSUPPORTED, "constraint %d joins two static bodies under the SplitSolver", k);
     if (!o.collide) { nocollide.push_back(cd.body_a); nocollide.push_back(cd.body_b); }
   }
   // bodies
@@ -1080,6 +1135,11 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
   P.pairs_cap = w.pairs_cap; P.contacts_cap = w.contacts_cap; P.rows_cap = w.rows_cap; P.bins_cap = w.bins_cap;
   P.compound = w.compound;
   P.jobs_cap = w.jobs_cap;
+  if (d->solver != CP_SOLVER_GS && d->solver != CP_SOLVER_SPLIT) return fail(CP_ERR_ARG, "solver %d", d->solver);
+  w.split = d->solver == CP_SOLVER_SPLIT;
+  P.split = w.split;
+  P.id_counter = d->equation_id_counter;
+  P.pool_c = P.pool_f = 0;
   // state allocation
   Layout L;
   size_t o_P = L.take(sizeof(DWorldParams));
@@ -1192,6 +1252,7 @@ int destroy_world(cp_ctx* c, int id) {
   if (!w.pooled) cudaStreamSynchronize(c->stream);
   if (w.state) dev_free(c, w.state, w.pooled);
   if (w.scratch) dev_free(c, w.scratch, w.pooled);
+  if (w.pool) cudaFree(w.pool);
   w = WorldRec();
   if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   return CP_OK;
@@ -1584,6 +1645,8 @@ int cp_world_step_static(cp_ctx* c, int32_t id, double dt, int32_t nsteps) {
     }
     if (p.num_rows > 0)
       CUDA_TRY(cudaMemcpyAsync(w.dw.rows, dw.rows, sizeof(DRow) * p.num_rows, cudaMemcpyDeviceToDevice, c->stream));
+    if (w.split && p.num_rows > 0)
+      CUDA_TRY(cudaMemcpyAsync(w.dw.row_id, dw.row_id, sizeof(long long) * p.num_rows, cudaMemcpyDeviceToDevice, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
   }
   return CP_OK;
@@ -1780,11 +1843,14 @@ int cp_world_get_rows(cp_ctx* c, int32_t id, cp_row* out, int32_t cap, int32_t* 
   if (p.num_rows > cap || (p.num_rows && !out)) return fail(CP_ERR_CAPACITY, "need room for %d rows", p.num_rows);
   std::vector<DRow> v(p.num_rows);
   if (p.num_rows) CUDA_TRY(cudaMemcpy(v.data(), w.dw.rows, sizeof(DRow) * v.size(), cudaMemcpyDeviceToHost));
+  std::vector<long long> ids(w.split ? p.num_rows : 0);
+  if (!ids.empty()) CUDA_TRY(cudaMemcpy(ids.data(), w.dw.row_id, sizeof(long long) * ids.size(), cudaMemcpyDeviceToHost));
   for (int i = 0; i < p.num_rows; i++) {
     cp_row& o = out[i];
     o.kind = v[i].kind; o.bi = v[i].bi; o.bj = v[i].bj; o.pad = 0;
     o.B = v[i].B; o.inv_c = v[i].invC; o.lambda = v[i].lambda; o.multiplier = v[i].mult;
     o.min_force = v[i].minF; o.max_force = v[i].maxF; o.eps = v[i].eps;
+    o.id = w.split ? ids[i] : -1;
   }
   return CP_OK;
 }

@@ -31,6 +31,9 @@ struct WorldRec {
   bool live = false;
   char* state = nullptr;   // device: params, bodies, shapes, hulls, materials, constraints, sap order, damping
   char* scratch = nullptr; // device: per-step lists
+  long long* pool = nullptr;  // device, SplitSolver: contact then friction equation pools (ids)
+  int pool_cap = 0;           // contact pool capacity (the friction pool holds twice as many)
+  bool split = false;         // SplitSolver
   size_t state_bytes = 0, scratch_bytes = 0;
   bool pooled = false;     // state and scratch come from the context's memory pool
   DWorld dw{};

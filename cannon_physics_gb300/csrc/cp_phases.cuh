@@ -42,7 +42,7 @@ struct __align__(16) Smem {
   int n_fric, n_cand, n_levels, cursor;
   int overflow, converged, wi, n_jobs;  // n_jobs: narrowphase jobs (shape pairs)
   int kcnt[16], kpos[16];  // narrowphase: heavy pairs per resolver kind, segment cursors
-  int cursor2, pad2[3];
+  int cursor2, split_e, pad2[2];  // split_e: contact equation objects the narrowphase took
   // where the narrowphase's contact cursor and overflow flag live: this
   // record's cursor / overflow for a one-block world, device memory for a
   // world spread over the grid
@@ -752,8 +752,10 @@ DI int pair_job(Smem& S, int job, PairJob& X, bool tests) {
                 (bi.type == CP_BODY_STATIC && bj.type == CP_BODY_KINEMATIC) ||
                 (bi.type == CP_BODY_KINEMATIC && bj.type == CP_BODY_KINEMATIC);
     if (P.events) W.pair_flag[job] = 0;
-    // a justTest pair only registers an overlap for the event feed
-    if (bi.shape < 0 || bj.shape < 0 || (just_test && !P.events)) return RK_NONE;
+    if (P.split) W.job_att[job] = 0;
+    // a justTest pair only registers an overlap for the event feed (and, with
+    // the SplitSolver, may still take an equation object, below)
+    if (bi.shape < 0 || bj.shape < 0 || (just_test && !P.events && !P.split)) return RK_NONE;
   }
   int shi, shj;
   f3 xi, xj;
@@ -767,6 +769,11 @@ DI int pair_job(Smem& S, int job, PairJob& X, bool tests) {
   if (tests && rk == RK_NONE) return RK_NONE;
   if (tests && !((si.mask & sj.group) != 0 && (sj.mask & si.group) != 0)) return RK_NONE;
   if (tests && distance_to(xi, xj) > si.bsr + sj.bsr) return RK_NONE;
+  // spherePlane takes its equation object before its depth test and its
+  // justTest return (narrow_phase.dart:781-799): the SplitSolver's equation
+  // ids count it, contact or not
+  if (tests && P.split && rk == RK_SP) W.job_att[job] = 1;
+  if (tests && just_test && !P.events) return RK_NONE;
   X.xA = swap ? xj : xi;
   X.xB = swap ? xi : xj;
   X.qA = swap ? qj : qi;
@@ -1458,7 +1465,8 @@ DI void ph_rows_assemble(Smem& S, double h) {
 // chunk the dynamic shared memory stays under the 48 KB default limit)
 #define CP_SMEM_LEVEL_MAX 8448
 
-DI void ph_levels(Smem& S, int* s_last, int last_cap, int2* s_pairs) {
+// order: the rows in the order the solver takes them (null: row order)
+DI void ph_levels(Smem& S, int* s_last, int last_cap, int2* s_pairs, const int* order = nullptr) {
   const DWorld& W = S.W;
   const int nrows = S.n_rows;
   const int nb = S.P.nb;
@@ -1470,7 +1478,10 @@ DI void ph_levels(Smem& S, int* s_last, int last_cap, int2* s_pairs) {
   for (int c0 = 0; c0 < nrows; c0 += CP_LEVEL_CHUNK) {
     const int n = min(CP_LEVEL_CHUNK, nrows - c0);
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += BT) s_pairs[i] = make_int2(W.rows[c0 + i].bi, W.rows[c0 + i].bj);
+    for (int i = threadIdx.x; i < n; i += BT) {
+      const int r = order ? order[c0 + i] : c0 + i;
+      s_pairs[i] = make_int2(W.rows[r].bi, W.rows[r].bj);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       for (int i = 0; i < n; i++) {
@@ -1485,7 +1496,7 @@ DI void ph_levels(Smem& S, int* s_last, int last_cap, int2* s_pairs) {
       }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += BT) W.level_of[c0 + i] = s_pairs[i].x;
+    for (int i = threadIdx.x; i < n; i += BT) W.level_of[order ? order[c0 + i] : c0 + i] = s_pairs[i].x;
   }
   if (threadIdx.x == 0) S.n_levels = nlev;
   __syncthreads();
@@ -1667,6 +1678,244 @@ DI void ph_solve_apply(Smem& S, double h) {
 }
 
 // ---------------------------------------------------------------------------
+// SplitSolver (split_solver.dart:53-126) over the GSSolver.
+//
+// Its islands are the connected groups of non-static bodies (getUnvisitedNode
+// skips static ones), each solved on its own: equations sorted by
+// Equation.id, highest first, and its own convergence test.  Islands share
+// no body that moves, so they are swept together here: the rows go through
+// the dependency levels in descending id order (within an island that is its
+// order), a row is skipped once its island has converged, and only the
+// bodies of islands with equations take the velocity update.  Ids: the
+// constraints' from their constructors, the contact and friction equations'
+// from the narrowphase's object pools (last step's equations pushed in order,
+// popped from the end; new objects take Equation.idCounter in creation
+// order), world_class.dart:506-527, narrow_phase.dart:492-586.
+
+DI bool split_moves(const DBody& b) { return b.type != CP_BODY_STATIC; }
+
+// equation ids of the step's contacts and friction candidates: contact c is
+// created after the cscr[c] friction objects of the contacts before it, the
+// two of its own right after it
+// Contact equation objects are taken in job order: one per contact, and
+// one per spherePlane job whether it makes a contact or not; contact c is
+// object e(c) of the step.
+DI void split_ids(Smem& S) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  const int Pc = P.pool_c, Pf = P.pool_f;
+  const long long idc = P.id_counter;
+  const int nj = S.n_jobs;
+  for (int j = threadIdx.x; j < nj; j += BT) W.job_base[j] = W.job_att[j] ? 1 : W.pair_cnt[j];
+  __syncthreads();
+  const int E = block_scan_array(S, W.job_base, nj);
+  if (threadIdx.x == 0) S.split_e = E;
+  for (int c = threadIdx.x; c < S.n_contacts; c += BT) {
+    const int job = W.contacts[c].pair;
+    const int e = W.job_base[job] + (c - W.heavy[job]);
+    const int F = W.cscr[c];
+    W.ct_id[c] = e < Pc ? W.pool_c[Pc - 1 - e] : idc + (e - Pc) + max(0, F - Pf);
+    const int f0 = W.contacts[c].frow;
+    if (f0 >= 0)
+      for (int j = 0; j < 2; j++) {
+        const int m = f0 + j;
+        W.fr_id[m] = m < Pf ? W.pool_f[Pf - 1 - m] : idc + max(0, e + 1 - Pc) + (m - Pf);
+      }
+  }
+  __syncthreads();
+}
+
+// id of the equation behind row candidate cd (friction, contact, then
+// constraint candidates)
+DI long long split_row_id(const DWorld& W, const DWorldParams& P, int cd, int nF, int nc) {
+  if (cd < nF) return W.fr_id[cd];
+  if (cd < nF + nc) return W.ct_id[cd - nF];
+  const int x = cd - nF - nc;
+  int lo = 0, hi = P.ncons - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (W.cons[mid].row0 <= x) lo = mid;
+    else hi = mid - 1;
+  }
+  return W.cons[lo].first_id + (x - W.cons[lo].row0);
+}
+
+DI int uf_root(const int* par, int x) {
+  int p = *(volatile const int*)&par[x];
+  while (p != x) {
+    x = p;
+    p = *(volatile const int*)&par[x];
+  }
+  return x;
+}
+// union by the smaller root: every island ends rooted at its smallest body
+DI void uf_union(int* par, int a, int b) {
+  for (;;) {
+    a = uf_root(par, a);
+    b = uf_root(par, b);
+    if (a == b) return;
+    if (a > b) { const int t = a; a = b; b = t; }
+    if (atomicCAS(&par[b], b, a) == b) return;
+  }
+}
+
+// row ids, islands and the rows in descending id order (sort_val)
+DI void split_prepare(Smem& S) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  const int nb = P.nb, nrows = S.n_rows;
+  for (int i = threadIdx.x; i < nb; i += BT) {
+    W.isl_par[i] = split_moves(W.bodies[i]) ? i : -1;
+    W.isl_rows[i] = 0;
+  }
+  const int N = W.sort_n;
+  for (int r = threadIdx.x; r < N; r += BT) {
+    W.sort_key[r] = r < nrows ? split_row_id(W, P, W.rows[r].src, S.n_fric, S.n_contacts) : LLONG_MIN;
+    W.sort_val[r] = r;
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < nrows; r += BT) {
+    const int a = W.rows[r].bi, b = W.rows[r].bj;
+    if (W.isl_par[a] >= 0 && W.isl_par[b] >= 0) uf_union(W.isl_par, a, b);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += BT)
+    if (W.isl_par[i] >= 0) W.isl_par[i] = uf_root(W.isl_par, i);
+  __syncthreads();
+  for (int r = threadIdx.x; r < nrows; r += BT) {
+    W.row_id[r] = W.sort_key[r];
+    const int a = W.rows[r].bi, b = W.rows[r].bj;
+    const int isl = W.isl_par[a] >= 0 ? W.isl_par[a] : W.isl_par[b];
+    W.row_isl[r] = isl;
+    if (isl >= 0) atomicAdd(&W.isl_rows[isl], 1);
+  }
+  // bitonic sort of (id, row), highest id first; ids are distinct
+  for (int k = 2; k <= N; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < N; i += BT) {
+        const int l = i ^ j;
+        if (l <= i) continue;
+        const long long ki = W.sort_key[i], kl = W.sort_key[l];
+        const bool up = (i & k) == 0;  // this run ends up highest first
+        if (up ? ki < kl : ki > kl) {
+          W.sort_key[i] = kl;
+          W.sort_key[l] = ki;
+          const int t = W.sort_val[i];
+          W.sort_val[i] = W.sort_val[l];
+          W.sort_val[l] = t;
+        }
+      }
+    }
+  __syncthreads();
+}
+
+// GSSolver.solve's sweeps for every island at once; returns the most
+// iterations any island took
+DI int split_sweeps(Smem& S) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  const int nb = P.nb, nrows = S.n_rows, nl = S.n_levels;
+  const VelRef V = vel_global(W);
+  const double tol2 = P.tolerance * P.tolerance;
+  for (int i = threadIdx.x; i < nb; i += BT) W.isl_iter[i] = W.isl_rows[i] > 0 ? -1 : 0;
+  if (threadIdx.x == 0) S.converged = 0;
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < P.iterations; sweep++) {
+    for (int i = threadIdx.x; i < nb; i += BT) W.isl_sum[i] = 0.0;
+    __syncthreads();
+    for (int l = 0; l < nl; l++) {
+      const int b = W.level_start[l], e = W.level_start[l + 1];
+      for (int p = b + threadIdx.x; p < e; p += BT) {
+        const int r = W.sw_orig[p];
+        const int isl = W.row_isl[r];
+        if (isl < 0 || W.isl_iter[isl] >= 0) continue;
+        const double a = gs_row_sw(W, V, p, W.sw_b[p]);
+        W.absdl[r] = a;
+        atomicAdd(&W.isl_sum[isl], a);
+      }
+      __syncthreads();
+    }
+    // per island: (sum of |dlambda| in its row order)^2 < tol^2, the
+    // order-free sum deciding unless it lies within the rounding band
+    int left = 0;
+    for (int i = threadIdx.x; i < nb; i += BT) {
+      if (W.isl_iter[i] >= 0) continue;
+      const double sp = W.isl_sum[i];
+      const double band = 2.2 * (double)W.isl_rows[i] * 1.1102230246251565e-16;
+      const double hi = sp * (1.0 + band), lo = sp * (1.0 - band);
+      int conv;
+      if (hi * hi * (1.0 + 4.5e-16) < tol2) conv = 1;
+      else if (lo * lo * (1.0 - 4.5e-16) >= tol2 && lo >= 0.0) conv = 0;
+      else {
+        double t = 0.0;
+        for (int q = 0; q < nrows; q++) {
+          const int r = W.sort_val[q];
+          if (W.row_isl[r] == i) t += W.absdl[r];
+        }
+        conv = t * t < tol2;
+      }
+      if (conv) W.isl_iter[i] = sweep;
+      else left = 1;
+    }
+    S.warp[threadIdx.x >> 5] = __any_sync(0xffffffffu, left);
+    __syncthreads();
+    int any = 0;
+    for (int w = 0; w < NWARP; w++) any |= S.warp[w];
+    __syncthreads();
+    if (!any) { sweep++; break; }
+  }
+  // islands still sweeping took every iteration
+  int most = 0;
+  for (int i = threadIdx.x; i < nb; i += BT) {
+    if (W.isl_rows[i] == 0) continue;
+    const int it = W.isl_iter[i] >= 0 ? W.isl_iter[i] : P.iterations;
+    most = max(most, it);
+  }
+  for (int o = 16; o > 0; o >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, o));
+  if ((threadIdx.x & 31) == 0) S.warp[threadIdx.x >> 5] = most;
+  __syncthreads();
+  int m = 0;
+  for (int w = 0; w < NWARP; w++) m = max(m, S.warp[w]);
+  __syncthreads();
+  (void)sweep;
+  return m;
+}
+
+// velocity update of the bodies of islands with equations; multipliers
+DI void split_apply(Smem& S, double h) {
+  const DWorld& W = S.W;
+  for (int i = threadIdx.x; i < S.P.nb; i += BT) {
+    const int isl = W.isl_par[i];
+    if (isl >= 0 && W.isl_rows[isl] > 0) apply_body(W, i);
+  }
+  const double invDt = 1 / h;
+  for (int p = threadIdx.x; p < S.n_rows; p += BT) apply_row(W, p, invDt);
+  __syncthreads();
+}
+
+// the step's equations back into the pools (world_class.dart:506-517): the
+// objects it did not pop stay at the bottom, its own go on top in creation
+// order
+DI void split_pools(Smem& S) {
+  const DWorld& W = S.W;
+  const DWorldParams& P = S.P;
+  const int nc = S.n_contacts, nF = S.n_fric, E = S.split_e;
+  const int bc = P.pool_c - min(P.pool_c, E), bf = P.pool_f - min(P.pool_f, nF);
+  __syncthreads();
+  for (int c = threadIdx.x; c < nc; c += BT) W.pool_c[bc + c] = W.ct_id[c];
+  for (int m = threadIdx.x; m < nF; m += BT) W.pool_f[bf + m] = W.fr_id[m];
+  if (threadIdx.x == 0) {
+    DWorldParams* gp = W.P;
+    gp->pool_c = bc + nc;
+    gp->pool_f = bf + nF;
+    gp->id_counter = P.id_counter + max(0, E - P.pool_c) + max(0, nF - P.pool_f);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
 // damping, integrate, clearForces, sleepTick (world_class.dart:647-700,
 // rigid_body.dart:263-300,627-680)
 DI void integrate_body(const DWorld& W, const DWorldParams& P, int i, double dt, bool qn, double time) {
@@ -1773,7 +2022,31 @@ DI bool step_pre(Smem& S, int* s_last, int last_cap, int2* s_pairs, double dt) {
   tick(S, 3);
   ph_rows_assemble(S, dt);
   tick(S, 4);
-  if (S.n_rows > 0) ph_levels(S, s_last, last_cap, s_pairs);
+  if (S.P.split) {
+    split_ids(S);
+    if (S.n_rows > 0) split_prepare(S);
+  }
+  if (S.n_rows > 0) ph_levels(S, s_last, last_cap, s_pairs, S.P.split ? S.W.sort_val : nullptr);
   tick(S, 5);
   return true;
+}
+
+// The rest of a step of a SplitSolver world, in the pre-step kernel's block:
+// island sweeps, velocity update, integration, the pools
+DI void step_split_rest(Smem& S, double dt, double time_inc) {
+  int iters = 0;
+  if (S.n_rows > 0) {
+    iters = split_sweeps(S);
+    split_apply(S, dt);
+  }
+  ph_integrate(S, dt);
+  split_pools(S);
+  if (threadIdx.x == 0) {
+    DWorldParams* gp = S.W.P;
+    gp->last_iterations = iters;
+    gp->stepnumber = S.P.stepnumber + 1;
+    gp->time = S.P.time + time_inc;
+    gp->presolved = 1;
+  }
+  __syncthreads();
 }

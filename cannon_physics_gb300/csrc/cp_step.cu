@@ -290,7 +290,7 @@ DI void joint_solve(Smem& S, Slot* slots, int K, double* s_acc, const VelRef* vr
 // up to last_cap bodies.
 template <int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_step_pre(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n,
-                                                           double dt, int* __restrict__ queue, int last_cap) {
+                                                           double dt, double time_inc, int* __restrict__ queue, int last_cap) {
   __shared__ Smem S;
   extern __shared__ int2 s_dyn[];
   int2* s_pairs = s_dyn;
@@ -321,8 +321,11 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step_pre(const DWorld* __rest
         gp->num_contacts = S.n_contacts;
         gp->num_rows = ok ? S.n_rows : 0;
         gp->num_levels = ok ? S.n_levels : 0;
+        gp->presolved = 0;
         if (!ok) gp->status = S.overflow;
       }
+      // a SplitSolver world finishes its step here; the solve kernel skips it
+      if (ok && S.P.split) step_split_rest(S, dt, time_inc);
     }
     __syncthreads();
   }
@@ -367,7 +370,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step_solve(const DWorld* __re
       sl.id = ids[k0 + threadIdx.x];
       sl.W = worlds[sl.id];
       sl.P = *sl.W.P;
-      sl.ok = sl.P.status == 0 && sl.P.stepnumber < sl.P.step_limit;
+      sl.ok = sl.P.status == 0 && sl.P.stepnumber < sl.P.step_limit && !sl.P.presolved;
       sl.n_rows = sl.ok ? sl.P.num_rows : 0;
       sl.n_levels = sl.P.num_levels;
       sl.done = 0;
@@ -480,7 +483,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) k_step_solve_w(const DWorld*
       t.id = ids[k0 + lane];
       t.W = worlds[t.id];
       t.P = *t.W.P;
-      t.ok = t.P.status == 0 && t.P.stepnumber < t.P.step_limit;
+      t.ok = t.P.status == 0 && t.P.stepnumber < t.P.step_limit && !t.P.presolved;
       t.n_rows = t.ok ? t.P.num_rows : 0;
       t.n_levels = t.P.num_levels;
       t.iters = 0;
@@ -848,7 +851,7 @@ cudaError_t cpk_set_resolver_profile(int on) {
 // that hide each other's waits, differs between them.  All compute
 // identical results.
 struct PreVariant {
-  void (*fn)(const DWorld*, const int*, int, double, int*, int);
+  void (*fn)(const DWorld*, const int*, int, double, double, int*, int);
   int threads;
   int minb;
 };
@@ -907,7 +910,7 @@ cudaError_t cpk_launch_step(const DWorld* d_worlds, const int* d_ids, const int*
   const PreVariant& P = kPre[variant / kNumSolve];
   const SolveVariant& V = kSolve[variant % kNumSolve];
   const int cap = last_cap_for(max_nb);
-  P.fn<<<grid_pre, P.threads, pre_smem(cap), stream>>>(d_worlds, d_ids, n, dt, d_queue, cap);
+  P.fn<<<grid_pre, P.threads, pre_smem(cap), stream>>>(d_worlds, d_ids, n, dt, time_inc, d_queue, cap);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   V.fn<<<grid_solve, V.threads, solve_smem(V), stream>>>(d_worlds, d_ids, d_gstart, ngroups, dt, time_inc, d_queue + 1);

@@ -116,6 +116,8 @@ struct __align__(16) DConstraint {
   float ri[4], rj[4], n[4];
   float rot_a[3][4], rot_b[3][4];  // world axes (axisA, axisB) of the rotational rows
   float ma[4], mb[4];              // motor axes
+  long long first_id;              // SplitSolver: Equation.id of row 0 (the others follow)
+  long long pad3;
 };
 
 struct __align__(16) DContact {
@@ -165,6 +167,11 @@ struct __align__(16) DWorldParams {
   long long step_limit;  // the step kernels leave the world alone once stepnumber reaches this
   int compound, jobs_cap;  // some body has several shapes; capacity of the shape-pair job list
   int num_jobs, pad3;  // narrowphase jobs of the last step (shape pairs; the pairs without compound bodies)
+  // SplitSolver: on; sizes of the contact / friction equation pools (stacks
+  // of ids); set by the pre-step kernel when it ran the whole step itself
+  int split, pool_c, pool_f, presolved;
+  long long id_counter;  // Equation.idCounter
+  long long pad5;
 };
 
 // A compound body's second, third, ... shape (Body.shapes[1..] with its
@@ -227,6 +234,23 @@ struct DWorld {
   // pair_flag and the queues are indexed by job.
   int* job_pair;
   int* job_sh;
+  // SplitSolver: the equation pools (persistent, outside the step scratch),
+  // the step's equation ids, islands and the rows in descending id order
+  long long* pool_c;   // contact equation ids, bottom first (capacity contacts_cap)
+  long long* pool_f;   // friction equation ids (capacity 2 * contacts_cap)
+  long long* ct_id;    // per contact
+  long long* fr_id;    // per friction candidate
+  long long* row_id;   // per row
+  long long* sort_key; // bitonic sort of the rows by id: keys, then row indices
+  int* sort_val;
+  int sort_n;          // power of two >= rows_cap
+  int* isl_par;        // per body: union-find parent, then the island (its smallest body), -1 static
+  int* isl_rows;       // per island: rows
+  int* isl_iter;       // per island: -1 while it sweeps, then its iterations
+  double* isl_sum;     // per island: the sweep's sum of |dlambda|
+  int* row_isl;        // per row: island
+  int* job_att;        // per narrowphase job: 1 when spherePlane took an equation object for it
+  int* job_base;       // per job: contact objects taken before it (scan)
   int* heavy;       // pairs queued for a resolver, (kind << 28) | pair; later scan scratch
   int* heavy2;      // queued pairs sorted by resolver kind (pairs + 16 * 32 slots)
   DContact* ctmp;

@@ -94,6 +94,8 @@ class Scene:
     time: float = 0.0
     stepnumber: int = 0
     friction_gravity: tuple = None
+    solver: int = A.SOLVER_GS
+    equation_id_counter: int = 0  # SPLIT: Equation.idCounter when the world is handed over
     # the extra shapes of compound bodies (bodies' extra_shapes_first / _count index it)
     body_shapes: np.ndarray = field(default_factory=lambda: np.zeros(0, dtype=A.BODY_SHAPE_DTYPE))
     _keep: list = field(default_factory=list)
@@ -138,8 +140,29 @@ class Scene:
         d.contact_materials = A.ptr(self.contact_materials)
         d.constraints = A.ptr(self.constraints)
         d.sap_axis_list = 0
+        d.solver = self.solver
+        d.equation_id_counter = self.equation_id_counter
         d.default_contact_material = A.default_contact_material(self.friction, self.restitution)
         return d
+
+
+# equations each constraint type's constructor creates (cp_constraint_desc)
+CONSTRAINT_EQUATIONS = {A.CON_P2P: 3, A.CON_HINGE: 6, A.CON_DISTANCE: 1, A.CON_LOCK: 6, A.CON_CONE_TWIST: 5,
+                        A.CON_SPRING: 1}
+
+
+def use_split_solver(scene, first_id=0):
+    """Switch a scene to the SplitSolver with the equation ids a fresh Dart
+    process gives it: the constraints' equations first (constructors run in
+    constraint order, ids from first_id), the contact and friction equations
+    of the steps after them."""
+    scene.solver = A.SOLVER_SPLIT
+    nxt = first_id
+    for c in scene.constraints:
+        c["first_equation_id"] = nxt
+        nxt += CONSTRAINT_EQUATIONS[int(c["type"])]
+    scene.equation_id_counter = nxt
+    return scene
 
 
 def _plane_body(bodies, shapes, i, shape_index, y=0.0):

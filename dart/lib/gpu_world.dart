@@ -368,8 +368,13 @@ class GpuWorld extends World {
       r.allowSleep = allowSleep ? 1 : 0;
       r.quatNormalizeSkip = quatNormalizeSkip;
       r.quatNormalizeFast = quatNormalizeFast ? 1 : 0;
+      // GSSolver, or SplitSolver over a GSSolver with the SplitSolver's
+      // iterations and tolerance (split_solver.dart:91-92); equation ids
+      // continue from Equation.idCounter
       r.solverIterations = solver.iterations;
-      r.solverTolerance = solver is GSSolver ? (solver as GSSolver).tolerance : 1e-7;
+      r.solverTolerance = solver.tolerance;
+      r.solver = solver is SplitSolver ? cpSolverSplit : cpSolverGs;
+      r.equationIdCounter = Equation.idCounter;
       r.useBoundingBoxes = broadphase.useBoundingBoxes ? 1 : 0;
       r.enableFrictionReduction = narrowphase.enableFrictionReduction ? 1 : 0;
       final bp = broadphase;
@@ -437,6 +442,7 @@ class GpuWorld extends World {
     d.bodyB = bodies.indexOf(c.bodyB);
     d.collideConnected = c.collideConnected ? 1 : 0;
     final eq = c.equations.first;
+    d.firstEquationId = eq.id;
     d.spookStiffness = eq.stiffness;
     d.spookRelaxation = eq.relaxation;
     d.spookTimeStep = 1 / 60;

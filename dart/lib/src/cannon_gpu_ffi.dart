@@ -22,6 +22,7 @@ const int cpShapeCapsule = 5, cpShapeCone = 6, cpShapeSizedPlane = 7;
 const int cpBroadNaive = 0, cpBroadSap = 1, cpBroadGrid = 2;
 const int cpConPointToPoint = 0, cpConHinge = 1, cpConDistance = 2;
 const int cpConLock = 3, cpConConeTwist = 4, cpConSpring = 5;
+const int cpSolverGs = 0, cpSolverSplit = 1;
 
 final class CpShapeDesc extends Struct {
   @Int32() external int type;
@@ -151,6 +152,7 @@ final class CpConstraintDesc extends Struct {
   @Array(6, 3) external Array<Array<Float>> lockAxes;
   @Double() external double angle;
   @Double() external double twistAngle;
+  @Int64() external int firstEquationId;
 }
 
 final class CpWorldDesc extends Struct {
@@ -185,7 +187,8 @@ final class CpWorldDesc extends Struct {
   external CpContactMaterial defaultContactMaterial;
   external Pointer<CpBodyShape> bodyShapes;
   @Int32() external int numBodyShapes;
-  @Int32() external int pad0;
+  @Int32() external int solver;
+  @Int64() external int equationIdCounter;
 }
 
 /// cp_ray: one ray of World.raycastClosest / Any / All.

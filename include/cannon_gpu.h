@@ -76,6 +76,16 @@ enum cp_constraint_type {
   CP_CON_SPRING = 5                 /* spring_constraint.dart */
 };
 
+/* World.solver: GSSolver (lib/solver/gs_solver.dart) or SplitSolver over a
+ * GSSolver with the same iterations and tolerance (lib/solver/split_solver.dart:
+ * islands of non-static bodies, each solved on its own with its equations in
+ * descending Equation.id order).  A SPLIT world keeps the reference's equation
+ * ids: constraint equations take their constructor's ids
+ * (cp_constraint_desc.first_equation_id ..), contact and friction equations
+ * are drawn from the same last-in-first-out object pools the reference
+ * recycles them through (world_class.dart:506-527, narrow_phase.dart:492-586). */
+enum cp_solver_kind { CP_SOLVER_GS = 0, CP_SOLVER_SPLIT = 1 };
+
 /* Equation classes appearing as solver rows, lib/equations/*.dart */
 enum cp_row_kind { CP_ROW_CONTACT = 0, CP_ROW_FRICTION = 1, CP_ROW_ROTATIONAL = 2, CP_ROW_MOTOR = 3 };
 
@@ -212,6 +222,7 @@ typedef struct cp_constraint_desc {
   double spook_stiffness, spook_relaxation, spook_time_step;
   float lock_axes[6][3];            /* LockConstraint xA, xB, yA, yB, zA, zB */
   double angle, twist_angle;        /* ConeTwistConstraint */
+  int64_t first_equation_id;        /* SPLIT: Equation.id of the first row; the others follow */
 } cp_constraint_desc;
 
 /* World (lib/world/world_class.dart:135-162) plus solver/broadphase settings. */
@@ -240,7 +251,11 @@ typedef struct cp_world_desc {
   cp_contact_material default_contact_material;
   const cp_body_shape* body_shapes; /* shapes after each body's first (compound bodies) */
   int32_t num_body_shapes;
-  int32_t pad0;
+  int32_t solver;                   /* cp_solver_kind */
+  /* SPLIT: Equation.idCounter when the world is handed over (the ids of the
+   * contact and friction equations created from then on follow it; the
+   * equation pools start empty) */
+  int64_t equation_id_counter;
 } cp_world_desc;
 
 /* One narrowphase contact, in the order the reference appends them. */
@@ -252,10 +267,12 @@ typedef struct cp_contact {
   double restitution;
 } cp_contact;
 
-/* One solver row, in GSSolver equation order. */
+/* One solver row, in World.internalStep's equation order (friction,
+ * contact, constraint rows). */
 typedef struct cp_row {
   int32_t kind, bi, bj, pad;
   double B, inv_c, lambda, multiplier, min_force, max_force, eps;
+  int64_t id;                       /* Equation.id under the SPLIT solver, else -1 */
 } cp_row;
 
 typedef struct cp_step_info {

@@ -670,6 +670,7 @@ struct Eq {
   double targetVelocity = 0;
   int pair = -1;
   double B = 0, invC = 0, lambda = 0;
+  long long id = -1;  // Equation.id (equation_class.dart:34-37), kept under the SplitSolver
 
   // equation_class.dart:53-60
   void setSpookParams(double stiffness, double relaxation, double timeStep) {
@@ -761,6 +762,18 @@ struct World {
   std::vector<cp_body_shape> bodyShapeTable;  // the compound bodies' extra shapes
   // events (world_class.dart:213-221,593-610,703-770), when recorded
   bool events = false;
+  // SplitSolver (split_solver.dart) and the equation ids it sorts by: the
+  // global Equation.idCounter and the narrowphase's reuse pools of contact
+  // and friction equation objects, as stacks of ids (world_class.dart:506-527)
+  bool split = false;
+  long long idCounter = 0;
+  std::vector<long long> contactPool, frictionPool;
+  long long takeId(std::vector<long long>& pool) {  // pool.removeLast() or a new object
+    if (pool.empty()) return idCounter++;
+    const long long id = pool.back();
+    pool.pop_back();
+    return id;
+  }
   std::vector<int> bodyIds, shapeIds;
   OverlapKeeper bodyOverlapKeeper, shapeOverlapKeeper;
   std::vector<cp_event> eventQueue;
@@ -973,6 +986,7 @@ struct World {
       c.restitution = materials[matA].restitution * materials[matB].restitution;
     c.si = rsi; c.sj = rsj;
     c.pair = curPair;
+    if (split) c.id = takeId(contactPool);
     return c;
   }
   // narrow_phase.dart:530-586
@@ -1002,6 +1016,10 @@ struct World {
       c1.enabled = ce.enabled; c2.enabled = ce.enabled;
       c1.si = c2.si = ce.si; c1.sj = c2.sj = ce.sj;
       c1.pair = c2.pair = ce.pair;
+      if (split) {  // c1 then c2 (narrow_phase.dart:556-557)
+        c1.id = takeId(frictionPool);
+        c2.id = takeId(frictionPool);
+      }
       frictionEqs.push_back(c1);
       frictionEqs.push_back(c2);
       return true;
@@ -1527,9 +1545,19 @@ struct World {
           curPair = k;
           if (justTest) {
             // a justTest resolver adds no contacts; where it would find one it
-            // registers the overlap (narrow_phase.dart:712-715)
+            // registers the overlap (narrow_phase.dart:712-715).  spherePlane
+            // takes its equation object before the justTest return
+            // (:781-799), and the object is lost to the pool
+            const bool spherePlane = (si.type == CP_SHAPE_SPHERE && sj.type == CP_SHAPE_PLANE) ||
+                                     (sj.type == CP_SHAPE_SPHERE && si.type == CP_SHAPE_PLANE);
+            if (split && spherePlane) takeId(contactPool);
             if (events) {
+              // the reference's resolvers return before creating equations:
+              // the trial leaves the pools and the id counter as they were
               const size_t nc = contacts.size(), nf = frictionEqs.size();
+              const std::vector<long long> keepC = split ? contactPool : std::vector<long long>();
+              const std::vector<long long> keepF = split ? frictionPool : std::vector<long long>();
+              const long long keepId = idCounter;
               if (si.type < sj.type) dispatch(si, sj, xi, xj, qi, qj, ibi, ibj, isi, isj, isi, isj);
               else dispatch(sj, si, xj, xi, qj, qi, ibj, ibi, isj, isi, isi, isj);
               if (contacts.size() > nc) {
@@ -1538,6 +1566,11 @@ struct World {
               }
               contacts.resize(nc);
               frictionEqs.resize(nf);
+              if (split) {
+                contactPool = keepC;
+                frictionPool = keepF;
+                idCounter = keepId;
+              }
             }
             continue;
           }
@@ -1684,13 +1717,72 @@ struct World {
   }
   // gs_solver.dart:74-180
   int solve(std::vector<Eq*>& eqs, double dt) {
+    std::vector<int> all(bodies.size());
+    for (size_t i = 0; i < all.size(); i++) all[i] = (int)i;
+    return gsSolve(eqs, all, dt);
+  }
+  // SplitSolver.solve (split_solver.dart:53-126): islands of non-static bodies
+  // in body order (getUnvisitedNode), each gathered by the node walk of bfs /
+  // visitFunc (:134-166), its equations sorted by id, highest first
+  // (sortById, :168-170), and solved by the GSSolver over the island's bodies.
+  // Returns the most iterations any island took.
+  int splitSolve(std::vector<Eq*>& eqs, double dt) {
+    const int N = (int)bodies.size();
+    std::vector<std::vector<int>> children(N);
+    std::vector<std::vector<Eq*>> nodeEqs(N);
+    for (Eq* e : eqs) {
+      children[e->bi].push_back(e->bj);
+      nodeEqs[e->bi].push_back(e);
+      children[e->bj].push_back(e->bi);
+      nodeEqs[e->bj].push_back(e);
+    }
+    std::vector<char> visited(N, 0);
+    auto unvisited = [&](const std::vector<int>& list) {
+      for (int i : list)
+        if (!visited[i] && bodies[i].type != CP_BODY_STATIC) return i;
+      return -1;
+    };
+    std::vector<int> all(N);
+    for (int i = 0; i < N; i++) all[i] = i;
+    int most = 0;
+    for (;;) {
+      const int root = unvisited(all);
+      if (root < 0) break;
+      std::vector<int> island;
+      std::vector<Eq*> ieqs;
+      auto visit = [&](int node) {
+        island.push_back(node);
+        for (Eq* e : nodeEqs[node])
+          if (std::find(ieqs.begin(), ieqs.end(), e) == ieqs.end()) ieqs.push_back(e);
+      };
+      std::vector<int> queue{root};
+      visited[root] = 1;
+      visit(root);
+      while (!queue.empty()) {
+        const int node = queue.back();
+        queue.pop_back();
+        for (;;) {
+          const int child = unvisited(children[node]);
+          if (child < 0) break;
+          visited[child] = 1;
+          visit(child);
+          queue.push_back(child);
+        }
+      }
+      std::sort(ieqs.begin(), ieqs.end(), [](const Eq* a, const Eq* b) { return a->id > b->id; });
+      most = std::max(most, gsSolve(ieqs, island, dt));
+    }
+    return most;
+  }
+  // GSSolver.solve (gs_solver.dart:27-133) over the given bodies
+  int gsSolve(std::vector<Eq*>& eqs, const std::vector<int>& bodyList, double dt) {
     int iter = 0;
     const int maxIter = iterations;
     const double tolSquared = tolerance * tolerance;
     const int nEq = (int)eqs.size();
-    const int nBodies = (int)bodies.size();
+    const int nBodies = (int)bodyList.size();
     const double h = dt;
-    if (nEq != 0) for (auto& b : bodies) updateSolveMassProperties(b);
+    if (nEq != 0) for (int bi : bodyList) updateSolveMassProperties(bodies[bi]);
     for (int i = 0; i != nEq; i++) {
       Eq& c = *eqs[i];
       c.lambda = 0.0;
@@ -1698,7 +1790,11 @@ struct World {
       c.invC = 1.0 / computeC(c);
     }
     if (nEq != 0) {
-      for (int i = 0; i != nBodies; i++) { setValues(bodies[i].vlambda, 0, 0, 0); setValues(bodies[i].wlambda, 0, 0, 0); }
+      for (int i = 0; i != nBodies; i++) {
+        Body& b = bodies[bodyList[i]];
+        setValues(b.vlambda, 0, 0, 0);
+        setValues(b.wlambda, 0, 0, 0);
+      }
       for (iter = 0; iter != maxIter; iter++) {
         double deltalambdaTot = 0.0;
         for (int j = 0; j != nEq; j++) {
@@ -1715,7 +1811,7 @@ struct World {
         if (deltalambdaTot * deltalambdaTot < tolSquared) break;
       }
       for (int i = 0; i != nBodies; i++) {
-        Body& b = bodies[i];
+        Body& b = bodies[bodyList[i]];
         multiply2(b.vlambda, b.linearFactor, b.vlambda);
         add2(b.velocity, b.vlambda, b.velocity);
         multiply2(b.wlambda, b.angularFactor, b.wlambda);
@@ -2044,6 +2140,10 @@ struct World {
       bodyOverlapKeeper.tick();
       shapeOverlapKeeper.tick();
     }
+    if (split) {  // last step's equations back into the pools, in order (world_class.dart:506-517)
+      for (const Eq& c : contacts) contactPool.push_back(c.id);
+      for (const Eq& f : frictionEqs) frictionPool.push_back(f.id);
+    }
     getContacts();
     std::vector<Eq*> eqs;
     for (auto& f : frictionEqs) addEquation(eqs, f);
@@ -2082,7 +2182,7 @@ struct World {
       updateConstraint(c);
       for (auto& e : c.eqs) addEquation(eqs, e);
     }
-    lastIterations = solve(eqs, dt);
+    lastIterations = split ? splitSolve(eqs, dt) : solve(eqs, dt);
     solverRows.clear();
     for (Eq* e : eqs) solverRows.push_back(*e);
     for (int i = 0; i != N; i++) {  // damping
@@ -2246,6 +2346,9 @@ static int buildWorld(const cp_world_desc& d, World& w) {
   if (w.broadphase == CP_BROAD_GRID && (w.gridN[0] <= 0 || w.gridN[1] <= 0 || w.gridN[2] <= 0)) return CP_ERR_ARG;
   w.enableFrictionReduction = d.enable_friction_reduction != 0;
   w.time = d.time;
+  if (d.solver < CP_SOLVER_GS || d.solver > CP_SOLVER_SPLIT) return CP_ERR_ARG;
+  w.split = d.solver == CP_SOLVER_SPLIT;
+  w.idCounter = d.equation_id_counter;
   w.stepnumber = d.stepnumber;
   w.axisList.resize(d.num_bodies);
   for (int i = 0; i < d.num_bodies; i++) w.axisList[i] = d.sap_axis_list ? d.sap_axis_list[i] : i;
@@ -2258,11 +2361,13 @@ static int buildWorld(const cp_world_desc& d, World& w) {
     c.collideConnected = cd.collide_connected != 0;
     c.pivotA = mk(cd.pivot_a[0], cd.pivot_a[1], cd.pivot_a[2]);
     c.pivotB = mk(cd.pivot_b[0], cd.pivot_b[1], cd.pivot_b[2]);
+    long long nextId = cd.first_equation_id;
     auto newEq = [&](int kind, double minF, double maxF) {
       Eq e;
       e.kind = kind; e.bi = cd.body_a; e.bj = cd.body_b;
       e.minForce = minF; e.maxForce = maxF;
       e.setSpookParams(cd.spook_stiffness, cd.spook_relaxation, cd.spook_time_step);
+      e.id = w.split ? nextId++ : -1;  // the constructor's equations, in equations-list order
       return e;
     };
     double mf = cd.max_force;
@@ -2493,6 +2598,7 @@ int orc_world_get_rows(orc_world* o, cp_row* out, int32_t cap, int32_t* count) {
     r.kind = e.kind; r.bi = e.bi; r.bj = e.bj; r.pad = 0;
     r.B = e.B; r.inv_c = e.invC; r.lambda = e.lambda; r.multiplier = e.multiplier;
     r.min_force = e.minForce; r.max_force = e.maxForce; r.eps = e.eps;
+    r.id = e.id;
   }
   return CP_OK;
 }

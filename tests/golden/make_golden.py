@@ -35,6 +35,8 @@ CASES = [
     ("column_sphere_box", lambda: scenes.column_world(120, 1234, "sphere_box"), 50),
     ("column_mixed", lambda: scenes.column_world(80, 4321, "mixed"), 50),
     ("compound_naive", lambda: scenes.compound_pile(20, seed=12), 60),
+    ("joints_hulls", lambda: scenes.joints_and_hulls(seed=44), 60),
+    ("chains_split", lambda: scenes.use_split_solver(scenes.mixed_chains(8, 4, 4, seed=5, chains=4, chain_len=8)), 60),
 ]
 
 BODY_FIELDS = ["position", "quaternion", "velocity", "angular_velocity", "inv_inertia_world", "sleep_state"]

@@ -7,7 +7,7 @@ BODY_FIELDS = ["position", "quaternion", "velocity", "angular_velocity", "force"
                "aabb_lower", "aabb_upper", "previous_position", "previous_quaternion", "sleep_state", "time_last_sleepy",
                "type"]
 CONTACT_FIELDS = ["bi", "bj", "si", "sj", "ni", "ri", "rj", "enabled", "pair", "restitution"]
-ROW_FIELDS = ["kind", "bi", "bj", "B", "inv_c", "lambda_", "multiplier", "min_force", "max_force", "eps"]
+ROW_FIELDS = ["kind", "bi", "bj", "B", "inv_c", "lambda_", "multiplier", "min_force", "max_force", "eps", "id"]
 
 
 def diff_records(a, b, fields, what):
