@@ -538,6 +538,66 @@ __global__ void k_w_assemble(const DWorld* dw, double h) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Lagged sweeps.  GSSolver sweeps the rows again and again in one order; a
+// row of sweep s+1 needs its bodies as the rows after it left them in sweep
+// s.  If every body's rows lie within D consecutive levels (D = 1 + the
+// largest span), then running level l of sweep s at step l + s*D meets every
+// such need: sweeps overlap, one world's solve takes nl + (K-1)*D steps
+// instead of K*nl, and each step holds several sweeps' rows.  The exit test
+// of sweep s is known only when its last level is done, by which time later
+// sweeps have started: each sweep keeps its rows' lambda and |dlambda| and
+// its bodies' vlambda / wlambda after their last row, in one of
+// CP_LAG_SLOTS history slots, and a sweep that ends the solve rolls the
+// later ones back.  The body update sequence is the reference's, so the bits
+// are.
+
+// per body its level span and last row; per level position the last-row
+// flags; then the lag (0: sweeps one after another)
+DI void lag_prepare(Smem& S) {
+  const DWorld& W = S.W;
+  DWide* x = W.wide;
+  __shared__ int s_span;
+  if (threadIdx.x == 0) { x->lag_d = 0; x->lag_r = 0; s_span = 0; }
+  if (!W.lag_lam || S.n_rows == 0 || S.P.iterations < 2) return;
+  const int nb = S.P.nb, nrows = S.n_rows, nl = S.n_levels;
+  for (int i = threadIdx.x; i < nb; i += BT) {
+    W.lag_bmin[i] = 0x7fffffff;
+    W.lag_bmax[i] = -1;
+    W.lag_blast[i] = -1;
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < nrows; r += BT) {
+    const int l = W.level_of[r];
+    const int a = W.rows[r].bi, b = W.rows[r].bj;
+    if (W.bscr[a].active) { atomicMin(&W.lag_bmin[a], l); atomicMax(&W.lag_bmax[a], l); atomicMax(&W.lag_blast[a], r); }
+    if (b != a && W.bscr[b].active) { atomicMin(&W.lag_bmin[b], l); atomicMax(&W.lag_bmax[b], l); atomicMax(&W.lag_blast[b], r); }
+  }
+  __syncthreads();
+  int span = 0;
+  for (int i = threadIdx.x; i < nb; i += BT)
+    if (W.lag_bmax[i] >= 0) span = max(span, W.lag_bmax[i] - W.lag_bmin[i]);
+  atomicMax(&s_span, span);
+  for (int p = threadIdx.x; p < nrows; p += BT) {
+    const int r = W.sw_orig[p];
+    const int2 bb = W.sw_b[p];
+    W.lag_last[p] = (unsigned char)((W.lag_blast[bb.x] == r ? 1 : 0) | (W.lag_blast[bb.y] == r ? 2 : 0));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int d = s_span + 1;
+    int r = (nl - 1) / d + 2;
+    if (r > CP_LAG_SLOTS) {
+      d = (nl - 1 + CP_LAG_SLOTS - 3) / (CP_LAG_SLOTS - 2);
+      r = (nl - 1) / d + 2;
+    }
+    if (d < nl) {
+      x->lag_d = d;
+      x->lag_r = r;
+    }
+  }
+}
+
 // dependency levels and the level-ordered sweep arrays: one block
 __global__ void __launch_bounds__(1024) k_w_levels(const DWorld* dw, int last_cap) {
   __shared__ Smem S;
@@ -548,6 +608,7 @@ __global__ void __launch_bounds__(1024) k_w_levels(const DWorld* dw, int last_ca
   if (S.n_rows == 0) return;
   ph_levels(S, (int*)(s_dyn + CP_LEVEL_CHUNK), last_cap, s_dyn);
   if (threadIdx.x == 0) S.W.wide->n_levels = S.n_levels;
+  lag_prepare(S);
 }
 
 // ---------------------------------------------------------------------------
@@ -589,6 +650,118 @@ DI bool wide_ok(DWide* x, int code, int idx, int bound) {
   return false;
 }
 
+// one row of sweep slot `slot` at level position p (the unsplit path of
+// the level sweeps, plus the history)
+DI void lag_row(const DWorld& W, const DWorldParams& P, DWide* x, float* vel, unsigned char* flg, int p, int slot,
+                double* s_sum) {
+  const int nrows = x->n_rows, nb = P.nb;
+  if (!wide_ok(x, 1, p, nrows)) return;
+  const RowRec R = load_row(W, p);
+  const int2 bb = W.sw_b[p];
+  if (!wide_ok(x, 2, bb.x, nb) || !wide_ok(x, 2, bb.y, nb)) return;
+  float4 va, wa, vb, wb;
+  wv_load(vel, flg, bb.x, va, wa);
+  wv_load(vel, flg, bb.y, vb, wb);
+  const bool aa = va.w != 0.f, ab = vb.w != 0.f;
+  const double ga = aa ? half_a(R, va, wa) : 0.0;
+  const double gb = ab ? half_b(R, vb, wb) : 0.0;
+  const double dl = row_dl(R, ga, aa, gb, ab);
+  const double lam = R.d1.y + dl;
+  const size_t rs = (size_t)P.rows_cap;
+  W.sw_d[W.sw_cap + p].y = lam;
+  W.lag_lam[slot * rs + p] = lam;
+  if (aa) wv_update_a(vel, bb.x, va, wa, R, dl);
+  if (ab) {
+    if (bb.x == bb.y) wv_load(vel, flg, bb.y, vb, wb);  // a constraint between a body and itself
+    wv_update_b(vel, bb.y, vb, wb, R, dl);
+  }
+  const unsigned last = W.lag_last[p];
+  if (last) {
+    float* hv = W.lag_vel + (size_t)slot * nb * 6;
+    if (last & 1) for (int e = 0; e < 6; e++) hv[6 * bb.x + e] = vel[6 * bb.x + e];
+    if (last & 2) for (int e = 0; e < 6; e++) hv[6 * bb.y + e] = vel[6 * bb.y + e];
+  }
+  const int r = W.sw_orig[p];
+  if (wide_ok(x, 3, r, nrows)) {
+    const double a = dl > 0.0 ? dl : -dl;
+    W.lag_abs[slot * rs + r] = a;
+    atomicAdd(&s_sum[slot], a);
+  }
+}
+
+// GSSolver's exit test (sum of |dlambda| in row order)^2 < tol^2 for a sweep
+// whose order-free sum is sp: decided by sp unless it lies within the
+// rounding band of the threshold, else by the row-order sum of abs[0..n)
+DI bool sweep_converged(double sp, const double* abs, int n, double tol2) {
+  const double band = 2.2 * (double)n * 1.1102230246251565e-16;
+  const double hi = sp * (1.0 + band), lo = sp * (1.0 - band);
+  if (hi * hi * (1.0 + 4.5e-16) < tol2) return true;
+  if (lo * lo * (1.0 - 4.5e-16) >= tol2 && lo >= 0.0) return false;
+  double t = 0.0;
+  for (int r = 0; r < n; r++) t += abs[r];
+  return t * t < tol2;
+}
+
+// the lagged sweeps of one world; returns GSSolver's iteration count
+DI int lag_sweeps(const DWorld& W, const DWorldParams& P, DWide* x, float* vel, unsigned char* flg, const int* ls, int nrows,
+                  int nl) {
+  __shared__ double s_sum[CP_LAG_SLOTS];
+  __shared__ int s_stop;
+  const int K = P.iterations, D = x->lag_d, R = x->lag_r;
+  const int T = nl + (K - 1) * D;
+  const double tol2 = P.tolerance * P.tolerance;
+  const size_t rs = (size_t)P.rows_cap;
+  if (threadIdx.x < CP_LAG_SLOTS) s_sum[threadIdx.x] = 0.0;
+  if (threadIdx.x == 0) s_stop = -1;
+  __syncthreads();
+  int t_end = T - 1, sstar = -1;
+  for (int t = 0; t < T; t++) {
+    const int s_hi = min(K - 1, t / D);
+    const int over = t - (nl - 1);
+    const int s_lo = over > 0 ? (over + D - 1) / D : 0;
+    int total = 0;
+    for (int s = s_lo; s <= s_hi; s++) total += ls[t - s * D + 1] - ls[t - s * D];
+    for (int f = threadIdx.x; f < total; f += BT) {
+      int s = s_lo, off = f;
+      for (;;) {
+        const int l = t - s * D;
+        const int c = ls[l + 1] - ls[l];
+        if (off < c) break;
+        off -= c;
+        s++;
+      }
+      lag_row(W, P, x, vel, flg, ls[t - s * D] + off, s % R, s_sum);
+    }
+    __syncthreads();
+    if (over >= 0 && over % D == 0) {  // sweep over / D has run its last level
+      const int sd = over / D;
+      if (threadIdx.x == 0) {
+        const int slot = sd % R;
+        if (sweep_converged(s_sum[slot], W.lag_abs + slot * rs, nrows, tol2)) s_stop = sd;
+        s_sum[slot] = 0.0;  // the slot's next sweep, sd + R, has not started
+      }
+      __syncthreads();
+      if (s_stop >= 0) {
+        sstar = s_stop;
+        t_end = t;
+        break;
+      }
+    }
+  }
+  if (sstar < 0) return K;
+  // sweeps after sstar that had started go back to the end of sweep sstar
+  if (min(K - 1, t_end / D) > sstar) {
+    const int slot = sstar % R;
+    const float* hv = W.lag_vel + (size_t)slot * P.nb * 6;
+    for (int b = threadIdx.x; b < P.nb; b += BT)
+      if (W.lag_blast[b] >= 0)
+        for (int e = 0; e < 6; e++) vel[6 * b + e] = hv[6 * b + e];
+    for (int p = threadIdx.x; p < nrows; p += BT) W.sw_d[W.sw_cap + p].y = W.lag_lam[slot * rs + p];
+    __syncthreads();
+  }
+  return sstar;
+}
+
 #define WS_THREADS 256  // 186 registers a thread, no spills
 #define WS_LEVELS_SMEM 4096  // level bounds kept in shared memory up to this many levels
 
@@ -627,7 +800,9 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve(const DWorld* dw, int
   const int split_off = (((int)threadIdx.x >> 6) << 5) | ((int)threadIdx.x & 31);
   const int partner = threadIdx.x ^ 32;
   int iters = S.P.iterations;
-  for (int sweep = 0; sweep < S.P.iterations; sweep++) {
+  const bool lagged = x->lag_d > 0;
+  if (lagged) iters = lag_sweeps(W, S.P, x, vel, flg, ls, nrows, nl);
+  for (int sweep = 0; !lagged && sweep < S.P.iterations; sweep++) {
     double acc = 0.0;
     // this thread's first row of level l
     auto first_row = [&](int l, int& p) {

@@ -115,3 +115,24 @@ def test_wide_equals_one_block(ctx):
     assert a.info().iterations == b.info().iterations
     a.destroy()
     b.destroy()
+
+
+@pytest.mark.parametrize("tol", [1e-3, 1e-5])
+def test_wide_lagged_sweeps_stop_early(wide_ctx, tol):
+    """A loose solver tolerance ends the sweeps before the iteration limit:
+    the lagged sweeps have started later sweeps by then and roll them back to
+    the end of the converged one (lambdas, vlambda / wlambda); rows, bodies
+    and iteration counts equal the oracle's."""
+    sc = scenes.box_pile(8, 8, 4, seed=31)
+    sc.tolerance = tol
+    sc.iterations = 30
+    info = run_parity(wide_ctx, sc, 40)
+    assert info.iterations < 30
+
+
+def test_wide_lagged_sweeps_long_chains(wide_ctx):
+    """Tall stacks give long level chains: the lag is raised so that the
+    sweeps in flight fit the history slots, and results stay the oracle's."""
+    sc = scenes.box_pile(3, 3, 24, seed=32, pitch=1.05)
+    sc.iterations = 25
+    run_parity(wide_ctx, sc, 60)
