@@ -986,12 +986,18 @@ static size_t solve_smem_bytes(int nb, bool vel) {
   return sizeof(int) * (WS_LEVELS_SMEM + 1) + (vel ? (size_t)nb * (6 * sizeof(float) + 1) : 0);
 }
 
+// the sweep kernel's own (static) shared memory, as compiled
+static int solve_static_smem() {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, (const void*)k_w_solve) != cudaSuccess) return 1 << 20;
+  return (int)fa.sharedSizeBytes;
+}
+
 int cpk_wide_smem_vel_max() {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t fixed = sizeof(Smem) + WS_THREADS * (sizeof(double) + sizeof(int)) + 64;
-  const long long room = (long long)optin - (long long)fixed - (long long)sizeof(int) * (WS_LEVELS_SMEM + 1);
+  const long long room = (long long)optin - solve_static_smem() - (long long)sizeof(int) * (WS_LEVELS_SMEM + 1);
   return room > 0 ? (int)(room / (6 * sizeof(float) + 1)) : 0;
 }
 
@@ -1103,10 +1109,12 @@ cudaError_t cpk_launch_wide_steps(const DWorld* dw, const DWorld& hw, const Wide
   if (dev >= 0 && dev < CP_MAX_DEVICES && !attr_done[dev]) {
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaFuncSetAttribute((const void*)k_w_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         optin - (int)(sizeof(Smem) + WS_THREADS * (sizeof(double) + sizeof(int)) + 64));
-    cudaFuncSetAttribute((const void*)k_w_levels, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(sizeof(int2) * CP_LEVEL_CHUNK + sizeof(int) * CP_SMEM_LEVEL_MAX));
+    cudaError_t e = cudaFuncSetAttribute((const void*)k_w_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         optin - solve_static_smem());
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute((const void*)k_w_levels, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(sizeof(int2) * CP_LEVEL_CHUNK + sizeof(int) * CP_SMEM_LEVEL_MAX));
+    if (e != cudaSuccess) return e;
     attr_done[dev] = true;
   }
   long long n = 0;
