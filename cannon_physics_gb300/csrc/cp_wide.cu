@@ -652,8 +652,7 @@ DI bool wide_ok(DWide* x, int code, int idx, int bound) {
 
 // one row of sweep slot `slot` at level position p (the unsplit path of
 // the level sweeps, plus the history)
-DI void lag_row(const DWorld& W, const DWorldParams& P, DWide* x, float* vel, unsigned char* flg, int p, int slot,
-                double* s_sum) {
+DI void lag_row(const DWorld& W, const DWorldParams& P, DWide* x, float* vel, unsigned char* flg, int p, int slot) {
   const int nrows = x->n_rows, nb = P.nb;
   if (!wide_ok(x, 1, p, nrows)) return;
   const RowRec R = load_row(W, p);
@@ -682,11 +681,7 @@ DI void lag_row(const DWorld& W, const DWorldParams& P, DWide* x, float* vel, un
     if (last & 2) for (int e = 0; e < 6; e++) hv[6 * bb.y + e] = vel[6 * bb.y + e];
   }
   const int r = W.sw_orig[p];
-  if (wide_ok(x, 3, r, nrows)) {
-    const double a = dl > 0.0 ? dl : -dl;
-    W.lag_abs[slot * rs + r] = a;
-    atomicAdd(&s_sum[slot], a);
-  }
+  if (wide_ok(x, 3, r, nrows)) W.lag_abs[slot * rs + r] = dl > 0.0 ? dl : -dl;
 }
 
 // GSSolver's exit test (sum of |dlambda| in row order)^2 < tol^2 for a sweep
@@ -703,15 +698,13 @@ DI bool sweep_converged(double sp, const double* abs, int n, double tol2) {
 }
 
 // the lagged sweeps of one world; returns GSSolver's iteration count
-DI int lag_sweeps(const DWorld& W, const DWorldParams& P, DWide* x, float* vel, unsigned char* flg, const int* ls, int nrows,
-                  int nl) {
-  __shared__ double s_sum[CP_LAG_SLOTS];
+DI int lag_sweeps(Smem& S, const DWorld& W, const DWorldParams& P, DWide* x, float* vel, unsigned char* flg, const int* ls,
+                  int nrows, int nl) {
   __shared__ int s_stop;
   const int K = P.iterations, D = x->lag_d, R = x->lag_r;
   const int T = nl + (K - 1) * D;
   const double tol2 = P.tolerance * P.tolerance;
   const size_t rs = (size_t)P.rows_cap;
-  if (threadIdx.x < CP_LAG_SLOTS) s_sum[threadIdx.x] = 0.0;
   if (threadIdx.x == 0) s_stop = -1;
   __syncthreads();
   int t_end = T - 1, sstar = -1;
@@ -730,16 +723,16 @@ DI int lag_sweeps(const DWorld& W, const DWorldParams& P, DWide* x, float* vel, 
         off -= c;
         s++;
       }
-      lag_row(W, P, x, vel, flg, ls[t - s * D] + off, s % R, s_sum);
+      lag_row(W, P, x, vel, flg, ls[t - s * D] + off, s % R);
     }
     __syncthreads();
     if (over >= 0 && over % D == 0) {  // sweep over / D has run its last level
       const int sd = over / D;
-      if (threadIdx.x == 0) {
-        const int slot = sd % R;
-        if (sweep_converged(s_sum[slot], W.lag_abs + slot * rs, nrows, tol2)) s_stop = sd;
-        s_sum[slot] = 0.0;  // the slot's next sweep, sd + R, has not started
-      }
+      const double* ab = W.lag_abs + (sd % R) * rs;
+      double part = 0.0;
+      for (int r = threadIdx.x; r < nrows; r += BT) part += ab[r];
+      const double sp = block_sum(S, part);  // order-free: the exit test's band covers it
+      if (threadIdx.x == 0 && sweep_converged(sp, ab, nrows, tol2)) s_stop = sd;
       __syncthreads();
       if (s_stop >= 0) {
         sstar = s_stop;
@@ -801,7 +794,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve(const DWorld* dw, int
   const int partner = threadIdx.x ^ 32;
   int iters = S.P.iterations;
   const bool lagged = x->lag_d > 0;
-  if (lagged) iters = lag_sweeps(W, S.P, x, vel, flg, ls, nrows, nl);
+  if (lagged) iters = lag_sweeps(S, W, S.P, x, vel, flg, ls, nrows, nl);
   for (int sweep = 0; !lagged && sweep < S.P.iterations; sweep++) {
     double acc = 0.0;
     // this thread's first row of level l
