@@ -18,6 +18,7 @@
 #include <cstdarg>
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <iterator>
 #include <map>
@@ -689,6 +690,8 @@ WideShape wide_shape(const WorldRec& w) {
   s.smem_vel = w.nb <= cpk_wide_smem_vel_max();
   s.compound = w.compound;
   s.jobs_cap = w.jobs_cap;
+  const char* ev = std::getenv("CP_WIDE_SOLVE");
+  s.solve_cl = !(ev && std::strcmp(ev, "block") == 0);
   return s;
 }
 
@@ -717,6 +720,7 @@ int ensure_lag(cp_ctx* c, int id) {
   const size_t o_bmax = L.take(sizeof(int) * nb);
   const size_t o_blast = L.take(sizeof(int) * nb);
   const size_t o_last = L.take(rows);
+  const size_t o_part = L.take(sizeof(double) * 32);
   if (L.off > w.lag_bytes) {
     if (w.lag) cudaFree(w.lag);
     w.lag = nullptr;
@@ -732,6 +736,7 @@ int ensure_lag(cp_ctx* c, int id) {
   w.dw.lag_bmax = (int*)(b + o_bmax);
   w.dw.lag_blast = (int*)(b + o_blast);
   w.dw.lag_last = (unsigned char*)(b + o_last);
+  w.dw.lag_part = (double*)(b + o_part);
   w.lag_rows_cap = w.rows_cap;
   return upload_world_entry(c, id);
 }

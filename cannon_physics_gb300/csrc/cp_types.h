@@ -301,4 +301,5 @@ struct DWorld {
   int* lag_bmax;    // per body: highest level
   int* lag_blast;   // per body: its last row (original order), -1 none
   unsigned char* lag_last;  // per level position: 1 last row of bi, 2 last row of bj
+  double* lag_part;         // the cluster sweep kernel's per-block partial sums
 };
