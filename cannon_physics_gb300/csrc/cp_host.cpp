@@ -18,7 +18,6 @@
 #include <cstdarg>
 #include <cstddef>
 #include <cstdio>
-#include <cstdlib>
 #include <cstring>
 #include <iterator>
 #include <map>
@@ -690,8 +689,6 @@ WideShape wide_shape(const WorldRec& w) {
   s.smem_vel = w.nb <= cpk_wide_smem_vel_max();
   s.compound = w.compound;
   s.jobs_cap = w.jobs_cap;
-  const char* ev = std::getenv("CP_WIDE_SOLVE");
-  s.solve_cl = !(ev && std::strcmp(ev, "block") == 0);
   return s;
 }
 
@@ -703,42 +700,6 @@ int wide_check(cp_ctx* c, const WorldRec& w, int id) {
   if (chk[0] != 0)
     return fail(CP_ERR_CUDA, "wide sweep kernel index check %d failed: world %d, index %d, bound %d", chk[0], id, chk[1], chk[2]);
   return CP_OK;
-}
-
-// The lagged wide sweeps' history for the world's current row capacity: made
-// when the world first takes the wide path, laid out again when its lists
-// have grown (its contents do not outlive a step)
-int ensure_lag(cp_ctx* c, int id) {
-  WorldRec& w = c->worlds[id];
-  if (w.lag && w.lag_rows_cap == w.rows_cap) return CP_OK;
-  const size_t rows = (size_t)w.rows_cap + 1, nb = (size_t)w.nb + 1;
-  Layout L;
-  const size_t o_lam = L.take(sizeof(double) * CP_LAG_SLOTS * rows);
-  const size_t o_abs = L.take(sizeof(double) * CP_LAG_SLOTS * rows);
-  const size_t o_vel = L.take(sizeof(float) * 6 * CP_LAG_SLOTS * nb);
-  const size_t o_bmin = L.take(sizeof(int) * nb);
-  const size_t o_bmax = L.take(sizeof(int) * nb);
-  const size_t o_blast = L.take(sizeof(int) * nb);
-  const size_t o_last = L.take(rows);
-  const size_t o_part = L.take(sizeof(double) * 32);
-  if (L.off > w.lag_bytes) {
-    if (w.lag) cudaFree(w.lag);
-    w.lag = nullptr;
-    w.lag_bytes = 0;
-    CUDA_TRY(cudaMalloc(&w.lag, L.off));
-    w.lag_bytes = L.off;
-  }
-  char* b = w.lag;
-  w.dw.lag_lam = (double*)(b + o_lam);
-  w.dw.lag_abs = (double*)(b + o_abs);
-  w.dw.lag_vel = (float*)(b + o_vel);
-  w.dw.lag_bmin = (int*)(b + o_bmin);
-  w.dw.lag_bmax = (int*)(b + o_bmax);
-  w.dw.lag_blast = (int*)(b + o_blast);
-  w.dw.lag_last = (unsigned char*)(b + o_last);
-  w.dw.lag_part = (double*)(b + o_part);
-  w.lag_rows_cap = w.rows_cap;
-  return upload_world_entry(c, id);
 }
 
 // nsteps internal steps of one world; its time advances by time_inc per step
@@ -754,10 +715,6 @@ int plain_steps(cp_ctx* c, int id, double dt, int nsteps, double time_inc) {
   const bool wide = is_wide(c, w);
   for (int guard = 0; guard < 64; guard++) {
     long long done = p.stepnumber;
-    if (wide) {
-      st = ensure_lag(c, id);
-      if (st) return st;
-    }
     if (wide && target > done)
       CUDA_TRY(cpk_launch_wide_steps(c->d_worlds + id, w.dw, wide_shape(w), dt, time_inc, (int)(target - done), c->stream,
                                      &c->launches));
@@ -917,7 +874,6 @@ int cp_destroy(cp_ctx* c) {
     if (w.state) dev_free(c, w.state, w.pooled);
     if (w.scratch) dev_free(c, w.scratch, w.pooled);
     if (w.pool) cudaFree(w.pool);
-    if (w.lag) cudaFree(w.lag);
   }
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->pool) cudaMemPoolDestroy(c->pool);
@@ -1297,7 +1253,6 @@ int destroy_world(cp_ctx* c, int id) {
   if (w.state) dev_free(c, w.state, w.pooled);
   if (w.scratch) dev_free(c, w.scratch, w.pooled);
   if (w.pool) cudaFree(w.pool);
-  if (w.lag) cudaFree(w.lag);
   w = WorldRec();
   if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   return CP_OK;

@@ -34,9 +34,6 @@ struct WorldRec {
   long long* pool = nullptr;  // device, SplitSolver: contact then friction equation pools (ids)
   int pool_cap = 0;           // contact pool capacity (the friction pool holds twice as many)
   bool split = false;         // SplitSolver
-  char* lag = nullptr;        // device: the lagged wide sweeps' history (made on the first wide step)
-  size_t lag_bytes = 0;
-  int lag_rows_cap = -1;      // rows_cap the lag layout was made for
   size_t state_bytes = 0, scratch_bytes = 0;
   bool pooled = false;     // state and scratch come from the context's memory pool
   DWorld dw{};

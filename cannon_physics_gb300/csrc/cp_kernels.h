@@ -53,7 +53,6 @@ struct WideShape {
   int pairs_cap, contacts_cap, rows_cap, bins_cap;
   int smem_vel;  // the sweeps keep vlambda / wlambda in shared memory
   int compound, jobs_cap;  // shape-pair jobs of compound bodies, their capacity
-  int solve_cl;            // the sweeps on a thread-block cluster (else one block)
 };
 int cpk_wide_smem_vel_max();
 // nsteps steps of the world whose device descriptor is dw (hw: its host

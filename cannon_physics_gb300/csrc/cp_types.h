@@ -193,11 +193,7 @@ struct __align__(16) DWide {
   int check[4];   // first failed index check of the sweep kernel: code, index, bound
   int kcnt[16], kpos[16];
   int total, n_jobs, pad[2];  // n_jobs: narrowphase jobs of a compound world
-  // lagged sweeps (k_w_solve): sweep s runs level l at step l + s * lag_d;
-  // lag_r history slots (0: sweeps one after another)
-  int lag_d, lag_r, pad2[2];
 };
-#define CP_LAG_SLOTS 16  // history slots of the lagged wide sweeps (sweeps in flight + 2)
 #define CP_WIDE_SCAN_BLOCKS 128
 
 struct DWorld {
@@ -290,16 +286,4 @@ struct DWorld {
   int* wpart;       // per-block partial sums of the wide scans (CP_WIDE_SCAN_BLOCKS + 1)
   float* wvel;      // wide sweeps: vlambda, wlambda (6 floats per body) when they do not fit in shared memory
   unsigned char* wflag;  // wide sweeps: solve flag per body
-  // lagged wide sweeps (a separate allocation, made when a world first takes
-  // the wide path): per history slot the rows' lambda and |dlambda| and the
-  // bodies' vlambda / wlambda after their last row of that sweep; per body
-  // its level span and last row; per level position the last-row flags
-  double* lag_lam;  // [CP_LAG_SLOTS][rows_cap]
-  double* lag_abs;  // [CP_LAG_SLOTS][rows_cap], by original row
-  float* lag_vel;   // [CP_LAG_SLOTS][nb][6]
-  int* lag_bmin;    // per body: lowest level of its rows
-  int* lag_bmax;    // per body: highest level
-  int* lag_blast;   // per body: its last row (original order), -1 none
-  unsigned char* lag_last;  // per level position: 1 last row of bi, 2 last row of bj
-  double* lag_part;         // the cluster sweep kernel's per-block partial sums
 };

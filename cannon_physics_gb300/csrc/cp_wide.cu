@@ -22,12 +22,8 @@
 #include <algorithm>
 #include <cstddef>
 
-#include <cooperative_groups.h>
-
 #include "cp_kernels.h"
 #include "cp_phases.cuh"
-
-namespace cg = cooperative_groups;
 
 #define WT 256  // threads per block of the grid-wide kernels
 #define WIDE_LOOP(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
@@ -542,66 +538,6 @@ __global__ void k_w_assemble(const DWorld* dw, double h) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// Lagged sweeps.  GSSolver sweeps the rows again and again in one order; a
-// row of sweep s+1 needs its bodies as the rows after it left them in sweep
-// s.  If every body's rows lie within D consecutive levels (D = 1 + the
-// largest span), then running level l of sweep s at step l + s*D meets every
-// such need: sweeps overlap, one world's solve takes nl + (K-1)*D steps
-// instead of K*nl, and each step holds several sweeps' rows.  The exit test
-// of sweep s is known only when its last level is done, by which time later
-// sweeps have started: each sweep keeps its rows' lambda and |dlambda| and
-// its bodies' vlambda / wlambda after their last row, in one of
-// CP_LAG_SLOTS history slots, and a sweep that ends the solve rolls the
-// later ones back.  The body update sequence is the reference's, so the bits
-// are.
-
-// per body its level span and last row; per level position the last-row
-// flags; then the lag (0: sweeps one after another)
-DI void lag_prepare(Smem& S) {
-  const DWorld& W = S.W;
-  DWide* x = W.wide;
-  __shared__ int s_span;
-  if (threadIdx.x == 0) { x->lag_d = 0; x->lag_r = 0; s_span = 0; }
-  if (!W.lag_lam || S.n_rows == 0) return;
-  const int nb = S.P.nb, nrows = S.n_rows, nl = S.n_levels;
-  for (int i = threadIdx.x; i < nb; i += BT) {
-    W.lag_bmin[i] = 0x7fffffff;
-    W.lag_bmax[i] = -1;
-    W.lag_blast[i] = -1;
-  }
-  __syncthreads();
-  for (int r = threadIdx.x; r < nrows; r += BT) {
-    const int l = W.level_of[r];
-    const int a = W.rows[r].bi, b = W.rows[r].bj;
-    if (W.bscr[a].active) { atomicMin(&W.lag_bmin[a], l); atomicMax(&W.lag_bmax[a], l); atomicMax(&W.lag_blast[a], r); }
-    if (b != a && W.bscr[b].active) { atomicMin(&W.lag_bmin[b], l); atomicMax(&W.lag_bmax[b], l); atomicMax(&W.lag_blast[b], r); }
-  }
-  __syncthreads();
-  int span = 0;
-  for (int i = threadIdx.x; i < nb; i += BT)
-    if (W.lag_bmax[i] >= 0) span = max(span, W.lag_bmax[i] - W.lag_bmin[i]);
-  atomicMax(&s_span, span);
-  for (int p = threadIdx.x; p < nrows; p += BT) {
-    const int r = W.sw_orig[p];
-    const int2 bb = W.sw_b[p];
-    W.lag_last[p] = (unsigned char)((W.lag_blast[bb.x] == r ? 1 : 0) | (W.lag_blast[bb.y] == r ? 2 : 0));
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int d = s_span + 1;
-    int r = (nl - 1) / d + 2;
-    if (r > CP_LAG_SLOTS) {
-      d = (nl - 1 + CP_LAG_SLOTS - 3) / (CP_LAG_SLOTS - 2);
-      r = (nl - 1) / d + 2;
-    }
-    if (d < nl && S.P.iterations > 1) {
-      x->lag_d = d;
-      x->lag_r = r;
-    }
-  }
-}
-
 // dependency levels and the level-ordered sweep arrays: one block
 __global__ void __launch_bounds__(1024) k_w_levels(const DWorld* dw, int last_cap) {
   __shared__ Smem S;
@@ -612,7 +548,6 @@ __global__ void __launch_bounds__(1024) k_w_levels(const DWorld* dw, int last_ca
   if (S.n_rows == 0) return;
   ph_levels(S, (int*)(s_dyn + CP_LEVEL_CHUNK), last_cap, s_dyn);
   if (threadIdx.x == 0) S.W.wide->n_levels = S.n_levels;
-  lag_prepare(S);
 }
 
 // ---------------------------------------------------------------------------
@@ -654,290 +589,8 @@ DI bool wide_ok(DWide* x, int code, int idx, int bound) {
   return false;
 }
 
-// one row of sweep slot `slot` at level position p (the unsplit path of
-// the level sweeps, plus the history)
-DI void lag_row(const DWorld& W, const DWorldParams& P, DWide* x, float* vel, unsigned char* flg, int p, int slot) {
-  const int nrows = x->n_rows, nb = P.nb;
-  if (!wide_ok(x, 1, p, nrows)) return;
-  const RowRec R = load_row(W, p);
-  const int2 bb = W.sw_b[p];
-  if (!wide_ok(x, 2, bb.x, nb) || !wide_ok(x, 2, bb.y, nb)) return;
-  float4 va, wa, vb, wb;
-  wv_load(vel, flg, bb.x, va, wa);
-  wv_load(vel, flg, bb.y, vb, wb);
-  const bool aa = va.w != 0.f, ab = vb.w != 0.f;
-  const double ga = aa ? half_a(R, va, wa) : 0.0;
-  const double gb = ab ? half_b(R, vb, wb) : 0.0;
-  const double dl = row_dl(R, ga, aa, gb, ab);
-  const double lam = R.d1.y + dl;
-  const size_t rs = (size_t)P.rows_cap;
-  W.sw_d[W.sw_cap + p].y = lam;
-  W.lag_lam[slot * rs + p] = lam;
-  if (aa) wv_update_a(vel, bb.x, va, wa, R, dl);
-  if (ab) {
-    if (bb.x == bb.y) wv_load(vel, flg, bb.y, vb, wb);  // a constraint between a body and itself
-    wv_update_b(vel, bb.y, vb, wb, R, dl);
-  }
-  const unsigned last = W.lag_last[p];
-  if (last) {
-    float* hv = W.lag_vel + (size_t)slot * nb * 6;
-    if (last & 1) for (int e = 0; e < 6; e++) hv[6 * bb.x + e] = vel[6 * bb.x + e];
-    if (last & 2) for (int e = 0; e < 6; e++) hv[6 * bb.y + e] = vel[6 * bb.y + e];
-  }
-  const int r = W.sw_orig[p];
-  if (wide_ok(x, 3, r, nrows)) W.lag_abs[slot * rs + r] = dl > 0.0 ? dl : -dl;
-}
-
-// GSSolver's exit test (sum of |dlambda| in row order)^2 < tol^2 for a sweep
-// whose order-free sum is sp: decided by sp unless it lies within the
-// rounding band of the threshold, else by the row-order sum of abs[0..n)
-DI bool sweep_converged(double sp, const double* abs, int n, double tol2) {
-  const double band = 2.2 * (double)n * 1.1102230246251565e-16;
-  const double hi = sp * (1.0 + band), lo = sp * (1.0 - band);
-  if (hi * hi * (1.0 + 4.5e-16) < tol2) return true;
-  if (lo * lo * (1.0 - 4.5e-16) >= tol2 && lo >= 0.0) return false;
-  double t = 0.0;
-  for (int r = 0; r < n; r++) t += abs[r];
-  return t * t < tol2;
-}
-
-// the lagged sweeps of one world; returns GSSolver's iteration count
-DI int lag_sweeps(Smem& S, const DWorld& W, const DWorldParams& P, DWide* x, float* vel, unsigned char* flg, const int* ls,
-                  int nrows, int nl) {
-  __shared__ int s_stop;
-  const int K = P.iterations, D = x->lag_d, R = x->lag_r;
-  const int T = nl + (K - 1) * D;
-  const double tol2 = P.tolerance * P.tolerance;
-  const size_t rs = (size_t)P.rows_cap;
-  if (threadIdx.x == 0) s_stop = -1;
-  __syncthreads();
-  int t_end = T - 1, sstar = -1;
-  for (int t = 0; t < T; t++) {
-    const int s_hi = min(K - 1, t / D);
-    const int over = t - (nl - 1);
-    const int s_lo = over > 0 ? (over + D - 1) / D : 0;
-    int total = 0;
-    for (int s = s_lo; s <= s_hi; s++) total += ls[t - s * D + 1] - ls[t - s * D];
-    for (int f = threadIdx.x; f < total; f += BT) {
-      int s = s_lo, off = f;
-      for (;;) {
-        const int l = t - s * D;
-        const int c = ls[l + 1] - ls[l];
-        if (off < c) break;
-        off -= c;
-        s++;
-      }
-      lag_row(W, P, x, vel, flg, ls[t - s * D] + off, s % R);
-    }
-    __syncthreads();
-    if (over >= 0 && over % D == 0) {  // sweep over / D has run its last level
-      const int sd = over / D;
-      const double* ab = W.lag_abs + (sd % R) * rs;
-      double part = 0.0;
-      for (int r = threadIdx.x; r < nrows; r += BT) part += ab[r];
-      const double sp = block_sum(S, part);  // order-free: the exit test's band covers it
-      if (threadIdx.x == 0 && sweep_converged(sp, ab, nrows, tol2)) s_stop = sd;
-      __syncthreads();
-      if (s_stop >= 0) {
-        sstar = s_stop;
-        t_end = t;
-        break;
-      }
-    }
-  }
-  if (sstar < 0) return K;
-  // sweeps after sstar that had started go back to the end of sweep sstar
-  if (min(K - 1, t_end / D) > sstar) {
-    const int slot = sstar % R;
-    const float* hv = W.lag_vel + (size_t)slot * P.nb * 6;
-    for (int b = threadIdx.x; b < P.nb; b += BT)
-      if (W.lag_blast[b] >= 0)
-        for (int e = 0; e < 6; e++) vel[6 * b + e] = hv[6 * b + e];
-    for (int p = threadIdx.x; p < nrows; p += BT) W.sw_d[W.sw_cap + p].y = W.lag_lam[slot * rs + p];
-    __syncthreads();
-  }
-  return sstar;
-}
-
-// ---------------------------------------------------------------------------
-// The sweeps over a thread-block cluster.  One block holds one SM's binary64
-// pipes; the sweeps of a large world are bound by them.  k_w_solve_cl runs
-// the (lagged) sweeps of one world on the CL blocks of a cluster: every step
-// of the lagged schedule spreads its rows over all the cluster's threads, and
-// a cluster barrier (release / acquire at cluster scope) ends the step.
-// vlambda / wlambda live in global memory (the world's wvel / wflag) and are
-// read past L1, as are the rows' lambdas and the histories, which other SMs
-// of the cluster write.
-#define CL_SIZE 8
-#define CL_THREADS 256
-#define WS_LEVELS_SMEM 4096  // level bounds kept in shared memory up to this many levels
-
-DI void wv_load_g(const float* vel, const unsigned char* flg, int i, float4& v, float4& w) {
-  const float* p = vel + 6 * i;
-  v = make_float4(__ldcg(p), __ldcg(p + 1), __ldcg(p + 2), __ldcg(flg + i) ? 1.f : 0.f);
-  w = make_float4(__ldcg(p + 3), __ldcg(p + 4), __ldcg(p + 5), 0.f);
-}
-DI void wv_store_g(float* vel, int i, float4 v, float4 w) {
-  float* p = vel + 6 * i;
-  __stcg(p, v.x); __stcg(p + 1, v.y); __stcg(p + 2, v.z);
-  __stcg(p + 3, w.x); __stcg(p + 4, w.y); __stcg(p + 5, w.z);
-}
-
-DI void cl_row(const DWorld& W, const DWorldParams& P, DWide* x, float* vel, unsigned char* flg, int p, int slot) {
-  const int nrows = x->n_rows, nb = P.nb;
-  if (!wide_ok(x, 1, p, nrows)) return;
-  RowRec R = load_row(W, p);
-  R.d1 = __ldcg(&W.sw_d[W.sw_cap + p]);  // eps, lambda: lambda is written by whichever block ran the row last
-  const int2 bb = W.sw_b[p];
-  if (!wide_ok(x, 2, bb.x, nb) || !wide_ok(x, 2, bb.y, nb)) return;
-  float4 va, wa, vb, wb;
-  wv_load_g(vel, flg, bb.x, va, wa);
-  wv_load_g(vel, flg, bb.y, vb, wb);
-  const bool aa = va.w != 0.f, ab = vb.w != 0.f;
-  const double ga = aa ? half_a(R, va, wa) : 0.0;
-  const double gb = ab ? half_b(R, vb, wb) : 0.0;
-  const double dl = row_dl(R, ga, aa, gb, ab);
-  const double lam = R.d1.y + dl;
-  const size_t rs = (size_t)P.rows_cap;
-  __stcg(&W.sw_d[W.sw_cap + p].y, lam);
-  __stcg(&W.lag_lam[slot * rs + p], lam);
-  float4 na = va, nwa = wa, nb4 = vb, nwb = wb;
-  if (aa) {
-    na = vstep(va, R.im.x * dl, R.j0.x, R.j0.y, R.j0.z);
-    nwa = vstep(wa, dl, R.j3.x, R.j3.y, R.j3.z);
-    wv_store_g(vel, bb.x, na, nwa);
-  }
-  if (ab) {
-    if (bb.x == bb.y) { vb = na; wb = nwa; }  // a constraint between a body and itself
-    nb4 = vstep(vb, R.im.y * dl, R.j1.z, R.j1.w, R.j2.x);
-    nwb = vstep(wb, dl, R.j3.w, R.j4.x, R.j4.y);
-    wv_store_g(vel, bb.y, nb4, nwb);
-  }
-  const unsigned last = W.lag_last[p];
-  if (last) {
-    float* hv = W.lag_vel + (size_t)slot * nb * 6;
-    if (last & 1) {
-      const float4 v = bb.x == bb.y && ab ? nb4 : na, w = bb.x == bb.y && ab ? nwb : nwa;
-      const float h[6] = {v.x, v.y, v.z, w.x, w.y, w.z};
-      for (int e = 0; e < 6; e++) __stcg(hv + 6 * bb.x + e, h[e]);
-    }
-    if (last & 2) {
-      const float h[6] = {nb4.x, nb4.y, nb4.z, nwb.x, nwb.y, nwb.z};
-      for (int e = 0; e < 6; e++) __stcg(hv + 6 * bb.y + e, h[e]);
-    }
-  }
-  const int r = W.sw_orig[p];
-  if (wide_ok(x, 3, r, nrows)) __stcg(&W.lag_abs[slot * rs + r], dl > 0.0 ? dl : -dl);
-}
-
-// one cluster: GSSolver's sweeps, lagged by x->lag_d levels (0: one after
-// another), then vlambda / wlambda back into the body scratch
-__global__ void __launch_bounds__(CL_THREADS, 1) k_w_solve_cl(const DWorld* dw) {
-  __shared__ Smem S;
-  __shared__ int s_ls[WS_LEVELS_SMEM + 1];
-  if (!wide_enter(S, dw)) return;  // the same for every block of the cluster
-  cg::cluster_group cl = cg::this_cluster();
-  const int rank = (int)cl.block_rank(), ncl = (int)cl.num_blocks();
-  const int gt = rank * CL_THREADS + (int)threadIdx.x, GT = ncl * CL_THREADS;
-  const DWorld& W = S.W;
-  const DWorldParams& P = S.P;
-  DWide* x = W.wide;
-  const int nrows = x->n_rows, nl = x->n_levels, nb = P.nb;
-  if (nrows == 0) return;
-  const bool ls_smem = nl + 1 <= WS_LEVELS_SMEM + 1;
-  if (ls_smem)
-    for (int l = threadIdx.x; l <= nl; l += BT) s_ls[l] = W.level_start[l];
-  const int* ls = ls_smem ? s_ls : W.level_start;
-  float* vel = W.wvel;
-  unsigned char* flg = W.wflag;
-  for (int i = gt; i < nb; i += GT) {
-    const float4 v = *(const float4*)W.bscr[i].vl, w = *(const float4*)W.bscr[i].wl;
-    wv_store_g(vel, i, v, w);
-    __stcg(flg + i, (unsigned char)(v.w != 0.f));
-  }
-  const int K = P.iterations;
-  const bool lagged = x->lag_d > 0;
-  const int D = lagged ? x->lag_d : nl, R = lagged ? x->lag_r : 2;
-  const int T = nl + (K - 1) * D;
-  const double tol2 = P.tolerance * P.tolerance;
-  const size_t rs = (size_t)P.rows_cap;
-  double* part = W.lag_part;
-  cl.sync();
-  int t_end = T - 1, sstar = -1;
-  for (int t = 0; t < T; t++) {
-    const int s_hi = min(K - 1, t / D);
-    const int over = t - (nl - 1);
-    const int s_lo = over > 0 ? (over + D - 1) / D : 0;
-    int total = 0;
-    for (int s = s_lo; s <= s_hi; s++) total += ls[t - s * D + 1] - ls[t - s * D];
-    for (int f = gt; f < total; f += GT) {
-      int s = s_lo, off = f;
-      for (;;) {
-        const int l = t - s * D;
-        const int c = ls[l + 1] - ls[l];
-        if (off < c) break;
-        off -= c;
-        s++;
-      }
-      cl_row(W, P, x, vel, flg, ls[t - s * D] + off, s % R);
-    }
-    cl.sync();
-    if (over >= 0 && over % D == 0) {  // sweep over / D has run its last level
-      const int sd = over / D;
-      const double* ab = W.lag_abs + (sd % R) * rs;
-      double sum = 0.0;
-      for (int r = gt; r < nrows; r += GT) sum += __ldcg(ab + r);
-      sum = block_sum(S, sum);
-      if (threadIdx.x == 0) __stcg(part + rank, sum);
-      cl.sync();
-      // every block adds the partial sums in the same order: one decision
-      double sp = 0.0;
-      for (int k = 0; k < ncl; k++) sp += __ldcg(part + k);
-      bool conv;
-      {
-        const double band = 2.2 * (double)nrows * 1.1102230246251565e-16;
-        const double hi = sp * (1.0 + band), lo = sp * (1.0 - band);
-        if (hi * hi * (1.0 + 4.5e-16) < tol2) conv = true;
-        else if (lo * lo * (1.0 - 4.5e-16) >= tol2 && lo >= 0.0) conv = false;
-        else {
-          if (threadIdx.x == 0) {
-            double e = 0.0;
-            for (int r = 0; r < nrows; r++) e += __ldcg(ab + r);
-            S.wi = e * e < tol2;
-          }
-          __syncthreads();
-          conv = S.wi != 0;
-        }
-      }
-      cl.sync();  // the partials are read before the next sweep's are written
-      if (conv) {
-        sstar = sd;
-        t_end = t;
-        break;
-      }
-    }
-  }
-  // sweeps after sstar that had started go back to the end of sweep sstar
-  if (sstar >= 0 && min(K - 1, t_end / D) > sstar) {
-    const int slot = sstar % R;
-    const float* hv = W.lag_vel + (size_t)slot * nb * 6;
-    for (int b = gt; b < nb; b += GT)
-      if (W.lag_blast[b] >= 0)
-        for (int e = 0; e < 6; e++) __stcg(vel + 6 * b + e, __ldcg(hv + 6 * b + e));
-    for (int p = gt; p < nrows; p += GT) __stcg(&W.sw_d[W.sw_cap + p].y, __ldcg(&W.lag_lam[slot * rs + p]));
-    cl.sync();
-  }
-  for (int i = gt; i < nb; i += GT) {
-    float4 v, w;
-    wv_load_g(vel, flg, i, v, w);
-    *(float4*)W.bscr[i].vl = v;
-    float4* gw = (float4*)W.bscr[i].wl;
-    *gw = make_float4(w.x, w.y, w.z, gw->w);
-  }
-  if (gt == 0) x->iters = sstar >= 0 ? sstar : K;
-}
-
 #define WS_THREADS 256  // 186 registers a thread, no spills
+#define WS_LEVELS_SMEM 4096  // level bounds kept in shared memory up to this many levels
 
 // dynamic shared memory: level bounds (WS_LEVELS_SMEM + 1 ints), then, when
 // smem_vel, the packed vlambda / wlambda (6 floats per body) and flags
@@ -974,9 +627,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve(const DWorld* dw, int
   const int split_off = (((int)threadIdx.x >> 6) << 5) | ((int)threadIdx.x & 31);
   const int partner = threadIdx.x ^ 32;
   int iters = S.P.iterations;
-  const bool lagged = x->lag_d > 0;
-  if (lagged) iters = lag_sweeps(S, W, S.P, x, vel, flg, ls, nrows, nl);
-  for (int sweep = 0; !lagged && sweep < S.P.iterations; sweep++) {
+  for (int sweep = 0; sweep < S.P.iterations; sweep++) {
     double acc = 0.0;
     // this thread's first row of level l
     auto first_row = [&](int l, int& p) {
@@ -1268,25 +919,7 @@ static cudaError_t wide_step(const DWorld* dw, const DWorld& hw, const WideShape
   const int last_cap = nb < CP_SMEM_LEVEL_MAX ? nb : CP_SMEM_LEVEL_MAX;
   const size_t lsm = sizeof(int2) * CP_LEVEL_CHUNK + sizeof(int) * (size_t)last_cap;
   WIDE_LAUNCH(k_w_levels, 1, 1024, lsm, dw, last_cap);
-  if (ws.solve_cl) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(CL_SIZE, 1, 1);
-    cfg.blockDim = dim3(CL_THREADS, 1, 1);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = CL_SIZE;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    cudaError_t e_ = cudaLaunchKernelEx(&cfg, k_w_solve_cl, dw);
-    if (e_ != cudaSuccess) return e_;
-    n++;
-  } else {
-    WIDE_LAUNCH(k_w_solve, 1, WS_THREADS, solve_smem_bytes(nb, ws.smem_vel), dw, ws.smem_vel ? 1 : 0);
-  }
+  WIDE_LAUNCH(k_w_solve, 1, WS_THREADS, solve_smem_bytes(nb, ws.smem_vel), dw, ws.smem_vel ? 1 : 0);
   WIDE_LAUNCH(k_w_apply, G, WT, 0, dw, dt);
   WIDE_LAUNCH(k_w_integrate, gb, WT, 0, dw, dt);
   WIDE_LAUNCH(k_w_end, 1, 1, 0, dw, time_inc);
