@@ -67,6 +67,11 @@ def parse():
     ap.add_argument("--serve-window", type=float, default=1.0, help="served form: seconds of arrivals")
     ap.add_argument("--serve-tick", type=int, default=4, help="served form: steps per tick")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-lanes", type=int, default=0,
+                    help="served form: wide lanes (threads stepping one large world each on the grid-wide path); 0: the "
+                         "server's default, -1: none")
+    ap.add_argument("--serve-wide-bodies", type=int, default=0,
+                    help="served form: body count from which a request takes a wide lane; 0: the server's default")
     ap.add_argument("--variant", type=int, default=None,
                     help="pin the batched kernel variant (no autotuning): the step kernels then launch in a known order, "
                          "two per warm-up step, for profiling")
@@ -263,7 +268,7 @@ def plain_configs(ctx, only=None):
     return out
 
 
-def serve_once(device, rate, window, seed, tick):
+def serve_once(device, rate, window, seed, tick, lanes=0, wide_bodies=0):
     """One served run: Poisson arrivals of rollout requests submitted on their
     arrival times to a fresh continuous-batching server (150 GB HBM budget);
     returns the request list, the scenes and the server's statistics."""
@@ -272,7 +277,7 @@ def serve_once(device, rate, window, seed, tick):
     from cannon_physics_gb300 import serve as S
     reqs = scenes.serve_requests(rate=rate, window=window, seed=seed)
     built = [engine.setup_scene(scenes.request_world(r)) for r in reqs]
-    srv = S.Server(device=device, hbm_budget=150e9, steps_per_tick=tick)
+    srv = S.Server(device=device, hbm_budget=150e9, steps_per_tick=tick, wide_lanes=lanes, wide_bodies=wide_bodies)
     warm = engine.setup_scene(scenes.request_world(scenes.Request(0.0, 64, 2, 5)))
     t = srv.submit(warm, warm.dt, 2)
     srv.wait(t)
@@ -324,11 +329,12 @@ def run_served(args, device):
     submission to result ready; throughput is completed body-steps over the
     span from the first submission to the last completion."""
     from cannon_physics_gb300 import engine
-    reqs, built, over = serve_once(device, args.serve_rate, args.serve_window, 77, args.serve_tick)
+    reqs, built, over = serve_once(device, args.serve_rate, args.serve_window, 77, args.serve_tick, args.serve_lanes,
+                                   args.serve_wide_bodies)
     mean_req = over["offered_body_steps_per_s"] * args.serve_window / max(1, len(reqs))
     rate70 = 0.7 * over["value"] / mean_req
     window70 = max(4.0, 150.0 / rate70)
-    _, _, sus = serve_once(device, rate70, window70, 78, args.serve_tick)
+    _, _, sus = serve_once(device, rate70, window70, 78, args.serve_tick, args.serve_lanes, args.serve_wide_bodies)
     # the plain per-request path: a sample of the same requests, each alone
     # through cp_world_step
     ctx = engine.Context(device=device)
