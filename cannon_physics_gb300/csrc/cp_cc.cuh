@@ -456,7 +456,7 @@ static __device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int
   if (!near) {
     // a binary32 separation certificate (not the bounding spheres, which are
     // the reference's own test) is checked against the full walk
-    if (*(volatile int*)&g_filter_check && !(distance_to(xAf, xBf) > SA.bsr + SB.bsr))
+    if (g_filter_check && !(distance_to(xAf, xBf) > SA.bsr + SB.bsr))
       cc_filter_check(W, shA, shB, xAf, xBf, qAf, qBf, false, d3{0.0, 0.0, 0.0});
     return 0;
   }
@@ -480,7 +480,7 @@ static __device__ __noinline__ int convex_convex(const NarrowCtx& C, int bA, int
       wnB[f] = dvmult(B.q, ldd3(W.faces[B.H.f0 + f].dnormal));
     }
     touch = sat64_compact(W, A, B, wnA, wnB, S32, U, sep);
-    if (*(volatile int*)&g_filter_check) cc_filter_check(W, shA, shB, xAf, xBf, qAf, qBf, touch, sep);
+    if (g_filter_check) cc_filter_check(W, shA, shB, xAf, xBf, qAf, qBf, touch, sep);
   }
   lanes = __ballot_sync(lanes, touch);
   if (!touch) return 0;

@@ -342,6 +342,9 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   const int hash_cap = w.broadphase == CP_BROAD_GRID ? pow2_at_least(2 * pc0 + 2) : 2;
   Layout L;
   size_t o_bscr = L.take(sizeof(DBodyScr) * (nb + 1));
+  size_t o_brec = L.take(sizeof(float4) * (nb + 1));
+  size_t o_bgm = L.take(sizeof(int2) * (nb + 1));
+  size_t o_cbox = L.take(sizeof(float4) * 2 * ((size_t)nb / 32 + 2));
   size_t o_tmp = L.take(sizeof(int) * (nb + 1));
   size_t o_pa = L.take(sizeof(int) * (pc0 + 1));
   size_t o_pb = L.take(sizeof(int) * (pc0 + 1));
@@ -396,6 +399,9 @@ size_t scratch_layout_into(const WorldRec& w, DWorld& d, char* base) {
   size_t o_wf = L.take((size_t)nb + 1);
   if (!base) return L.off;
   d.bscr = (DBodyScr*)(base + o_bscr);
+  d.brec = (float4*)(base + o_brec);
+  d.bgm = (int2*)(base + o_bgm);
+  d.cbox = (float4*)(base + o_cbox);
   d.sap_tmp = (int*)(base + o_tmp);
   d.pair_a = (int*)(base + o_pa);
   d.pair_b = (int*)(base + o_pb);

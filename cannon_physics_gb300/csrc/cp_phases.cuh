@@ -43,6 +43,7 @@ struct __align__(16) Smem {
   int overflow, converged, wi, n_jobs;  // n_jobs: narrowphase jobs (shape pairs)
   int kcnt[16], kpos[16];  // narrowphase: heavy pairs per resolver kind, segment cursors
   int cursor2, split_e, pad2[2];  // split_e: contact equation objects the narrowphase took
+  int bcnt[2][16 * 8 + 4];        // naive broadphase: per (sub-round, warp) counts, then offsets; [128]: total
   // where the narrowphase's contact cursor and overflow flag live: this
   // record's cursor / overflow for a one-block world, device memory for a
   // world spread over the grid
@@ -200,6 +201,11 @@ DI void prepare_body(const DWorld& W, const DWorldParams& P, int i) {
   q4 qs = qmul(q, ld4q(B.shape_quat));
   st3(W.bscr[i].xs, xs);
   st4q(W.bscr[i].qs, qs);
+  {
+    const bool ss = B.type == CP_BODY_STATIC || B.sleep_state == CP_SLEEPING;
+    W.brec[i] = make_float4(p.x, p.y, p.z, ss ? -fabsf(B.brad32) : fabsf(B.brad32));
+    W.bgm[i] = make_int2(B.group, B.mask);
+  }
   if ((B.flags & BF_AABB_DIRTY) && B.shape >= 0) {
     const DShape s = W.shapes[B.shape];
     if (aabb_all || (aabb_grid && s.type != CP_SHAPE_SPHERE && s.type != CP_SHAPE_PLANE)) {
@@ -267,9 +273,284 @@ DI bool intersection_test(const DWorldParams& P, const DBody& A, const DBody& B)
 }
 DI bool intersection_test(const Smem& S, const DBody& A, const DBody& B) { return intersection_test(S.P, A, B); }
 
+// NaiveBroadphase.collisionPairs with the bounding-sphere test
+// (naive_broadphase.dart:14-33, broadphase.dart:44-86) over the records of
+// the prepare phase: the pair (bodies[i], bodies[j]) at flattened index
+// k = i (i - 1) / 2 + j, j < i.  needBroadphaseCollision first (filter
+// groups, not both static or sleeping), then |xB - xA|^2 < (rA + rB)^2 in
+// binary64, settled in binary32 outside a relative band as sphere_overlap
+// does.  `cur` caches body i's record between calls; `check` is the filter
+// check switch, read once per phase.
+struct NaiveRow {
+  int cur;
+  bool check;
+  float4 a;
+  int2 ga;
+  DI void init() {
+    cur = -1;
+    check = g_filter_check != 0;
+  }
+};
+
+DI bool naive_rec_test(const DWorld& W, int i, int j, NaiveRow& R) {
+  if (i != R.cur) {
+    R.a = W.brec[i];
+    R.ga = W.bgm[i];
+    R.cur = i;
+  }
+  const float4 b = W.brec[j];
+  const int2 gb = W.bgm[j];
+  if ((R.ga.x & gb.y) == 0 || (gb.x & R.ga.y) == 0) return false;
+  if (__float_as_int(R.a.w) < 0 && __float_as_int(b.w) < 0) return false;
+  const f3 r = sub(f3{b.x, b.y, b.z}, f3{R.a.x, R.a.y, R.a.z});
+  const float sf = fabsf(R.a.w) + fabsf(b.w);
+  const float bf = sf * sf;
+  int dec = -1;  // the binary32 verdict, -1 inside the band
+  if (bf < 1e30f) {
+    const float n2f = r.x * r.x + r.y * r.y + r.z * r.z;
+    if (n2f < bf * 0.999996f) dec = 1;
+    else if (n2f > bf * 1.000004f) dec = 0;
+  }
+  if (dec >= 0 && !R.check) return dec;
+  const double s = W.bodies[i].bounding_radius + W.bodies[j].bounding_radius;
+  const bool exact = length2(r) < s * s;
+  if (dec >= 0) {  // filter check: the binary32 verdict against binary64
+    atomicAdd(&g_filter_count[0], 1ull);
+    if ((dec == 1) != exact) atomicAdd(&g_filter_count[1], 1ull);
+  }
+  return exact;
+}
+
+// (i, j) of flattened index k
+DI void naive_from_flat(long long k, int& i, int& j) {
+  i = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)k)) * 0.5f);
+  while ((long long)i * (i - 1) / 2 > k) i--;
+  while ((long long)(i + 1) * i / 2 <= k) i++;
+  j = (int)(k - (long long)i * (i - 1) / 2);
+}
+
+// (i, j) advanced by `by` flattened positions
+DI void naive_advance(int& i, int& j, int by) {
+  j += by;
+  while (j >= i) {
+    j -= i;
+    i++;
+  }
+}
+
+// One block-wide tile of the triangle: thread t tests items
+// k0 + m * BT + t, m < NAIVE_SUB, below kend, so that a warp reads
+// consecutive records.  (i, j) is the thread's item k0 + t on entry and
+// k0 + NAIVE_SUB * BT + t on return.  Returns the tile's pairs; with
+// `write`, stores them in flattened order from `out` (below `cap`).  The
+// offsets come from per-warp ballots and one scan of NAIVE_SUB * NWARP
+// counts; two count buffers alternate, so a tile needs two barriers.
+// Blocks of at most 256 threads (NAIVE_SUB * 8 warps counts).
+#define NAIVE_SUB 16
+DI int naive_tile(Smem& S, long long k0, long long kend, bool write, int out, int cap, int& i, int& j, NaiveRow& R,
+                  int& buf) {
+  const DWorld& W = S.W;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int* cnt = S.bcnt[buf];
+  buf ^= 1;
+  unsigned bal[NAIVE_SUB];
+  int pi[NAIVE_SUB], pj[NAIVE_SUB];
+#pragma unroll
+  for (int m = 0; m < NAIVE_SUB; m++) {
+    const long long k = k0 + (long long)m * BT + threadIdx.x;
+    const bool h = k < kend && naive_rec_test(W, i, j, R);
+    bal[m] = __ballot_sync(0xffffffffu, h);
+    pi[m] = i;
+    pj[m] = j;
+    if (lane == 0) cnt[m * NWARP + wid] = __popc(bal[m]);
+    naive_advance(i, j, BT);
+  }
+  __syncthreads();
+  if (wid == 0) {  // exclusive scan of the counts in (m, warp) order: the flattened order
+    const int n = NAIVE_SUB * NWARP;
+    int v[4], sum = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int e = lane * 4 + q;
+      v[q] = e < n ? cnt[e] : 0;
+      sum += v[q];
+    }
+    int x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    int ex = x - sum;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int e = lane * 4 + q;
+      if (e < n) cnt[e] = ex;
+      ex += v[q];
+    }
+    if (lane == 31) cnt[NAIVE_SUB * 8] = x;
+  }
+  __syncthreads();
+  if (write) {
+    const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+    for (int m = 0; m < NAIVE_SUB; m++) {
+      if ((bal[m] >> lane) & 1u) {
+        const int o = out + cnt[m * NWARP + wid] + __popc(bal[m] & below);
+        if (o < cap) {
+          W.pair_a[o] = pi[m];
+          W.pair_b[o] = pj[m];
+        }
+      }
+    }
+  }
+  return cnt[NAIVE_SUB * 8];
+}
+
+// The one-block form walks the triangle row by row, a warp per row i, 32
+// candidates j at a time, and skips the chunks of 32 consecutive bodies
+// whose sphere box lies clear of body i's sphere on some axis by a relative
+// margin (bodies are usually created in spatial order, so most chunks are
+// clear of a given body).  A skipped chunk holds no pair: on that axis
+// xj - xi exceeds ri + rj for every body j of it by far more than the
+// rounding of the binary32 difference and of the radii.  Pass 0 counts each
+// row's pairs, a scan gives each row its offset, pass 1 writes them: row
+// order, then j ascending, is the flattened order.
+
+// chunk boxes (warp per chunk); a NaN coordinate or radius drops out of the
+// box, which is sound because such a body never passes the sphere test
+DI void naive_chunk_boxes(const DWorld& W, int nb) {
+  const int lane = threadIdx.x & 31;
+  const int nch = (nb + 31) >> 5;
+  for (int c = threadIdx.x >> 5; c < nch; c += NWARP) {
+    const int j = c * 32 + lane;
+    float lx = INFINITY, ly = INFINITY, lz = INFINITY, hx = -INFINITY, hy = -INFINITY, hz = -INFINITY, rm = 0.0f;
+    if (j < nb) {
+      const float4 b = W.brec[j];
+      const float r = fabsf(b.w);
+      lx = __fsub_rd(b.x, r);
+      ly = __fsub_rd(b.y, r);
+      lz = __fsub_rd(b.z, r);
+      hx = __fadd_ru(b.x, r);
+      hy = __fadd_ru(b.y, r);
+      hz = __fadd_ru(b.z, r);
+      rm = r;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+      ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+      lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o));
+      hx = fmaxf(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+      hy = fmaxf(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+      hz = fmaxf(hz, __shfl_xor_sync(0xffffffffu, hz, o));
+      rm = fmaxf(rm, __shfl_xor_sync(0xffffffffu, rm, o));
+    }
+    if (lane == 0) {
+      W.cbox[2 * c] = make_float4(lx, ly, lz, 0.0f);
+      W.cbox[2 * c + 1] = make_float4(hx, hy, hz, rm);
+    }
+  }
+}
+
+// true when body (a, |a.w|) is clear of the chunk box: on some axis the gap
+// g (rounded down) beyond the box exceeds r by 1e-6 of (|g| + r + the
+// chunk's largest radius), about 17 binary32 roundings
+DI bool naive_chunk_clear(float4 a, float4 lo, float4 hi) {
+  const float r = fabsf(a.w);
+  const float m = hi.w;
+  float g = __fsub_rd(lo.x, a.x);
+  if (__fsub_rd(g, r) > 1e-6f * (fabsf(g) + r + m)) return true;
+  g = __fsub_rd(a.x, hi.x);
+  if (__fsub_rd(g, r) > 1e-6f * (fabsf(g) + r + m)) return true;
+  g = __fsub_rd(lo.y, a.y);
+  if (__fsub_rd(g, r) > 1e-6f * (fabsf(g) + r + m)) return true;
+  g = __fsub_rd(a.y, hi.y);
+  if (__fsub_rd(g, r) > 1e-6f * (fabsf(g) + r + m)) return true;
+  g = __fsub_rd(lo.z, a.z);
+  if (__fsub_rd(g, r) > 1e-6f * (fabsf(g) + r + m)) return true;
+  g = __fsub_rd(a.z, hi.z);
+  return __fsub_rd(g, r) > 1e-6f * (fabsf(g) + r + m);
+}
+
+// Row i (warp-wide): its pairs in j order; counts them, and with `write`
+// stores them from `off`.  With the filter check on, skipped chunks are
+// tested too: g_filter_count[0] counts them, [1] those holding a pair.
+DI int naive_row(const DWorld& W, int i, NaiveRow& R, bool write, int off, int cap) {
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  R.a = W.brec[i];
+  R.ga = W.bgm[i];
+  R.cur = i;
+  const int nch = (i + 31) >> 5;  // chunks holding some j < i
+  int cnt = 0;
+  for (int c0 = 0; c0 < nch; c0 += 32) {
+    const int c = c0 + lane;
+    const bool clear = c < nch && naive_chunk_clear(R.a, W.cbox[2 * c], W.cbox[2 * c + 1]);
+    const unsigned skip = __ballot_sync(0xffffffffu, clear);
+    unsigned todo = __ballot_sync(0xffffffffu, c < nch && (!clear || R.check));
+    while (todo) {
+      const int cc = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const int j = (c0 + cc) * 32 + lane;
+      const bool hit = j < i && naive_rec_test(W, i, j, R);
+      const unsigned hb = __ballot_sync(0xffffffffu, hit);
+      if ((skip >> cc) & 1u) {  // filter check of a skipped chunk
+        if (lane == 0) {
+          atomicAdd(&g_filter_count[0], 1ull);
+          if (hb) atomicAdd(&g_filter_count[1], 1ull);
+        }
+      }
+      if (write && hit) {
+        const int o = off + cnt + __popc(hb & below);
+        if (o < cap) {
+          W.pair_a[o] = i;
+          W.pair_b[o] = j;
+        }
+      }
+      cnt += __popc(hb);
+    }
+  }
+  return cnt;
+}
+
+DI void ph_broad_naive_spheres(Smem& S) {
+  const DWorld& W = S.W;
+  const int nb = S.P.nb;
+  const int cap = S.P.pairs_cap;
+  const int lane = threadIdx.x & 31;
+  int* rows = W.sap_tmp;  // per row: pairs, then offsets (SAP's scratch; free here)
+  NaiveRow R;
+  R.init();
+  naive_chunk_boxes(W, nb);
+  __syncthreads();
+  for (int i = threadIdx.x >> 5; i < nb; i += NWARP) {
+    const int n = i > 0 ? naive_row(W, i, R, false, 0, 0) : 0;
+    if (lane == 0) rows[i] = n;
+  }
+  __syncthreads();
+  const int total = nb > 0 ? block_scan_array(S, rows, nb) : 0;
+  if (total <= cap) {
+    for (int i = 1 + (threadIdx.x >> 5); i < nb; i += NWARP) {
+      const int end = i + 1 < nb ? rows[i + 1] : total;
+      if (end > rows[i]) naive_row(W, i, R, true, rows[i], cap);
+    }
+  }
+  if (threadIdx.x == 0) {
+    S.n_pairs = total;
+    if (total > cap) S.overflow |= ST_PAIRS_OVERFLOW;
+  }
+  __syncthreads();
+}
+
 // NaiveBroadphase.collisionPairs (naive_broadphase.dart:14-33): i ascending,
-// j < i ascending, pair (bodies[i], bodies[j]).
+// j < i ascending, pair (bodies[i], bodies[j]).  With useBoundingBoxes the
+// test is AABB.overlaps on the bodies' own records.
 DI void ph_broad_naive(Smem& S) {
+  if (!S.P.use_bb) {
+    ph_broad_naive_spheres(S);
+    return;
+  }
   const DWorld& W = S.W;
   const int nb = S.P.nb;
   const long long T = (long long)nb * (nb - 1) / 2;
@@ -798,7 +1079,7 @@ DI int pair_job(Smem& S, int job, PairJob& X, bool tests) {
         atomicAdd(&S.r_cyc[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], (unsigned long long)(clock64() - t_res));
         atomicAdd(&S.r_cnt[10 + (rk == RK_SB ? 2 : (rk == RK_SP ? 0 : 1))], 1u);
       }
-      if (*(volatile int*)&g_filter_check) certificate_check(S, job, rk, X);
+      if (g_filter_check) certificate_check(S, job, rk, X);
       return RK_NONE;
     }
   }
@@ -909,7 +1190,7 @@ DI void narrow_stage1(Smem& S, int h, int* nq2) {
       W.pair_tstart[k] = __float_as_int(U);  // until the binary64 stage sets it
       W.heavy[atomicAdd(nq2, 1)] = (int)e;
     } else {
-      if (*(volatile int*)&g_filter_check &&
+      if (g_filter_check &&
           !(distance_to(X.xA, X.xB) > W.shapes[X.shA].bsr + W.shapes[X.shB].bsr))
         cc_filter_check(W, X.shA, X.shB, X.xA, X.xB, X.qA, X.qB, false, d3{0.0, 0.0, 0.0});
       W.pair_cnt[k] = 0;

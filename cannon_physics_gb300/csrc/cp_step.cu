@@ -291,6 +291,7 @@ DI void joint_solve(Smem& S, Slot* slots, int K, double* s_acc, const VelRef* vr
 template <int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_step_pre(const DWorld* __restrict__ worlds, const int* __restrict__ ids, int n,
                                                            double dt, double time_inc, int* __restrict__ queue, int last_cap) {
+  static_assert(THREADS <= 256, "the naive broadphase's count buffers hold 8 warps");
   __shared__ Smem S;
   extern __shared__ int2 s_dyn[];
   int2* s_pairs = s_dyn;

@@ -219,6 +219,16 @@ struct DWorld {
   DBodyShape* bshapes;  // compound bodies' further shapes
   // scratch
   DBodyScr* bscr;
+  // Sphere-broadphase records, one per body, written by the prepare phase:
+  // brec = (position, bounding radius rounded to binary32, its sign bit set
+  // for a static or sleeping body), bgm = (collisionFilterGroup,
+  // collisionFilterMask); consecutive bodies in consecutive memory.
+  float4* brec;
+  int2* bgm;
+  // per chunk of 32 consecutive bodies: the box of their bounding spheres,
+  // rounded outward (cbox[2c] = lower corner, cbox[2c + 1] = upper corner
+  // with the largest radius in w)
+  float4* cbox;
   int* sap_order;
   int* sap_tmp;
   int* pair_a;

@@ -243,7 +243,7 @@ __global__ void k_w_sap_pairs(const DWorld* dw, int write) {
 // takes a contiguous range of the triangle; pass 0 counts its pairs into
 // wpart[b], pass 1 (after a scan of wpart) writes them from its offset in
 // the same order, BT * 4 candidates at a time.
-DI void naive_tile(const Smem& S, long long k0, long long T, int& bits, int& cnt, int& i, int& j) {
+DI void naive_tile_bodies(const Smem& S, long long k0, long long T, int& bits, int& cnt, int& i, int& j) {
   const DWorld& W = S.W;
   bits = cnt = 0;
   i = j = 0;
@@ -274,10 +274,20 @@ __global__ void k_w_naive(const DWorld* dw, int pass) {
   const long long c0 = min(T, (long long)blockIdx.x * chunk), c1 = min(T, c0 + chunk);
   if (pass == 1 && W.wide->n_cand_pairs > S.P.pairs_cap) return;
   int out = pass == 1 ? W.wpart[blockIdx.x] : 0;
+  if (!S.P.use_bb) {  // bounding spheres: the prepare phase's records
+    int i = 0, j = 0, buf = 0;
+    NaiveRow R;
+    R.init();
+    if (c0 < c1) naive_from_flat(c0 + threadIdx.x, i, j);
+    for (long long k0 = c0; k0 < c1; k0 += (long long)NAIVE_SUB * BT)
+      out += naive_tile(S, k0, c1, pass == 1, out, S.P.pairs_cap, i, j, R, buf);
+    if (pass == 0 && threadIdx.x == 0) W.wpart[blockIdx.x] = out;
+    return;
+  }
   for (long long tile = c0; tile < c1; tile += BT * 4) {
     const long long k0 = tile + (long long)threadIdx.x * 4;
     int bits, cnt, i, j;
-    naive_tile(S, k0, c1, bits, cnt, i, j);
+    naive_tile_bodies(S, k0, c1, bits, cnt, i, j);
     int tot;
     const int pre = block_excl_scan(S, cnt, tot);
     if (pass == 1 && cnt) {
