@@ -268,10 +268,16 @@ def plain_configs(ctx, only=None):
     return out
 
 
-def serve_once(device, rate, window, seed, tick, lanes=0, wide_bodies=0):
+SERVE_CLIENTS = 8
+
+
+def serve_once(device, rate, window, seed, tick, lanes=0, wide_bodies=0, clients=SERVE_CLIENTS):
     """One served run: Poisson arrivals of rollout requests submitted on their
-    arrival times to a fresh continuous-batching server (150 GB HBM budget);
-    returns the request list, the scenes and the server's statistics."""
+    arrival times to a fresh continuous-batching server (150 GB HBM budget)
+    by `clients` client threads (request i from client i mod clients; a
+    submission lays its world out on the client's thread, as a client
+    process would); returns the request list, the scenes and the server's
+    statistics."""
     import threading
     from cannon_physics_gb300 import engine, scenes
     from cannon_physics_gb300 import serve as S
@@ -286,9 +292,11 @@ def serve_once(device, rate, window, seed, tick, lanes=0, wide_bodies=0):
     tickets = [None] * len(reqs)
     lag = [0.0]
 
-    def submitter():
-        t0 = time.perf_counter()
-        for i, (r, sc) in enumerate(zip(reqs, built)):
+    t0 = time.perf_counter() + 0.05
+
+    def client(c):
+        for i in range(c, len(reqs), clients):
+            r, sc = reqs[i], built[i]
             delay = t0 + r.arrival - time.perf_counter()
             if delay > 0:
                 time.sleep(delay)
@@ -298,9 +306,11 @@ def serve_once(device, rate, window, seed, tick, lanes=0, wide_bodies=0):
 
     clocks = Clocks(device)
     clocks.start()
-    th = threading.Thread(target=submitter)
-    th.start()
-    th.join()
+    ths = [threading.Thread(target=client, args=(c,)) for c in range(clients)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
     for t in tickets:
         if srv.wait(t) != S.DONE:
             raise RuntimeError(f"served request {t} did not complete")
@@ -313,7 +323,8 @@ def serve_once(device, rate, window, seed, tick, lanes=0, wide_bodies=0):
         "rate_req_per_s": rate, "window_s": window, "requests": len(reqs), "completed": st["completed"],
         "value": st["body_steps"] / st["span_s"], "unit": UNIT,
         "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
-        "offered_body_steps_per_s": offered / window, "span_s": st["span_s"], "submit_lag_max_s": lag[0],
+        "offered_body_steps_per_s": offered / window, "span_s": st["span_s"], "clients": clients,
+        "submit_lag_max_s": lag[0],
         "ticks": st["ticks"], "steps_per_tick": tick,
         "step_s": st["device_s"],  # time the server thread spent in step launches (the rest: admission, uploads, results)
         "bytes_peak_gb": st["bytes_peak"] / 1e9, "clocks": clk}

@@ -932,6 +932,7 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
   std::vector<float> hverts, hedges;
   std::vector<double> hvd, hed;
   std::vector<int> hfi, hconn, hcanon;
+  std::vector<char> on_f;
   for (int s = 0; s < ns; s++) {
     const cp_shape_desc& sd = d->shapes[s];
     if (sd.material < -1 || sd.material >= nm) return fail(CP_ERR_ARG, "shape %d: material out of range", s);
@@ -990,16 +991,21 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
       std::memset(&F, 0, sizeof(F));
       F.i0 = (int)hfi.size(); F.n = (int)h.faces[f].size();
       for (int vi : h.faces[f]) hfi.push_back(vi);
-      // connected faces of face f in the order clipFaceAgainstHull builds them (convex_polyhedron.dart:457-473)
+      // connected faces of face f in the order clipFaceAgainstHull builds them
+      // (convex_polyhedron.dart:457-473): every other face sharing a vertex
+      // with f, ascending (each joins at its first shared vertex)
       F.c0 = (int)hconn.size();
-      std::vector<int> conn;
-      for (size_t i = 0; i < h.faces.size(); i++)
+      on_f.assign(h.verts.size(), 0);
+      for (int vi : h.faces[f]) on_f[vi] = 1;
+      for (size_t i = 0; i < h.faces.size(); i++) {
+        if (i == f) continue;
         for (int vj : h.faces[i])
-          if (std::find(h.faces[f].begin(), h.faces[f].end(), vj) != h.faces[f].end() && i != f &&
-              std::find(conn.begin(), conn.end(), (int)i) == conn.end())
-            conn.push_back((int)i);
-      for (int x : conn) hconn.push_back(x);
-      F.nc = (int)conn.size();
+          if (on_f[vj]) {
+            hconn.push_back((int)i);
+            break;
+          }
+      }
+      F.nc = (int)hconn.size() - F.c0;
       F.normal[0] = h.normals[f].x; F.normal[1] = h.normals[f].y; F.normal[2] = h.normals[f].z;
       F.dnormal[0] = h.normals[f].x; F.dnormal[1] = h.normals[f].y; F.dnormal[2] = h.normals[f].z;
       F.plane_const = -dot3(h.normals[f], h.verts[h.faces[f][0]]);  // getPlaneConstantOfFace
