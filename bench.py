@@ -68,8 +68,8 @@ def parse():
     ap.add_argument("--serve-tick", type=int, default=4, help="served form: steps per tick")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-lanes", type=int, default=0,
-                    help="served form: wide lanes (threads stepping one large world each on the grid-wide path); 0: the "
-                         "server's default, -1: none")
+                    help="served form: wide lanes (threads stepping one large world each on the grid-wide path); 0 or -1: "
+                         "none (the server's default)")
     ap.add_argument("--serve-wide-bodies", type=int, default=0,
                     help="served form: body count from which a request takes a wide lane; 0: the server's default")
     ap.add_argument("--variant", type=int, default=None,

@@ -20,14 +20,16 @@
 // on which other worlds share its ticks: every world is stepped by the same
 // kernels on its own data, so results match stepping it alone bit for bit.
 //
-// Large worlds (at least `wide_bodies` bodies) do not join the ticks: each of
-// `wide_lanes` lane threads takes one at a time, on a context (a CUDA stream)
-// of its own, and steps it to its horizon through the wide kernels (the world
-// spread over the whole GPU), in chunks of a few steps so that a
-// cancellation takes effect.  The lanes' work overlaps with the ticks of the
-// small worlds on the device, so a small request never waits for the serial
-// solver levels of a large one in its tick, and the large ones take the
-// faster path.  Both classes share the HBM budget.
+// Optional wide lanes (wide_lanes > 0): large worlds (at least `wide_bodies`
+// bodies) then do not join the ticks; each lane thread takes one at a time,
+// on a context (a CUDA stream) of its own, and steps it to its horizon
+// through the wide kernels (the world spread over the whole GPU), in chunks
+// of a few steps so that a cancellation takes effect.  The lanes' work
+// overlaps with the ticks of the small worlds on the device.  A lane gives
+// one large world a short step, but steps only that world, so under load
+// the ticks, which step every admitted world at once, deliver several times
+// the throughput; the lanes are off unless configured.  Both classes share
+// the HBM budget.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -393,7 +395,7 @@ int cp_serve_start(const cp_serve_config* cfg, cp_server** out) {
   s->ctx = ctx;
   s->cfg = *cfg;
   if (s->cfg.steps_per_tick == 0) s->cfg.steps_per_tick = 2;
-  const int nlanes = cfg->wide_lanes > 0 ? cfg->wide_lanes : (cfg->wide_lanes == 0 ? 4 : 0);
+  const int nlanes = cfg->wide_lanes > 0 ? cfg->wide_lanes : 0;
   s->wide_bodies = cfg->wide_bodies > 0 ? cfg->wide_bodies : CP_WIDE_BODIES_DEFAULT;
   for (int l = 0; l < nlanes; l++) {
     cp_ctx* lc = nullptr;

@@ -614,10 +614,13 @@ typedef struct cp_serve_config {
    * alone with CP_ERR_CAPACITY; the other requests of its ticks go on.
    * 0 = no limit */
   int64_t max_list_entries;
-  /* worlds of at least wide_bodies bodies (0 = 1024) are not batched into
-   * the ticks: each of wide_lanes lanes (0 = 4, -1 = none) steps one at a
-   * time to its horizon, spread over the whole GPU (cp_set_wide_bodies),
-   * on a stream of its own, concurrently with the ticks */
+  /* wide_lanes > 0: worlds of at least wide_bodies bodies (0 = 1024) are
+   * not batched into the ticks; each of wide_lanes lanes steps one at a time
+   * to its horizon, spread over the whole GPU (cp_set_wide_bodies), on a
+   * stream of its own, concurrently with the ticks.  This lowers a large
+   * world's latency on an idle server but costs throughput under load: a
+   * lane steps one world at a time.  0 or -1 = no lanes (every world joins
+   * the ticks) */
   int32_t wide_bodies;
   int32_t wide_lanes;
 } cp_serve_config;

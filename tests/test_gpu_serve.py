@@ -166,7 +166,9 @@ def test_served_requests_of_the_full_size_range_match_the_oracle():
     """Requests drawn from the served workload's own distribution (16 to 4096
     bodies in the 40/40/20 sphere/box/cylinder mix), including worlds above
     the solve kernel's shared-memory group limit (640 bodies per 128 threads)
-    next to small ones, each checked against the oracle at its horizon."""
+    next to small ones, each checked against the oracle at its horizon: once
+    with every world in the ticks (the default), once with two wide lanes
+    taking the worlds of 1024 bodies or more onto the grid-wide kernels."""
     from oracle import oracle_py as O
     reqs = scenes.serve_requests(rate=2000.0, window=1.0, seed=77)
     big = [r for r in reqs if r.n_bodies > 2000][:2]
@@ -178,12 +180,16 @@ def test_served_requests_of_the_full_size_range_match_the_oracle():
     for r in chosen:
         r.horizon = min(r.horizon, 24)  # keeps the oracle's share of the test short
         built.append((r, engine.setup_scene(scenes.request_world(r))))
-    srv = S.Server(hbm_budget=20e9, steps_per_tick=4)
-    tickets = [srv.submit(sc, sc.dt, r.horizon) for r, sc in built]
-    for t, (r, sc) in zip(tickets, built):
-        assert srv.wait(t, 600.0) == S.DONE
-        out, inf = srv.result(t)
+    expect = []
+    for r, sc in built:
         ow = O.OracleWorld(O.setup_scene(scenes.request_world(r)))
         ow.step(sc.dt, r.horizon)
-        assert out.tobytes() == ow.bodies().tobytes(), f"{sc.name} ({sc.num_bodies} bodies)"
-    srv.close()
+        expect.append(ow.bodies().tobytes())
+    for lanes in (0, 2):
+        srv = S.Server(hbm_budget=20e9, steps_per_tick=4, wide_lanes=lanes)
+        tickets = [srv.submit(sc, sc.dt, r.horizon) for r, sc in built]
+        for t, (r, sc), want in zip(tickets, built, expect):
+            assert srv.wait(t, 600.0) == S.DONE
+            out, inf = srv.result(t)
+            assert out.tobytes() == want, f"lanes {lanes}: {sc.name} ({sc.num_bodies} bodies)"
+        srv.close()
