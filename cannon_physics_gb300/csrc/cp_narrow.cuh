@@ -283,8 +283,15 @@ static __device__ __noinline__ int sphere_convex(const NarrowCtx& C, int bA, int
   double R = W.shapes[shA].radius;
   ContactOut g;
   bool got = false;
+  // World vertices, each formed once: the reference forms a vertex's world
+  // position anew wherever it uses it (vertex, face and edge tests), with
+  // the same operations on the same values, so one copy gives the same bits.
+  // The vertex loop fills all of them unless it finds a contact.
+  f3 wv[CP_MAX_HULL_VERTS];
+  if (H.nv > CP_MAX_HULL_VERTS) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
   for (int i = 0; i < H.nv && !got; i++) {
     f3 wc = add(vmult(qB, hv(W, H.v0 + i)), xB);
+    wv[i] = wc;
     f3 s2c = sub(wc, xA);
     if (length2(s2c) < R * R) {
       g.ri = normalized(s2c);
@@ -297,7 +304,7 @@ static __device__ __noinline__ int sphere_convex(const NarrowCtx& C, int bA, int
   for (int i = 0; i < H.nf && !got; i++) {
     const DFace F = W.faces[H.f0 + i];
     f3 wn = vmult(qB, ld3(F.normal));
-    f3 wp = add(vmult(qB, hv(W, H.v0 + W.hfi[F.i0])), xB);
+    f3 wp = wv[W.hfi[F.i0]];
     f3 wsp = add(xA, scale(wn, -R));
     f3 pv = sub(wsp, wp);
     double pen = dot(pv, wn);
@@ -306,7 +313,7 @@ static __device__ __noinline__ int sphere_convex(const NarrowCtx& C, int bA, int
       f3 fv[CP_MAX_FACE_VERTS];
       if (F.n > CP_MAX_FACE_VERTS) { atomicOr(C.overflow, ST_HULL_OVERFLOW); return 0; }
       int nfv = F.n;
-      for (int j = 0; j < nfv; j++) fv[j] = add(vmult(qB, hv(W, H.v0 + W.hfi[F.i0 + j])), xB);
+      for (int j = 0; j < nfv; j++) fv[j] = wv[W.hfi[F.i0 + j]];
       if (point_in_polygon(fv, nfv, wn, xA)) {
         g.ri = scale(wn, -R);
         g.ni = neg(wn);
@@ -319,8 +326,8 @@ static __device__ __noinline__ int sphere_convex(const NarrowCtx& C, int bA, int
         got = true;
       } else {
         for (int j = 0; j < nfv && !got; j++) {
-          f3 v1 = add(vmult(qB, hv(W, H.v0 + W.hfi[F.i0 + (j + 1) % nfv])), xB);
-          f3 v2 = add(vmult(qB, hv(W, H.v0 + W.hfi[F.i0 + (j + 2) % nfv])), xB);
+          f3 v1 = fv[(j + 1) % nfv];
+          f3 v2 = fv[(j + 2) % nfv];
           f3 edge = sub(v2, v1);
           f3 eu = unit(edge);
           f3 v1x = sub(xA, v1);
