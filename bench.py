@@ -511,7 +511,7 @@ def run_ours(args):
             "unit": "G binary64 thread-instructions/s per GPU", "frac": fp64_per_bs * value / ws / 1e9 / FP64_PEAK_G_PER_S,
             "peak_kind": "nominal (1.25 TFLOP/s)",
             "note": "add, multiply and fused multiply-add instructions per body-step from the committed ncu capture; "
-                    "the binary64 pipe itself is 41-52 % busy because most binary64 warp instructions run with part of their lanes"},
+                    "the binary64 pipe itself is 45-52 % busy because most binary64 warp instructions run with part of their lanes"},
         "gpu_launches": launches,
         "clocks": clk,
         "autotune": dict(ctx.autotune_info(), warmup_calls=args.warmup, tune_calls=tune_calls, preroll=args.preroll),
