@@ -61,15 +61,16 @@ DI bool index_ok(int code, int world, int idx, int bound) {
 struct LevelRow {
   int k, p;
   int2 bb;
+  int r;  // the row's index in the row list (sw_orig)
 };
 
 // The first row of level `slot` (a ring entry of per-world level bounds)
 // that falls to this thread (both halves of a split level take the same
-// rows), with its body pair loaded and the rest of its record prefetched to
-// L2.  Prepared one level ahead and consumed one level later, so that none
-// of these loads lies on a level's path.
+// rows), with its body pair and row-list index loaded and the rest of its
+// record prefetched to L2.  Prepared one level ahead and consumed one level
+// later, so that none of these loads lies on a level's path.
 DI LevelRow level_row(const Slot* slots, int K, const int* lb, const int* lc) {
-  LevelRow R{-1, 0, make_int2(0, 0)};
+  LevelRow R{-1, 0, make_int2(0, 0), -1};
   int total = 0;
   for (int k = 0; k < K; k++) total += lc[k];
   const int half = BT >> 1;
@@ -88,6 +89,7 @@ DI LevelRow level_row(const Slot* slots, int K, const int* lb, const int* lc) {
   R.k = k;
   R.p = p;
   R.bb = W.sw_b[p];
+  R.r = W.sw_orig[p];
   return R;
 }
 DI bool row_bodies_ok(const Slot& sl, int2 bb) {
@@ -199,7 +201,7 @@ DI void joint_solve(Smem& S, Slot* slots, int K, double* s_acc, const VelRef* vr
             W.sw_d[W.sw_cap + cur.p].y = R.d1.y + dl;
             if (act) update_a(pme, v, w, R, dl);
             if (same && ao) update_b(pme, pme[0], pme[1], R, dl);  // the same body, after its first update
-            const int r = W.sw_orig[cur.p];
+            const int r = cur.r;
             if (index_ok(4, sl.id, r, sl.n_rows)) {
               const double a = dl > 0.0 ? dl : -dl;
               W.absdl[r] = a;
@@ -211,13 +213,14 @@ DI void joint_solve(Smem& S, Slot* slots, int K, double* s_acc, const VelRef* vr
         }
       } else {
         for (int x = threadIdx.x; x < total; x += BT) {
-          int k, p;
+          int k, p, r;
           int2 bb;
           if (x == (int)threadIdx.x) {
             if (cur.k < 0) continue;  // a failed index check (recorded)
             k = cur.k;
             p = cur.p;
             bb = cur.bb;
+            r = cur.r;
           } else {
             int off = x;
             k = 0;
@@ -227,13 +230,15 @@ DI void joint_solve(Smem& S, Slot* slots, int K, double* s_acc, const VelRef* vr
             p = lb[k] + off;
             if (!index_ok(8, sl.id, p, sl.n_rows)) continue;
             bb = sl.W.sw_b[p];
+            r = sl.W.sw_orig[p];
           }
           const Slot& sl = slots[k];
           if (!row_bodies_ok(sl, bb)) continue;
           const DWorld& W = sl.W;
-          const int r = W.sw_orig[p];
-          if (!index_ok(4, sl.id, r, sl.n_rows)) continue;
+          // the row-list index only places |dlambda|; checked after the row
+          // so that its load does not delay the row's own
           double a = gs_row_sw(W, vref[k], p, bb);
+          if (!index_ok(4, sl.id, r, sl.n_rows)) continue;
           W.absdl[r] = a;
           s_acc[k * BT + threadIdx.x] += a;
         }

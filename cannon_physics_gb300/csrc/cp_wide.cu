@@ -649,9 +649,11 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve(const DWorld* dw, int
     first_row(0, pn);
     RowRec Rn;
     int2 bbn = make_int2(0, 0);
+    int rn = -1;
     if (pn >= 0 && wide_ok(x, 1, pn, nrows)) {
       Rn = load_row(W, pn);
       bbn = W.sw_b[pn];
+      rn = W.sw_orig[pn];
     } else {
       pn = -1;
     }
@@ -660,11 +662,13 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve(const DWorld* dw, int
       const int pc = pn;
       const RowRec Rc = Rn;
       const int2 bbc = bbn;
+      const int rc = rn;
       if (l + 1 < nl) {
         first_row(l + 1, pn);
         if (pn >= 0 && wide_ok(x, 1, pn, nrows)) {
           Rn = load_row(W, pn);
           bbn = W.sw_b[pn];
+          rn = W.sw_orig[pn];
         } else {
           pn = -1;
         }
@@ -697,7 +701,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve(const DWorld* dw, int
               wv_load(vel, flg, me, v2, w2);
               wv_update_b(vel, me, v2, w2, Rc, dl);
             }
-            const int r = W.sw_orig[pc];
+            const int r = rc;
             if (wide_ok(x, 3, r, nrows)) {
               const double a = dl > 0.0 ? dl : -dl;
               W.absdl[r] = a;
@@ -711,17 +715,19 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve(const DWorld* dw, int
         for (int off = threadIdx.x; off < cnt; off += BT) {
           RowRec R;
           int2 bb;
-          int p;
+          int p, r;
           if (off == (int)threadIdx.x) {
             if (pc < 0) continue;
             R = Rc;
             bb = bbc;
             p = pc;
+            r = rc;
           } else {
             p = b + off;
             if (!wide_ok(x, 1, p, nrows)) continue;
             R = load_row(W, p);
             bb = W.sw_b[p];
+            r = W.sw_orig[p];
           }
           if (!wide_ok(x, 2, bb.x, nb) || !wide_ok(x, 2, bb.y, nb)) continue;
           float4 va, wa, vb, wb;
@@ -737,7 +743,6 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve(const DWorld* dw, int
             if (bb.x == bb.y) wv_load(vel, flg, bb.y, vb, wb);  // a constraint between a body and itself
             wv_update_b(vel, bb.y, vb, wb, R, dl);
           }
-          const int r = W.sw_orig[p];
           if (wide_ok(x, 3, r, nrows)) {
             const double a = dl > 0.0 ? dl : -dl;
             W.absdl[r] = a;
