@@ -708,17 +708,47 @@ int wide_check(cp_ctx* c, const WorldRec& w, int id) {
   return CP_OK;
 }
 
-// nsteps internal steps of one world; its time advances by time_inc per step
+// nsteps internal steps of one world; its time advances by time_inc per step.
+// One-block worlds: the world's parameters before the launches, after them
+// and the index check record come back in one copy sequence with a single
+// stream synchronisation; a step that overflowed a capacity (rare) then
+// takes the retry loop below, which reads as it goes.
 int plain_steps(cp_ctx* c, int id, double dt, int nsteps, double time_inc) {
   WorldRec& w = c->worlds[id];
   int st = ensure_dt(c, w, dt);
   if (st) return st;
-  CUDA_TRY(cudaMemcpyAsync(c->d_one, &id, sizeof(int), cudaMemcpyHostToDevice, c->stream));
-  DWorldParams p;
-  st = read_params(c, w, p);
-  if (st) return st;
-  long long target = p.stepnumber + nsteps;
   const bool wide = is_wide(c, w);
+  cp_ctx::PlainStage* hs = c->h_plain;
+  if (c->plain_id != id) {
+    hs->id = id;  // pinned: the copy reads it when it runs, and nothing rewrites it before the synchronisation below
+    CUDA_TRY(cudaMemcpyAsync(c->d_one, &hs->id, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    c->plain_id = id;
+  }
+  DWorldParams p;
+  long long target;
+  if (!wide) {
+    CUDA_TRY(cudaMemcpyAsync(&hs->before, w.dw.P, sizeof(DWorldParams), cudaMemcpyDeviceToHost, c->stream));
+    for (int s = 0; s < nsteps; s++) {
+      CUDA_TRY(cpk_launch_step(c->d_worlds, c->d_one, c->d_one_group, 1, dt, time_inc, c->d_queue, 1, 1, c->stream,
+                               w.nb > 512 ? 0 : c->plain_variant, 1, w.nb));
+      c->launches += 2;  // the two step kernels (the queue reset is a memset)
+    }
+    CUDA_TRY(cudaMemcpyAsync(&hs->after, w.dw.P, sizeof(DWorldParams), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cpk_read_check_async(hs->chk, c->stream));
+    const cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+      c->plain_id = -1;
+      return fail(CP_ERR_CUDA, "%s", cudaGetErrorString(e));
+    }
+    if (hs->chk[0] != 0) return kernel_check();  // reads the record again, clears it and reports it
+    p = hs->after;
+    target = hs->before.stepnumber + nsteps;
+    if (p.status == 0 && p.stepnumber == target) return CP_OK;
+  } else {
+    st = read_params(c, w, p);
+    if (st) return st;
+    target = p.stepnumber + nsteps;
+  }
   for (int guard = 0; guard < 64; guard++) {
     long long done = p.stepnumber;
     if (wide && target > done)
@@ -850,6 +880,7 @@ int cp_create(const cp_config* cfg, cp_ctx** out) {
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_queue, 2 * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_one, sizeof(int));
+  if (e == cudaSuccess) e = cudaHostAlloc((void**)&c->h_plain, sizeof(cp_ctx::PlainStage), cudaHostAllocDefault);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_one_group, 2 * sizeof(int));
   if (e == cudaSuccess) {
     int og[2] = {0, 1};
@@ -888,6 +919,7 @@ int cp_destroy(cp_ctx* c) {
   if (c->d_status) cudaFree(c->d_status);
   if (c->d_queue) cudaFree(c->d_queue);
   if (c->d_one) cudaFree(c->d_one);
+  if (c->h_plain) cudaFreeHost(c->h_plain);
   if (c->d_one_group) cudaFree(c->d_one_group);
   if (c->d_gstart) cudaFree(c->d_gstart);
   if (c->d_io_ids) cudaFree(c->d_io_ids);

@@ -93,6 +93,16 @@ struct cp_ctx {
   int d_ids_cap = 0;
   int* d_queue = nullptr;
   int* d_one = nullptr;  // world id of the plain path
+  // pinned staging of the plain path: the world id it uploads, the index
+  // check record and the world's parameters before and after its launches,
+  // read back with one stream synchronisation per call
+  struct PlainStage {
+    int id, pad;
+    int chk[4];
+    DWorldParams before, after;
+  };
+  PlainStage* h_plain = nullptr;
+  int plain_id = -1;  // the id d_one holds (-1: unknown)
   int* d_one_group = nullptr;  // {0, 1}: the plain path's single group
   int* d_gstart = nullptr;  // batched path: group boundaries into d_ids
   int ngroups = 0;

@@ -85,6 +85,9 @@ cudaError_t cpk_static_scratch(int device, void** ptr, size_t* bytes);
 // First failed index check of the solve kernel since the last read, as
 // {code, world id, index, bound} (code 0: none); clears it once read.
 cudaError_t cpk_read_check(int out[4]);
+// the same record copied on `stream` into `out` (pinned host memory), without
+// clearing it; cpk_read_check reads and clears it once a copy showed a failure
+cudaError_t cpk_read_check_async(int* out, cudaStream_t stream);
 // World.raycastClosest / Any / All over one world (cp_ray.cu): refresh the
 // AABBs that need it (and re-sort a SAP axis list), then one ray per thread
 cudaError_t cpk_raycast(const DWorld* d_world, const cp_ray* d_rays, int n, int mode, cp_ray_hit* d_hits, int max_hits,

@@ -814,6 +814,10 @@ cudaError_t cpk_static_scratch(int device, void** ptr, size_t* bytes) {
   return cudaSuccess;
 }
 
+cudaError_t cpk_read_check_async(int* out, cudaStream_t stream) {
+  return cudaMemcpyFromSymbolAsync(out, g_check, sizeof(int) * 4, 0, cudaMemcpyDeviceToHost, stream);
+}
+
 cudaError_t cpk_read_check(int out[4]) {
   cudaError_t e = cudaMemcpyFromSymbol(out, g_check, sizeof(int) * 4);
   if (e == cudaSuccess && out[0] != 0) {
