@@ -144,6 +144,29 @@ def test_large_batch_equals_plain(ctx):
         w.destroy()
 
 
+def test_bench_batch_every_world_equals_plain(ctx):
+    """The benchmark's own 4096-world batch: every world after 20 batched
+    steps (two calls, the second replaying the captured graph, with the
+    autotuner switching kernel variants) equals the same world stepped alone
+    through cp_world_step, bit for bit."""
+    scs = scenes.batch_worlds(4096, 1000)  # rank 0's worlds in bench.py
+    for s in scs:
+        engine.setup_scene(s)
+    ws = [ctx.world(s) for s in scs]
+    ctx.batch_step(ws, 1 / 60, 10)
+    ctx.batch_step(ws, 1 / 60, 10)
+    bad = []
+    for i, s in enumerate(scs):
+        p = ctx.world(s)
+        p.step(1 / 60, 20)
+        if p.bodies().tobytes() != ws[i].bodies().tobytes():
+            bad.append(s.name)
+        p.destroy()
+    for w in ws:
+        w.destroy()
+    assert not bad, f"{len(bad)} worlds differ from the plain path, first {bad[:5]}"
+
+
 def test_every_kernel_variant_gives_the_same_bits(ctx):
     """The autotuner may switch kernel variants between steps: every variant
     (block size, register budget) must produce identical state."""
