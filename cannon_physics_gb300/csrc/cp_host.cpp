@@ -708,6 +708,55 @@ int wide_check(cp_ctx* c, const WorldRec& w, int id) {
   return CP_OK;
 }
 
+// The slot-scheduled sweeps' buffers of a wide world (DSched), sized for its
+// row capacity, iteration count and bodies; remade when the row capacity has
+// grown.  Above kSchedMaxBytes the world keeps the level-by-level sweeps
+// (the device sees a zero-sized DSched).
+const size_t kSchedMaxBytes = (size_t)1 << 30;
+int ensure_sched(cp_ctx* c, int id) {
+  WorldRec& w = c->worlds[id];
+  DSched& D = w.dw.sched;
+  const long long R = w.rows_cap, S = w.iterations, N = w.nb;
+  if (D.rows >= R && D.iters == S && D.nb >= N && w.sched_mem) return CP_OK;
+  if (S <= 0 || R <= 0) return CP_OK;
+  Layout L;
+  const size_t o_lam = L.take(sizeof(double) * S * R), o_abs = L.take(sizeof(double) * S * R);
+  const size_t o_slot = L.take(sizeof(int) * S * R), o_first = L.take((size_t)(S * R));
+  const size_t o_items = L.take(sizeof(int) * S * R), o_ends = L.take(sizeof(int) * (S * R + 1));
+  const size_t o_bt = L.take(sizeof(int) * N), o_bs = L.take(sizeof(int) * N), o_act = L.take((size_t)R);
+  const size_t o_ps = L.take(sizeof(double) * S * 256), o_ck = L.take(sizeof(float) * 6 * S * N);
+  if (w.sched_mem) {
+    dev_free(c, w.sched_mem, w.pooled);
+    w.sched_mem = nullptr;
+    w.sched_bytes = 0;
+  }
+  std::memset(&D, 0, sizeof(D));
+  if (L.off <= kSchedMaxBytes) {
+    char* base = nullptr;
+    if (dev_alloc(c, (void**)&base, L.off, "sweep schedule") == CP_OK) {
+      w.sched_mem = base;
+      w.sched_bytes = L.off;
+      D.lam = (double*)(base + o_lam);
+      D.absdl = (double*)(base + o_abs);
+      D.slot = (int*)(base + o_slot);
+      D.first = (unsigned char*)(base + o_first);
+      D.items = (int*)(base + o_items);
+      D.ends = (int*)(base + o_ends);
+      D.body_t = (int*)(base + o_bt);
+      D.body_s = (int*)(base + o_bs);
+      D.act = (unsigned char*)(base + o_act);
+      D.psum = (double*)(base + o_ps);
+      D.ckpt = (float*)(base + o_ck);
+      D.rows = (int)R;
+      D.iters = (int)S;
+      D.nb = (int)N;
+    } else {
+      g_err.clear();  // no room: the level-by-level sweeps need none of it
+    }
+  }
+  return upload_world_entry(c, id);
+}
+
 // nsteps internal steps of one world; its time advances by time_inc per step.
 // One-block worlds: the world's parameters before the launches, after them
 // and the index check record come back in one copy sequence with a single
@@ -751,6 +800,10 @@ int plain_steps(cp_ctx* c, int id, double dt, int nsteps, double time_inc) {
   }
   for (int guard = 0; guard < 64; guard++) {
     long long done = p.stepnumber;
+    if (wide) {
+      st = ensure_sched(c, id);
+      if (st) return st;
+    }
     if (wide && target > done)
       CUDA_TRY(cpk_launch_wide_steps(c->d_worlds + id, w.dw, wide_shape(w), dt, time_inc, (int)(target - done), c->stream,
                                      &c->launches));
@@ -1181,6 +1234,7 @@ int prepare_world(const cp_world_desc* d, PreparedWorld& out) {
   P.jobs_cap = w.jobs_cap;
   if (d->solver != CP_SOLVER_GS && d->solver != CP_SOLVER_SPLIT) return fail(CP_ERR_ARG, "solver %d", d->solver);
   w.split = d->solver == CP_SOLVER_SPLIT;
+  w.iterations = d->solver_iterations;
   P.split = w.split;
   P.id_counter = d->equation_id_counter;
   P.pool_c = P.pool_f = 0;
@@ -1297,6 +1351,7 @@ int destroy_world(cp_ctx* c, int id) {
   if (w.state) dev_free(c, w.state, w.pooled);
   if (w.scratch) dev_free(c, w.scratch, w.pooled);
   if (w.pool) cudaFree(w.pool);
+  if (w.sched_mem) dev_free(c, w.sched_mem, w.pooled);
   w = WorldRec();
   if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   return CP_OK;

@@ -34,6 +34,9 @@ struct WorldRec {
   long long* pool = nullptr;  // device, SplitSolver: contact then friction equation pools (ids)
   int pool_cap = 0;           // contact pool capacity (the friction pool holds twice as many)
   bool split = false;         // SplitSolver
+  int iterations = 0;         // GSSolver.iterations
+  char* sched_mem = nullptr;  // device: the slot-scheduled wide sweeps' buffers (DSched), made at the first wide step
+  size_t sched_bytes = 0;
   size_t state_bytes = 0, scratch_bytes = 0;
   bool pooled = false;     // state and scratch come from the context's memory pool
   DWorld dw{};

@@ -192,7 +192,30 @@ struct __align__(16) DWide {
   int n_queued, n_queued2, nh_padded, cursor;
   int check[4];   // first failed index check of the sweep kernel: code, index, bound
   int kcnt[16], kpos[16];
-  int total, n_jobs, pad[2];  // n_jobs: narrowphase jobs of a compound world
+  int total, n_jobs;  // n_jobs: narrowphase jobs of a compound world
+  int sched;          // this step's sweeps run on the slot schedule (k_w_sched)
+  int n_slots;        // its slots
+  int early;          // the last solve stopped before its last sweep (0 at the first step)
+  int slow;           // steps left on the level-by-level sweeps after a schedule that saved too little
+  int pad[2];
+};
+
+// Buffers of the slot-scheduled sweeps of a wide world (its own allocation,
+// sized for `rows` rows, `iters` sweeps and `nb` bodies; null when absent).
+// Instance i = s * n_rows + p is sweep s of the row at level position p.
+struct DSched {
+  double* lam;        // [iters * rows] lambda after each instance
+  double* absdl;      // [iters * rows] |dlambda| by sweep and row-list index
+  int* slot;          // [iters * rows] the instance's slot (-1: skipped by a failed index check)
+  unsigned char* first;  // [iters * rows] bit 0 / 1: the instance is the first of its sweep on bi / bj
+  int* items;         // [iters * rows] instances ordered by slot
+  int* ends;          // [iters * rows + 1] end of each slot in items
+  int* body_t;        // [nb] slot of the body's last instance
+  int* body_s;        // [nb] sweep of the body's last instance (-1: no row touches it)
+  unsigned char* act; // [rows] bit 0 / 1: the row's bi / bj takes velocity updates
+  double* psum;       // [iters * 256] per-thread sums of |dlambda| by sweep
+  float* ckpt;        // [iters * nb * 6] vlambda, wlambda of a body before its first instance of a sweep
+  int rows, iters, nb, pad;
 };
 #define CP_WIDE_SCAN_BLOCKS 128
 
@@ -296,4 +319,5 @@ struct DWorld {
   int* wpart;       // per-block partial sums of the wide scans (CP_WIDE_SCAN_BLOCKS + 1)
   float* wvel;      // wide sweeps: vlambda, wlambda (6 floats per body) when they do not fit in shared memory
   unsigned char* wflag;  // wide sweeps: solve flag per body
+  DSched sched;          // slot-scheduled wide sweeps (zeroed when not allocated)
 };
