@@ -724,7 +724,7 @@ int ensure_sched(cp_ctx* c, int id) {
   const size_t o_slot = L.take(sizeof(int) * S * R), o_first = L.take((size_t)(S * R));
   const size_t o_items = L.take(sizeof(int) * S * R), o_ends = L.take(sizeof(int) * (S * R + 1));
   const size_t o_bt = L.take(sizeof(int) * N), o_bs = L.take(sizeof(int) * N), o_act = L.take((size_t)R);
-  const size_t o_ps = L.take(sizeof(double) * S * 256), o_ck = L.take(sizeof(float) * 6 * S * N);
+  const size_t o_ck = L.take(sizeof(float) * 6 * S * N);
   if (w.sched_mem) {
     dev_free(c, w.sched_mem, w.pooled);
     w.sched_mem = nullptr;
@@ -745,7 +745,6 @@ int ensure_sched(cp_ctx* c, int id) {
       D.body_t = (int*)(base + o_bt);
       D.body_s = (int*)(base + o_bs);
       D.act = (unsigned char*)(base + o_act);
-      D.psum = (double*)(base + o_ps);
       D.ckpt = (float*)(base + o_ck);
       D.rows = (int)R;
       D.iters = (int)S;

@@ -205,7 +205,7 @@ struct __align__(16) DWide {
 // Instance i = s * n_rows + p is sweep s of the row at level position p.
 struct DSched {
   double* lam;        // [iters * rows] lambda after each instance
-  double* absdl;      // [iters * rows] |dlambda| by sweep and row-list index
+  double* absdl;      // [iters * rows] |dlambda| by sweep and row-list index (the exit tests sum them)
   int* slot;          // [iters * rows] the instance's slot (-1: skipped by a failed index check)
   unsigned char* first;  // [iters * rows] bit 0 / 1: the instance is the first of its sweep on bi / bj
   int* items;         // [iters * rows] instances ordered by slot
@@ -213,7 +213,6 @@ struct DSched {
   int* body_t;        // [nb] slot of the body's last instance
   int* body_s;        // [nb] sweep of the body's last instance (-1: no row touches it)
   unsigned char* act; // [rows] bit 0 / 1: the row's bi / bj takes velocity updates
-  double* psum;       // [iters * 256] per-thread sums of |dlambda| by sweep
   float* ckpt;        // [iters * nb * 6] vlambda, wlambda of a body before its first instance of a sweep
   int rows, iters, nb, pad;
 };

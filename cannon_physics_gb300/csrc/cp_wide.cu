@@ -959,21 +959,24 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve_sched(const DWorld* d
     wv_store(vel, i, v, w);
     flg[i] = v.w != 0.f;
   }
-  for (int s = 0; s < iters; s++) D.psum[s * WS_THREADS + threadIdx.x] = 0.0;
   __syncthreads();
   const int cap = W.sw_cap;
-  // the thread's first instance of the next slot and its constant record
-  // (all but lambda), loaded while the current slot runs: the instance at
-  // the slot's start, the record after the slot's rows
+  // the thread's first instance of the next slot and its record, loaded
+  // while the current slot runs: the instance at the slot's start, the
+  // record after the slot's rows.  Its row's lambda from the sweep before
+  // is loaded with it when that instance ran two or more slots earlier
+  // (its value is final then), else after the barrier.
   auto first_item = [&](int t) -> int {
     if (t >= nslots) return -1;
     const int k = (t > 0 ? D.ends[t - 1] : 0) + (int)threadIdx.x;
     return k < D.ends[t] && k < ninst ? D.items[k] : -1;
   };
-  int in_ = first_item(0), fln = 0, rn = 0;
+  int in_ = first_item(0), fln = 0, rn = 0, tpn = -1;
+  double lamn = 0.0;
   RowRec Rn;
   int2 bbn = make_int2(0, 0);
-  auto fetch = [&]() {
+  // t: the slot the fetched instance runs in (loads made during slot t - 1)
+  auto fetch = [&](int t) {
     if (in_ < 0 || in_ >= ninst) {
       in_ = -1;
       return;
@@ -983,11 +986,15 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve_sched(const DWorld* d
     bbn = W.sw_b[p];
     rn = W.sw_orig[p];
     fln = D.first[in_];
+    tpn = in_ >= nrows ? D.slot[in_ - nrows] : -1;
+    lamn = in_ >= nrows ? D.lam[in_ - nrows] : Rn.d1.y;
+    (void)t;
   };
-  fetch();
+  fetch(0);
   for (int t = 0; t < nslots; t++) {
     const int b = t > 0 ? D.ends[t - 1] : 0, e = D.ends[t];
-    const int ic = in_, flc = fln, rc = rn;
+    const int ic = in_, flc = fln, rc = rn, tpc = tpn;
+    const double lamc = lamn;
     const RowRec Rc = Rn;
     const int2 bbc = bbn;
     in_ = first_item(t + 1);
@@ -1001,7 +1008,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve_sched(const DWorld* d
       const int2 bb = first ? bbc : W.sw_b[p];
       const int r = first ? rc : W.sw_orig[p];
       if (!wide_ok(x, 2, bb.x, nb) || !wide_ok(x, 2, bb.y, nb) || !wide_ok(x, 3, r, nrows)) continue;
-      const double lam0 = s > 0 ? D.lam[i - nrows] : R.d1.y;
+      // the prefetched lambda holds when its instance ran before slot t - 1
+      const double lam0 = s == 0 ? R.d1.y : (first && tpc >= 0 && tpc + 2 <= t ? lamc : D.lam[i - nrows]);
       R.d1.y = lam0;
       const int fl = first ? flc : D.first[i];
       float4 va, wa, vb, wb;
@@ -1019,18 +1027,19 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve_sched(const DWorld* d
         if (bb.x == bb.y) wv_load(vel, flg, bb.y, vb, wb);  // a constraint between a body and itself
         wv_update_b(vel, bb.y, vb, wb, R, dl);
       }
-      const double a = dl > 0.0 ? dl : -dl;
-      D.absdl[(size_t)s * nrows + r] = a;
-      D.psum[s * WS_THREADS + threadIdx.x] += a;
+      D.absdl[(size_t)s * nrows + r] = dl > 0.0 ? dl : -dl;
     }
-    fetch();
+    fetch(t + 1);
     __syncthreads();
   }
   // the exit test of each sweep, in order: (sum of |dlambda| in row order)^2
   // < tol^2, the order-free sum deciding outside the rounding band
   int sconv = -1;
   for (int s = 0; s < iters; s++) {
-    const double sp = block_sum(S, D.psum[s * WS_THREADS + threadIdx.x]);
+    const double* ad = D.absdl + (size_t)s * nrows;
+    double part = 0.0;
+    for (int r = threadIdx.x; r < nrows; r += BT) part += ad[r];
+    const double sp = block_sum(S, part);
     if (threadIdx.x == 0) {
       const double tol2 = S.P.tolerance * S.P.tolerance;
       const double band = 2.2 * (double)nrows * 1.1102230246251565e-16;
@@ -1040,7 +1049,6 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_w_solve_sched(const DWorld* d
       else if (lo * lo * (1.0 - 4.5e-16) >= tol2 && lo >= 0.0) conv = 0;
       else {
         double tt = 0.0;
-        const double* ad = D.absdl + (size_t)s * nrows;
         for (int r = 0; r < nrows; r++) tt += ad[r];
         conv = tt * tt < tol2;
       }
