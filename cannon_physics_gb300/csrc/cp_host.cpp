@@ -717,8 +717,12 @@ int ensure_sched(cp_ctx* c, int id) {
   WorldRec& w = c->worlds[id];
   DSched& D = w.dw.sched;
   const long long R = w.rows_cap, S = w.iterations, N = w.nb;
-  if (D.rows >= R && D.iters == S && D.nb >= N && w.sched_mem) return CP_OK;
-  if (S <= 0 || R <= 0) return CP_OK;
+  if (D.rows >= R && D.iters == S && D.nb >= N && w.sched_mem) {
+    if (D.mode == c->sched_mode) return CP_OK;
+    D.mode = c->sched_mode;
+    return upload_world_entry(c, id);
+  }
+  if (S <= 0 || R <= 0 || w.sched_skip_rows >= R) return CP_OK;
   Layout L;
   const size_t o_lam = L.take(sizeof(double) * S * R), o_abs = L.take(sizeof(double) * S * R);
   const size_t o_slot = L.take(sizeof(int) * S * R), o_first = L.take((size_t)(S * R));
@@ -749,10 +753,12 @@ int ensure_sched(cp_ctx* c, int id) {
       D.rows = (int)R;
       D.iters = (int)S;
       D.nb = (int)N;
+      D.mode = c->sched_mode;
     } else {
       g_err.clear();  // no room: the level-by-level sweeps need none of it
     }
   }
+  if (!w.sched_mem) w.sched_skip_rows = R;
   return upload_world_entry(c, id);
 }
 
@@ -2272,6 +2278,14 @@ int cp_set_wide_bodies(cp_ctx* c, int32_t bodies) {
   if (bodies < 0) return fail(CP_ERR_ARG, "bodies must be >= 0");
   std::lock_guard<std::mutex> lock(c->mu);
   c->wide_bodies = bodies;
+  return CP_OK;
+}
+
+int cp_set_sweep_schedule(cp_ctx* c, int32_t mode) {
+  if (!c) return fail(CP_ERR_ARG, "null context");
+  if (mode < -1 || mode > 1) return fail(CP_ERR_ARG, "sweep schedule mode must be -1, 0 or 1");
+  std::lock_guard<std::mutex> lock(c->mu);
+  c->sched_mode = mode;
   return CP_OK;
 }
 

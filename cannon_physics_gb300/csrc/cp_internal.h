@@ -37,6 +37,7 @@ struct WorldRec {
   int iterations = 0;         // GSSolver.iterations
   char* sched_mem = nullptr;  // device: the slot-scheduled wide sweeps' buffers (DSched), made at the first wide step
   size_t sched_bytes = 0;
+  long long sched_skip_rows = -1;  // row capacity for which the buffers were too large or could not be had
   size_t state_bytes = 0, scratch_bytes = 0;
   bool pooled = false;     // state and scratch come from the context's memory pool
   DWorld dw{};
@@ -114,6 +115,7 @@ struct cp_ctx {
   // cp_world_step on a world of at least this many bodies runs the wide
   // kernels (the world spread over the whole GPU); 0: never
   int wide_bodies = CP_WIDE_BODIES_DEFAULT;
+  int sched_mode = 0;  // cp_set_sweep_schedule
   // a world whose pair, contact, row or bin list would grow beyond this many
   // entries fails with CP_ERR_CAPACITY instead (0: no limit)
   long long list_cap_limit = 0;

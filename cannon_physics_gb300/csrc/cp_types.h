@@ -214,7 +214,8 @@ struct DSched {
   int* body_s;        // [nb] sweep of the body's last instance (-1: no row touches it)
   unsigned char* act; // [rows] bit 0 / 1: the row's bi / bj takes velocity updates
   float* ckpt;        // [iters * nb * 6] vlambda, wlambda of a body before its first instance of a sweep
-  int rows, iters, nb, pad;
+  int rows, iters, nb;
+  int mode;           // cp_set_sweep_schedule: 0 where it pays, 1 wherever it fits, -1 never
 };
 #define CP_WIDE_SCAN_BLOCKS 128
 

@@ -845,8 +845,8 @@ __global__ void __launch_bounds__(1024, 1) k_w_sched(const DWorld* dw) {
   DWide* x = W.wide;
   const DSched& D = W.sched;
   const int nrows = x->n_rows, nl = x->n_levels, nb = S.P.nb, iters = S.P.iterations;
-  const bool use = nrows > 0 && nl > 0 && iters > 0 && D.rows >= nrows && D.iters == iters && D.nb >= nb && !x->early &&
-                   x->slow == 0 && sched_fits(nb, nrows, nl, iters);
+  const bool use = nrows > 0 && nl > 0 && iters > 0 && D.rows >= nrows && D.iters == iters && D.nb >= nb &&
+                   sched_fits(nb, nrows, nl, iters) && D.mode >= 0 && (D.mode == 1 || (!x->early && x->slow == 0));
   __syncthreads();  // every thread has read x->early and x->slow before they change
   if (threadIdx.x == 0) {
     x->sched = use ? 1 : 0;

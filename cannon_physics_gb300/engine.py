@@ -66,6 +66,7 @@ def lib():
         L.cp_set_variant.argtypes = [vp, i32]
         L.cp_set_group_bodies.argtypes = [vp, i32]
         L.cp_set_wide_bodies.argtypes = [vp, i32]
+        L.cp_set_sweep_schedule.argtypes = [vp, i32]
         L.cp_set_filter_check.argtypes = [vp, i32]
         L.cp_filter_check_counts.argtypes = [vp, vp, vp, i32]
         _lib = L
@@ -146,6 +147,11 @@ class Context:
         """Single-world steps of worlds with at least n bodies spread over the
         whole GPU (0: never)."""
         check(lib().cp_set_wide_bodies(self.h, n), "cp_set_wide_bodies")
+
+    def set_sweep_schedule(self, mode):
+        """Sweeps of wide worlds: 0 on the slot schedule where it pays, 1
+        wherever it fits, -1 always level by level (same bits)."""
+        check(lib().cp_set_sweep_schedule(self.h, mode), "cp_set_sweep_schedule")
 
     def set_group_bodies(self, n):
         check(lib().cp_set_group_bodies(self.h, n), "cp_set_group_bodies")

@@ -569,6 +569,14 @@ int cp_set_group_bodies(cp_ctx* ctx, int32_t bodies);
  * 0 keeps every world on one block.  No counterpart in the reference. */
 int cp_set_wide_bodies(cp_ctx* ctx, int32_t bodies);
 
+/* The Gauss-Seidel sweeps of a world stepped over the whole GPU run either
+ * level by level or on a slot schedule across sweeps (the same bits either
+ * way).  0 (default): the schedule where it pays (the last solve ran every
+ * sweep, the schedule saves two thirds of the level steps, its tables fit);
+ * 1: the schedule wherever its tables fit; -1: always level by level.  A
+ * test switch; no counterpart in the reference. */
+int cp_set_sweep_schedule(cp_ctx* ctx, int32_t mode);
+
 /* Filter check, a test switch with no counterpart in the reference (off by
  * default; per device).  Where a binary32 filter settles a pair without the
  * reference's binary64 arithmetic (the no-contact certificates of

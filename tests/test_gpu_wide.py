@@ -4,7 +4,10 @@ the oracle and against the one-block path, bit for bit.
 cp_set_wide_bodies(1) sends every world, however small, through the wide
 kernels, so the small scenes that reach every branch of World.step (edge
 scenes, all three broadphases, constraints, sleeping, capacity regrowth)
-check the wide path against the oracle step by step.  The full-size box pile
+check the wide path against the oracle step by step, with the sweeps on
+the library's choice of schedule, on the slot schedule wherever it fits
+(cp_set_sweep_schedule(1): early exits then roll back at every step that
+stops early) and level by level.  The full-size box pile
 (4097 bodies, SAP) and the mixed scene with chains (8193 bodies, grid,
 sleeping) take the wide path by default; they are checked against the
 oracle over horizons long enough for the pile to be in contact everywhere.
@@ -30,10 +33,18 @@ def ctx():
     c.close()
 
 
-@pytest.fixture
-def wide_ctx(ctx):
+# The wide path's Gauss-Seidel sweeps run level by level or on a slot
+# schedule across sweeps; every small-scene test runs with the library's
+# choice, with the schedule forced wherever it fits, and with it off.
+SCHEDULE_MODES = {"sched_auto": 0, "sched_forced": 1, "levels_only": -1}
+
+
+@pytest.fixture(params=sorted(SCHEDULE_MODES))
+def wide_ctx(ctx, request):
     ctx.set_wide_bodies(1)
+    ctx.set_sweep_schedule(SCHEDULE_MODES[request.param])
     yield ctx
+    ctx.set_sweep_schedule(0)
     ctx.set_wide_bodies(1024)
 
 
@@ -88,6 +99,18 @@ def test_box_pile_full_size_in_contact(ctx):
     the oracle continued from the same state, for 60 more steps."""
     run_parity(ctx, scenes.box_pile(), 10, every=5)
     info = run_parity(ctx, scenes.box_pile(), 60, every=10, start=100)
+    assert info.num_contacts > 6000
+
+
+@pytest.mark.parametrize("mode", [1, -1])
+def test_box_pile_full_size_schedule_modes(ctx, mode):
+    """The full-size pile from step 100 with the slot-scheduled sweeps forced
+    on every step, and with them off."""
+    ctx.set_sweep_schedule(mode)
+    try:
+        info = run_parity(ctx, scenes.box_pile(), 20, every=10, start=100)
+    finally:
+        ctx.set_sweep_schedule(0)
     assert info.num_contacts > 6000
 
 
